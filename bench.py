@@ -1,0 +1,259 @@
+"""Benchmark of the GB300 statevector engine.
+
+Headline workload (metric "gate HBM GB/s at 28q"): one dense, uncontrolled
+1-qubit gate at a time on a 28-qubit complex128 state (2^28 x 16 B = 4 GiB,
+far larger than the 129 MB L2, so no flush is needed between launches).
+One step applies H then RX(theta) to each of the 28 targets (56 launches).
+Algorithmic bytes per gate = 2 x S (read + write of every amplitude).
+
+  value  : 56 * 2S / device time of the step (CUDA events on the state's
+           stream), inputs resident in HBM.
+  e2e    : the same step through the public pybind11 API with the gate
+           parameters coming from host memory, plus a device->host read of a
+           result (the marginal probability of wire 0) every step.
+  roofline: the gate kernel's average launch time vs the measured HBM copy
+           bandwidth of this GPU.
+  cpu_baseline: the CPU oracle (C++/OpenMP restatement of the reference
+           semantics) applying the same gate to a 28-qubit state on the host.
+
+`--impl reference` times the reference's CPU path for this workload on the
+host cores (the oracle port; the reference's own GPU path needs the closed
+cuStateVec library, which is absent).
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_QUBITS = 28
+THETA = 0.7345
+PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
+
+
+def _peaks():
+    try:
+        with open(PEAKS_FILE) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle-reason samples during the timed region."""
+
+    QUERY = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, period_ms=200):
+        self.period_ms = period_ms
+        self.proc = None
+        self.lines = []
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "--query-gpu=" + self.QUERY, "--format=csv,noheader,nounits", "-i", "0",
+                 "-lms", str(self.period_ms)], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[3:7]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def _gate_list(n):
+    return [("Hadamard", w) for w in range(n)] + [("RX", w) for w in range(n)]
+
+
+def cpu_baseline_sample(n, gates=2):
+    """Oracle (CPU) single-gate GB/s on the host cores: a bounded sample of
+    `gates` dense 1-qubit gates on an n-qubit complex128 state."""
+    from oracle import oracle as O
+
+    state = np.zeros(1 << n, np.complex128)
+    state[0] = 1.0
+    c, s = np.cos(THETA / 2), np.sin(THETA / 2)
+    rx = np.array([[c, -1j * s], [-1j * s, c]])
+    h = np.array([[1, 1], [1, -1]]) / np.sqrt(2)
+    O.apply_1q_inplace(state, 0, h)  # warm the pages and the thread pool
+    t0 = time.perf_counter()
+    for k in range(gates):
+        O.apply_1q_inplace(state, (k * 7) % n, rx if k % 2 else h)
+    dt = time.perf_counter() - t0
+    S = state.nbytes
+    return {"value": round(gates * 2 * S / dt / 1e9, 2), "unit": "GB/s", "cores": os.cpu_count(),
+            "kind": "port", "sample": "%d dense 1-qubit gates on a %d-qubit complex128 state (%.1f GiB)" % (
+                gates, n, S / 2**30)}
+
+
+def run_reference(args):
+    """CPU reference arm: the oracle port on all host threads, same metric."""
+    n = args.qubits
+    vals = []
+    for _ in range(args.warmup):
+        cpu_baseline_sample(n, gates=1)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        vals.append(cpu_baseline_sample(n, gates=2)["value"])
+    wall = time.perf_counter() - t0
+    v = statistics.median(vals)
+    line = {"metric": "gate HBM GB/s at 28q", "value": v, "unit": "GB/s", "impl": "reference", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * wall / max(1, args.steps), 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128 (f64)",
+            "data": "synthetic", "config": {"workload": "dense 1-qubit gates on a %d-qubit complex128 state" % n,
+                                            "qubits": n, "l2": "state larger than L2"},
+            "cpu_baseline": {"value": v, "unit": "GB/s", "cores": os.cpu_count(), "kind": "port",
+                             "sample": "2 dense 1-qubit gates per step on a %d-qubit complex128 state" % n},
+            "e2e": {"value": v, "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def run_ours(args):
+    import torch
+
+    import pennylane_lightning_gpu_gb300 as pkg
+
+    m = pkg.native()
+    n = args.qubits
+    S = (1 << n) * 16
+    gates = _gate_list(n)
+    sv = m.LightningGPU_C128(n)
+    sv.Hadamard([0], False, [])
+    torch.cuda.synchronize()
+
+    def step_device(events=None):
+        for i, (g, w) in enumerate(gates):
+            if events is not None:
+                events[i][0].record()
+            if g == "Hadamard":
+                sv.Hadamard([w], False, [])
+            else:
+                sv.RX([w], False, [THETA])
+            if events is not None:
+                events[i][1].record()
+
+    for _ in range(args.warmup):
+        step_device()
+    torch.cuda.synchronize()
+
+    # ---- device-timed steps (value) and per-launch events (roofline) ----
+    ev = [[(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in gates]
+          for _ in range(args.steps)]
+    clocks = ClockSampler()
+    clocks.start()
+    time.sleep(0.3)
+    torch.cuda.synchronize()
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    start.record()
+    for s in range(args.steps):
+        step_device(ev[s])
+    end.record()
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    total_ms = start.elapsed_time(end)
+    ms_per_step = total_ms / args.steps
+    bytes_per_step = len(gates) * 2 * S
+    value = bytes_per_step / (ms_per_step / 1e3) / 1e9
+    per_launch = np.array([[a.elapsed_time(b) for a, b in row] for row in ev])  # [steps, gates] ms
+    avg_launch_ms = float(per_launch.mean())
+    per_target = {}
+    for i, (g, w) in enumerate(gates):
+        per_target.setdefault(g, []).append(round(2 * S / (float(np.median(per_launch[:, i])) / 1e3) / 1e9, 1))
+
+    # ---- end to end: public API, host params, D2H result read every step ----
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        for g, w in gates:
+            if g == "Hadamard":
+                sv.Hadamard([w], False, [])
+            else:
+                sv.RX([w], False, [THETA])
+        p0 = sv.Probability([0])  # blocking D2H of the step's result
+    e2e_s = (time.perf_counter() - t0) / args.steps
+    e2e_value = (bytes_per_step + S) / e2e_s / 1e9  # + one read pass for the probability
+
+    peak, peak_kind = _peaks()
+    achieved = 2 * S / (avg_launch_ms / 1e3) / 1e9
+    line = {
+        "metric": "gate HBM GB/s at 28q", "value": round(value, 1), "unit": "GB/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_per_step, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "c128 (f64)", "data": "synthetic",
+        "config": {"workload": "dense 1-qubit gates (H and RX) on each target of a 28-qubit complex128 state",
+                   "qubits": n, "state_bytes": S, "gates_per_step": len(gates),
+                   "l2": "state (4 GiB) larger than L2 (129 MB): no flush needed"},
+        "e2e": {"value": round(e2e_value, 1), "unit": "GB/s", "h2d_bytes_per_step": 8 * n,
+                "d2h_bytes_per_step": 16},
+        "gpu_launches": len(gates) * args.steps,
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                     "frac": round(achieved / peak, 4), "traffic": None, "peak_source": peak_kind,
+                     "kernel": "gate1_kernel", "algorithmic_bytes_per_launch": 2 * S},
+        "per_target_gbs": per_target,
+        "clocks": clk,
+    }
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline_sample(n, gates=args.cpu_gates)
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--qubits", type=int, default=N_QUBITS)
+    ap.add_argument("--cpu-gates", type=int, default=4)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", "0"))
+    if args.impl == "reference":
+        if rank == 0:
+            run_reference(args)
+        return
+    run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

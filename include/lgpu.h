@@ -1,0 +1,241 @@
+/*
+ * lgpu.h — the C ABI of the GB300 statevector engine (liblgpu_gb300.so).
+ *
+ * Every entry point is plain C: device pointers, sizes, host arrays and a
+ * CUDA stream.  No C++ or torch types cross this boundary.  The C++ drop-in
+ * classes (StateVectorCudaManaged<T>, AdjointJacobianGPU<T>, the observable
+ * family) are the intended callers; they replace the closed-library calls of
+ * the reference PennyLane-Lightning-GPU 0.33 at the file:line cited beside
+ * each function.
+ *
+ * Conventions
+ *   - A state is 2^n contiguous amplitudes, interleaved (re, im):
+ *     LGPU_C64 = float2 (8 B), LGPU_C128 = double2 (16 B).
+ *   - Qubits are addressed by STATE-INDEX BIT positions (0 = least
+ *     significant).  PennyLane wire w of an n-qubit state is bit n-1-w; the
+ *     C++ layer performs that mapping.
+ *   - Matrices are row-major 2^t x 2^t complex128 (interleaved doubles);
+ *     matrix row/column index bit (t-1-k) corresponds to tgts[k] (the first
+ *     target is the most significant matrix bit).
+ *   - Controls: bits that must equal ctrl_vals[k] (NULL = all ones).
+ *   - Results of reductions are written to `out`; when out_on_device is 0
+ *     the call synchronises the stream and `out` is host memory, otherwise
+ *     `out` is device memory and the call is asynchronous.
+ *   - The library never frees caller memory.  Scratch memory for reductions
+ *     and sampling comes from an lgpu_context_t owned by the caller; a context
+ *     must not be used from two streams at the same time.
+ *   - Every function returns an lgpu_status_t; lgpu_last_error_string()
+ *     holds the message of the last failure on the calling thread.
+ */
+#ifndef LGPU_H
+#define LGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct CUstream_st *lgpu_stream_t; /* identical to cudaStream_t */
+
+typedef enum {
+    LGPU_OK = 0,
+    LGPU_ERR_INVALID_ARG = 1,
+    LGPU_ERR_OOM = 2,
+    LGPU_ERR_CUDA = 3,
+    LGPU_ERR_TIMEOUT = 4,
+    LGPU_ERR_UNSUPPORTED = 5,
+    LGPU_ERR_NO_DEVICE = 6
+} lgpu_status_t;
+
+typedef enum { LGPU_C64 = 0, LGPU_C128 = 1 } lgpu_dtype_t;
+
+typedef enum { LGPU_H2D = 0, LGPU_D2H = 1, LGPU_D2D = 2 } lgpu_copy_kind_t;
+
+#define LGPU_MAX_QUBITS 34
+#define LGPU_MAX_DENSE_TARGETS 12
+#define LGPU_MAX_CONTROLS 16
+
+typedef struct lgpu_context_s *lgpu_context_t;
+
+/* ---- library / errors ------------------------------------------------ */
+int lgpu_abi_version(void);
+const char *lgpu_last_error_string(void);
+
+/* ---- device and memory (DataBuffer.hpp:31-218, cuda_helpers.hpp:796-837,
+ *      Bindings.cpp:1736-1748; the C++ layer needs no CUDA runtime of its own) */
+lgpu_status_t lgpu_device_count(int *count);
+lgpu_status_t lgpu_get_device(int *device);
+lgpu_status_t lgpu_set_device(int device);
+lgpu_status_t lgpu_device_arch(int device, int *major, int *minor);
+lgpu_status_t lgpu_device_sm_count(int device, int *sms);
+lgpu_status_t lgpu_device_reset(void);
+lgpu_status_t lgpu_mem_info(size_t *free_bytes, size_t *total_bytes);
+lgpu_status_t lgpu_malloc(void **ptr, size_t bytes);
+lgpu_status_t lgpu_free(void *ptr);
+lgpu_status_t lgpu_host_alloc_pinned(void **ptr, size_t bytes);
+lgpu_status_t lgpu_host_free_pinned(void *ptr);
+lgpu_status_t lgpu_memcpy(void *dst, const void *src, size_t bytes, lgpu_copy_kind_t kind,
+                          int async, lgpu_stream_t stream);
+lgpu_status_t lgpu_memset(void *dst, int value, size_t bytes, lgpu_stream_t stream);
+lgpu_status_t lgpu_stream_create(lgpu_stream_t *stream);
+lgpu_status_t lgpu_stream_destroy(lgpu_stream_t stream);
+lgpu_status_t lgpu_stream_sync(lgpu_stream_t stream);
+lgpu_status_t lgpu_peer_access_all(void);
+
+/* ---- scratch context -------------------------------------------------- */
+lgpu_status_t lgpu_context_create(int device, lgpu_context_t *ctx);
+lgpu_status_t lgpu_context_destroy(lgpu_context_t ctx);
+/* Grow the context's scratch to at least `bytes` now (optional; reductions
+ * grow it on first use). */
+lgpu_status_t lgpu_context_reserve(lgpu_context_t ctx, size_t bytes);
+
+/* ---- state preparation (initSV.cu:64-117; StateVectorCudaManaged.hpp:144-185;
+ *      StateVectorCudaBase.hpp:234-240) */
+/* sv = 0 everywhere except sv[index] = (re, im). */
+lgpu_status_t lgpu_set_basis(void *sv, uint32_t n, lgpu_dtype_t dt, uint64_t index, double re,
+                             double im, lgpu_stream_t stream);
+/* Optionally zero sv, then sv[indices[i]] = values[i] (device arrays;
+ * values of the state's dtype). */
+lgpu_status_t lgpu_scatter(void *sv, uint32_t n, lgpu_dtype_t dt, const void *values,
+                           const int64_t *indices, uint64_t count, int zero_first,
+                           lgpu_stream_t stream);
+
+/* ---- gates -------------------------------------------------------------- */
+/* Dense controlled 2^t x 2^t matrix from HOST memory, t <= 12
+ * (custatevecApplyMatrix at StateVectorCudaManaged.hpp:1433-1471, 1517-1555).
+ * 1-target matrices are classified on the host (phase-only, diagonal,
+ * permutation, real, RX-like, dense) and run the cheapest kernel body. */
+lgpu_status_t lgpu_apply_matrix(void *sv, uint32_t n, lgpu_dtype_t dt, const double *matrix,
+                                uint32_t t, const int32_t *tgts, uint32_t c, const int32_t *ctrls,
+                                const int32_t *ctrl_vals, int adjoint, lgpu_stream_t stream);
+
+/* The same gate applied to `nstates` states of equal size in one launch
+ * (the adjoint sweep's bra updates, AdjointDiffGPU.hpp:279-319). */
+lgpu_status_t lgpu_apply_matrix_multi(void *const *svs, uint32_t nstates, uint32_t n,
+                                      lgpu_dtype_t dt, const double *matrix, uint32_t t,
+                                      const int32_t *tgts, uint32_t c, const int32_t *ctrls,
+                                      const int32_t *ctrl_vals, int adjoint,
+                                      lgpu_stream_t stream);
+
+/* exp(i * angle * P) for the Pauli word `paulis` (chars I,X,Y,Z) on tgts,
+ * under controls (custatevecApplyPauliRotation at
+ * StateVectorCudaManaged.hpp:1374-1385; the reference passes angle = -param/2,
+ * or +param/2 for the adjoint). */
+lgpu_status_t lgpu_apply_pauli_rotation(void *sv, uint32_t n, lgpu_dtype_t dt, double angle,
+                                        uint32_t t, const int32_t *tgts, const char *paulis,
+                                        uint32_t c, const int32_t *ctrls,
+                                        const int32_t *ctrl_vals, lgpu_stream_t stream);
+
+lgpu_status_t lgpu_apply_pauli_rotation_multi(void *const *svs, uint32_t nstates, uint32_t n,
+                                              lgpu_dtype_t dt, double angle, uint32_t t,
+                                              const int32_t *tgts, const char *paulis, uint32_t c,
+                                              const int32_t *ctrls, const int32_t *ctrl_vals,
+                                              lgpu_stream_t stream);
+
+/* ---- fused gate blocks (shared-memory tiles) -------------------------------
+ * A block is a list of 1- and 2-target gates (controls allowed) whose target
+ * bits all lie in the tile bit set.  One launch streams the state once:
+ * each CTA loads a tile of 2^k amplitudes (the tile bits vary, every other bit
+ * is fixed), applies all gates in order in shared memory and stores the tile.
+ * Gate record layout (lgpu_fused_gate_t): see below. */
+typedef struct {
+    int32_t ntgt;      /* 1 or 2 */
+    int32_t tgt[2];    /* state bits; tgt[0] = most significant matrix bit */
+    int32_t nctrl;     /* 0..4 */
+    int32_t ctrl[4];   /* state bits */
+    int32_t ctrl_val[4];
+    double m[32];      /* row-major 2^ntgt x 2^ntgt complex (interleaved) */
+} lgpu_fused_gate_t;
+
+/* tile_bits: k distinct state bits (k <= 13 for C64, <= 12 for C128); gates
+ * must target only tile bits (controls may be anywhere). */
+lgpu_status_t lgpu_apply_fused_block(void *sv, uint32_t n, lgpu_dtype_t dt, uint32_t k,
+                                     const int32_t *tile_bits, uint32_t ngates,
+                                     const lgpu_fused_gate_t *gates, lgpu_stream_t stream);
+
+/* ---- measurements ----------------------------------------------------------- */
+/* <sv|M|sv> for a dense 2^t x 2^t host matrix on tgts, t <= 10; out = (re, im)
+ * (custatevecComputeExpectation at StateVectorCudaManaged.hpp:1602-1639, 1674-1712). */
+lgpu_status_t lgpu_expval_matrix(lgpu_context_t ctx, const void *sv, uint32_t n, lgpu_dtype_t dt,
+                                 const double *matrix, uint32_t t, const int32_t *tgts,
+                                 double *out, int out_on_device, lgpu_stream_t stream);
+
+/* <P_j> for nwords Pauli words given as bit masks: flip = X|Y bits,
+ * sign = Y|Z bits, ny = number of Y letters (custatevecComputeExpectationsOnPauliBasis
+ * at StateVectorCudaManaged.hpp:1117-1128).  Words with equal flip masks are
+ * evaluated in one pass.  out[j] = Re <P_j> (the imaginary part vanishes for a
+ * normalised state); FP64 accumulation for both dtypes. */
+lgpu_status_t lgpu_expval_pauli_words(lgpu_context_t ctx, const void *sv, uint32_t n,
+                                      lgpu_dtype_t dt, uint32_t nwords, const uint64_t *flip,
+                                      const uint64_t *sign, const uint8_t *ny, double *out,
+                                      int out_on_device, lgpu_stream_t stream);
+
+/* Marginal probabilities: out[idx] sums |sv_i|^2 over i whose bit bits[q]
+ * equals bit q of idx (custatevecAbs2SumArray at StateVectorCudaManaged.hpp:957-967).
+ * k <= 24. */
+lgpu_status_t lgpu_probs(lgpu_context_t ctx, const void *sv, uint32_t n, lgpu_dtype_t dt,
+                         uint32_t k, const int32_t *bits, double *out, int out_on_device,
+                         lgpu_stream_t stream);
+
+/* Inverse-CDF sampling (custatevecSampler* at StateVectorCudaManaged.hpp:1015-1035):
+ * for each draw r in [0,1) return the smallest index i with
+ * cdf_i > r * sum|sv|^2 (FP64 prefix sums); a draw past the end selects the last
+ * index of non-zero probability.  draws and out_idx are HOST arrays; out_idx
+ * is in draw order (the caller sorts for the reference's ascending order). */
+lgpu_status_t lgpu_sample(lgpu_context_t ctx, const void *sv, uint32_t n, lgpu_dtype_t dt,
+                          const double *draws, uint64_t shots, uint64_t *out_idx,
+                          lgpu_stream_t stream);
+
+/* <a|b> = sum conj(a_i) b_i, FP64 accumulation (cublasZdotc/Cdotc at
+ * cuda_helpers.hpp:456-497); out = (re, im). */
+lgpu_status_t lgpu_dot(lgpu_context_t ctx, const void *a, const void *b, uint32_t n,
+                       lgpu_dtype_t dt, double *out, int out_on_device, lgpu_stream_t stream);
+
+/* y += alpha * x (cublasZaxpy/Caxpy at cuda_helpers.hpp:512-528). */
+lgpu_status_t lgpu_axpy(double alpha_re, double alpha_im, const void *x, void *y, uint32_t n,
+                        lgpu_dtype_t dt, lgpu_stream_t stream);
+/* x *= alpha (cublasScalEx at cuda_helpers.hpp:544-560). */
+lgpu_status_t lgpu_scale(double alpha_re, double alpha_im, void *x, uint32_t n, lgpu_dtype_t dt,
+                         lgpu_stream_t stream);
+/* dst = src over 2^n amplitudes (StateVectorCudaBase.hpp:104-219 D2D copies). */
+lgpu_status_t lgpu_copy(void *dst, const void *src, uint32_t n, lgpu_dtype_t dt,
+                        lgpu_stream_t stream);
+
+/* out = sum_t coeff_t * P_t |in> for Pauli words (flip/sign/ny masks as in
+ * lgpu_expval_pauli_words), one pass per distinct flip mask
+ * (HamiltonianGPU::applyInPlace at ObservablesGPU.hpp:346-362). `in` and `out`
+ * must not alias. */
+lgpu_status_t lgpu_apply_pauli_sum(const void *in, void *out, uint32_t n, lgpu_dtype_t dt,
+                                   uint32_t nterms, const double *coeffs /* complex, interleaved */,
+                                   const uint64_t *flip, const uint64_t *sign, const uint8_t *ny,
+                                   lgpu_stream_t stream);
+
+/* CSR sparse matrix (2^n rows; int64 offsets/columns; values of the state
+ * dtype; all device arrays).  y = H x (cusparseSpMV at ObservablesGPU.hpp:516-586)
+ * and <x|H|x> (StateVectorCudaManaged.hpp:795-922). */
+lgpu_status_t lgpu_spmv_csr(const int64_t *offsets, const int64_t *cols, const void *vals,
+                            const void *x, void *y, uint32_t n, lgpu_dtype_t dt,
+                            lgpu_stream_t stream);
+lgpu_status_t lgpu_expval_csr(lgpu_context_t ctx, const int64_t *offsets, const int64_t *cols,
+                              const void *vals, const void *x, uint32_t n, lgpu_dtype_t dt,
+                              double *out, int out_on_device, lgpu_stream_t stream);
+
+/* ---- adjoint sweep (AdjointDiffGPU.hpp:499-596) --------------------------------
+ * One fused pass of the reverse sweep for one operation:
+ *   out[k] = Im <bras[k]| G |ket>        (k < nbras; before the update)
+ * then, if apply_udag != 0,  ket <- U^dag ket  and  bras[k] <- U^dag bras[k].
+ * G and U are dense host matrices on the same bit set `bits` (w <= 4 bits,
+ * bits[0] = most significant matrix bit); G may be NULL (no expectation).
+ * `out` is a device array of nbras doubles (accumulated with '=' semantics). */
+lgpu_status_t lgpu_adjoint_step(lgpu_context_t ctx, void *ket, void *const *bras, uint32_t nbras,
+                                uint32_t n, lgpu_dtype_t dt, uint32_t w, const int32_t *bits,
+                                const double *gen, const double *udag, int apply_udag,
+                                double *out_dev, lgpu_stream_t stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* LGPU_H */

@@ -1,0 +1,843 @@
+// liblgpu_gb300: gate application.
+//
+//  * gate1_kernel     one target bit, streaming pairs (i, i | 1<<t) with
+//                     128-bit loads per amplitude (c128) and several pairs in
+//                     flight per thread; the body is chosen on the host from
+//                     the matrix structure so that FP64 work is minimal.
+//  * phase_kernel     multiply the amplitudes whose bits match a mask by one
+//                     phase (PhaseShift, S, T, Z, CZ, controlled phases):
+//                     only the touched half/quarter of the state is streamed.
+//  * gatek_kernel     dense 2^t x 2^t (t = 2..5) with the matrix in the
+//                     kernel-parameter bank (uniform broadcast reads).
+//  * gatebig_kernel   dense t = 6..12, matrix in global memory, groups staged
+//                     in shared memory.
+//  * pauli_rot_kernel exp(i angle P) for Pauli words, pairwise (i, i^flip).
+//  * fused_kernel     a block of 1/2-target gates applied to shared-memory
+//                     tiles of 2^k amplitudes: one HBM pass for many gates.
+#include "lgpu_internal.cuh"
+
+namespace lgpu {
+
+constexpr int kGateBlock = 256;
+
+enum Body1 : int { B_DENSE = 0, B_DIAG = 1, B_PERM = 2, B_ANTIDIAG = 3, B_REAL = 4, B_RXLIKE = 5 };
+
+template <class T, class I> struct G1Params {
+    Holes holes;
+    I tbit;
+    I cset;
+    I ngroups;
+    T m[8];
+};
+
+template <class T, int BODY>
+__device__ __forceinline__ void body1(const T *m, cplx_t<T> &a0, cplx_t<T> &a1) {
+    using C = cplx_t<T>;
+    const C x = a0, y = a1;
+    if constexpr (BODY == B_PERM) {
+        a0 = y;
+        a1 = x;
+    } else if constexpr (BODY == B_DIAG) {
+        a0 = mk<T>(fmaT(m[0], x.x, -m[1] * x.y), fmaT(m[0], x.y, m[1] * x.x));
+        a1 = mk<T>(fmaT(m[6], y.x, -m[7] * y.y), fmaT(m[6], y.y, m[7] * y.x));
+    } else if constexpr (BODY == B_ANTIDIAG) {
+        a0 = mk<T>(fmaT(m[2], y.x, -m[3] * y.y), fmaT(m[2], y.y, m[3] * y.x));
+        a1 = mk<T>(fmaT(m[4], x.x, -m[5] * x.y), fmaT(m[4], x.y, m[5] * x.x));
+    } else if constexpr (BODY == B_REAL) {
+        a0 = mk<T>(fmaT(m[0], x.x, m[2] * y.x), fmaT(m[0], x.y, m[2] * y.y));
+        a1 = mk<T>(fmaT(m[4], x.x, m[6] * y.x), fmaT(m[4], x.y, m[6] * y.y));
+    } else if constexpr (BODY == B_RXLIKE) {
+        // m00 = m11 = c (real), m01 = i*u, m10 = i*v (u, v real)
+        const T c = m[0], u = m[3], v = m[5];
+        a0 = mk<T>(fmaT(c, x.x, -u * y.y), fmaT(c, x.y, u * y.x));
+        a1 = mk<T>(fmaT(c, y.x, -v * x.y), fmaT(c, y.y, v * x.x));
+    } else {
+        C r0 = mk<T>(m[0] * x.x, m[0] * x.y);
+        r0.x = fmaT(-m[1], x.y, r0.x);
+        r0.y = fmaT(m[1], x.x, r0.y);
+        r0.x = fmaT(m[2], y.x, r0.x);
+        r0.y = fmaT(m[2], y.y, r0.y);
+        r0.x = fmaT(-m[3], y.y, r0.x);
+        r0.y = fmaT(m[3], y.x, r0.y);
+        C r1 = mk<T>(m[4] * x.x, m[4] * x.y);
+        r1.x = fmaT(-m[5], x.y, r1.x);
+        r1.y = fmaT(m[5], x.x, r1.y);
+        r1.x = fmaT(m[6], y.x, r1.x);
+        r1.y = fmaT(m[6], y.y, r1.y);
+        r1.x = fmaT(-m[7], y.y, r1.x);
+        r1.y = fmaT(m[7], y.x, r1.y);
+        a0 = r0;
+        a1 = r1;
+    }
+}
+
+// ITEMS pairs per thread in flight: all loads are issued before any math.
+template <class T, class I, int BODY, int ITEMS>
+__global__ void __launch_bounds__(kGateBlock)
+    gate1_kernel(cplx_t<T> *__restrict__ sv, const G1Params<T, I> p, const unsigned nstates,
+                 cplx_t<T> *const *__restrict__ svs) {
+    using C = cplx_t<T>;
+    C *s = nstates ? svs[blockIdx.y] : sv;
+    T m[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++) m[k] = p.m[k];
+    const I stride = I(gridDim.x) * kGateBlock;
+    for (I g = I(blockIdx.x) * kGateBlock + threadIdx.x; g < p.ngroups; g += stride * ITEMS) {
+        C a0[ITEMS], a1[ITEMS];
+        I i0[ITEMS];
+#pragma unroll
+        for (int k = 0; k < ITEMS; k++) {
+            const I gk = g + I(k) * stride;
+            i0[k] = (gk < p.ngroups) ? (insert_holes<I>(gk, p.holes) | p.cset) : I(0);
+        }
+#pragma unroll
+        for (int k = 0; k < ITEMS; k++) {
+            if (g + I(k) * stride < p.ngroups) {
+                a0[k] = __ldcs(&s[i0[k]]);
+                a1[k] = __ldcs(&s[i0[k] | p.tbit]);
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < ITEMS; k++) body1<T, BODY>(m, a0[k], a1[k]);
+#pragma unroll
+        for (int k = 0; k < ITEMS; k++) {
+            if (g + I(k) * stride < p.ngroups) {
+                __stcs(&s[i0[k]], a0[k]);
+                __stcs(&s[i0[k] | p.tbit], a1[k]);
+            }
+        }
+    }
+}
+
+template <class T, class I> struct PhaseParams {
+    Holes holes;
+    I set;  // bits forced to 1
+    I ngroups;
+    T re, im;
+};
+
+template <class T, class I, bool NEG, int ITEMS>
+__global__ void __launch_bounds__(kGateBlock)
+    phase_kernel(cplx_t<T> *__restrict__ sv, const PhaseParams<T, I> p, const unsigned nstates,
+                 cplx_t<T> *const *__restrict__ svs) {
+    using C = cplx_t<T>;
+    C *s = nstates ? svs[blockIdx.y] : sv;
+    const I stride = I(gridDim.x) * kGateBlock;
+    for (I g = I(blockIdx.x) * kGateBlock + threadIdx.x; g < p.ngroups; g += stride * ITEMS) {
+        C a[ITEMS];
+        I idx[ITEMS];
+#pragma unroll
+        for (int k = 0; k < ITEMS; k++) {
+            const I gk = g + I(k) * stride;
+            idx[k] = (gk < p.ngroups) ? (insert_holes<I>(gk, p.holes) | p.set) : I(0);
+            if (gk < p.ngroups) a[k] = __ldcs(&s[idx[k]]);
+        }
+#pragma unroll
+        for (int k = 0; k < ITEMS; k++) {
+            const C x = a[k];
+            if constexpr (NEG)
+                a[k] = mk<T>(-x.x, -x.y);
+            else
+                a[k] = mk<T>(fmaT(p.re, x.x, -p.im * x.y), fmaT(p.re, x.y, p.im * x.x));
+        }
+#pragma unroll
+        for (int k = 0; k < ITEMS; k++)
+            if (g + I(k) * stride < p.ngroups) __stcs(&s[idx[k]], a[k]);
+    }
+}
+
+// Dense t-target gate, matrix in the parameter bank.
+template <class T, class I, int TT> struct GkParams {
+    Holes holes;
+    I cset;
+    I ngroups;
+    I off[1 << TT];
+    double m[2 * (1 << TT) * (1 << TT)];
+};
+
+template <class T, class I, int TT>
+__global__ void __launch_bounds__(TT >= 4 ? 128 : kGateBlock)
+    gatek_kernel(cplx_t<T> *__restrict__ sv, const GkParams<T, I, TT> p, const unsigned nstates,
+                 cplx_t<T> *const *__restrict__ svs) {
+    using C = cplx_t<T>;
+    constexpr int D = 1 << TT;
+    C *s = nstates ? svs[blockIdx.y] : sv;
+    const I stride = I(gridDim.x) * blockDim.x;
+    for (I g = I(blockIdx.x) * blockDim.x + threadIdx.x; g < p.ngroups; g += stride) {
+        const I base = insert_holes<I>(g, p.holes) | p.cset;
+        C a[D];
+#pragma unroll
+        for (int c = 0; c < D; c++) a[c] = s[base | p.off[c]];
+#pragma unroll 1
+        for (int r = 0; r < D; r++) {
+            T xr = 0, xi = 0;
+#pragma unroll
+            for (int c = 0; c < D; c++) {
+                const T mr = T(p.m[2 * (r * D + c)]), mi = T(p.m[2 * (r * D + c) + 1]);
+                xr = fmaT(mr, a[c].x, xr);
+                xr = fmaT(-mi, a[c].y, xr);
+                xi = fmaT(mr, a[c].y, xi);
+                xi = fmaT(mi, a[c].x, xi);
+            }
+            s[base | p.off[r]] = mk<T>(xr, xi);
+        }
+    }
+}
+
+// Dense t-target gate, t = 6..12, matrix (state dtype) in global memory.
+// Each CTA stages GPB groups of D amplitudes in shared memory; thread j of the
+// CTA produces rows j, j+blockDim, ... of every staged group.
+template <class T, class I> struct GbigParams {
+    Holes holes;
+    I cset;
+    I ngroups;
+    int t;
+    const I *off;          // D offsets (device)
+    const cplx_t<T> *mat;  // D x D row-major (device)
+};
+
+template <class T, class I>
+__global__ void __launch_bounds__(256) gatebig_kernel(cplx_t<T> *__restrict__ sv, const GbigParams<T, I> p) {
+    using C = cplx_t<T>;
+    extern __shared__ unsigned char smem_raw[];
+    C *tile = reinterpret_cast<C *>(smem_raw);
+    const int D = 1 << p.t;
+    for (I g = blockIdx.x; g < p.ngroups; g += gridDim.x) {
+        const I base = insert_holes<I>(g, p.holes) | p.cset;
+        __syncthreads();
+        for (int c = threadIdx.x; c < D; c += blockDim.x) tile[c] = sv[base | p.off[c]];
+        __syncthreads();
+        for (int r = threadIdx.x; r < D; r += blockDim.x) {
+            double xr = 0, xi = 0;
+            const C *row = p.mat + size_t(r) * D;
+            for (int c = 0; c < D; c++) {
+                const C mv = row[c];
+                const C av = tile[c];
+                xr = fma(double(mv.x), double(av.x), fma(-double(mv.y), double(av.y), xr));
+                xi = fma(double(mv.x), double(av.y), fma(double(mv.y), double(av.x), xi));
+            }
+            sv[base | p.off[r]] = mk<T>(T(xr), T(xi));
+        }
+    }
+}
+
+// exp(i angle P): pairs (i, j = i ^ flip) with i's lowest flip bit clear.
+template <class T, class I> struct PRParams {
+    Holes holes;
+    I cset;
+    I ngroups;
+    I flip;
+    I sgn;
+    T c, s;     // cos(angle), sin(angle)
+    T qr, qi;   // q = s * i^(ny+1)
+};
+
+template <class T, class I>
+__global__ void __launch_bounds__(kGateBlock)
+    pauli_rot_kernel(cplx_t<T> *__restrict__ sv, const PRParams<T, I> p, const unsigned nstates,
+                     cplx_t<T> *const *__restrict__ svs) {
+    using C = cplx_t<T>;
+    C *s = nstates ? svs[blockIdx.y] : sv;
+    const I stride = I(gridDim.x) * kGateBlock;
+    for (I g = I(blockIdx.x) * kGateBlock + threadIdx.x; g < p.ngroups; g += stride) {
+        const I i = insert_holes<I>(g, p.holes) | p.cset;
+        if (p.flip == 0) {
+            const C a = s[i];
+            const T sg = (__popcll(uint64_t(i & p.sgn)) & 1) ? T(-1) : T(1);
+            const T si = p.s * sg;  // (c + i s sg) a
+            s[i] = mk<T>(fmaT(p.c, a.x, -si * a.y), fmaT(p.c, a.y, si * a.x));
+        } else {
+            const I j = i ^ p.flip;
+            const C a = s[i], b = s[j];
+            const T sj = (__popcll(uint64_t(j & p.sgn)) & 1) ? T(-1) : T(1);
+            const T si = (__popcll(uint64_t(i & p.sgn)) & 1) ? T(-1) : T(1);
+            // out_i = c a + sj q b ; out_j = c b + si q a
+            const T qbr = sj * (p.qr * b.x - p.qi * b.y), qbi = sj * (p.qr * b.y + p.qi * b.x);
+            const T qar = si * (p.qr * a.x - p.qi * a.y), qai = si * (p.qr * a.y + p.qi * a.x);
+            s[i] = mk<T>(fmaT(p.c, a.x, qbr), fmaT(p.c, a.y, qbi));
+            s[j] = mk<T>(fmaT(p.c, b.x, qar), fmaT(p.c, b.y, qai));
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Fused shared-memory tiles
+// ---------------------------------------------------------------------------
+constexpr int kFusedMaxGates = 96;
+constexpr int kFusedMatPool = 3072;  // doubles
+constexpr int kFusedBlock = 512;
+
+struct FGate {
+    uint8_t ntgt, q0, q1, pad;
+    uint32_t in_mask, in_val;  // controls inside the tile (tile positions)
+    uint32_t mat_off;          // into the matrix pool (doubles)
+    uint64_t out_mask, out_val;  // controls outside the tile (state bits)
+};
+
+template <class I> struct FusedParams {
+    Holes holes;       // tile bits (sorted) as holes: tile base = insert(tau)
+    I ntiles;
+    int k;             // tile bits
+    int m;             // low bits 0..m-1 are the lowest tile bits (contiguous runs)
+    I hi_off[64];      // offsets of the high tile bits (k - m <= 6 -> 64 entries)
+    int ngates;
+    FGate gates[kFusedMaxGates];
+    double mats[kFusedMatPool];
+};
+
+static_assert(sizeof(FusedParams<uint64_t>) <= 32000, "fused kernel parameters exceed the 32 KB limit");
+
+template <class T, class I>
+__global__ void __launch_bounds__(kFusedBlock) fused_kernel(cplx_t<T> *__restrict__ sv, const FusedParams<I> p) {
+    using C = cplx_t<T>;
+    extern __shared__ unsigned char smem_raw[];
+    C *tile = reinterpret_cast<C *>(smem_raw);
+    const int E = 1 << p.k;
+    const int lowmask = (1 << p.m) - 1;
+    for (I tau = blockIdx.x; tau < p.ntiles; tau += gridDim.x) {
+        const I base = insert_holes<I>(tau, p.holes);
+        __syncthreads();
+        for (int e = threadIdx.x; e < E; e += kFusedBlock)
+            tile[e] = __ldcs(&sv[base + p.hi_off[e >> p.m] + I(e & lowmask)]);
+        __syncthreads();
+        for (int gi = 0; gi < p.ngates; gi++) {
+            const FGate &g = p.gates[gi];
+            if ((uint64_t(base) & g.out_mask) != g.out_val) continue;  // tile-uniform
+            const double *mm = p.mats + g.mat_off;
+            if (g.ntgt == 1) {
+                const T m0r = T(mm[0]), m0i = T(mm[1]), m1r = T(mm[2]), m1i = T(mm[3]);
+                const T m2r = T(mm[4]), m2i = T(mm[5]), m3r = T(mm[6]), m3i = T(mm[7]);
+                const int q = g.q0;
+                const int lo = (1 << q) - 1;
+                for (int pr = threadIdx.x; pr < (E >> 1); pr += kFusedBlock) {
+                    const int e0 = ((pr & ~lo) << 1) | (pr & lo);
+                    if ((uint32_t(e0) & g.in_mask) != g.in_val) continue;
+                    const int e1 = e0 | (1 << q);
+                    const C x = tile[e0], y = tile[e1];
+                    C r0, r1;
+                    r0.x = m0r * x.x - m0i * x.y + m1r * y.x - m1i * y.y;
+                    r0.y = m0r * x.y + m0i * x.x + m1r * y.y + m1i * y.x;
+                    r1.x = m2r * x.x - m2i * x.y + m3r * y.x - m3i * y.y;
+                    r1.y = m2r * x.y + m2i * x.x + m3r * y.y + m3i * y.x;
+                    tile[e0] = r0;
+                    tile[e1] = r1;
+                }
+            } else {
+                const int qa = g.q0, qb = g.q1;  // qa = most significant matrix bit
+                const int lo_b = min(qa, qb), hi_b = max(qa, qb);
+                const int lm1 = (1 << lo_b) - 1;
+                for (int pr = threadIdx.x; pr < (E >> 2); pr += kFusedBlock) {
+                    int e = ((pr & ~lm1) << 1) | (pr & lm1);
+                    const int lm2 = (1 << hi_b) - 1;
+                    e = ((e & ~lm2) << 1) | (e & lm2);
+                    if ((uint32_t(e) & g.in_mask) != g.in_val) continue;
+                    int idx[4];
+                    idx[0] = e;
+                    idx[1] = e | (1 << qb);
+                    idx[2] = e | (1 << qa);
+                    idx[3] = e | (1 << qa) | (1 << qb);
+                    C a[4];
+#pragma unroll
+                    for (int c = 0; c < 4; c++) a[c] = tile[idx[c]];
+#pragma unroll
+                    for (int r = 0; r < 4; r++) {
+                        T xr = 0, xi = 0;
+#pragma unroll
+                        for (int c = 0; c < 4; c++) {
+                            const T mr = T(mm[2 * (r * 4 + c)]), mi = T(mm[2 * (r * 4 + c) + 1]);
+                            xr += mr * a[c].x - mi * a[c].y;
+                            xi += mr * a[c].y + mi * a[c].x;
+                        }
+                        tile[idx[r]] = mk<T>(xr, xi);
+                    }
+                }
+            }
+            __syncthreads();
+        }
+        for (int e = threadIdx.x; e < E; e += kFusedBlock)
+            __stcs(&sv[base + p.hi_off[e >> p.m] + I(e & lowmask)], tile[e]);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Host side
+// ---------------------------------------------------------------------------
+struct Cm {
+    double re, im;
+};
+static inline bool eq(Cm a, double re, double im) { return a.re == re && a.im == im; }
+
+struct GateGeometry {
+    std::vector<int> tgts, ctrls, cvals;
+    uint64_t cset = 0;
+};
+
+static lgpu_status_t geometry(uint32_t n, uint32_t t, const int32_t *tgts, uint32_t c,
+                              const int32_t *ctrls, const int32_t *ctrl_vals, GateGeometry *g) {
+    if (t < 1 || t > LGPU_MAX_DENSE_TARGETS)
+        return fail(LGPU_ERR_INVALID_ARG, "number of targets must be in [1, 12]");
+    if (c > LGPU_MAX_CONTROLS) return fail(LGPU_ERR_INVALID_ARG, "too many controls");
+    LGPU_TRY(check_bits(n, t, tgts, "target", &g->tgts));
+    LGPU_TRY(check_bits(n, c, ctrls, "control", &g->ctrls));
+    std::vector<int> all(g->tgts);
+    all.insert(all.end(), g->ctrls.begin(), g->ctrls.end());
+    std::vector<int> srt(all);
+    std::sort(srt.begin(), srt.end());
+    if (std::adjacent_find(srt.begin(), srt.end()) != srt.end())
+        return fail(LGPU_ERR_INVALID_ARG, "target and control bits must be distinct");
+    if (all.size() > n) return fail(LGPU_ERR_INVALID_ARG, "more wires than qubits");
+    for (uint32_t k = 0; k < c; k++) {
+        const int v = ctrl_vals ? ctrl_vals[k] : 1;
+        if (v != 0 && v != 1) return fail(LGPU_ERR_INVALID_ARG, "control values must be 0 or 1");
+        g->cvals.push_back(v);
+        if (v) g->cset |= uint64_t(1) << g->ctrls[k];
+    }
+    return LGPU_OK;
+}
+
+template <class T, class I, int BODY>
+static void launch_gate1(cplx_t<T> *sv, const G1Params<T, I> &p, unsigned nstates,
+                         cplx_t<T> *const *svs, cudaStream_t s) {
+    constexpr int ITEMS = sizeof(T) == 8 ? 2 : 4;
+    const unsigned gx = grid_for(uint64_t(p.ngroups), kGateBlock, ITEMS, 8);
+    dim3 grid(gx, nstates ? nstates : 1);
+    gate1_kernel<T, I, BODY, ITEMS><<<grid, kGateBlock, 0, s>>>(sv, p, nstates, svs);
+}
+
+template <class T, class I>
+static lgpu_status_t run_gate1(cplx_t<T> *sv, unsigned nstates, cplx_t<T> *const *svs, uint32_t n,
+                               const Cm m[4], const GateGeometry &g, cudaStream_t s) {
+    const int tb = g.tgts[0];
+    // Phase-only gates touch the amplitudes of one target value only.
+    const bool diag = eq(m[1], 0, 0) && eq(m[2], 0, 0);
+    if (diag && (eq(m[0], 1, 0) || eq(m[3], 1, 0))) {
+        const bool on_one = eq(m[0], 1, 0);
+        const Cm ph = on_one ? m[3] : m[0];
+        if (eq(ph, 1, 0)) return LGPU_OK;  // identity
+        std::vector<int> holes(g.ctrls);
+        holes.push_back(tb);
+        PhaseParams<T, I> p{};
+        p.holes = make_holes(holes);
+        p.set = I(g.cset | (on_one ? (uint64_t(1) << tb) : 0));
+        p.ngroups = I(uint64_t(1) << (n - holes.size()));
+        p.re = T(ph.re);
+        p.im = T(ph.im);
+        constexpr int ITEMS = sizeof(T) == 8 ? 2 : 4;
+        dim3 grid(grid_for(uint64_t(p.ngroups), kGateBlock, ITEMS, 8), nstates ? nstates : 1);
+        if (eq(ph, -1, 0))
+            phase_kernel<T, I, true, ITEMS><<<grid, kGateBlock, 0, s>>>(sv, p, nstates, svs);
+        else
+            phase_kernel<T, I, false, ITEMS><<<grid, kGateBlock, 0, s>>>(sv, p, nstates, svs);
+        LGPU_CHECK_LAUNCH();
+        return LGPU_OK;
+    }
+    std::vector<int> holes(g.ctrls);
+    holes.push_back(tb);
+    G1Params<T, I> p{};
+    p.holes = make_holes(holes);
+    p.tbit = I(uint64_t(1) << tb);
+    p.cset = I(g.cset);
+    p.ngroups = I(uint64_t(1) << (n - holes.size()));
+    for (int k = 0; k < 4; k++) {
+        p.m[2 * k] = T(m[k].re);
+        p.m[2 * k + 1] = T(m[k].im);
+    }
+    const bool anti = eq(m[0], 0, 0) && eq(m[3], 0, 0);
+    const bool real = m[0].im == 0 && m[1].im == 0 && m[2].im == 0 && m[3].im == 0;
+    const bool rxlike = m[0].im == 0 && m[3].im == 0 && m[0].re == m[3].re && m[1].re == 0 && m[2].re == 0;
+    if (diag)
+        launch_gate1<T, I, B_DIAG>(sv, p, nstates, svs, s);
+    else if (anti && eq(m[1], 1, 0) && eq(m[2], 1, 0))
+        launch_gate1<T, I, B_PERM>(sv, p, nstates, svs, s);
+    else if (anti)
+        launch_gate1<T, I, B_ANTIDIAG>(sv, p, nstates, svs, s);
+    else if (real)
+        launch_gate1<T, I, B_REAL>(sv, p, nstates, svs, s);
+    else if (rxlike)
+        launch_gate1<T, I, B_RXLIKE>(sv, p, nstates, svs, s);
+    else
+        launch_gate1<T, I, B_DENSE>(sv, p, nstates, svs, s);
+    LGPU_CHECK_LAUNCH();
+    return LGPU_OK;
+}
+
+template <class T, class I, int TT>
+static lgpu_status_t run_gatek(cplx_t<T> *sv, unsigned nstates, cplx_t<T> *const *svs, uint32_t n,
+                               const std::vector<Cm> &m, const GateGeometry &g, cudaStream_t s) {
+    constexpr int D = 1 << TT;
+    auto *p = new GkParams<T, I, TT>();
+    std::vector<int> holes(g.ctrls);
+    holes.insert(holes.end(), g.tgts.begin(), g.tgts.end());
+    p->holes = make_holes(holes);
+    p->cset = I(g.cset);
+    p->ngroups = I(uint64_t(1) << (n - holes.size()));
+    for (int r = 0; r < D; r++) {
+        uint64_t o = 0;
+        for (int k = 0; k < TT; k++)
+            if ((r >> (TT - 1 - k)) & 1) o |= uint64_t(1) << g.tgts[size_t(k)];
+        p->off[r] = I(o);
+    }
+    for (int e = 0; e < D * D; e++) {
+        p->m[2 * e] = m[size_t(e)].re;
+        p->m[2 * e + 1] = m[size_t(e)].im;
+    }
+    const int block = TT >= 4 ? 128 : kGateBlock;
+    dim3 grid(grid_for(uint64_t(p->ngroups), block, 1, 8), nstates ? nstates : 1);
+    gatek_kernel<T, I, TT><<<grid, block, 0, s>>>(sv, *p, nstates, svs);
+    delete p;
+    LGPU_CHECK_LAUNCH();
+    return LGPU_OK;
+}
+
+template <class T, class I>
+static lgpu_status_t run_gatebig(cplx_t<T> *sv, uint32_t n, const std::vector<Cm> &m,
+                                 const GateGeometry &g, cudaStream_t s) {
+    const int t = int(g.tgts.size());
+    const int D = 1 << t;
+    std::vector<I> off(static_cast<size_t>(D));
+    for (int r = 0; r < D; r++) {
+        uint64_t o = 0;
+        for (int k = 0; k < t; k++)
+            if ((r >> (t - 1 - k)) & 1) o |= uint64_t(1) << g.tgts[size_t(k)];
+        off[size_t(r)] = I(o);
+    }
+    std::vector<cplx_t<T>> mh(size_t(D) * D);
+    for (size_t e = 0; e < mh.size(); e++) mh[e] = mk<T>(T(m[e].re), T(m[e].im));
+    // Stream-ordered pool allocation for the device copy of the matrix.
+    void *dbuf = nullptr;
+    const size_t mbytes = mh.size() * sizeof(cplx_t<T>), obytes = off.size() * sizeof(I);
+    LGPU_CUDA_TRY(cudaMallocAsync(&dbuf, mbytes + obytes + 256, s));
+    auto *dmat = static_cast<cplx_t<T> *>(dbuf);
+    auto *doff = reinterpret_cast<I *>(static_cast<char *>(dbuf) + ((mbytes + 255) & ~size_t(255)));
+    LGPU_CUDA_TRY(cudaMemcpyAsync(dmat, mh.data(), mbytes, cudaMemcpyHostToDevice, s));
+    LGPU_CUDA_TRY(cudaMemcpyAsync(doff, off.data(), obytes, cudaMemcpyHostToDevice, s));
+    std::vector<int> holes(g.ctrls);
+    holes.insert(holes.end(), g.tgts.begin(), g.tgts.end());
+    GbigParams<T, I> p{};
+    p.holes = make_holes(holes);
+    p.cset = I(g.cset);
+    p.ngroups = I(uint64_t(1) << (n - holes.size()));
+    p.t = t;
+    p.off = doff;
+    p.mat = dmat;
+    const size_t smem = size_t(D) * sizeof(cplx_t<T>);
+    if (smem > 48 * 1024)
+        LGPU_CUDA_TRY(cudaFuncSetAttribute(gatebig_kernel<T, I>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           int(smem)));
+    const unsigned grid = unsigned(std::min<uint64_t>(uint64_t(p.ngroups), uint64_t(sm_count()) * 4));
+    gatebig_kernel<T, I><<<grid, 256, smem, s>>>(sv, p);
+    LGPU_CHECK_LAUNCH();
+    LGPU_CUDA_TRY(cudaFreeAsync(dbuf, s));
+    return LGPU_OK;
+}
+
+template <class T, class I>
+static lgpu_status_t apply_matrix_t(cplx_t<T> *sv, unsigned nstates, cplx_t<T> *const *svs, uint32_t n,
+                                    const double *matrix, uint32_t t, const GateGeometry &g,
+                                    int adjoint, cudaStream_t s) {
+    const int D = 1 << t;
+    std::vector<Cm> m(size_t(D) * D);
+    for (int r = 0; r < D; r++)
+        for (int c = 0; c < D; c++) {
+            const int src = adjoint ? (c * D + r) : (r * D + c);
+            m[size_t(r * D + c)] = {matrix[2 * src], adjoint ? -matrix[2 * src + 1] : matrix[2 * src + 1]};
+        }
+    switch (t) {
+    case 1: return run_gate1<T, I>(sv, nstates, svs, n, m.data(), g, s);
+    case 2: return run_gatek<T, I, 2>(sv, nstates, svs, n, m, g, s);
+    case 3: return run_gatek<T, I, 3>(sv, nstates, svs, n, m, g, s);
+    case 4: return run_gatek<T, I, 4>(sv, nstates, svs, n, m, g, s);
+    case 5: return run_gatek<T, I, 5>(sv, nstates, svs, n, m, g, s);
+    default:
+        // t > 5: multi-state calls are split per state by the caller
+        return run_gatebig<T, I>(sv, n, m, g, s);
+    }
+}
+
+// Multi-state launches read the state pointers from a small device array held
+// in stream-ordered pool memory.
+template <class T>
+static lgpu_status_t with_state_array(void *const *svs, uint32_t nstates, cudaStream_t s,
+                                      cplx_t<T> ***dev_out, void **to_free) {
+    void *buf = nullptr;
+    LGPU_CUDA_TRY(cudaMallocAsync(&buf, sizeof(void *) * nstates, s));
+    LGPU_CUDA_TRY(cudaMemcpyAsync(buf, svs, sizeof(void *) * nstates, cudaMemcpyHostToDevice, s));
+    *dev_out = static_cast<cplx_t<T> **>(buf);
+    *to_free = buf;
+    return LGPU_OK;
+}
+
+template <class T>
+static lgpu_status_t apply_matrix_dispatch(void *sv, void *const *svs, uint32_t nstates, uint32_t n,
+                                           const double *matrix, uint32_t t, const GateGeometry &g,
+                                           int adjoint, cudaStream_t s) {
+    if (nstates && t > 5) {
+        for (uint32_t k = 0; k < nstates; k++) {
+            lgpu_status_t st = n <= 32 ? apply_matrix_t<T, uint32_t>(static_cast<cplx_t<T> *>(svs[k]), 0,
+                                                                     nullptr, n, matrix, t, g, adjoint, s)
+                                       : apply_matrix_t<T, uint64_t>(static_cast<cplx_t<T> *>(svs[k]), 0,
+                                                                     nullptr, n, matrix, t, g, adjoint, s);
+            if (st != LGPU_OK) return st;
+        }
+        return LGPU_OK;
+    }
+    cplx_t<T> **dev = nullptr;
+    void *to_free = nullptr;
+    if (nstates) LGPU_TRY(with_state_array<T>(svs, nstates, s, &dev, &to_free));
+    lgpu_status_t st = n <= 32 ? apply_matrix_t<T, uint32_t>(static_cast<cplx_t<T> *>(sv), nstates, dev, n,
+                                                             matrix, t, g, adjoint, s)
+                               : apply_matrix_t<T, uint64_t>(static_cast<cplx_t<T> *>(sv), nstates, dev, n,
+                                                             matrix, t, g, adjoint, s);
+    if (to_free) cudaFreeAsync(to_free, s);
+    return st;
+}
+
+template <class T, class I>
+static lgpu_status_t pauli_rot_t(cplx_t<T> *sv, unsigned nstates, cplx_t<T> *const *svs, uint32_t n,
+                                 double angle, const GateGeometry &g, const char *paulis, cudaStream_t s) {
+    uint64_t flip = 0, sgn = 0;
+    int ny = 0;
+    for (size_t k = 0; k < g.tgts.size(); k++) {
+        const uint64_t b = uint64_t(1) << g.tgts[k];
+        switch (paulis[k]) {
+        case 'X': flip |= b; break;
+        case 'Y': flip |= b; sgn |= b; ny++; break;
+        case 'Z': sgn |= b; break;
+        case 'I': break;
+        default: return fail(LGPU_ERR_INVALID_ARG, std::string("bad Pauli letter '") + paulis[k] + "'");
+        }
+    }
+    PRParams<T, I> p{};
+    std::vector<int> holes(g.ctrls);
+    if (flip) holes.push_back(__builtin_ctzll(flip));
+    p.holes = make_holes(holes);
+    p.cset = I(g.cset);
+    p.ngroups = I(uint64_t(1) << (n - holes.size()));
+    p.flip = I(flip);
+    p.sgn = I(sgn);
+    p.c = T(std::cos(angle));
+    p.s = T(std::sin(angle));
+    // q = s * i^(ny+1)
+    const double sv_ = std::sin(angle);
+    switch ((ny + 1) & 3) {
+    case 0: p.qr = T(sv_); p.qi = 0; break;
+    case 1: p.qr = 0; p.qi = T(sv_); break;
+    case 2: p.qr = T(-sv_); p.qi = 0; break;
+    default: p.qr = 0; p.qi = T(-sv_); break;
+    }
+    dim3 grid(grid_for(uint64_t(p.ngroups), kGateBlock, 2, 8), nstates ? nstates : 1);
+    pauli_rot_kernel<T, I><<<grid, kGateBlock, 0, s>>>(sv, p, nstates, svs);
+    LGPU_CHECK_LAUNCH();
+    return LGPU_OK;
+}
+
+template <class T>
+static lgpu_status_t pauli_rot_dispatch(void *sv, void *const *svs, uint32_t nstates, uint32_t n,
+                                        double angle, const GateGeometry &g, const char *paulis,
+                                        cudaStream_t s) {
+    cplx_t<T> **dev = nullptr;
+    void *to_free = nullptr;
+    if (nstates) LGPU_TRY(with_state_array<T>(svs, nstates, s, &dev, &to_free));
+    lgpu_status_t st = n <= 32 ? pauli_rot_t<T, uint32_t>(static_cast<cplx_t<T> *>(sv), nstates, dev, n, angle,
+                                                          g, paulis, s)
+                               : pauli_rot_t<T, uint64_t>(static_cast<cplx_t<T> *>(sv), nstates, dev, n,
+                                                          angle, g, paulis, s);
+    if (to_free) cudaFreeAsync(to_free, s);
+    return st;
+}
+
+template <class T, class I>
+static lgpu_status_t fused_t(cplx_t<T> *sv, uint32_t n, const std::vector<int> &tile_bits,
+                             uint32_t ngates, const lgpu_fused_gate_t *gates, cudaStream_t s) {
+    const int k = int(tile_bits.size());
+    // Tile position of each state bit
+    std::vector<int> pos(n, -1);
+    for (int q = 0; q < k; q++) pos[size_t(tile_bits[size_t(q)])] = q;
+    int m = 0;
+    while (m < k && tile_bits[size_t(m)] == m) m++;
+    if (k - m > 6) return fail(LGPU_ERR_INVALID_ARG, "fused tile: at most 6 tile bits above the contiguous low run");
+    auto *p = new FusedParams<I>();
+    p->holes = make_holes(tile_bits);
+    p->ntiles = I(uint64_t(1) << (n - k));
+    p->k = k;
+    p->m = m;
+    for (int h = 0; h < (1 << (k - m)); h++) {
+        uint64_t o = 0;
+        for (int q = m; q < k; q++)
+            if ((h >> (q - m)) & 1) o |= uint64_t(1) << tile_bits[size_t(q)];
+        p->hi_off[h] = I(o);
+    }
+    uint32_t done = 0;
+    lgpu_status_t st = LGPU_OK;
+    while (done < ngates && st == LGPU_OK) {
+        int cnt = 0;
+        uint32_t pool = 0;
+        while (done + cnt < ngates && cnt < kFusedMaxGates) {
+            const lgpu_fused_gate_t &src = gates[done + cnt];
+            const uint32_t need = src.ntgt == 1 ? 8u : 32u;
+            if (pool + need > uint32_t(kFusedMatPool)) break;
+            FGate &dst = p->gates[cnt];
+            dst = FGate{};
+            dst.ntgt = uint8_t(src.ntgt);
+            if (src.ntgt != 1 && src.ntgt != 2) { st = fail(LGPU_ERR_INVALID_ARG, "fused gate: 1 or 2 targets"); break; }
+            for (int j = 0; j < src.ntgt; j++) {
+                if (src.tgt[j] < 0 || uint32_t(src.tgt[j]) >= n || pos[size_t(src.tgt[j])] < 0) {
+                    st = fail(LGPU_ERR_INVALID_ARG, "fused gate target outside the tile");
+                    break;
+                }
+            }
+            if (st != LGPU_OK) break;
+            dst.q0 = uint8_t(pos[size_t(src.tgt[0])]);
+            dst.q1 = src.ntgt == 2 ? uint8_t(pos[size_t(src.tgt[1])]) : 0;
+            if (src.ntgt == 2 && dst.q0 == dst.q1) { st = fail(LGPU_ERR_INVALID_ARG, "fused gate: repeated target"); break; }
+            if (src.nctrl < 0 || src.nctrl > 4) { st = fail(LGPU_ERR_INVALID_ARG, "fused gate: at most 4 controls"); break; }
+            for (int j = 0; j < src.nctrl; j++) {
+                const int b = src.ctrl[j];
+                if (b < 0 || uint32_t(b) >= n) { st = fail(LGPU_ERR_INVALID_ARG, "fused gate control out of range"); break; }
+                for (int q = 0; q < src.ntgt; q++)
+                    if (src.tgt[q] == b) { st = fail(LGPU_ERR_INVALID_ARG, "fused gate: control equals target"); break; }
+                const int v = src.ctrl_val[j] ? 1 : 0;
+                if (pos[size_t(b)] >= 0) {
+                    dst.in_mask |= 1u << pos[size_t(b)];
+                    if (v) dst.in_val |= 1u << pos[size_t(b)];
+                } else {
+                    dst.out_mask |= uint64_t(1) << b;
+                    if (v) dst.out_val |= uint64_t(1) << b;
+                }
+            }
+            if (st != LGPU_OK) break;
+            dst.mat_off = pool;
+            std::memcpy(p->mats + pool, src.m, need * sizeof(double));
+            pool += need;
+            cnt++;
+        }
+        if (st != LGPU_OK) break;
+        p->ngates = cnt;
+        const size_t smem = (size_t(1) << k) * sizeof(cplx_t<T>);
+        if (smem > 48 * 1024) {
+            cudaError_t e = cudaFuncSetAttribute(fused_kernel<T, I>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                 int(smem));
+            if (e != cudaSuccess) { st = cuda_fail(e, "cudaFuncSetAttribute(fused)"); break; }
+        }
+        const int per_sm = std::max(1, int((200 * 1024) / smem));
+        const unsigned grid = unsigned(std::min<uint64_t>(uint64_t(p->ntiles), uint64_t(sm_count()) * per_sm));
+        fused_kernel<T, I><<<grid, kFusedBlock, smem, s>>>(sv, *p);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) st = cuda_fail(e, "fused kernel launch");
+        done += uint32_t(cnt);
+    }
+    delete p;
+    return st;
+}
+
+}  // namespace lgpu
+
+using namespace lgpu;
+
+extern "C" {
+
+lgpu_status_t lgpu_apply_matrix(void *sv, uint32_t n, lgpu_dtype_t dt, const double *matrix, uint32_t t,
+                                const int32_t *tgts, uint32_t c, const int32_t *ctrls,
+                                const int32_t *ctrl_vals, int adjoint, lgpu_stream_t stream) {
+    LGPU_TRY(check_state(sv, n, dt));
+    if (!matrix) return fail(LGPU_ERR_INVALID_ARG, "matrix is null");
+    GateGeometry g;
+    LGPU_TRY(geometry(n, t, tgts, c, ctrls, ctrl_vals, &g));
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    return dt == LGPU_C128 ? apply_matrix_dispatch<double>(sv, nullptr, 0, n, matrix, t, g, adjoint, s)
+                           : apply_matrix_dispatch<float>(sv, nullptr, 0, n, matrix, t, g, adjoint, s);
+}
+
+lgpu_status_t lgpu_apply_matrix_multi(void *const *svs, uint32_t nstates, uint32_t n, lgpu_dtype_t dt,
+                                      const double *matrix, uint32_t t, const int32_t *tgts, uint32_t c,
+                                      const int32_t *ctrls, const int32_t *ctrl_vals, int adjoint,
+                                      lgpu_stream_t stream) {
+    if (nstates == 0) return LGPU_OK;
+    if (!svs) return fail(LGPU_ERR_INVALID_ARG, "state array is null");
+    if (nstates > 65535) return fail(LGPU_ERR_INVALID_ARG, "too many states in one launch");
+    for (uint32_t k = 0; k < nstates; k++) LGPU_TRY(check_state(svs[k], n, dt));
+    if (!matrix) return fail(LGPU_ERR_INVALID_ARG, "matrix is null");
+    GateGeometry g;
+    LGPU_TRY(geometry(n, t, tgts, c, ctrls, ctrl_vals, &g));
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    return dt == LGPU_C128 ? apply_matrix_dispatch<double>(nullptr, svs, nstates, n, matrix, t, g, adjoint, s)
+                           : apply_matrix_dispatch<float>(nullptr, svs, nstates, n, matrix, t, g, adjoint, s);
+}
+
+lgpu_status_t lgpu_apply_pauli_rotation(void *sv, uint32_t n, lgpu_dtype_t dt, double angle, uint32_t t,
+                                        const int32_t *tgts, const char *paulis, uint32_t c,
+                                        const int32_t *ctrls, const int32_t *ctrl_vals,
+                                        lgpu_stream_t stream) {
+    LGPU_TRY(check_state(sv, n, dt));
+    if (!paulis) return fail(LGPU_ERR_INVALID_ARG, "paulis is null");
+    if (t < 1 || t > n) return fail(LGPU_ERR_INVALID_ARG, "bad number of Pauli targets");
+    GateGeometry g;
+    if (c > LGPU_MAX_CONTROLS) return fail(LGPU_ERR_INVALID_ARG, "too many controls");
+    LGPU_TRY(check_bits(n, t, tgts, "target", &g.tgts));
+    LGPU_TRY(check_bits(n, c, ctrls, "control", &g.ctrls));
+    std::vector<int> all(g.tgts);
+    all.insert(all.end(), g.ctrls.begin(), g.ctrls.end());
+    std::sort(all.begin(), all.end());
+    if (std::adjacent_find(all.begin(), all.end()) != all.end())
+        return fail(LGPU_ERR_INVALID_ARG, "target and control bits must be distinct");
+    for (uint32_t k = 0; k < c; k++) {
+        const int v = ctrl_vals ? ctrl_vals[k] : 1;
+        g.cvals.push_back(v);
+        if (v) g.cset |= uint64_t(1) << g.ctrls[k];
+    }
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    return dt == LGPU_C128 ? pauli_rot_dispatch<double>(sv, nullptr, 0, n, angle, g, paulis, s)
+                           : pauli_rot_dispatch<float>(sv, nullptr, 0, n, angle, g, paulis, s);
+}
+
+lgpu_status_t lgpu_apply_pauli_rotation_multi(void *const *svs, uint32_t nstates, uint32_t n, lgpu_dtype_t dt,
+                                              double angle, uint32_t t, const int32_t *tgts,
+                                              const char *paulis, uint32_t c, const int32_t *ctrls,
+                                              const int32_t *ctrl_vals, lgpu_stream_t stream) {
+    if (nstates == 0) return LGPU_OK;
+    if (!svs || !paulis) return fail(LGPU_ERR_INVALID_ARG, "null argument");
+    if (nstates > 65535) return fail(LGPU_ERR_INVALID_ARG, "too many states in one launch");
+    for (uint32_t k = 0; k < nstates; k++) LGPU_TRY(check_state(svs[k], n, dt));
+    if (t < 1 || t > n) return fail(LGPU_ERR_INVALID_ARG, "bad number of Pauli targets");
+    GateGeometry g;
+    if (c > LGPU_MAX_CONTROLS) return fail(LGPU_ERR_INVALID_ARG, "too many controls");
+    LGPU_TRY(check_bits(n, t, tgts, "target", &g.tgts));
+    LGPU_TRY(check_bits(n, c, ctrls, "control", &g.ctrls));
+    std::vector<int> all(g.tgts);
+    all.insert(all.end(), g.ctrls.begin(), g.ctrls.end());
+    std::sort(all.begin(), all.end());
+    if (std::adjacent_find(all.begin(), all.end()) != all.end())
+        return fail(LGPU_ERR_INVALID_ARG, "target and control bits must be distinct");
+    for (uint32_t k = 0; k < c; k++) {
+        const int v = ctrl_vals ? ctrl_vals[k] : 1;
+        g.cvals.push_back(v);
+        if (v) g.cset |= uint64_t(1) << g.ctrls[k];
+    }
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    return dt == LGPU_C128 ? pauli_rot_dispatch<double>(nullptr, svs, nstates, n, angle, g, paulis, s)
+                           : pauli_rot_dispatch<float>(nullptr, svs, nstates, n, angle, g, paulis, s);
+}
+
+lgpu_status_t lgpu_apply_fused_block(void *sv, uint32_t n, lgpu_dtype_t dt, uint32_t k,
+                                     const int32_t *tile_bits, uint32_t ngates,
+                                     const lgpu_fused_gate_t *gates, lgpu_stream_t stream) {
+    LGPU_TRY(check_state(sv, n, dt));
+    if (ngates == 0) return LGPU_OK;
+    if (!gates) return fail(LGPU_ERR_INVALID_ARG, "gates is null");
+    const uint32_t kmax = dt == LGPU_C128 ? 12u : 13u;
+    if (k < 1 || k > kmax || k > n)
+        return fail(LGPU_ERR_INVALID_ARG, "fused tile size out of range");
+    std::vector<int> tb;
+    LGPU_TRY(check_bits(n, k, tile_bits, "tile", &tb));
+    std::sort(tb.begin(), tb.end());
+    if (std::adjacent_find(tb.begin(), tb.end()) != tb.end())
+        return fail(LGPU_ERR_INVALID_ARG, "tile bits must be distinct");
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    if (dt == LGPU_C128)
+        return n <= 32 ? fused_t<double, uint32_t>(static_cast<double2 *>(sv), n, tb, ngates, gates, s)
+                       : fused_t<double, uint64_t>(static_cast<double2 *>(sv), n, tb, ngates, gates, s);
+    return n <= 32 ? fused_t<float, uint32_t>(static_cast<float2 *>(sv), n, tb, ngates, gates, s)
+                   : fused_t<float, uint64_t>(static_cast<float2 *>(sv), n, tb, ngates, gates, s);
+}
+
+}  // extern "C"

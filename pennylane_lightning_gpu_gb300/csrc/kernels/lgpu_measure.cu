@@ -1,0 +1,828 @@
+// liblgpu_gb300: measurements.
+//
+//  * expval of a dense matrix on t bits (FP64 accumulation, deterministic)
+//  * Pauli-word expectations grouped by flip mask: one streaming pass per
+//    distinct flip mask evaluates up to 8 words (bit-parity signs)
+//  * marginal probabilities: shared-memory histogram per CTA with register
+//    run-length accumulation, then a fixed-order cross-CTA sum
+//  * sampling: FP64 chunk sums -> single-CTA exclusive scan -> one warp per
+//    draw searches its chunk with a warp prefix sum
+//  * sum_t c_t P_t |psi> (Hamiltonian apply) and CSR sparse products
+#include "lgpu_internal.cuh"
+#include "lgpu_reduce.cuh"
+
+namespace lgpu {
+
+// ---------------------------------------------------------------------------
+// Dense matrix expectation, t <= 5 (matrix in the parameter bank)
+// ---------------------------------------------------------------------------
+template <class T, class I, int TT> struct ExpvalBody {
+    Holes holes;
+    I off[1 << TT];
+    double m[2 * (1 << TT) * (1 << TT)];
+    const cplx_t<T> *sv;
+    __device__ __forceinline__ void operator()(I g, double2 *acc) const {
+        constexpr int D = 1 << TT;
+        const I base = insert_holes<I>(g, holes);
+        double ar[D], ai[D];
+#pragma unroll
+        for (int c = 0; c < D; c++) {
+            const cplx_t<T> v = sv[base | off[c]];
+            ar[c] = double(v.x);
+            ai[c] = double(v.y);
+        }
+#pragma unroll
+        for (int r = 0; r < D; r++) {
+            double xr = 0, xi = 0;
+#pragma unroll
+            for (int c = 0; c < D; c++) {
+                const double mr = m[2 * (r * D + c)], mi = m[2 * (r * D + c) + 1];
+                xr = fma(mr, ar[c], fma(-mi, ai[c], xr));
+                xi = fma(mr, ai[c], fma(mi, ar[c], xi));
+            }
+            // conj(a_r) * x
+            acc[0].x = fma(ar[r], xr, fma(ai[r], xi, acc[0].x));
+            acc[0].y = fma(ar[r], xi, fma(-ai[r], xr, acc[0].y));
+        }
+    }
+};
+
+// t = 6..10: one group per CTA iteration, rows split across threads.
+template <class T, class I>
+__global__ void __launch_bounds__(kReduceBlock)
+    expval_big_kernel(const cplx_t<T> *__restrict__ sv, Holes holes, I ngroups, int t, const I *off,
+                      const double2 *mat, double2 *partials, unsigned *counter, double2 *out) {
+    extern __shared__ double2 stile[];
+    __shared__ double2 sm[kReduceBlock / 32];
+    const int D = 1 << t;
+    double2 acc = make_double2(0.0, 0.0);
+    for (I g = blockIdx.x; g < ngroups; g += gridDim.x) {
+        const I base = insert_holes<I>(g, holes);
+        __syncthreads();
+        for (int c = threadIdx.x; c < D; c += kReduceBlock) {
+            const cplx_t<T> v = sv[base | off[c]];
+            stile[c] = make_double2(double(v.x), double(v.y));
+        }
+        __syncthreads();
+        for (int r = threadIdx.x; r < D; r += kReduceBlock) {
+            double xr = 0, xi = 0;
+            const double2 *row = mat + size_t(r) * D;
+            for (int c = 0; c < D; c++) {
+                const double2 mv = row[c], av = stile[c];
+                xr = fma(mv.x, av.x, fma(-mv.y, av.y, xr));
+                xi = fma(mv.x, av.y, fma(mv.y, av.x, xi));
+            }
+            const double2 a = stile[r];
+            acc.x = fma(a.x, xr, fma(a.y, xi, acc.x));
+            acc.y = fma(a.x, xi, fma(-a.y, xr, acc.y));
+        }
+    }
+    __syncthreads();
+    double2 v = block_reduce_d2<kReduceBlock>(acc, sm);
+    if (threadIdx.x == 0) partials[blockIdx.x] = v;
+    if (last_block_arrive(counter)) {
+        double2 s = make_double2(0.0, 0.0);
+        for (unsigned b = threadIdx.x; b < gridDim.x; b += kReduceBlock) {
+            const double2 p = __ldcg(&partials[b]);
+            s.x += p.x;
+            s.y += p.y;
+        }
+        __syncthreads();
+        s = block_reduce_d2<kReduceBlock>(s, sm);
+        if (threadIdx.x == 0) {
+            *out = s;
+            *counter = 0u;
+        }
+    }
+}
+
+template <class T, class I, int TT>
+static lgpu_status_t expval_small(lgpu_context_t ctx, const cplx_t<T> *sv, uint32_t n, const double *matrix,
+                                  const std::vector<int> &tg, double *out, int out_on_device, cudaStream_t s) {
+    constexpr int D = 1 << TT;
+    auto *b = new ExpvalBody<T, I, TT>();
+    b->holes = make_holes(tg);
+    for (int r = 0; r < D; r++) {
+        uint64_t o = 0;
+        for (int k = 0; k < TT; k++)
+            if ((r >> (TT - 1 - k)) & 1) o |= uint64_t(1) << tg[size_t(k)];
+        b->off[r] = I(o);
+    }
+    std::memcpy(b->m, matrix, sizeof(double) * 2 * D * D);
+    b->sv = sv;
+    const I ngroups = I(uint64_t(1) << (n - TT));
+    const unsigned g = reduce_grid(uint64_t(ngroups));
+    ReduceScratch rs;
+    lgpu_status_t st = reduce_scratch(ctx, g, 1, &rs);
+    if (st != LGPU_OK) {
+        delete b;
+        return st;
+    }
+    double2 *res = rs.partials + size_t(g);
+    reduce_kernel<1, I><<<g, kReduceBlock, 0, s>>>(*b, ngroups, rs.partials, rs.counter, res);
+    delete b;
+    LGPU_CHECK_LAUNCH();
+    return deliver(ctx, res, 1, out, out_on_device, s);
+}
+
+template <class T, class I>
+static lgpu_status_t expval_big(lgpu_context_t ctx, const cplx_t<T> *sv, uint32_t n, const double *matrix,
+                                const std::vector<int> &tg, double *out, int out_on_device, cudaStream_t s) {
+    const int t = int(tg.size());
+    const int D = 1 << t;
+    std::vector<I> off(static_cast<size_t>(D));
+    for (int r = 0; r < D; r++) {
+        uint64_t o = 0;
+        for (int k = 0; k < t; k++)
+            if ((r >> (t - 1 - k)) & 1) o |= uint64_t(1) << tg[size_t(k)];
+        off[size_t(r)] = I(o);
+    }
+    const uint64_t ngroups = uint64_t(1) << (n - t);
+    const unsigned g = unsigned(std::min<uint64_t>(ngroups, uint64_t(sm_count()) * 4));
+    const size_t mbytes = size_t(D) * D * sizeof(double2);
+    const size_t obytes = size_t(D) * sizeof(I);
+    void *p = nullptr;
+    const size_t head = 256 + size_t(g) * sizeof(double2) + 256;
+    LGPU_TRY(ctx_scratch(ctx, head + mbytes + obytes + 256, &p));
+    auto *counter = static_cast<unsigned *>(p);
+    auto *partials = reinterpret_cast<double2 *>(static_cast<char *>(p) + 256);
+    auto *res = partials + g;
+    auto *dmat = reinterpret_cast<double2 *>(static_cast<char *>(p) + head);
+    auto *doff = reinterpret_cast<I *>(static_cast<char *>(p) + head + mbytes);
+    LGPU_CUDA_TRY(cudaMemcpyAsync(dmat, matrix, mbytes, cudaMemcpyHostToDevice, s));
+    LGPU_CUDA_TRY(cudaMemcpyAsync(doff, off.data(), obytes, cudaMemcpyHostToDevice, s));
+    const size_t smem = size_t(D) * sizeof(double2);
+    if (smem > 48 * 1024)
+        LGPU_CUDA_TRY(cudaFuncSetAttribute(expval_big_kernel<T, I>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           int(smem)));
+    expval_big_kernel<T, I><<<g, kReduceBlock, smem, s>>>(sv, make_holes(tg), I(ngroups), t, doff, dmat, partials,
+                                                         counter, res);
+    LGPU_CHECK_LAUNCH();
+    return deliver(ctx, res, 1, out, out_on_device, s);
+}
+
+template <class T, class I>
+static lgpu_status_t expval_dispatch(lgpu_context_t ctx, const void *sv, uint32_t n, const double *matrix,
+                                     const std::vector<int> &tg, double *out, int od, cudaStream_t s) {
+    const auto *p = static_cast<const cplx_t<T> *>(sv);
+    switch (tg.size()) {
+    case 1: return expval_small<T, I, 1>(ctx, p, n, matrix, tg, out, od, s);
+    case 2: return expval_small<T, I, 2>(ctx, p, n, matrix, tg, out, od, s);
+    case 3: return expval_small<T, I, 3>(ctx, p, n, matrix, tg, out, od, s);
+    case 4: return expval_small<T, I, 4>(ctx, p, n, matrix, tg, out, od, s);
+    default: return expval_big<T, I>(ctx, p, n, matrix, tg, out, od, s);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Pauli words
+// ---------------------------------------------------------------------------
+constexpr int kWordsPerPass = 8;
+
+template <class T, class I> struct PauliBody {
+    const cplx_t<T> *sv;
+    Holes holes;   // lowest flip bit (empty when flip == 0)
+    I flip;
+    int nt;
+    I sgn[kWordsPerPass];
+    int kappa_neg[kWordsPerPass];  // parity(flip & sgn) odd
+    __device__ __forceinline__ void operator()(I g, double2 *acc) const {
+        if (flip == 0) {
+            const I i = g;
+            const cplx_t<T> a = sv[i];
+            const double p = fma(double(a.x), double(a.x), double(a.y) * double(a.y));
+#pragma unroll
+            for (int t = 0; t < kWordsPerPass; t++) {
+                if (t < nt) acc[t].x += (__popcll(uint64_t(i & sgn[t])) & 1) ? -p : p;
+            }
+        } else {
+            const I i = insert_holes<I>(g, holes);
+            const I j = i ^ flip;
+            const cplx_t<T> a = sv[i], b = sv[j];
+            // w = conj(a) b
+            const double wr = fma(double(a.x), double(b.x), double(a.y) * double(b.y));
+            const double wi = fma(double(a.x), double(b.y), -double(a.y) * double(b.x));
+#pragma unroll
+            for (int t = 0; t < kWordsPerPass; t++) {
+                if (t < nt) {
+                    const double sg = (__popcll(uint64_t(i & sgn[t])) & 1) ? -2.0 : 2.0;
+                    if (kappa_neg[t])
+                        acc[t].y -= sg * wi;
+                    else
+                        acc[t].x += sg * wr;
+                }
+            }
+        }
+    }
+};
+
+template <class T, class I>
+static lgpu_status_t pauli_words_t(lgpu_context_t ctx, const void *sv, uint32_t n, uint32_t nwords,
+                                   const uint64_t *flip, const uint64_t *sign, const uint8_t *ny, double *out,
+                                   int out_on_device, cudaStream_t s) {
+    // Group words by flip mask (stable order of first appearance).
+    std::vector<uint64_t> keys;
+    std::vector<std::vector<uint32_t>> groups;
+    for (uint32_t w = 0; w < nwords; w++) {
+        size_t gi = 0;
+        for (; gi < keys.size(); gi++)
+            if (keys[gi] == flip[w]) break;
+        if (gi == keys.size()) {
+            keys.push_back(flip[w]);
+            groups.emplace_back();
+        }
+        groups[gi].push_back(w);
+    }
+    // Each pass: up to kWordsPerPass words sharing one flip mask.
+    struct Pass {
+        uint64_t flip;
+        std::vector<uint32_t> words;
+    };
+    std::vector<Pass> passes;
+    for (size_t gi = 0; gi < keys.size(); gi++)
+        for (size_t o = 0; o < groups[gi].size(); o += kWordsPerPass)
+            passes.push_back({keys[gi], std::vector<uint32_t>(groups[gi].begin() + o,
+                                                               groups[gi].begin() + std::min(groups[gi].size(),
+                                                                                             o + kWordsPerPass))});
+    const uint64_t N = uint64_t(1) << n;
+    const unsigned g = reduce_grid(N);
+    // scratch: counter | partials (g * 8) | results (passes * 8)
+    void *p = nullptr;
+    const size_t pbytes = size_t(g) * kWordsPerPass * sizeof(double2);
+    const size_t rbytes = passes.size() * kWordsPerPass * sizeof(double2);
+    LGPU_TRY(ctx_scratch(ctx, 256 + pbytes + rbytes, &p));
+    auto *counter = static_cast<unsigned *>(p);
+    auto *partials = reinterpret_cast<double2 *>(static_cast<char *>(p) + 256);
+    auto *results = reinterpret_cast<double2 *>(static_cast<char *>(p) + 256 + pbytes);
+    for (size_t pi = 0; pi < passes.size(); pi++) {
+        PauliBody<T, I> b{};
+        b.sv = static_cast<const cplx_t<T> *>(sv);
+        b.flip = I(passes[pi].flip);
+        std::vector<int> hole;
+        if (passes[pi].flip) hole.push_back(__builtin_ctzll(passes[pi].flip));
+        b.holes = make_holes(hole);
+        b.nt = int(passes[pi].words.size());
+        for (int t = 0; t < b.nt; t++) {
+            const uint32_t w = passes[pi].words[size_t(t)];
+            b.sgn[t] = I(sign[w]);
+            b.kappa_neg[t] = __builtin_popcountll(flip[w] & sign[w]) & 1;
+        }
+        const uint64_t items = passes[pi].flip ? N / 2 : N;
+        reduce_kernel<kWordsPerPass, I><<<g, kReduceBlock, 0, s>>>(b, I(items), partials, counter,
+                                                                   results + pi * kWordsPerPass);
+        LGPU_CHECK_LAUNCH();
+    }
+    std::vector<double2> host(passes.size() * kWordsPerPass);
+    if (!passes.empty()) {
+        void *pin = nullptr;
+        LGPU_TRY(ctx_pinned(ctx, rbytes, &pin));
+        LGPU_CUDA_TRY(cudaMemcpyAsync(pin, results, rbytes, cudaMemcpyDeviceToHost, s));
+        LGPU_CUDA_TRY(cudaStreamSynchronize(s));
+        std::memcpy(host.data(), pin, rbytes);
+    }
+    std::vector<double> vals(nwords, 0.0);
+    for (size_t pi = 0; pi < passes.size(); pi++)
+        for (size_t t = 0; t < passes[pi].words.size(); t++) {
+            const uint32_t w = passes[pi].words[t];
+            const double2 v = host[pi * kWordsPerPass + t];
+            // <P> = Re(i^ny * (v.x + i v.y))
+            double re = 0;
+            switch (ny[w] & 3) {
+            case 0: re = v.x; break;
+            case 1: re = -v.y; break;
+            case 2: re = -v.x; break;
+            default: re = v.y; break;
+            }
+            vals[w] = re;
+        }
+    if (out_on_device)
+        LGPU_CUDA_TRY(cudaMemcpyAsync(out, vals.data(), nwords * sizeof(double), cudaMemcpyHostToDevice, s));
+    else
+        std::memcpy(out, vals.data(), nwords * sizeof(double));
+    if (out_on_device) LGPU_CUDA_TRY(cudaStreamSynchronize(s));
+    return LGPU_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Probabilities
+// ---------------------------------------------------------------------------
+struct BinMap {
+    int k;
+    int bits[24];
+};
+
+template <class I> __device__ __forceinline__ uint32_t bin_of(I i, const BinMap &bm) {
+    uint32_t b = 0;
+#pragma unroll 4
+    for (int q = 0; q < bm.k; q++) b |= uint32_t((i >> bm.bits[q]) & 1) << q;
+    return b;
+}
+
+template <class T, class I>
+__global__ void __launch_bounds__(256)
+    probs_hist_kernel(const cplx_t<T> *__restrict__ sv, I N, int chunk_log2, BinMap bm, double *partials,
+                      unsigned *counter, double *out) {
+    extern __shared__ double hist[];
+    const int nb = 1 << bm.k;
+    for (int b = threadIdx.x; b < nb; b += 256) hist[b] = 0.0;
+    __syncthreads();
+    const I chunk = I(1) << chunk_log2;
+    const I nchunks = N >> chunk_log2;
+    for (I c = blockIdx.x; c < nchunks; c += gridDim.x) {
+        const I base = c * chunk;
+        uint32_t cur = 0xffffffffu;
+        double run = 0.0;
+        for (I o = threadIdx.x; o < chunk; o += 256) {
+            const I i = base + o;
+            const cplx_t<T> a = sv[i];
+            const double p = fma(double(a.x), double(a.x), double(a.y) * double(a.y));
+            const uint32_t b = bin_of<I>(i, bm);
+            if (b != cur) {
+                if (cur != 0xffffffffu) atomicAdd(&hist[cur], run);
+                cur = b;
+                run = p;
+            } else {
+                run += p;
+            }
+        }
+        if (cur != 0xffffffffu) atomicAdd(&hist[cur], run);
+    }
+    __syncthreads();
+    for (int b = threadIdx.x; b < nb; b += 256) partials[size_t(blockIdx.x) * nb + b] = hist[b];
+    if (last_block_arrive(counter)) {
+        for (int b = threadIdx.x; b < nb; b += 256) {
+            double s = 0.0;
+            for (unsigned k = 0; k < gridDim.x; k++) s += __ldcg(&partials[size_t(k) * nb + b]);
+            out[b] = s;
+        }
+        if (threadIdx.x == 0) *counter = 0u;
+    }
+}
+
+template <class T, class I>
+__global__ void probs_atomic_kernel(const cplx_t<T> *__restrict__ sv, I N, BinMap bm, double *out) {
+    const I stride = I(gridDim.x) * blockDim.x;
+    for (I i = I(blockIdx.x) * blockDim.x + threadIdx.x; i < N; i += stride) {
+        const cplx_t<T> a = sv[i];
+        atomicAdd(&out[bin_of<I>(i, bm)], fma(double(a.x), double(a.x), double(a.y) * double(a.y)));
+    }
+}
+
+template <class T, class I>
+static lgpu_status_t probs_t(lgpu_context_t ctx, const void *svv, uint32_t n, const std::vector<int> &bits,
+                             double *out, int out_on_device, cudaStream_t s) {
+    const auto *sv = static_cast<const cplx_t<T> *>(svv);
+    BinMap bm{};
+    bm.k = int(bits.size());
+    for (int q = 0; q < bm.k; q++) bm.bits[q] = bits[size_t(q)];
+    const uint64_t N = uint64_t(1) << n;
+    const size_t nb = size_t(1) << bm.k;
+    void *p = nullptr;
+    double *res = nullptr;
+    if (bm.k <= 12) {
+        int chunk_log2 = std::max(8, int(n) - 12);
+        if (chunk_log2 > int(n)) chunk_log2 = int(n);
+        const uint64_t nchunks = N >> chunk_log2;
+        const unsigned g = unsigned(std::min<uint64_t>(nchunks, uint64_t(sm_count()) * 4));
+        LGPU_TRY(ctx_scratch(ctx, 256 + size_t(g) * nb * sizeof(double) + nb * sizeof(double), &p));
+        auto *counter = static_cast<unsigned *>(p);
+        auto *partials = reinterpret_cast<double *>(static_cast<char *>(p) + 256);
+        res = partials + size_t(g) * nb;
+        const size_t smem = nb * sizeof(double);
+        if (smem > 48 * 1024)
+            LGPU_CUDA_TRY(cudaFuncSetAttribute(probs_hist_kernel<T, I>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                               int(smem)));
+        if (n < 8) chunk_log2 = int(n);
+        probs_hist_kernel<T, I><<<g, 256, smem, s>>>(sv, I(N), chunk_log2, bm, partials, counter, res);
+        LGPU_CHECK_LAUNCH();
+    } else {
+        LGPU_TRY(ctx_scratch(ctx, 256 + nb * sizeof(double), &p));
+        res = reinterpret_cast<double *>(static_cast<char *>(p) + 256);
+        LGPU_CUDA_TRY(cudaMemsetAsync(res, 0, nb * sizeof(double), s));
+        probs_atomic_kernel<T, I><<<grid_for(N, 256, 4), 256, 0, s>>>(sv, I(N), bm, res);
+        LGPU_CHECK_LAUNCH();
+    }
+    if (out_on_device) {
+        LGPU_CUDA_TRY(cudaMemcpyAsync(out, res, nb * sizeof(double), cudaMemcpyDeviceToDevice, s));
+        return LGPU_OK;
+    }
+    LGPU_CUDA_TRY(cudaMemcpyAsync(out, res, nb * sizeof(double), cudaMemcpyDeviceToHost, s));
+    LGPU_CUDA_TRY(cudaStreamSynchronize(s));
+    return LGPU_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Sampling
+// ---------------------------------------------------------------------------
+template <class T>
+__global__ void __launch_bounds__(256)
+    chunk_sums_kernel(const cplx_t<T> *__restrict__ sv, uint64_t nchunks, int chunk_log2, double *csum) {
+    __shared__ double2 sm[8];
+    const uint64_t chunk = uint64_t(1) << chunk_log2;
+    for (uint64_t c = blockIdx.x; c < nchunks; c += gridDim.x) {
+        double acc = 0.0;
+        for (uint64_t o = threadIdx.x; o < chunk; o += 256) {
+            const cplx_t<T> a = sv[c * chunk + o];
+            acc += fma(double(a.x), double(a.x), double(a.y) * double(a.y));
+        }
+        double2 v = block_reduce_d2<256>(make_double2(acc, 0.0), sm);
+        if (threadIdx.x == 0) csum[c] = v.x;
+        __syncthreads();
+    }
+}
+
+// Exclusive scan of csum (in place) by one CTA; writes the total to *total.
+__global__ void __launch_bounds__(1024) scan_kernel(double *csum, uint64_t nchunks, double *total) {
+    __shared__ double part[1024];
+    const uint64_t per = (nchunks + 1023) / 1024;
+    const uint64_t lo = threadIdx.x * per, hi = min(nchunks, lo + per);
+    double s = 0.0;
+    for (uint64_t i = lo; i < hi; i++) s += csum[i];
+    part[threadIdx.x] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double run = 0.0;
+        for (int t = 0; t < 1024; t++) {
+            const double v = part[t];
+            part[t] = run;
+            run += v;
+        }
+        *total = run;
+    }
+    __syncthreads();
+    double run = part[threadIdx.x];
+    for (uint64_t i = lo; i < hi; i++) {
+        const double v = csum[i];
+        csum[i] = run;
+        run += v;
+    }
+}
+
+// One warp per draw.
+template <class T>
+__global__ void __launch_bounds__(256)
+    search_kernel(const cplx_t<T> *__restrict__ sv, const double *__restrict__ cstart, uint64_t nchunks,
+                  int chunk_log2, const double *total_p, const double *draws, uint64_t shots, uint64_t *out) {
+    const int lane = threadIdx.x & 31;
+    const uint64_t warp = (uint64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    const uint64_t nwarps = (uint64_t(gridDim.x) * blockDim.x) >> 5;
+    const double total = *total_p;
+    const uint64_t chunk = uint64_t(1) << chunk_log2;
+    for (uint64_t sidx = warp; sidx < shots; sidx += nwarps) {
+        const double target = draws[sidx] * total;
+        // chunk: last c with cstart[c] <= target (binary search)
+        uint64_t lo = 0, hi = nchunks;  // invariant: answer in [lo, hi)
+        while (hi - lo > 1) {
+            const uint64_t mid = (lo + hi) >> 1;
+            if (cstart[mid] <= target)
+                lo = mid;
+            else
+                hi = mid;
+        }
+        // Walk forward through chunks (handles rounding at chunk borders: a
+        // crossing that falls exactly on a border lands on the first index of
+        // non-zero probability of a later chunk).
+        uint64_t found = ~uint64_t(0), last_nz = ~uint64_t(0);
+        for (uint64_t c = lo; c < nchunks && found == ~uint64_t(0); c++) {
+            double run = cstart[c];
+            for (uint64_t o = 0; o < chunk; o += 32) {
+                double p = 0.0;
+                if (o + lane < chunk) {
+                    const cplx_t<T> a = sv[c * chunk + o + lane];
+                    p = fma(double(a.x), double(a.x), double(a.y) * double(a.y));
+                }
+                double x = p;  // inclusive warp scan
+#pragma unroll
+                for (int d = 1; d < 32; d <<= 1) {
+                    const double y = __shfl_up_sync(0xffffffffu, x, d);
+                    if (lane >= d) x += y;
+                }
+                const double incl = run + x;
+                const unsigned hit = __ballot_sync(0xffffffffu, incl > target && p > 0.0);
+                const unsigned nz = __ballot_sync(0xffffffffu, p > 0.0);
+                if (nz) last_nz = c * chunk + o + (31 - __clz(nz));
+                if (hit) {
+                    found = c * chunk + o + (__ffs(hit) - 1);
+                    break;
+                }
+                run += __shfl_sync(0xffffffffu, x, 31);
+            }
+        }
+        if (found == ~uint64_t(0)) {
+            // Past the end (rounding): the last index of non-zero probability,
+            // searched backwards from chunk lo when the walk saw none.
+            for (uint64_t c = lo + 1; c-- > 0 && last_nz == ~uint64_t(0);) {
+                for (uint64_t o = 0; o < chunk; o += 32) {
+                    double p = 0.0;
+                    if (o + lane < chunk) {
+                        const cplx_t<T> a = sv[c * chunk + o + lane];
+                        p = fma(double(a.x), double(a.x), double(a.y) * double(a.y));
+                    }
+                    const unsigned nz = __ballot_sync(0xffffffffu, p > 0.0);
+                    if (nz) last_nz = c * chunk + o + (31 - __clz(nz));
+                }
+            }
+            found = last_nz == ~uint64_t(0) ? 0 : last_nz;
+        }
+        if (lane == 0) out[sidx] = found;
+    }
+}
+
+template <class T>
+static lgpu_status_t sample_t(lgpu_context_t ctx, const void *svv, uint32_t n, const double *draws, uint64_t shots,
+                              uint64_t *out_idx, cudaStream_t s) {
+    const auto *sv = static_cast<const cplx_t<T> *>(svv);
+    int chunk_log2 = std::max(5, int(n) - 18);
+    if (chunk_log2 > int(n)) chunk_log2 = int(n);
+    if (chunk_log2 < 5 && n >= 5) chunk_log2 = 5;
+    const uint64_t nchunks = (uint64_t(1) << n) >> chunk_log2;
+    // scratch: total(256) | csum | draws | out
+    const size_t cbytes = nchunks * sizeof(double);
+    const size_t dbytes = shots * sizeof(double);
+    const size_t obytes = shots * sizeof(uint64_t);
+    void *p = nullptr;
+    LGPU_TRY(ctx_scratch(ctx, 256 + ((cbytes + 255) & ~size_t(255)) + ((dbytes + 255) & ~size_t(255)) + obytes, &p));
+    char *cp = static_cast<char *>(p);
+    auto *total = reinterpret_cast<double *>(cp);
+    auto *csum = reinterpret_cast<double *>(cp + 256);
+    auto *ddraws = reinterpret_cast<double *>(cp + 256 + ((cbytes + 255) & ~size_t(255)));
+    auto *dout = reinterpret_cast<uint64_t *>(cp + 256 + ((cbytes + 255) & ~size_t(255)) +
+                                              ((dbytes + 255) & ~size_t(255)));
+    void *pin = nullptr;
+    LGPU_TRY(ctx_pinned(ctx, std::max(dbytes, obytes), &pin));
+    std::memcpy(pin, draws, dbytes);
+    LGPU_CUDA_TRY(cudaMemcpyAsync(ddraws, pin, dbytes, cudaMemcpyHostToDevice, s));
+    const unsigned g1 = unsigned(std::min<uint64_t>(nchunks, uint64_t(sm_count()) * 8));
+    if (n < 5) {
+        // tiny states: a single chunk
+        chunk_sums_kernel<T><<<1, 256, 0, s>>>(sv, 1, int(n), csum);
+    } else {
+        chunk_sums_kernel<T><<<g1, 256, 0, s>>>(sv, nchunks, chunk_log2, csum);
+    }
+    LGPU_CHECK_LAUNCH();
+    const uint64_t nch = n < 5 ? 1 : nchunks;
+    const int clog = n < 5 ? int(n) : chunk_log2;
+    scan_kernel<<<1, 1024, 0, s>>>(csum, nch, total);
+    LGPU_CHECK_LAUNCH();
+    const unsigned g2 = unsigned(std::max<uint64_t>(1, std::min<uint64_t>((shots + 7) / 8, uint64_t(sm_count()) * 8)));
+    search_kernel<T><<<g2, 256, 0, s>>>(sv, csum, nch, clog, total, ddraws, shots, dout);
+    LGPU_CHECK_LAUNCH();
+    // Copy back through the pinned buffer; the draws have already been consumed
+    // by the H2D copy that precedes this D2H copy in stream order.
+    LGPU_CUDA_TRY(cudaMemcpyAsync(pin, dout, obytes, cudaMemcpyDeviceToHost, s));
+    LGPU_CUDA_TRY(cudaStreamSynchronize(s));
+    std::memcpy(out_idx, pin, obytes);
+    return LGPU_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Pauli sum apply: out = sum_t c_t P_t in
+// ---------------------------------------------------------------------------
+constexpr int kSumTerms = 16;
+
+template <class T> struct PSumParams {
+    uint64_t flip;
+    int nt;
+    int accumulate;
+    uint64_t sgn[kSumTerms];
+    double cr[kSumTerms], ci[kSumTerms];  // c_t * i^ny_t
+};
+
+template <class T>
+__global__ void __launch_bounds__(256)
+    pauli_sum_kernel(const cplx_t<T> *__restrict__ in, cplx_t<T> *__restrict__ out, uint64_t N, const PSumParams<T> p) {
+    const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
+    for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < N; i += stride) {
+        const uint64_t j = i ^ p.flip;
+        // (P_t in)_i = i^ny sigma_t(j) in_j
+        double fr = 0, fi = 0;
+        for (int t = 0; t < p.nt; t++) {
+            const double sg = (__popcll(j & p.sgn[t]) & 1) ? -1.0 : 1.0;
+            fr += sg * p.cr[t];
+            fi += sg * p.ci[t];
+        }
+        const cplx_t<T> b = in[j];
+        double yr = fr * double(b.x) - fi * double(b.y);
+        double yi = fr * double(b.y) + fi * double(b.x);
+        if (p.accumulate) {
+            const cplx_t<T> o = out[i];
+            yr += double(o.x);
+            yi += double(o.y);
+        }
+        out[i] = mk<T>(T(yr), T(yi));
+    }
+}
+
+template <class T>
+static lgpu_status_t pauli_sum_t(const void *in, void *out, uint32_t n, uint32_t nterms, const double *coeffs,
+                                 const uint64_t *flip, const uint64_t *sign, const uint8_t *ny, cudaStream_t s) {
+    std::vector<uint64_t> keys;
+    std::vector<std::vector<uint32_t>> groups;
+    for (uint32_t w = 0; w < nterms; w++) {
+        size_t gi = 0;
+        for (; gi < keys.size(); gi++)
+            if (keys[gi] == flip[w]) break;
+        if (gi == keys.size()) {
+            keys.push_back(flip[w]);
+            groups.emplace_back();
+        }
+        groups[gi].push_back(w);
+    }
+    const uint64_t N = uint64_t(1) << n;
+    bool first = true;
+    if (nterms == 0) {
+        LGPU_CUDA_TRY(cudaMemsetAsync(out, 0, N * sizeof(cplx_t<T>), s));
+        return LGPU_OK;
+    }
+    for (size_t gi = 0; gi < keys.size(); gi++) {
+        for (size_t o = 0; o < groups[gi].size(); o += kSumTerms) {
+            PSumParams<T> p{};
+            p.flip = keys[gi];
+            p.accumulate = first ? 0 : 1;
+            first = false;
+            p.nt = int(std::min<size_t>(kSumTerms, groups[gi].size() - o));
+            for (int t = 0; t < p.nt; t++) {
+                const uint32_t w = groups[gi][o + size_t(t)];
+                p.sgn[t] = sign[w];
+                double cr = coeffs[2 * w], ci = coeffs[2 * w + 1];
+                for (int q = 0; q < (ny[w] & 3); q++) {  // multiply by i
+                    const double tr = -ci;
+                    ci = cr;
+                    cr = tr;
+                }
+                p.cr[t] = cr;
+                p.ci[t] = ci;
+            }
+            pauli_sum_kernel<T><<<grid_for(N, 256, 4), 256, 0, s>>>(static_cast<const cplx_t<T> *>(in),
+                                                                    static_cast<cplx_t<T> *>(out), N, p);
+            LGPU_CHECK_LAUNCH();
+        }
+    }
+    return LGPU_OK;
+}
+
+// ---------------------------------------------------------------------------
+// CSR
+// ---------------------------------------------------------------------------
+template <class T>
+__global__ void spmv_kernel(const int64_t *__restrict__ off, const int64_t *__restrict__ cols,
+                            const cplx_t<T> *__restrict__ vals, const cplx_t<T> *__restrict__ x, cplx_t<T> *y,
+                            uint64_t nrows) {
+    const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
+    for (uint64_t r = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; r < nrows; r += stride) {
+        double ar = 0, ai = 0;
+        for (int64_t q = off[r]; q < off[r + 1]; q++) {
+            const cplx_t<T> v = vals[q], b = x[cols[q]];
+            ar += double(v.x) * b.x - double(v.y) * b.y;
+            ai += double(v.x) * b.y + double(v.y) * b.x;
+        }
+        y[r] = mk<T>(T(ar), T(ai));
+    }
+}
+
+template <class T> struct CsrExpBody {
+    const int64_t *off;
+    const int64_t *cols;
+    const cplx_t<T> *vals;
+    const cplx_t<T> *x;
+    __device__ __forceinline__ void operator()(uint64_t r, double2 *acc) const {
+        double ar = 0, ai = 0;
+        for (int64_t q = off[r]; q < off[r + 1]; q++) {
+            const cplx_t<T> v = vals[q], b = x[cols[q]];
+            ar += double(v.x) * b.x - double(v.y) * b.y;
+            ai += double(v.x) * b.y + double(v.y) * b.x;
+        }
+        const cplx_t<T> a = x[r];
+        acc[0].x += double(a.x) * ar + double(a.y) * ai;
+        acc[0].y += double(a.x) * ai - double(a.y) * ar;
+    }
+};
+
+}  // namespace lgpu
+
+using namespace lgpu;
+
+extern "C" {
+
+lgpu_status_t lgpu_expval_matrix(lgpu_context_t ctx, const void *sv, uint32_t n, lgpu_dtype_t dt,
+                                 const double *matrix, uint32_t t, const int32_t *tgts, double *out,
+                                 int out_on_device, lgpu_stream_t stream) {
+    LGPU_TRY(check_state(sv, n, dt));
+    if (!matrix || !out) return fail(LGPU_ERR_INVALID_ARG, "null matrix/output");
+    if (t < 1 || t > 10 || t > n) return fail(LGPU_ERR_INVALID_ARG, "expval: number of targets must be in [1, 10]");
+    std::vector<int> tg;
+    LGPU_TRY(check_bits(n, t, tgts, "target", &tg));
+    std::vector<int> srt(tg);
+    std::sort(srt.begin(), srt.end());
+    if (std::adjacent_find(srt.begin(), srt.end()) != srt.end())
+        return fail(LGPU_ERR_INVALID_ARG, "repeated target bit");
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    if (dt == LGPU_C128)
+        return n <= 32 ? expval_dispatch<double, uint32_t>(ctx, sv, n, matrix, tg, out, out_on_device, s)
+                       : expval_dispatch<double, uint64_t>(ctx, sv, n, matrix, tg, out, out_on_device, s);
+    return n <= 32 ? expval_dispatch<float, uint32_t>(ctx, sv, n, matrix, tg, out, out_on_device, s)
+                   : expval_dispatch<float, uint64_t>(ctx, sv, n, matrix, tg, out, out_on_device, s);
+}
+
+lgpu_status_t lgpu_expval_pauli_words(lgpu_context_t ctx, const void *sv, uint32_t n, lgpu_dtype_t dt,
+                                      uint32_t nwords, const uint64_t *flip, const uint64_t *sign,
+                                      const uint8_t *ny, double *out, int out_on_device, lgpu_stream_t stream) {
+    LGPU_TRY(check_state(sv, n, dt));
+    if (nwords == 0) return LGPU_OK;
+    if (!flip || !sign || !ny || !out) return fail(LGPU_ERR_INVALID_ARG, "null argument");
+    const uint64_t full = n >= 64 ? ~uint64_t(0) : ((uint64_t(1) << n) - 1);
+    for (uint32_t w = 0; w < nwords; w++)
+        if ((flip[w] | sign[w]) & ~full) return fail(LGPU_ERR_INVALID_ARG, "Pauli word mask exceeds the qubit count");
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    if (dt == LGPU_C128)
+        return n <= 32 ? pauli_words_t<double, uint32_t>(ctx, sv, n, nwords, flip, sign, ny, out, out_on_device, s)
+                       : pauli_words_t<double, uint64_t>(ctx, sv, n, nwords, flip, sign, ny, out, out_on_device, s);
+    return n <= 32 ? pauli_words_t<float, uint32_t>(ctx, sv, n, nwords, flip, sign, ny, out, out_on_device, s)
+                   : pauli_words_t<float, uint64_t>(ctx, sv, n, nwords, flip, sign, ny, out, out_on_device, s);
+}
+
+lgpu_status_t lgpu_probs(lgpu_context_t ctx, const void *sv, uint32_t n, lgpu_dtype_t dt, uint32_t k,
+                         const int32_t *bits, double *out, int out_on_device, lgpu_stream_t stream) {
+    LGPU_TRY(check_state(sv, n, dt));
+    if (!out) return fail(LGPU_ERR_INVALID_ARG, "output is null");
+    if (k > 24 || k > n) return fail(LGPU_ERR_INVALID_ARG, "probs: at most 24 bits");
+    std::vector<int> b;
+    LGPU_TRY(check_bits(n, k, bits, "probability", &b));
+    std::vector<int> srt(b);
+    std::sort(srt.begin(), srt.end());
+    if (std::adjacent_find(srt.begin(), srt.end()) != srt.end())
+        return fail(LGPU_ERR_INVALID_ARG, "repeated probability bit");
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    if (dt == LGPU_C128)
+        return n <= 32 ? probs_t<double, uint32_t>(ctx, sv, n, b, out, out_on_device, s)
+                       : probs_t<double, uint64_t>(ctx, sv, n, b, out, out_on_device, s);
+    return n <= 32 ? probs_t<float, uint32_t>(ctx, sv, n, b, out, out_on_device, s)
+                   : probs_t<float, uint64_t>(ctx, sv, n, b, out, out_on_device, s);
+}
+
+lgpu_status_t lgpu_sample(lgpu_context_t ctx, const void *sv, uint32_t n, lgpu_dtype_t dt, const double *draws,
+                          uint64_t shots, uint64_t *out_idx, lgpu_stream_t stream) {
+    LGPU_TRY(check_state(sv, n, dt));
+    if (shots == 0) return LGPU_OK;
+    if (!draws || !out_idx) return fail(LGPU_ERR_INVALID_ARG, "null draws/output");
+    for (uint64_t i = 0; i < shots; i++)
+        if (!(draws[i] >= 0.0 && draws[i] < 1.0)) return fail(LGPU_ERR_INVALID_ARG, "draws must lie in [0, 1)");
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    return dt == LGPU_C128 ? sample_t<double>(ctx, sv, n, draws, shots, out_idx, s)
+                           : sample_t<float>(ctx, sv, n, draws, shots, out_idx, s);
+}
+
+lgpu_status_t lgpu_apply_pauli_sum(const void *in, void *out, uint32_t n, lgpu_dtype_t dt, uint32_t nterms,
+                                   const double *coeffs, const uint64_t *flip, const uint64_t *sign,
+                                   const uint8_t *ny, lgpu_stream_t stream) {
+    LGPU_TRY(check_state(in, n, dt));
+    LGPU_TRY(check_state(out, n, dt));
+    if (in == out) return fail(LGPU_ERR_INVALID_ARG, "pauli sum: in and out must not alias");
+    if (nterms && (!coeffs || !flip || !sign || !ny)) return fail(LGPU_ERR_INVALID_ARG, "null argument");
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    return dt == LGPU_C128 ? pauli_sum_t<double>(in, out, n, nterms, coeffs, flip, sign, ny, s)
+                           : pauli_sum_t<float>(in, out, n, nterms, coeffs, flip, sign, ny, s);
+}
+
+lgpu_status_t lgpu_spmv_csr(const int64_t *offsets, const int64_t *cols, const void *vals, const void *x, void *y,
+                            uint32_t n, lgpu_dtype_t dt, lgpu_stream_t stream) {
+    LGPU_TRY(check_state(x, n, dt));
+    LGPU_TRY(check_state(y, n, dt));
+    if (!offsets || !cols || !vals) return fail(LGPU_ERR_INVALID_ARG, "null CSR array");
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    const uint64_t N = uint64_t(1) << n;
+    if (dt == LGPU_C128)
+        spmv_kernel<double><<<grid_for(N, 256, 1), 256, 0, s>>>(offsets, cols, static_cast<const double2 *>(vals),
+                                                                static_cast<const double2 *>(x),
+                                                                static_cast<double2 *>(y), N);
+    else
+        spmv_kernel<float><<<grid_for(N, 256, 1), 256, 0, s>>>(offsets, cols, static_cast<const float2 *>(vals),
+                                                               static_cast<const float2 *>(x),
+                                                               static_cast<float2 *>(y), N);
+    LGPU_CHECK_LAUNCH();
+    return LGPU_OK;
+}
+
+lgpu_status_t lgpu_expval_csr(lgpu_context_t ctx, const int64_t *offsets, const int64_t *cols, const void *vals,
+                              const void *x, uint32_t n, lgpu_dtype_t dt, double *out, int out_on_device,
+                              lgpu_stream_t stream) {
+    LGPU_TRY(check_state(x, n, dt));
+    if (!offsets || !cols || !vals || !out) return fail(LGPU_ERR_INVALID_ARG, "null argument");
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    const uint64_t N = uint64_t(1) << n;
+    const unsigned g = reduce_grid(N);
+    ReduceScratch rs;
+    LGPU_TRY(reduce_scratch(ctx, g, 1, &rs));
+    double2 *res = rs.partials + size_t(g);
+    if (dt == LGPU_C128) {
+        CsrExpBody<double> b{offsets, cols, static_cast<const double2 *>(vals), static_cast<const double2 *>(x)};
+        reduce_kernel<1, uint64_t><<<g, kReduceBlock, 0, s>>>(b, N, rs.partials, rs.counter, res);
+    } else {
+        CsrExpBody<float> b{offsets, cols, static_cast<const float2 *>(vals), static_cast<const float2 *>(x)};
+        reduce_kernel<1, uint64_t><<<g, kReduceBlock, 0, s>>>(b, N, rs.partials, rs.counter, res);
+    }
+    LGPU_CHECK_LAUNCH();
+    return deliver(ctx, res, 1, out, out_on_device, s);
+}
+
+}  // extern "C"

@@ -1,0 +1,347 @@
+"""GPU parity of the drop-in classes against the CPU oracle.
+
+Tolerances (written per test): complex128 1e-10 absolute per amplitude /
+expectation, complex64 1e-5, both against the FP64 oracle; sampling indices
+bit-exact for the same seeded draw stream.
+"""
+import itertools
+import zlib
+
+import numpy as np
+import pytest
+
+from helpers import (apply_ops, cls_name, make_sv, np_dtype, random_hermitian, random_state, random_unitary,
+                     to_oracle_ops, tol)
+
+pytestmark = pytest.mark.gpu
+
+DTYPES = ["c128", "c64"]
+
+# (name, number of wires, number of params)
+GATES = [
+    ("Identity", 1, 0), ("PauliX", 1, 0), ("PauliY", 1, 0), ("PauliZ", 1, 0), ("Hadamard", 1, 0), ("S", 1, 0),
+    ("T", 1, 0), ("RX", 1, 1), ("RY", 1, 1), ("RZ", 1, 1), ("PhaseShift", 1, 1), ("Rot", 1, 3),
+    ("CNOT", 2, 0), ("CY", 2, 0), ("CZ", 2, 0), ("SWAP", 2, 0), ("CRX", 2, 1), ("CRY", 2, 1), ("CRZ", 2, 1),
+    ("CRot", 2, 3), ("ControlledPhaseShift", 2, 1), ("IsingXX", 2, 1), ("IsingYY", 2, 1), ("IsingZZ", 2, 1),
+    ("SingleExcitation", 2, 1), ("SingleExcitationMinus", 2, 1), ("SingleExcitationPlus", 2, 1),
+    ("CSWAP", 3, 0), ("Toffoli", 3, 0), ("DoubleExcitation", 4, 1), ("DoubleExcitationMinus", 4, 1),
+    ("DoubleExcitationPlus", 4, 1), ("MultiRZ", 1, 1), ("MultiRZ", 3, 1), ("MultiRZ", 5, 1),
+]
+
+
+def _check(native, oracle, dtype, n, ops, rng, per_gate=False):
+    psi = random_state(n, rng)
+    sv = make_sv(native, dtype, psi)
+    if per_gate:
+        for o in ops:
+            getattr(sv, o[0])(list(o[1]), bool(o[3]), list(o[2]))
+    else:
+        apply_ops(sv, ops)
+    got = sv.GetState()
+    ref = oracle.apply_ops(psi, to_oracle_ops(ops))
+    err = np.max(np.abs(got - ref))
+    assert err < tol(dtype), (ops, err)
+
+
+@pytest.mark.parametrize("dtype", DTYPES)
+@pytest.mark.parametrize("n", [5, 7])
+@pytest.mark.parametrize("name,nw,npar", GATES)
+def test_named_gate(native, oracle, dtype, n, name, nw, npar):
+    rng = np.random.default_rng(zlib.crc32(('%s-%d-%d-%s' % (name, nw, n, dtype)).encode()))
+    for trial in range(4):
+        wires = [int(x) for x in rng.choice(n, size=nw, replace=False)]
+        params = [float(x) for x in rng.uniform(0, 2 * np.pi, npar)]
+        for adj in (False, True):
+            _check(native, oracle, dtype, n, [(name, wires, params, adj)], rng)
+
+
+@pytest.mark.parametrize("dtype", DTYPES)
+@pytest.mark.parametrize("name,nw,npar", [g for g in GATES if g[0] != "Identity"])
+def test_per_gate_methods(native, oracle, dtype, name, nw, npar):
+    rng = np.random.default_rng(7 + nw)
+    n = 6
+    for _ in range(3):
+        wires = [int(x) for x in rng.choice(n, size=nw, replace=False)]
+        params = [float(x) for x in rng.uniform(0, 2 * np.pi, npar)]
+        for adj in (False, True):
+            _check(native, oracle, dtype, n, [(name, wires, params, adj)], rng, per_gate=True)
+
+
+@pytest.mark.parametrize("dtype", DTYPES)
+def test_controlled_per_gate_semantics(native, oracle, dtype):
+    """Per-gate methods take wires[:-1] as controls (PauliX on 3 wires = Toffoli)."""
+    rng = np.random.default_rng(3)
+    n = 5
+    psi = random_state(n, rng)
+    sv = make_sv(native, dtype, psi)
+    sv.PauliX([0, 3, 1], False, [])
+    sv.RY([4, 2], True, [0.7])
+    ref = oracle.apply_ops(psi, [("Toffoli", [0, 3, 1], [], False, None), ("CRY", [4, 2], [0.7], True, None)])
+    assert np.max(np.abs(sv.GetState() - ref)) < tol(dtype)
+
+
+@pytest.mark.parametrize("dtype", DTYPES)
+@pytest.mark.parametrize("t", [1, 2, 3, 4, 5, 6, 7])
+def test_dense_matrix(native, oracle, dtype, t):
+    rng = np.random.default_rng(100 + t)
+    n = max(t + 2, 6)
+    for adj in (False, True):
+        u = random_unitary(1 << t, rng)
+        wires = [int(x) for x in rng.choice(n, size=t, replace=False)]
+        _check(native, oracle, dtype, n, [("QubitUnitary", wires, [], adj, u)], rng)
+
+
+@pytest.mark.parametrize("dtype", DTYPES)
+def test_unsupported_gate_raises(native, dtype):
+    sv = getattr(native, cls_name(dtype))(3)
+    with pytest.raises(native.PLException, match="Currently unsupported gate: NoSuchGate"):
+        sv.apply("NoSuchGate", [0], False, [], np.zeros(0))
+
+
+@pytest.mark.parametrize("dtype", DTYPES)
+def test_bad_wire_raises(native, dtype):
+    sv = getattr(native, cls_name(dtype))(3)
+    with pytest.raises(native.PLException):
+        sv.RX([5], False, [0.1])
+
+
+@pytest.mark.parametrize("dtype", DTYPES)
+@pytest.mark.parametrize("n,layers", [(6, 3), (9, 4), (12, 3), (13, 2)])
+def test_fused_random_circuit(native, oracle, dtype, n, layers):
+    from pennylane_lightning_gpu_gb300 import workloads
+
+    rng = np.random.default_rng(n * 31 + layers)
+    ops = workloads.random_circuit(n, layers, rng)
+    ops += [("IsingXX", [0, n - 1], [0.3], False), ("SWAP", [1, 2], [], False), ("Toffoli", [0, 1, 2], [], False),
+            ("S", [n - 2], [], True), ("MultiRZ", list(range(min(n, 5))), [0.9], False)]
+    psi = random_state(n, rng)
+    for fusion in (True, False):
+        sv = make_sv(native, dtype, psi)
+        sv.setFusion(fusion)
+        sv.apply([o[0] for o in ops], [o[1] for o in ops], [o[3] for o in ops], [o[2] for o in ops])
+        ref = oracle.apply_ops(psi, to_oracle_ops(ops))
+        err = np.max(np.abs(sv.GetState() - ref))
+        assert err < tol(dtype) * (10 if dtype == "c64" else 1), (fusion, err)
+
+
+@pytest.mark.parametrize("dtype", DTYPES)
+@pytest.mark.parametrize("k", [1, 2, 3, 4, 5, 6, 7])
+def test_expval_matrix(native, oracle, dtype, k):
+    rng = np.random.default_rng(200 + k)
+    n = k + 3
+    psi = random_state(n, rng)
+    sv = make_sv(native, dtype, psi)
+    h = random_hermitian(1 << k, rng)
+    wires = [int(x) for x in rng.choice(n, size=k, replace=False)]
+    got = sv.ExpectationValue(wires, h.ravel())
+    ref = oracle.expval_matrix(psi, h, wires).real
+    assert abs(got - ref) < tol(dtype) * max(1.0, np.abs(h).max()) * 10
+    got2 = sv.ExpectationValue("Hermitian_%d" % k, wires, [], h.ravel())
+    assert abs(got2 - ref) < tol(dtype) * max(1.0, np.abs(h).max()) * 10
+
+
+@pytest.mark.parametrize("dtype", DTYPES)
+def test_named_observable_expval(native, oracle, dtype):
+    rng = np.random.default_rng(11)
+    n = 6
+    psi = random_state(n, rng)
+    sv = make_sv(native, dtype, psi)
+    mats = {"PauliX": np.array([[0, 1], [1, 0]]), "PauliY": np.array([[0, -1j], [1j, 0]]),
+            "PauliZ": np.diag([1, -1]), "Hadamard": np.array([[1, 1], [1, -1]]) / np.sqrt(2)}
+    for name, m in mats.items():
+        for w in range(n):
+            got = sv.ExpectationValue(name, [w], [], np.zeros(0, np.complex128))
+            ref = oracle.expval_matrix(psi, m, [w]).real
+            assert abs(got - ref) < tol(dtype)
+    # tensor observable via the vector-of-names overload
+    m = np.kron(mats["PauliX"], mats["PauliZ"])
+    got = sv.ExpectationValue(["PauliX", "PauliZ"], [4, 1], [[], []], m.ravel())
+    assert abs(got - oracle.expval_matrix(psi, m, [4, 1]).real) < tol(dtype)
+
+
+@pytest.mark.parametrize("dtype", DTYPES)
+@pytest.mark.parametrize("n", [4, 9, 14])
+def test_pauli_words(native, oracle, dtype, n):
+    from pennylane_lightning_gpu_gb300 import workloads
+
+    rng = np.random.default_rng(300 + n)
+    psi = random_state(n, rng)
+    sv = make_sv(native, dtype, psi)
+    ham = workloads.random_pauli_hamiltonian(n, 40, rng, max_wires=min(6, n))
+    ham += [(0.5, "ZZ", [0, 1]), (-0.25, "ZZ", [1, 2]), (0.1, "XX", [0, 1]), (0.2, "XX", [0, 1]), (0.3, "I", [0])]
+    words = [h[1] for h in ham]
+    wires = [h[2] for h in ham]
+    coeffs = np.array([h[0] for h in ham], np.complex128)
+    got = sv.ExpectationValue(words, wires, coeffs.astype(np_dtype(dtype)))
+    ref = oracle.expval_pauli_words(psi, words, wires, coeffs)
+    assert abs(got - ref) < tol(dtype) * len(ham)
+    per = sv.PauliWordExpectations(words, wires)
+    for j, h in enumerate(ham):
+        rj = oracle.expval_pauli_words(psi, [h[1]], [h[2]], np.array([1.0]))
+        assert abs(per[j] - rj) < tol(dtype), (h, per[j], rj)
+
+
+@pytest.mark.parametrize("dtype", DTYPES)
+@pytest.mark.parametrize("n", [3, 8, 14])
+def test_probabilities(native, oracle, dtype, n):
+    rng = np.random.default_rng(400 + n)
+    psi = random_state(n, rng)
+    sv = make_sv(native, dtype, psi)
+    for k in sorted({1, 2, min(n, 5), n - 1, n}):
+        for _ in range(2):
+            wires = [int(x) for x in rng.choice(n, size=k, replace=False)]
+            got = sv.Probability(wires)
+            ref = oracle.probs(psi, wires)
+            assert np.max(np.abs(got - ref)) < tol(dtype), (wires,)
+    got = sv.Probability(sorted(range(n)))
+    assert abs(np.sum(got) - 1.0) < tol(dtype) * 10
+
+
+@pytest.mark.parametrize("dtype", DTYPES)
+@pytest.mark.parametrize("n", [1, 4, 10, 16])
+def test_sampling_bit_exact(native, oracle, dtype, n):
+    rng = np.random.default_rng(500 + n)
+    psi = random_state(n, rng)
+    if n >= 4:
+        psi[:: 3] = 0  # zero-probability entries must never be drawn
+        psi /= np.linalg.norm(psi)
+    sv = make_sv(native, dtype, psi)
+    seed = 1234 + n
+    shots = 3000
+    sv.setSeed(seed)
+    got = sv.GenerateSampleIndices(shots, True)
+    # oracle on the state the device actually holds (c64 rounding included)
+    held = sv.GetState().astype(np.complex128)
+    ref = oracle.sample_indices(held, seed, shots, float_draws=(dtype == "c64"))
+    mism = int(np.sum(got != ref))
+    assert mism == 0, "%d of %d samples differ" % (mism, shots)
+    assert np.all(np.abs(held[got.astype(np.int64)]) > 0)
+    # decoded samples: wire 0 is the most significant bit
+    sv.setSeed(seed)
+    bits = sv.GenerateSamples(n, shots)
+    assert bits.shape == (shots, n)
+    assert np.array_equal(bits, oracle.decode_samples(ref, n))
+
+
+@pytest.mark.gpu
+def test_sampling_statistics(native):
+    """Histogram of 1e5 shots within 0.05 of |psi|^2 (the reference's own check)."""
+    rng = np.random.default_rng(9)
+    n = 3
+    psi = random_state(n, rng)
+    sv = make_sv(native, "c128", psi)
+    sv.setSeed(5)
+    idx = sv.GenerateSampleIndices(100000, True)
+    hist = np.bincount(idx.astype(np.int64), minlength=1 << n) / 1e5
+    assert np.max(np.abs(hist - np.abs(psi) ** 2)) < 0.05
+
+
+@pytest.mark.parametrize("dtype", DTYPES)
+def test_sparse_hamiltonian_expval(native, oracle, dtype):
+    scipy_sparse = pytest.importorskip("scipy.sparse")
+    rng = np.random.default_rng(600)
+    n = 6
+    psi = random_state(n, rng)
+    sv = make_sv(native, dtype, psi)
+    h = random_hermitian(1 << n, rng)
+    h[np.abs(h) < 0.8] = 0
+    h = (h + h.conj().T) / 2
+    csr = scipy_sparse.csr_matrix(h)
+    itype = np.int64 if dtype == "c128" else np.int32
+    got = sv.ExpectationValue(csr.indptr.astype(itype), csr.indices.astype(itype), csr.data.astype(np_dtype(dtype)))
+    ref = oracle.expval_sparse(psi, csr.indptr, csr.indices, csr.data)
+    assert abs(got - ref) < tol(dtype) * 100
+
+
+@pytest.mark.parametrize("dtype", DTYPES)
+def test_basis_and_state_prep(native, dtype):
+    n = 5
+    sv = getattr(native, cls_name(dtype))(n)
+    sv.setBasisState(13, False)
+    st = sv.GetState()
+    assert st[13] == 1 and np.count_nonzero(st) == 1
+    idx = np.array([1, 5, 30], dtype=np.int64 if dtype == "c128" else np.int32)
+    vals = np.array([0.6, 0.8j, 0.0], dtype=np_dtype(dtype))
+    sv.setStateVector(idx, vals, False)
+    st = sv.GetState()
+    assert np.allclose(st[[1, 5, 30]], vals) and np.count_nonzero(st) == 2
+    sv.resetGPU()
+    st = sv.GetState()
+    assert st[0] == 1 and np.count_nonzero(st) == 1
+
+
+def _obs_native(native, dtype, spec):
+    """spec: (is_ham, [(coeff, [(name, wires, matrix)])]) -> native observable."""
+    suf = "C128" if dtype == "c128" else "C64"
+    is_ham, terms = spec
+
+    def term_obj(factors):
+        objs = []
+        for name, wires, mat in factors:
+            if mat is None:
+                objs.append(getattr(native, "NamedObsGPU_" + suf)(name, wires))
+            else:
+                objs.append(getattr(native, "HermitianObsGPU_" + suf)(np.asarray(mat, np_dtype(dtype)).ravel(), wires))
+        return objs[0] if len(objs) == 1 else getattr(native, "TensorProdObsGPU_" + suf)(objs)
+
+    if not is_ham:
+        return term_obj(terms[0][1])
+    coeffs = np.array([t[0] for t in terms], dtype=np.float64 if dtype == "c128" else np.float32)
+    return getattr(native, "HamiltonianGPU_" + suf)(coeffs, [term_obj(t[1]) for t in terms])
+
+
+ADJ_OPS = ["RX", "RY", "RZ", "PhaseShift", "CRX", "CRY", "CRZ", "ControlledPhaseShift", "IsingXX", "IsingYY",
+           "IsingZZ", "SingleExcitation", "SingleExcitationMinus", "SingleExcitationPlus", "DoubleExcitation",
+           "DoubleExcitationMinus", "DoubleExcitationPlus", "MultiRZ"]
+NW = {"RX": 1, "RY": 1, "RZ": 1, "PhaseShift": 1, "DoubleExcitation": 4, "DoubleExcitationMinus": 4,
+      "DoubleExcitationPlus": 4, "MultiRZ": 3}
+
+
+@pytest.mark.parametrize("dtype", DTYPES)
+@pytest.mark.parametrize("seed", [0, 1, 2])
+def test_adjoint_jacobian_vs_oracle(native, oracle, dtype, seed):
+    rng = np.random.default_rng(700 + seed)
+    n = 6
+    ops = [("Hadamard", [w], [], False) for w in range(n)]
+    for name in ADJ_OPS:
+        nw = NW.get(name, 2)
+        wires = [int(x) for x in rng.choice(n, size=nw, replace=False)]
+        ops.append((name, wires, [float(rng.uniform(0, 2 * np.pi))], bool(rng.integers(2))))
+        ops.append(("CNOT", [int(x) for x in rng.choice(n, size=2, replace=False)], [], False))
+    ops.append(("QubitUnitary", [1, 4], [], False, random_unitary(4, rng)))
+    nparam = sum(1 for o in ops if o[2])
+    tp = sorted(int(x) for x in rng.choice(nparam, size=min(nparam, 12), replace=False))
+    obs_specs = [
+        (False, [(1.0, [("PauliZ", [0], None)])]),
+        (False, [(1.0, [("PauliX", [1], None), ("PauliY", [3], None)])]),
+        (True, [(0.3, [("PauliZ", [2], None)]), (-0.7, [("PauliX", [0], None), ("PauliZ", [5], None)]),
+                (0.2, [("PauliY", [4], None)])]),
+        (False, [(1.0, [("Hermitian", [2, 5], random_hermitian(4, rng))])]),
+        (True, [(0.5, [("Hadamard", [3], None)]), (1.5, [("PauliZ", [1], None)])]),
+    ]
+    sv = getattr(native, cls_name(dtype))(n)
+    apply_ops(sv, ops)
+    adj = getattr(native, "AdjointJacobianGPU_" + ("C128" if dtype == "c128" else "C64"))()
+    rdt = np.float64 if dtype == "c128" else np.float32
+    opsd = adj.create_ops_list([o[0] for o in ops], [np.array(o[2], rdt) for o in ops], [o[1] for o in ops],
+                               [o[3] for o in ops],
+                               [np.asarray(o[4], np_dtype(dtype)).ravel() if len(o) > 4 else np.zeros(0, np_dtype(dtype))
+                                for o in ops])
+    obs = [_obs_native(native, dtype, s) for s in obs_specs]
+    jac = np.asarray(adj.adjoint_jacobian(sv, obs, opsd, tp))
+    final = oracle.run(n, to_oracle_ops(ops))
+    oobs = [(s[0], [(c, [(nm, w, m) for nm, w, m in f]) for c, f in s[1]]) for s in obs_specs]
+    ref = oracle.adjoint_jacobian(final, to_oracle_ops(ops), oobs, tp)
+    assert jac.shape == ref.shape
+    assert np.max(np.abs(jac - ref)) < tol(dtype) * 50, np.max(np.abs(jac - ref))
+
+
+@pytest.mark.parametrize("dtype", DTYPES)
+def test_adjoint_rejects_multiparam(native, dtype):
+    suf = "C128" if dtype == "c128" else "C64"
+    rdt = np.float64 if dtype == "c128" else np.float32
+    sv = getattr(native, cls_name(dtype))(2)
+    adj = getattr(native, "AdjointJacobianGPU_" + suf)()
+    opsd = adj.create_ops_list(["Rot"], [np.array([0.1, 0.2, 0.3], rdt)], [[0]], [False], [np.zeros(0, np_dtype(dtype))])
+    with pytest.raises(native.PLException, match="not supported using the adjoint"):
+        adj.adjoint_jacobian(sv, [getattr(native, "NamedObsGPU_" + suf)("PauliZ", [0])], opsd, [0])
