@@ -149,6 +149,49 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+def _apply_gate(sv, g, w):
+    if g == "Hadamard":
+        sv.Hadamard([w], False, [])
+    else:
+        sv.RX([w], False, [THETA])
+
+
+def gate_sweep(m, cls, n, steps, warmup, f64_mode=None):
+    """Device-timed sweep of H and RX over every target; returns
+    (GB/s of algorithmic bytes, avg launch ms, per-target GB/s, state)."""
+    import torch
+
+    if f64_mode is not None:
+        m.set_f64_mode(f64_mode)
+    amp = 16 if cls.endswith("128") else 8
+    S = (1 << n) * amp
+    gates = _gate_list(n)
+    sv = getattr(m, cls)(n)
+    sv.Hadamard([0], False, [])
+    for _ in range(warmup):
+        for g, w in gates:
+            _apply_gate(sv, g, w)
+    torch.cuda.synchronize()
+    ev = [[(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in gates]
+          for _ in range(steps)]
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    start.record()
+    for s in range(steps):
+        for i, (g, w) in enumerate(gates):
+            ev[s][i][0].record()
+            _apply_gate(sv, g, w)
+            ev[s][i][1].record()
+    end.record()
+    torch.cuda.synchronize()
+    ms_per_step = start.elapsed_time(end) / steps
+    per_launch = np.array([[a.elapsed_time(b) for a, b in row] for row in ev])
+    per_target = {}
+    for i, (g, w) in enumerate(gates):
+        per_target.setdefault(g, []).append(round(2 * S / (float(np.median(per_launch[:, i])) / 1e3) / 1e9, 1))
+    gbs = len(gates) * 2 * S / (ms_per_step / 1e3) / 1e9
+    return gbs, float(per_launch.mean()), per_target, ms_per_step, sv
+
+
 def run_ours(args):
     import torch
 
@@ -158,59 +201,34 @@ def run_ours(args):
     n = args.qubits
     S = (1 << n) * 16
     gates = _gate_list(n)
-    sv = m.LightningGPU_C128(n)
-    sv.Hadamard([0], False, [])
-    torch.cuda.synchronize()
+    default_mode = m.get_f64_mode()
 
-    def step_device(events=None):
-        for i, (g, w) in enumerate(gates):
-            if events is not None:
-                events[i][0].record()
-            if g == "Hadamard":
-                sv.Hadamard([w], False, [])
-            else:
-                sv.RX([w], False, [THETA])
-            if events is not None:
-                events[i][1].record()
+    # variants first (each frees its state before the next)
+    variants = {}
+    if not args.no_variants:
+        g, _, _, _, sv = gate_sweep(m, "LightningGPU_C128", n, max(2, args.steps // 2), 2, f64_mode=0)
+        variants["c128_native_fp64_gbs"] = round(g, 1)
+        del sv
+        g, _, _, _, sv = gate_sweep(m, "LightningGPU_C64", n, max(2, args.steps // 2), 2, f64_mode=default_mode)
+        variants["c64_gbs"] = round(g, 1)
+        del sv
+        torch.cuda.synchronize()
 
-    for _ in range(args.warmup):
-        step_device()
-    torch.cuda.synchronize()
-
-    # ---- device-timed steps (value) and per-launch events (roofline) ----
-    ev = [[(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in gates]
-          for _ in range(args.steps)]
     clocks = ClockSampler()
     clocks.start()
     time.sleep(0.3)
-    torch.cuda.synchronize()
-    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    start.record()
-    for s in range(args.steps):
-        step_device(ev[s])
-    end.record()
-    torch.cuda.synchronize()
+    value, avg_launch_ms, per_target, ms_per_step, sv = gate_sweep(m, "LightningGPU_C128", n, args.steps,
+                                                                   args.warmup, f64_mode=default_mode)
     clk = clocks.stop()
-    total_ms = start.elapsed_time(end)
-    ms_per_step = total_ms / args.steps
     bytes_per_step = len(gates) * 2 * S
-    value = bytes_per_step / (ms_per_step / 1e3) / 1e9
-    per_launch = np.array([[a.elapsed_time(b) for a, b in row] for row in ev])  # [steps, gates] ms
-    avg_launch_ms = float(per_launch.mean())
-    per_target = {}
-    for i, (g, w) in enumerate(gates):
-        per_target.setdefault(g, []).append(round(2 * S / (float(np.median(per_launch[:, i])) / 1e3) / 1e9, 1))
 
     # ---- end to end: public API, host params, D2H result read every step ----
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(args.steps):
         for g, w in gates:
-            if g == "Hadamard":
-                sv.Hadamard([w], False, [])
-            else:
-                sv.RX([w], False, [THETA])
-        p0 = sv.Probability([0])  # blocking D2H of the step's result
+            _apply_gate(sv, g, w)
+        sv.Probability([0])  # blocking D2H of the step's result
     e2e_s = (time.perf_counter() - t0) / args.steps
     e2e_value = (bytes_per_step + S) / e2e_s / 1e9  # + one read pass for the probability
 
@@ -222,6 +240,7 @@ def run_ours(args):
         "scaling": "weak", "vs_baseline": None, "dtype": "c128 (f64)", "data": "synthetic",
         "config": {"workload": "dense 1-qubit gates (H and RX) on each target of a 28-qubit complex128 state",
                    "qubits": n, "state_bytes": S, "gates_per_step": len(gates),
+                   "f64_mode": "fp64 fma + integer-pipe multiply" if default_mode == 1 else "native fp64",
                    "l2": "state (4 GiB) larger than L2 (129 MB): no flush needed"},
         "e2e": {"value": round(e2e_value, 1), "unit": "GB/s", "h2d_bytes_per_step": 8 * n,
                 "d2h_bytes_per_step": 16},
@@ -229,9 +248,11 @@ def run_ours(args):
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": None, "peak_source": peak_kind,
                      "kernel": "gate1_kernel", "algorithmic_bytes_per_launch": 2 * S},
+        "variants": variants,
         "per_target_gbs": per_target,
         "clocks": clk,
     }
+    del sv
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline_sample(n, gates=args.cpu_gates)
     print(json.dumps(line))
@@ -246,6 +267,7 @@ def main():
     ap.add_argument("--qubits", type=int, default=N_QUBITS)
     ap.add_argument("--cpu-gates", type=int, default=4)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-variants", action="store_true")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     if args.impl == "reference":

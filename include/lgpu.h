@@ -63,6 +63,16 @@ typedef struct lgpu_context_s *lgpu_context_t;
 int lgpu_abi_version(void);
 const char *lgpu_last_error_string(void);
 
+/* complex128 arithmetic mode of the streaming gate kernels (process-wide):
+ * 0 = native FP64; 1 (default) = one FP64 FMA plus one integer-pipe multiply
+ * per output component, which halves FP64 issue on GB300 (whose FP64 rate is
+ * about 2 FMA/clock/SM).  The integer multiply equals the IEEE product except
+ * on exact rounding ties.  The environment variable LGPU_F64_EMUL=0 selects
+ * mode 0 at start-up.  No counterpart in the reference (cuStateVec chooses
+ * its arithmetic internally). */
+lgpu_status_t lgpu_set_f64_mode(int mode);
+int lgpu_get_f64_mode(void);
+
 /* ---- device and memory (DataBuffer.hpp:31-218, cuda_helpers.hpp:796-837,
  *      Bindings.cpp:1736-1748; the C++ layer needs no CUDA runtime of its own) */
 lgpu_status_t lgpu_device_count(int *count);

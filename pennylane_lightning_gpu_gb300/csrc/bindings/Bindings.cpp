@@ -526,6 +526,10 @@ PYBIND11_MODULE(lightning_gpu_qubit_ops, m) {
     m.def("get_gpu_arch", &cuUtil::getGPUArch, py::arg("device_number") = 0,
           "Returns the given GPU major and minor GPU support.");
     m.def("abi_version", &lgpu_abi_version);
+    m.def(
+        "set_f64_mode", [](int mode) { PL_LGPU_IS_SUCCESS(lgpu_set_f64_mode(mode)); },
+        "complex128 arithmetic of the streaming gate kernels: 0 native FP64, 1 FP64 FMA + integer-pipe multiplies");
+    m.def("get_f64_mode", &lgpu_get_f64_mode);
 
     py::class_<DevPool>(m, "DevPool")
         .def(py::init<>())

@@ -1,5 +1,7 @@
 // liblgpu_gb300: errors, device and memory services, scratch contexts, state
 // preparation, and the BLAS-1 style kernels (copy, axpy, scale, dot).
+#include <atomic>
+#include <cstdlib>
 #include <mutex>
 
 #include "lgpu_internal.cuh"
@@ -21,6 +23,18 @@ lgpu_status_t cuda_fail(cudaError_t e, const char *what) {
                       cudaGetErrorString(e) + ")";
     if (e == cudaErrorMemoryAllocation) return fail(LGPU_ERR_OOM, msg);
     return fail(LGPU_ERR_CUDA, msg);
+}
+
+static std::atomic<int> g_f64_mode{-1};
+
+int f64_mode() {
+    int m = g_f64_mode.load(std::memory_order_relaxed);
+    if (m < 0) {
+        const char *e = std::getenv("LGPU_F64_EMUL");
+        m = (e && e[0] == '0') ? 0 : 1;
+        g_f64_mode.store(m, std::memory_order_relaxed);
+    }
+    return m;
 }
 
 int current_device() {
@@ -206,6 +220,14 @@ using namespace lgpu;
 extern "C" {
 
 int lgpu_abi_version(void) { return 1; }
+
+lgpu_status_t lgpu_set_f64_mode(int mode) {
+    if (mode != 0 && mode != 1) return fail(LGPU_ERR_INVALID_ARG, "f64 mode must be 0 (native) or 1 (emulated multiplies)");
+    g_f64_mode.store(mode, std::memory_order_relaxed);
+    return LGPU_OK;
+}
+
+int lgpu_get_f64_mode(void) { return f64_mode(); }
 
 const char *lgpu_last_error_string(void) { return g_last_error.c_str(); }
 

@@ -14,6 +14,7 @@
 //  * pauli_rot_kernel exp(i angle P) for Pauli words, pairwise (i, i^flip).
 //  * fused_kernel     a block of 1/2-target gates applied to shared-memory
 //                     tiles of 2^k amplitudes: one HBM pass for many gates.
+#include "lgpu_f64emu.cuh"
 #include "lgpu_internal.cuh"
 
 namespace lgpu {
@@ -28,6 +29,7 @@ template <class T, class I> struct G1Params {
     I cset;
     I ngroups;
     T m[8];
+    KConst k[4];  // integer-pipe multipliers (complex128 EMU bodies)
 };
 
 template <class T, int BODY>
@@ -71,8 +73,44 @@ __device__ __forceinline__ void body1(const T *m, cplx_t<T> &a0, cplx_t<T> &a1) 
     }
 }
 
+// complex128 bodies with one DFMA + one integer-pipe multiply per output
+// component (half the FP64 issue of body1).  k[] holds the constants the
+// host prepared for the body (see run_gate1).
+template <int BODY>
+__device__ __forceinline__ void body1_emu(const double *m, const KConst *k, double2 &a0, double2 &a1) {
+    const double2 x = a0, y = a1;
+    if constexpr (BODY == B_PERM) {
+        a0 = y;
+        a1 = x;
+    } else if constexpr (BODY == B_DIAG) {  // k = {-m00i, m00i, -m11i, m11i}
+        a0 = make_double2(__fma_rn(m[0], x.x, emul(x.y, k[0])), __fma_rn(m[0], x.y, emul(x.x, k[1])));
+        a1 = make_double2(__fma_rn(m[6], y.x, emul(y.y, k[2])), __fma_rn(m[6], y.y, emul(y.x, k[3])));
+    } else if constexpr (BODY == B_ANTIDIAG) {  // k = {-m01i, m01i, -m10i, m10i}
+        a0 = make_double2(__fma_rn(m[2], y.x, emul(y.y, k[0])), __fma_rn(m[2], y.y, emul(y.x, k[1])));
+        a1 = make_double2(__fma_rn(m[4], x.x, emul(x.y, k[2])), __fma_rn(m[4], x.y, emul(x.x, k[3])));
+    } else if constexpr (BODY == B_REAL) {  // k = {m01r, m10r}
+        a0 = make_double2(__fma_rn(m[0], x.x, emul(y.x, k[0])), __fma_rn(m[0], x.y, emul(y.y, k[0])));
+        a1 = make_double2(__fma_rn(m[6], y.x, emul(x.x, k[1])), __fma_rn(m[6], y.y, emul(x.y, k[1])));
+    } else if constexpr (BODY == B_RXLIKE) {  // k = {-u, u, -v, v}
+        const double c = m[0];
+        a0 = make_double2(__fma_rn(c, x.x, emul(y.y, k[0])), __fma_rn(c, x.y, emul(y.x, k[1])));
+        a1 = make_double2(__fma_rn(c, y.x, emul(x.y, k[2])), __fma_rn(c, y.y, emul(x.x, k[3])));
+    } else {
+        body1<double, B_DENSE>(m, a0, a1);
+    }
+}
+
+template <class T, int BODY, bool EMU>
+__device__ __forceinline__ void body1_sel(const T *m, const KConst *k, cplx_t<T> &a0, cplx_t<T> &a1) {
+    if constexpr (EMU && sizeof(T) == 8)
+        body1_emu<BODY>(reinterpret_cast<const double *>(m), k, reinterpret_cast<double2 &>(a0),
+                        reinterpret_cast<double2 &>(a1));
+    else
+        body1<T, BODY>(m, a0, a1);
+}
+
 // ITEMS pairs per thread in flight: all loads are issued before any math.
-template <class T, class I, int BODY, int ITEMS>
+template <class T, class I, int BODY, int ITEMS, bool EMU>
 __global__ void __launch_bounds__(kGateBlock)
     gate1_kernel(cplx_t<T> *__restrict__ sv, const G1Params<T, I> p, const unsigned nstates,
                  cplx_t<T> *const *__restrict__ svs) {
@@ -81,6 +119,9 @@ __global__ void __launch_bounds__(kGateBlock)
     T m[8];
 #pragma unroll
     for (int k = 0; k < 8; k++) m[k] = p.m[k];
+    KConst kc[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++) kc[k] = p.k[k];
     const I stride = I(gridDim.x) * kGateBlock;
     for (I g = I(blockIdx.x) * kGateBlock + threadIdx.x; g < p.ngroups; g += stride * ITEMS) {
         C a0[ITEMS], a1[ITEMS];
@@ -98,7 +139,7 @@ __global__ void __launch_bounds__(kGateBlock)
             }
         }
 #pragma unroll
-        for (int k = 0; k < ITEMS; k++) body1<T, BODY>(m, a0[k], a1[k]);
+        for (int k = 0; k < ITEMS; k++) body1_sel<T, BODY, EMU>(m, kc, a0[k], a1[k]);
 #pragma unroll
         for (int k = 0; k < ITEMS; k++) {
             if (g + I(k) * stride < p.ngroups) {
@@ -114,9 +155,10 @@ template <class T, class I> struct PhaseParams {
     I set;  // bits forced to 1
     I ngroups;
     T re, im;
+    KConst k[2];  // {-im, im} for the complex128 EMU variant
 };
 
-template <class T, class I, bool NEG, int ITEMS>
+template <class T, class I, bool NEG, int ITEMS, bool EMU>
 __global__ void __launch_bounds__(kGateBlock)
     phase_kernel(cplx_t<T> *__restrict__ sv, const PhaseParams<T, I> p, const unsigned nstates,
                  cplx_t<T> *const *__restrict__ svs) {
@@ -135,10 +177,14 @@ __global__ void __launch_bounds__(kGateBlock)
 #pragma unroll
         for (int k = 0; k < ITEMS; k++) {
             const C x = a[k];
-            if constexpr (NEG)
+            if constexpr (NEG) {
                 a[k] = mk<T>(-x.x, -x.y);
-            else
+            } else if constexpr (EMU && sizeof(T) == 8) {
+                const double xr = double(x.x), xi = double(x.y), pr = double(p.re);
+                a[k] = mk<T>(T(__fma_rn(pr, xr, emul(xi, p.k[0]))), T(__fma_rn(pr, xi, emul(xr, p.k[1]))));
+            } else {
                 a[k] = mk<T>(fmaT(p.re, x.x, -p.im * x.y), fmaT(p.re, x.y, p.im * x.x));
+            }
         }
 #pragma unroll
         for (int k = 0; k < ITEMS; k++)
@@ -401,7 +447,13 @@ static void launch_gate1(cplx_t<T> *sv, const G1Params<T, I> &p, unsigned nstate
     constexpr int ITEMS = sizeof(T) == 8 ? 2 : 4;
     const unsigned gx = grid_for(uint64_t(p.ngroups), kGateBlock, ITEMS, 8);
     dim3 grid(gx, nstates ? nstates : 1);
-    gate1_kernel<T, I, BODY, ITEMS><<<grid, kGateBlock, 0, s>>>(sv, p, nstates, svs);
+    if constexpr (sizeof(T) == 8) {
+        if (f64_mode() == 1) {
+            gate1_kernel<T, I, BODY, ITEMS, true><<<grid, kGateBlock, 0, s>>>(sv, p, nstates, svs);
+            return;
+        }
+    }
+    gate1_kernel<T, I, BODY, ITEMS, false><<<grid, kGateBlock, 0, s>>>(sv, p, nstates, svs);
 }
 
 template <class T, class I>
@@ -422,12 +474,20 @@ static lgpu_status_t run_gate1(cplx_t<T> *sv, unsigned nstates, cplx_t<T> *const
         p.ngroups = I(uint64_t(1) << (n - holes.size()));
         p.re = T(ph.re);
         p.im = T(ph.im);
+        p.k[0] = make_kconst(-ph.im);
+        p.k[1] = make_kconst(ph.im);
         constexpr int ITEMS = sizeof(T) == 8 ? 2 : 4;
         dim3 grid(grid_for(uint64_t(p.ngroups), kGateBlock, ITEMS, 8), nstates ? nstates : 1);
-        if (eq(ph, -1, 0))
-            phase_kernel<T, I, true, ITEMS><<<grid, kGateBlock, 0, s>>>(sv, p, nstates, svs);
-        else
-            phase_kernel<T, I, false, ITEMS><<<grid, kGateBlock, 0, s>>>(sv, p, nstates, svs);
+        bool emu = false;
+        if constexpr (sizeof(T) == 8) emu = f64_mode() == 1;
+        if (eq(ph, -1, 0)) {
+            phase_kernel<T, I, true, ITEMS, false><<<grid, kGateBlock, 0, s>>>(sv, p, nstates, svs);
+        } else if (emu) {
+            if constexpr (sizeof(T) == 8)
+                phase_kernel<T, I, false, ITEMS, true><<<grid, kGateBlock, 0, s>>>(sv, p, nstates, svs);
+        } else {
+            phase_kernel<T, I, false, ITEMS, false><<<grid, kGateBlock, 0, s>>>(sv, p, nstates, svs);
+        }
         LGPU_CHECK_LAUNCH();
         return LGPU_OK;
     }
@@ -445,6 +505,18 @@ static lgpu_status_t run_gate1(cplx_t<T> *sv, unsigned nstates, cplx_t<T> *const
     const bool anti = eq(m[0], 0, 0) && eq(m[3], 0, 0);
     const bool real = m[0].im == 0 && m[1].im == 0 && m[2].im == 0 && m[3].im == 0;
     const bool rxlike = m[0].im == 0 && m[3].im == 0 && m[0].re == m[3].re && m[1].re == 0 && m[2].re == 0;
+    if (diag) {
+        p.k[0] = make_kconst(-m[0].im); p.k[1] = make_kconst(m[0].im);
+        p.k[2] = make_kconst(-m[3].im); p.k[3] = make_kconst(m[3].im);
+    } else if (anti) {
+        p.k[0] = make_kconst(-m[1].im); p.k[1] = make_kconst(m[1].im);
+        p.k[2] = make_kconst(-m[2].im); p.k[3] = make_kconst(m[2].im);
+    } else if (real) {
+        p.k[0] = make_kconst(m[1].re); p.k[1] = make_kconst(m[2].re);
+    } else if (rxlike) {
+        p.k[0] = make_kconst(-m[1].im); p.k[1] = make_kconst(m[1].im);
+        p.k[2] = make_kconst(-m[2].im); p.k[3] = make_kconst(m[2].im);
+    }
     if (diag)
         launch_gate1<T, I, B_DIAG>(sv, p, nstates, svs, s);
     else if (anti && eq(m[1], 1, 0) && eq(m[2], 1, 0))

@@ -44,6 +44,9 @@ lgpu_status_t cuda_fail(cudaError_t e, const char *what);
 // ---------------------------------------------------------------------------
 int sm_count();          // SMs of the current device
 int current_device();
+// complex128 arithmetic mode: 0 = native FP64, 1 = FP64 FMA + integer-pipe
+// multiplies (lgpu_f64emu.cuh).  Process-wide; see lgpu_set_f64_mode().
+int f64_mode();
 
 // ---------------------------------------------------------------------------
 // Scratch context

@@ -345,3 +345,44 @@ def test_adjoint_rejects_multiparam(native, dtype):
     opsd = adj.create_ops_list(["Rot"], [np.array([0.1, 0.2, 0.3], rdt)], [[0]], [False], [np.zeros(0, np_dtype(dtype))])
     with pytest.raises(native.PLException, match="not supported using the adjoint"):
         adj.adjoint_jacobian(sv, [getattr(native, "NamedObsGPU_" + suf)("PauliZ", [0])], opsd, [0])
+
+
+@pytest.mark.parametrize("mode", [0, 1])
+@pytest.mark.parametrize("name,nw,npar", [g for g in GATES if g[1] <= 2])
+def test_f64_modes(native, oracle, mode, name, nw, npar):
+    """complex128 gates agree with the oracle with native FP64 and with the
+    integer-pipe multiplies."""
+    old = native.get_f64_mode()
+    native.set_f64_mode(mode)
+    try:
+        rng = np.random.default_rng(zlib.crc32(("mode-%s-%d" % (name, mode)).encode()))
+        n = 8
+        for _ in range(3):
+            wires = [int(x) for x in rng.choice(n, size=nw, replace=False)]
+            params = [float(x) for x in rng.uniform(0, 2 * np.pi, npar)]
+            for adj in (False, True):
+                _check(native, oracle, "c128", n, [(name, wires, params, adj)], rng)
+    finally:
+        native.set_f64_mode(old)
+
+
+def test_f64_mode_bits_close(native):
+    """The two complex128 modes differ by at most a few ulp after many gates."""
+    from pennylane_lightning_gpu_gb300 import workloads
+
+    rng = np.random.default_rng(5)
+    n = 12
+    ops = workloads.layered_ansatz(n, 6, rng) + [("Hadamard", [w], [], False) for w in range(n)]
+    psi = random_state(n, rng)
+    out = []
+    old = native.get_f64_mode()
+    try:
+        for mode in (0, 1):
+            native.set_f64_mode(mode)
+            sv = make_sv(native, "c128", psi)
+            sv.setFusion(False)
+            apply_ops(sv, ops)
+            out.append(sv.GetState())
+    finally:
+        native.set_f64_mode(old)
+    assert np.max(np.abs(out[0] - out[1])) < 1e-13
