@@ -1,0 +1,175 @@
+"""The Python LightningGPU device end to end against the oracle.
+
+Tolerances: complex128 1e-10 (expvals, states, Jacobians), complex64 1e-5;
+central differences (h = 1e-4, complex128) agree with the adjoint to 1e-7.
+"""
+import numpy as np
+import pytest
+
+from pennylane_lightning_gpu_gb300 import ops as Q
+from pennylane_lightning_gpu_gb300 import workloads
+
+pytestmark = pytest.mark.gpu
+
+
+def _dev(n, dtype=np.complex128, **kw):
+    from pennylane_lightning_gpu_gb300.lightning_gpu import LightningGPU
+
+    return LightningGPU(n, c_dtype=dtype, **kw)
+
+
+def _oracle_ops(tape_ops):
+    out = []
+    for o in tape_ops:
+        if isinstance(o, Q.Adjoint):
+            out.append((o.name, o.wires, o.parameters, True, o.base._matrix))
+        else:
+            out.append((o.name, o.wires, o.parameters, False, o._matrix))
+    return out
+
+
+def _ops(n, rng, layers=2):
+    ops = [Q.op(*o[:2], *o[2]) for o in workloads.random_circuit(n, layers, rng)]
+    ops.append(Q.op("IsingYY", [0, 1], 0.37).adjoint())
+    ops.append(Q.QubitUnitary(np.linalg.qr(rng.normal(size=(4, 4)) + 1j * rng.normal(size=(4, 4)))[0], [2, 0]))
+    return ops
+
+
+@pytest.mark.parametrize("dtype,tol", [(np.complex128, 1e-10), (np.complex64, 1e-5)])
+def test_execute_measurements(oracle, dtype, tol):
+    rng = np.random.default_rng(0)
+    n = 6
+    ops = _ops(n, rng)
+    H = Q.Hamiltonian([0.3, -0.8, 0.25], [Q.PauliZ(0) @ Q.PauliX(3), Q.PauliY(1), Q.PauliZ(5)])
+    herm = rng.normal(size=(4, 4)) + 1j * rng.normal(size=(4, 4))
+    herm = herm + herm.conj().T
+    tape = Q.QuantumTape(ops, [Q.expval(Q.PauliX(2)), Q.expval(H), Q.var(Q.PauliY(4)),
+                               Q.expval(Q.Hermitian(herm, [1, 4])), Q.probs([0, 2, 3]),
+                               Q.expval(Q.Projector([1, 0], [2, 3]))])
+    dev = _dev(n, dtype)
+    res = dev.execute(tape)
+    psi = oracle.run(n, _oracle_ops(ops))
+    assert abs(res[0] - oracle.expval_matrix(psi, np.array([[0, 1], [1, 0]]), [2]).real) < tol
+    assert abs(res[1] - oracle.expval_matrix(psi, H.matrix(list(range(n))), list(range(n))).real) < tol * 10
+    y = np.array([[0, -1j], [1j, 0]])
+    v = 1 - oracle.expval_matrix(psi, y, [4]).real ** 2
+    assert abs(res[2] - v) < tol * 10
+    assert abs(res[3] - oracle.expval_matrix(psi, herm, [1, 4]).real) < tol * 10
+    # probabilities in PennyLane order (first wire most significant)
+    p = oracle.probs(psi, [0, 2, 3]).reshape(2, 2, 2).transpose().reshape(-1)
+    assert np.max(np.abs(res[4] - p)) < tol
+    p23 = oracle.probs(psi, [2, 3]).reshape(2, 2).T.reshape(-1)  # PennyLane order over wires [2, 3]
+    assert abs(res[5] - p23[0b10]) < tol
+
+
+def test_state_prep_and_basis_state(oracle):
+    rng = np.random.default_rng(1)
+    n = 5
+    dev = _dev(n)
+    sub = rng.normal(size=4) + 1j * rng.normal(size=4)
+    sub /= np.linalg.norm(sub)
+    dev.apply([Q.StatePrep(sub, [3, 1]), Q.op("RX", 2, 0.4)])
+    full = np.zeros(32, complex)
+    for k in range(4):
+        idx = ((k >> 1) & 1) << (n - 1 - 3) | (k & 1) << (n - 1 - 1)
+        full[idx] = sub[k]
+    ref = oracle.apply_ops(full, [("RX", [2], [0.4], False, None)])
+    assert np.allclose(dev.state, ref, atol=1e-12)
+    dev.reset()
+    dev.apply([Q.BasisState([1, 0, 1], [0, 2, 4])])
+    st = dev.state
+    assert st[0b10101] == 1
+    with pytest.raises(Exception):
+        dev.apply([Q.op("RX", 0, 0.1), Q.BasisState([1], [0])])
+
+
+def test_samples_and_shot_expval():
+    n = 3
+    dev = _dev(n, shots=20000, seed=11)
+    ops = [Q.op("RY", 0, 1.1), Q.op("CNOT", [0, 1]), Q.op("RX", 2, 0.6)]
+    dev.reset()
+    dev.apply(ops)
+    s = dev.generate_samples()
+    assert s.shape == (20000, n) and set(np.unique(s)) <= {0, 1}
+    assert np.all(s[:, 0] == s[:, 1])
+    tape = Q.QuantumTape(ops, [Q.expval(Q.PauliZ(0)), Q.expval(Q.PauliX(2))])
+    r = dev.execute(tape)
+    assert abs(r[0] - np.cos(1.1)) < 0.03
+    assert abs(r[1]) < 0.03
+
+
+@pytest.mark.parametrize("split", [False, True])
+def test_adjoint_jacobian_vs_oracle_and_fd(oracle, split):
+    rng = np.random.default_rng(2)
+    n = 5
+    ops = [Q.op("RX", w, rng.uniform(0, 6)) for w in range(n)]
+    ops += [Q.op("CNOT", [0, 1]), Q.op("CRY", [1, 3], 0.7), Q.op("Rot", 2, 0.1, 0.8, -0.4),
+            Q.op("IsingZZ", [2, 4], 1.3), Q.op("PhaseShift", 0, 0.5).adjoint(), Q.op("SingleExcitation", [3, 4], 0.9)]
+    H = Q.Hamiltonian([0.4, -1.2, 0.7], [Q.PauliZ(0) @ Q.PauliZ(1), Q.PauliX(3), Q.PauliY(2) @ Q.PauliZ(4)])
+    tape = Q.QuantumTape(ops, [Q.expval(Q.PauliZ(2)), Q.expval(H)])
+    dev = _dev(n)
+    jac = dev.adjoint_jacobian(tape, split_terms=split)
+    # central differences on the device
+    params = [p for o in ops for p in o.parameters]
+
+    def f(ps):
+        k = 0
+        new = []
+        for o in ops:
+            m = len(o.parameters)
+            base = Q.Operation(o.name, o.wires, ps[k:k + m], o._matrix)
+            new.append(base.adjoint() if isinstance(o, Q.Adjoint) else base)
+            k += m
+        return np.array(dev.execute(Q.QuantumTape(new, tape.measurements)))
+
+    h = 1e-4
+    fd = np.zeros_like(jac)
+    for i in range(len(params)):
+        e = np.zeros(len(params))
+        e[i] = h
+        fd[:, i] = (f(np.array(params) + e) - f(np.array(params) - e)) / (2 * h)
+    assert np.max(np.abs(jac - fd)) < 1e-7
+    # oracle adjoint on the serialised (Rot-expanded) ops
+    from pennylane_lightning_gpu_gb300._serialize import _expand_rot
+
+    flat = []
+    for o in ops:
+        flat.extend(_expand_rot(o) if o.name == "Rot" else [o])
+    final = oracle.run(n, _oracle_ops(flat))
+    obs = [(False, [(1.0, [("PauliZ", [2], None)])]),
+           (True, [(0.4, [("PauliZ", [0], None), ("PauliZ", [1], None)]), (-1.2, [("PauliX", [3], None)]),
+                   (0.7, [("PauliY", [2], None), ("PauliZ", [4], None)])])]
+    ref = oracle.adjoint_jacobian(final, _oracle_ops(flat), obs, list(range(len(params))))
+    assert np.max(np.abs(jac - ref)) < 1e-10
+
+
+def test_vjp(oracle):
+    rng = np.random.default_rng(3)
+    n = 4
+    ops = [Q.op("RY", w, rng.uniform(0, 6)) for w in range(n)] + [Q.op("CZ", [0, 1]), Q.op("RZ", 1, 0.3)]
+    meas = [Q.expval(Q.PauliZ(0)), Q.expval(Q.PauliX(1) @ Q.PauliY(2))]
+    tape = Q.QuantumTape(ops, meas)
+    dev = _dev(n)
+    dy = np.array([0.7, -1.3])
+    v = dev.vjp(meas, dy)(tape)
+    jac = dev.adjoint_jacobian(tape)
+    assert np.allclose(v, dy @ jac, atol=1e-10)
+
+
+def test_adjoint_rejects_unsupported():
+    from pennylane_lightning_gpu_gb300.lightning_gpu import QuantumFunctionError
+
+    dev = _dev(2)
+    tape = Q.QuantumTape([Q.op("RX", 0, 0.1)], [Q.var(Q.PauliZ(0))])
+    with pytest.raises(QuantumFunctionError):
+        dev.adjoint_jacobian(tape)
+    tape = Q.QuantumTape([Q.op("RX", 0, 0.1)], [Q.expval(Q.Hermitian(np.eye(2), [0]))])
+    with pytest.raises(QuantumFunctionError):
+        dev.adjoint_jacobian(tape)
+
+
+def test_mpi_rejected():
+    from pennylane_lightning_gpu_gb300.lightning_gpu import DeviceError
+
+    with pytest.raises(DeviceError):
+        _dev(2, mpi=True)
