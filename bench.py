@@ -212,6 +212,11 @@ def run_ours(args):
         g, _, _, _, sv = gate_sweep(m, "LightningGPU_C64", n, max(2, args.steps // 2), 2, f64_mode=default_mode)
         variants["c64_gbs"] = round(g, 1)
         del sv
+        m.set_stream_mode(0)
+        g, _, _, _, sv = gate_sweep(m, "LightningGPU_C128", n, max(2, args.steps // 2), 2, f64_mode=default_mode)
+        variants["c128_gridstride_kernel_gbs"] = round(g, 1)
+        del sv
+        m.set_stream_mode(1)
         torch.cuda.synchronize()
 
     clocks = ClockSampler()
@@ -241,13 +246,15 @@ def run_ours(args):
         "config": {"workload": "dense 1-qubit gates (H and RX) on each target of a 28-qubit complex128 state",
                    "qubits": n, "state_bytes": S, "gates_per_step": len(gates),
                    "f64_mode": "fp64 fma + integer-pipe multiply" if default_mode == 1 else "native fp64",
+                   "kernel_family": "bulk-copy pipelined tiles" if m.get_stream_mode() == 1 else "grid-stride",
                    "l2": "state (4 GiB) larger than L2 (129 MB): no flush needed"},
         "e2e": {"value": round(e2e_value, 1), "unit": "GB/s", "h2d_bytes_per_step": 8 * n,
                 "d2h_bytes_per_step": 16},
         "gpu_launches": len(gates) * args.steps,
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": None, "peak_source": peak_kind,
-                     "kernel": "gate1_kernel", "algorithmic_bytes_per_launch": 2 * S},
+                     "kernel": "gate1_bulk_kernel" if m.get_stream_mode() == 1 else "gate1_kernel",
+                     "algorithmic_bytes_per_launch": 2 * S},
         "variants": variants,
         "per_target_gbs": per_target,
         "clocks": clk,

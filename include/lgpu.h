@@ -73,6 +73,20 @@ const char *lgpu_last_error_string(void);
 lgpu_status_t lgpu_set_f64_mode(int mode);
 int lgpu_get_f64_mode(void);
 
+/* Kernel family for uncontrolled 1-target gates on states of >= 13 (c128) /
+ * 14 (c64) qubits (process-wide): 1 (default) = persistent CTAs streaming
+ * 64 KB tiles through a 3-stage shared-memory ring with cp.async.bulk loads
+ * and stores; 0 = grid-stride kernel.  LGPU_BULK=0 selects 0 at start-up.
+ * No counterpart in the reference. */
+lgpu_status_t lgpu_set_stream_mode(int mode);
+int lgpu_get_stream_mode(void);
+
+/* Device-side error flag of the engine's bounded waits (1 = a kernel gave up
+ * waiting for a bulk copy and left its tile unprocessed).  reset != 0 clears
+ * it.  The C++ layer checks it at every synchronisation point.  No
+ * counterpart in the reference. */
+lgpu_status_t lgpu_device_error(int *code, int reset);
+
 /* ---- device and memory (DataBuffer.hpp:31-218, cuda_helpers.hpp:796-837,
  *      Bindings.cpp:1736-1748; the C++ layer needs no CUDA runtime of its own) */
 lgpu_status_t lgpu_device_count(int *count);

@@ -530,6 +530,10 @@ PYBIND11_MODULE(lightning_gpu_qubit_ops, m) {
         "set_f64_mode", [](int mode) { PL_LGPU_IS_SUCCESS(lgpu_set_f64_mode(mode)); },
         "complex128 arithmetic of the streaming gate kernels: 0 native FP64, 1 FP64 FMA + integer-pipe multiplies");
     m.def("get_f64_mode", &lgpu_get_f64_mode);
+    m.def(
+        "set_stream_mode", [](int mode) { PL_LGPU_IS_SUCCESS(lgpu_set_stream_mode(mode)); },
+        "1-target gate kernels: 1 bulk-copy pipelined tiles, 0 grid-stride");
+    m.def("get_stream_mode", &lgpu_get_stream_mode);
 
     py::class_<DevPool>(m, "DevPool")
         .def(py::init<>())

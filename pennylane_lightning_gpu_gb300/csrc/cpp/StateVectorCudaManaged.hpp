@@ -552,7 +552,12 @@ class StateVectorCudaManaged : public StateVectorCudaBase<Precision, StateVector
     }
 
     // ---- misc -------------------------------------------------------------------
-    void sync() const { PL_LGPU_IS_SUCCESS(lgpu_stream_sync(BaseType::lstream())); }
+    void sync() const {
+        PL_LGPU_IS_SUCCESS(lgpu_stream_sync(BaseType::lstream()));
+        int code = 0;
+        PL_LGPU_IS_SUCCESS(lgpu_device_error(&code, 1));
+        PL_ABORT_IF(code != 0, "A GPU kernel timed out waiting for a bulk copy; the state is invalid");
+    }
     lgpu_context_t ctx() const { return ctx_->get(); }
     static constexpr lgpu_dtype_t dt() { return cuUtil::dtype_of<Precision>(); }
     uint32_t nq() const { return uint32_t(BaseType::getNumQubits()); }

@@ -37,6 +37,18 @@ int f64_mode() {
     return m;
 }
 
+static std::atomic<int> g_bulk_mode{-1};
+
+int bulk_enabled() {
+    int m = g_bulk_mode.load(std::memory_order_relaxed);
+    if (m < 0) {
+        const char *e = std::getenv("LGPU_BULK");
+        m = (e && e[0] == '0') ? 0 : 1;
+        g_bulk_mode.store(m, std::memory_order_relaxed);
+    }
+    return m;
+}
+
 int current_device() {
     int d = 0;
     cudaGetDevice(&d);
@@ -228,6 +240,14 @@ lgpu_status_t lgpu_set_f64_mode(int mode) {
 }
 
 int lgpu_get_f64_mode(void) { return f64_mode(); }
+
+lgpu_status_t lgpu_set_stream_mode(int mode) {
+    if (mode != 0 && mode != 1) return fail(LGPU_ERR_INVALID_ARG, "stream mode must be 0 or 1");
+    g_bulk_mode.store(mode, std::memory_order_relaxed);
+    return LGPU_OK;
+}
+
+int lgpu_get_stream_mode(void) { return bulk_enabled(); }
 
 const char *lgpu_last_error_string(void) { return g_last_error.c_str(); }
 

@@ -150,6 +150,185 @@ __global__ void __launch_bounds__(kGateBlock)
     }
 }
 
+// ---------------------------------------------------------------------------
+// Bulk-copy pipelined variant for uncontrolled 1-target gates.
+//
+// Persistent CTAs (one per SM) stream tiles of 2*CH amplitudes through a ring
+// of STAGES shared-memory buffers.  Loads are 1-D cp.async.bulk copies (TMA
+// engine) that complete on an mbarrier with a transaction count; stores are
+// bulk copies back to global memory.  For a target bit t >= log2(CH) a tile
+// is two runs of CH amplitudes 2^t apart (bit t = 0 and 1); otherwise a tile
+// is one contiguous run of 2*CH amplitudes with the pairs interleaved.  Every
+// wait is bounded: on time-out the CTA records an error in
+// g_lgpu_device_error and leaves.
+// ---------------------------------------------------------------------------
+__device__ unsigned int g_lgpu_device_error = 0;
+
+constexpr int kBulkThreads = 512;
+constexpr int kBulkStages = 3;
+constexpr uint32_t kWaitLimit = 1u << 24;  // try_wait polls before giving up
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+__device__ __forceinline__ void bulk_load(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
+__device__ __forceinline__ void bulk_store(void *dst, const void *src, uint32_t bytes) {
+    asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(dst), "r"(smem_u32(src)),
+                 "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void bulk_wait_read1() { asm volatile("cp.async.bulk.wait_group.read 1;" ::: "memory"); }
+__device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
+__device__ __forceinline__ void fence_async_shared() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+template <class T> struct BulkParams {
+    uint64_t ntiles;
+    int t;           // target bit
+    int ch_log2;     // log2(CH)
+    T m[8];
+    KConst k[4];
+};
+
+template <class T, int BODY, bool EMU>
+__global__ void __launch_bounds__(kBulkThreads, 1)
+    gate1_bulk_kernel(cplx_t<T> *__restrict__ sv, const BulkParams<T> p) {
+    using C = cplx_t<T>;
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    __shared__ __align__(8) uint64_t full_bar[kBulkStages];
+    C *ring = reinterpret_cast<C *>(smem_raw);
+    const uint32_t CH = 1u << p.ch_log2;
+    const uint32_t half_bytes = CH * uint32_t(sizeof(C));
+    const bool split = p.t >= p.ch_log2;
+    const uint64_t G = gridDim.x;
+    T m[8];
+#pragma unroll
+    for (int q = 0; q < 8; q++) m[q] = p.m[q];
+    KConst kc[4];
+#pragma unroll
+    for (int q = 0; q < 4; q++) kc[q] = p.k[q];
+
+    // global amplitude index of the start of each half of tile `tile`
+    auto tile_base = [&](uint64_t tile) -> uint64_t {
+        if (!split) return tile << (p.ch_log2 + 1);
+        const int hb = p.t - p.ch_log2;  // bit of the block index that is the target bit
+        const uint64_t lo = tile & ((uint64_t(1) << hb) - 1);
+        return (((tile >> hb) << (hb + 1)) | lo) << p.ch_log2;
+    };
+    auto issue_load = [&](uint64_t tile, int s) {
+        C *buf = ring + size_t(s) * 2 * CH;
+        const uint64_t b0 = tile_base(tile);
+        mbar_expect_tx(&full_bar[s], 2 * half_bytes);
+        if (split) {
+            bulk_load(buf, sv + b0, half_bytes, &full_bar[s]);
+            bulk_load(buf + CH, sv + b0 + (uint64_t(1) << p.t), half_bytes, &full_bar[s]);
+        } else {
+            bulk_load(buf, sv + b0, 2 * half_bytes, &full_bar[s]);
+        }
+    };
+    auto issue_store = [&](uint64_t tile, int s) {
+        C *buf = ring + size_t(s) * 2 * CH;
+        const uint64_t b0 = tile_base(tile);
+        if (split) {
+            bulk_store(sv + b0, buf, half_bytes);
+            bulk_store(sv + b0 + (uint64_t(1) << p.t), buf + CH, half_bytes);
+        } else {
+            bulk_store(sv + b0, buf, 2 * half_bytes);
+        }
+        bulk_commit();
+    };
+
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int s = 0; s < kBulkStages; s++) mbar_init(&full_bar[s], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < kBulkStages; s++) {
+            const uint64_t tile = blockIdx.x + uint64_t(s) * G;
+            if (tile < p.ntiles) issue_load(tile, s);
+        }
+    }
+    bool failed = false;
+    for (uint64_t j = 0;; j++) {
+        const uint64_t tile = blockIdx.x + j * G;
+        if (tile >= p.ntiles) break;
+        const int s = int(j % kBulkStages);
+        const uint32_t parity = uint32_t((j / kBulkStages) & 1);
+        uint32_t spins = 0;
+        bool timed_out = false;
+        while (!mbar_try_wait(&full_bar[s], parity)) {
+            if (++spins > kWaitLimit) {
+                timed_out = true;
+                break;
+            }
+        }
+        // Every thread leaves its bounded wait; the CTA then decides together.
+        failed = __syncthreads_or(timed_out) != 0;
+        if (failed) {
+            if (threadIdx.x == 0) atomicOr(&g_lgpu_device_error, 1u);
+            break;
+        }
+        C *buf = ring + size_t(s) * 2 * CH;
+        if (split) {
+            for (uint32_t q = threadIdx.x; q < CH; q += kBulkThreads) {
+                C a0 = buf[q], a1 = buf[CH + q];
+                body1_sel<T, BODY, EMU>(m, kc, a0, a1);
+                buf[q] = a0;
+                buf[CH + q] = a1;
+            }
+        } else {
+            const uint32_t lo = (1u << p.t) - 1;
+            for (uint32_t q = threadIdx.x; q < CH; q += kBulkThreads) {
+                const uint32_t e0 = ((q & ~lo) << 1) | (q & lo), e1 = e0 | (1u << p.t);
+                C a0 = buf[e0], a1 = buf[e1];
+                body1_sel<T, BODY, EMU>(m, kc, a0, a1);
+                buf[e0] = a0;
+                buf[e1] = a1;
+            }
+        }
+        fence_async_shared();
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            issue_store(tile, s);
+            if (j >= 1) {
+                // refill the previous stage once its store has finished reading it
+                const uint64_t jp = j - 1;
+                const uint64_t next = blockIdx.x + (jp + kBulkStages) * G;
+                if (next < p.ntiles) {
+                    bulk_wait_read1();
+                    issue_load(next, int(jp % kBulkStages));
+                }
+            }
+        }
+    }
+    if (threadIdx.x == 0) bulk_wait_all();
+}
+
 template <class T, class I> struct PhaseParams {
     Holes holes;
     I set;  // bits forced to 1
@@ -456,6 +635,42 @@ static void launch_gate1(cplx_t<T> *sv, const G1Params<T, I> &p, unsigned nstate
     gate1_kernel<T, I, BODY, ITEMS, false><<<grid, kGateBlock, 0, s>>>(sv, p, nstates, svs);
 }
 
+template <class T, int BODY, bool EMU>
+static lgpu_status_t launch_bulk_t(cplx_t<T> *sv, const BulkParams<T> &bp, cudaStream_t s) {
+    const size_t smem = size_t(kBulkStages) * (size_t(2) << bp.ch_log2) * sizeof(cplx_t<T>);
+    static bool attr_set = false;  // per instantiation; set once (idempotent)
+    if (!attr_set) {
+        cudaError_t e = cudaFuncSetAttribute(gate1_bulk_kernel<T, BODY, EMU>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+        if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(gate1_bulk)");
+        attr_set = true;
+    }
+    const unsigned grid = unsigned(std::min<uint64_t>(bp.ntiles, uint64_t(sm_count())));
+    gate1_bulk_kernel<T, BODY, EMU><<<grid, kBulkThreads, smem, s>>>(sv, bp);
+    LGPU_CHECK_LAUNCH();
+    return LGPU_OK;
+}
+
+template <class T, bool EMU>
+static lgpu_status_t launch_bulk_body(cplx_t<T> *sv, const BulkParams<T> &bp, int body, cudaStream_t s) {
+    switch (body) {
+    case B_DIAG: return launch_bulk_t<T, B_DIAG, EMU>(sv, bp, s);
+    case B_PERM: return launch_bulk_t<T, B_PERM, false>(sv, bp, s);
+    case B_ANTIDIAG: return launch_bulk_t<T, B_ANTIDIAG, EMU>(sv, bp, s);
+    case B_REAL: return launch_bulk_t<T, B_REAL, EMU>(sv, bp, s);
+    case B_RXLIKE: return launch_bulk_t<T, B_RXLIKE, EMU>(sv, bp, s);
+    default: return launch_bulk_t<T, B_DENSE, false>(sv, bp, s);
+    }
+}
+
+template <class T>
+static lgpu_status_t launch_gate1_bulk(cplx_t<T> *sv, const BulkParams<T> &bp, int body, cudaStream_t s) {
+    if constexpr (sizeof(T) == 8) {
+        if (f64_mode() == 1) return launch_bulk_body<T, true>(sv, bp, body, s);
+    }
+    return launch_bulk_body<T, false>(sv, bp, body, s);
+}
+
 template <class T, class I>
 static lgpu_status_t run_gate1(cplx_t<T> *sv, unsigned nstates, cplx_t<T> *const *svs, uint32_t n,
                                const Cm m[4], const GateGeometry &g, cudaStream_t s) {
@@ -516,6 +731,20 @@ static lgpu_status_t run_gate1(cplx_t<T> *sv, unsigned nstates, cplx_t<T> *const
     } else if (rxlike) {
         p.k[0] = make_kconst(-m[1].im); p.k[1] = make_kconst(m[1].im);
         p.k[2] = make_kconst(-m[2].im); p.k[3] = make_kconst(m[2].im);
+    }
+    if (nstates == 0 && g.ctrls.empty() && bulk_enabled()) {
+        const int ch_log2 = sizeof(T) == 8 ? 11 : 12;  // 32 KB halves, 64 KB tiles
+        if (int(n) >= ch_log2 + 2) {
+            BulkParams<T> bp{};
+            bp.ntiles = (uint64_t(1) << n) >> (ch_log2 + 1);
+            bp.t = tb;
+            bp.ch_log2 = ch_log2;
+            for (int q = 0; q < 8; q++) bp.m[q] = p.m[q];
+            for (int q = 0; q < 4; q++) bp.k[q] = p.k[q];
+            const int body = diag ? B_DIAG : (anti && eq(m[1], 1, 0) && eq(m[2], 1, 0)) ? B_PERM : anti ? B_ANTIDIAG
+                             : real ? B_REAL : rxlike ? B_RXLIKE : B_DENSE;
+            return launch_gate1_bulk<T>(sv, bp, body, s);
+        }
     }
     if (diag)
         launch_gate1<T, I, B_DIAG>(sv, p, nstates, svs, s);
@@ -807,6 +1036,18 @@ static lgpu_status_t fused_t(cplx_t<T> *sv, uint32_t n, const std::vector<int> &
 using namespace lgpu;
 
 extern "C" {
+
+lgpu_status_t lgpu_device_error(int *code, int reset) {
+    if (!code) return fail(LGPU_ERR_INVALID_ARG, "code is null");
+    unsigned v = 0;
+    LGPU_CUDA_TRY(cudaMemcpyFromSymbol(&v, g_lgpu_device_error, sizeof(v)));
+    *code = int(v);
+    if (reset && v) {
+        unsigned z = 0;
+        LGPU_CUDA_TRY(cudaMemcpyToSymbol(g_lgpu_device_error, &z, sizeof(z)));
+    }
+    return LGPU_OK;
+}
 
 lgpu_status_t lgpu_apply_matrix(void *sv, uint32_t n, lgpu_dtype_t dt, const double *matrix, uint32_t t,
                                 const int32_t *tgts, uint32_t c, const int32_t *ctrls,

@@ -47,6 +47,9 @@ int current_device();
 // complex128 arithmetic mode: 0 = native FP64, 1 = FP64 FMA + integer-pipe
 // multiplies (lgpu_f64emu.cuh).  Process-wide; see lgpu_set_f64_mode().
 int f64_mode();
+// Uncontrolled 1-target gates use the bulk-copy pipelined kernel when 1
+// (default); the grid-stride kernel when 0.  See lgpu_set_stream_mode().
+int bulk_enabled();
 
 // ---------------------------------------------------------------------------
 // Scratch context

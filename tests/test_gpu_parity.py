@@ -386,3 +386,31 @@ def test_f64_mode_bits_close(native):
     finally:
         native.set_f64_mode(old)
     assert np.max(np.abs(out[0] - out[1])) < 1e-13
+
+
+@pytest.mark.parametrize("dtype", DTYPES)
+@pytest.mark.parametrize("n", [14, 16])
+def test_bulk_stream_kernel_all_targets(native, oracle, dtype, n):
+    """The bulk-copy pipelined 1-target kernel (split and interleaved tiles,
+    every body) against the oracle and the grid-stride kernel."""
+    rng = np.random.default_rng(900 + n)
+    psi = random_state(n, rng)
+    gates = [("Hadamard", []), ("RX", [0.3]), ("RY", [1.1]), ("RZ", [2.2]), ("PauliX", []), ("PauliY", []),
+             ("Rot", [0.2, 0.5, 0.9])]
+    ops = []
+    for w in range(n):
+        g, par = gates[w % len(gates)]
+        ops.append((g, [w], par, bool(w % 2)))
+    old = native.get_stream_mode()
+    outs = []
+    try:
+        for mode in (1, 0):
+            native.set_stream_mode(mode)
+            sv = make_sv(native, dtype, psi)
+            apply_ops(sv, ops)
+            outs.append(sv.GetState())
+    finally:
+        native.set_stream_mode(old)
+    ref = oracle.apply_ops(psi, to_oracle_ops(ops))
+    assert np.max(np.abs(outs[0] - ref)) < tol(dtype)
+    assert np.max(np.abs(outs[1] - ref)) < tol(dtype)
