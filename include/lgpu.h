@@ -258,6 +258,75 @@ lgpu_status_t lgpu_adjoint_step(lgpu_context_t ctx, void *ket, void *const *bras
                                 const double *gen, const double *udag, int apply_udag,
                                 double *out_dev, lgpu_stream_t stream);
 
+/* ---- CUDA graphs (stream capture) ------------------------------------------
+ * Capture everything issued on `stream` between begin and end into an
+ * executable graph; launch replays it on any stream. */
+typedef struct lgpu_graph_s *lgpu_graph_t;
+lgpu_status_t lgpu_graph_begin(lgpu_stream_t stream);
+lgpu_status_t lgpu_graph_end(lgpu_stream_t stream, lgpu_graph_t *graph);
+lgpu_status_t lgpu_graph_launch(lgpu_graph_t graph, lgpu_stream_t stream);
+lgpu_status_t lgpu_graph_destroy(lgpu_graph_t graph);
+
+/* ---- batched circuits (one persistent launch) --------------------------------
+ * Many independent circuits run in one launch of a persistent kernel.  The
+ * host lowers and fuses each circuit into blocks of gates whose targets fit a
+ * shared-memory tile of 2^k amplitudes (k <= kmax; a circuit with n <= kmax
+ * qubits is a single block holding the whole state) and uploads the records
+ * below.  Gate matrices live in a device pool; parametric ones are rebuilt
+ * from a device parameter array by lgpu_batch_prepare, so a captured graph
+ * [params H2D, prepare, counter reset, run, results D2H] can be replayed with
+ * new parameters.  No counterpart in the reference (it runs one circuit per
+ * device call). */
+typedef struct {
+    uint8_t kind;      /* 0 dense 1q, 1 diagonal 1q, 2 X, 3 real 1q, 4 RX-like 1q, 5 dense 2q, 6 SWAP */
+    uint8_t pkind;     /* 0 fixed matrix, 1 RX, 2 RY, 3 RZ, 4 PhaseShift, 5 Rot, 6 IsingXX, 7 IsingYY, 8 IsingZZ */
+    uint8_t q0, q1;    /* tile positions of the targets, q0 = most significant matrix bit */
+    uint32_t cmask;    /* controls inside the tile (tile positions) and their values */
+    uint32_t cval;
+    int32_t param;     /* index of the first parameter (-1: none) */
+    uint32_t flags;    /* bit 0: adjoint (parametric gates) */
+    uint32_t mat;      /* offset of the gate's slot in the pool, in doubles (16 for 1q, 32 for 2q) */
+    uint64_t omask;    /* controls outside the tile (state bits) and their values */
+    uint64_t oval;
+} lgpu_bgate_t;
+
+typedef struct {
+    uint32_t n, block_off, block_cnt, obs_off, obs_cnt, out;
+} lgpu_bcircuit_t;
+
+typedef struct {
+    uint8_t k, m, pad0, pad1; /* tile bits, length of the low run 0..m-1 (k - m <= 6) */
+    uint8_t bits[16];         /* sorted tile bits */
+    uint32_t gate_off, gate_cnt;
+} lgpu_bblock_t;
+
+typedef struct {
+    uint64_t tflip;  /* X|Y bits of the Pauli word in tile positions of the circuit's last block */
+    uint64_t sign;   /* Y|Z bits (state bits) */
+    double cr, ci;   /* coefficient * i^(number of Y) */
+} lgpu_bterm_t;
+
+typedef struct {
+    const lgpu_bcircuit_t *circuits;
+    const uint32_t *order;   /* processing order (NULL: identity) */
+    uint32_t ncircuits;
+    uint32_t kmax;           /* tile bits, <= 13 (C128) / 14 (C64) */
+    const lgpu_bblock_t *blocks;
+    const lgpu_bgate_t *gates;
+    const double *pool;
+    const lgpu_bterm_t *terms;
+    void *scratch;           /* grid * scratch_amps amplitudes (states above kmax qubits) */
+    uint64_t scratch_amps;
+    unsigned *counter;       /* work-queue counter, zero before each launch */
+    double *out;             /* one result per circuit */
+    uint32_t threads;        /* 128, 256 or 512 */
+    uint32_t pad;
+} lgpu_batch_args_t;
+
+lgpu_status_t lgpu_batch_prepare(const lgpu_bgate_t *gates, uint64_t ngates, const double *params, double *pool,
+                                 lgpu_stream_t stream);
+lgpu_status_t lgpu_batch_run(const lgpu_batch_args_t *args, lgpu_dtype_t dt, unsigned grid, lgpu_stream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

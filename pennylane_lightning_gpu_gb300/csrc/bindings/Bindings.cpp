@@ -10,6 +10,7 @@
 #include <sstream>
 
 #include "AdjointDiffGPU.hpp"
+#include "BatchedExecutor.hpp"
 
 namespace py = pybind11;
 using namespace Pennylane;
@@ -512,6 +513,70 @@ template <class PrecisionT, class ParamT> void sv_class_bindings(py::module_ &m)
             });
 }
 
+template <class PrecisionT> void batched_bindings(py::module_ &m) {
+    using BE = BatchedExecutor<PrecisionT>;
+    const std::string name = std::string("BatchedExecutor_C") + (std::is_same_v<PrecisionT, double> ? "128" : "64");
+    py::class_<BE>(m, name.c_str())
+        .def(py::init<int, int, int>(), py::arg("kmax") = 0, py::arg("threads") = 256, py::arg("grid") = 0)
+        .def(
+            "add_circuit",
+            [](BE &be, size_t n, const std::vector<std::string> &names, const std::vector<std::vector<size_t>> &wires,
+               const std::vector<std::vector<double>> &params, const std::vector<bool> &inverses,
+               const std::vector<std::tuple<double, std::string, std::vector<size_t>>> &obs) {
+                std::vector<typename BE::PTerm> terms;
+                for (const auto &t : obs) terms.push_back({std::get<0>(t), std::get<1>(t), std::get<2>(t)});
+                return be.addCircuit(n, names, wires, params, inverses, terms);
+            },
+            "Add a circuit (ops as names/wires/params/inverses, observable as (coeff, word, wires) terms).")
+        .def("prepare", &BE::prepare, py::call_guard<py::gil_scoped_release>(),
+             "Plan, upload and capture the CUDA graph.")
+        .def(
+            "run",
+            [](BE &be, py::object params) {
+                std::vector<double> out;
+                if (params.is_none()) {
+                    py::gil_scoped_release r;
+                    out = be.run(nullptr);
+                } else {
+                    auto p = params.cast<std::vector<double>>();
+                    py::gil_scoped_release r;
+                    out = be.run(&p);
+                }
+                return py::array_t<double>(out.size(), out.data());
+            },
+            py::arg("params") = py::none(), "Replay the graph and return one result per circuit.")
+        .def(
+            "launch_async",
+            [](BE &be, py::object params) {
+                if (params.is_none()) {
+                    be.launchAsync(nullptr);
+                } else {
+                    auto p = params.cast<std::vector<double>>();
+                    be.launchAsync(&p);
+                }
+            },
+            py::arg("params") = py::none())
+        .def(
+            "wait",
+            [](BE &be) {
+                std::vector<double> out;
+                {
+                    py::gil_scoped_release r;
+                    out = be.wait();
+                }
+                return py::array_t<double>(out.size(), out.data());
+            })
+        .def("num_params", &BE::numParams)
+        .def("num_circuits", &BE::numCircuits)
+        .def("param_offset", &BE::paramOffset)
+        .def("params", [](const BE &be) { return be.params(); })
+        .def("num_gates", &BE::numGates)
+        .def("num_blocks", &BE::numBlocks)
+        .def("grid", &BE::grid)
+        .def("kmax", &BE::kmax)
+        .def("scratch_bytes", &BE::scratchBytes);
+}
+
 } // namespace
 
 PYBIND11_MODULE(lightning_gpu_qubit_ops, m) {
@@ -560,4 +625,6 @@ PYBIND11_MODULE(lightning_gpu_qubit_ops, m) {
 
     sv_class_bindings<float, float>(m);
     sv_class_bindings<double, double>(m);
+    batched_bindings<float>(m);
+    batched_bindings<double>(m);
 }

@@ -1,0 +1,354 @@
+// liblgpu_gb300: batched execution of many independent circuits in one
+// persistent launch.
+//
+//  * bprep_kernel   builds every gate's matrix (and, for complex128, the
+//                   integer-pipe multiplier constants) from a device parameter
+//                   buffer, so that a captured CUDA graph can be replayed with
+//                   new parameters by copying only the parameter buffer.
+//  * batch_kernel   persistent CTAs take circuits from an atomic work queue
+//                   (host orders them largest first).  A circuit with
+//                   n <= kmax qubits lives entirely in shared memory; a larger
+//                   one is streamed through shared-memory tiles block by block
+//                   (the host fuses its gates into blocks whose targets fit a
+//                   tile) using a per-CTA scratch state in global memory.  The
+//                   observable (a sum of Pauli words) is evaluated on the
+//                   tiles of the last block and reduced inside the CTA, so each
+//                   result is written by exactly one CTA in a fixed order.
+#include "lgpu_f64emu.cuh"
+#include "lgpu_internal.cuh"
+
+namespace lgpu {
+
+// body kinds
+enum BKind : uint8_t { BK_DENSE1 = 0, BK_DIAG1, BK_X1, BK_REAL1, BK_RXLIKE1, BK_DENSE2, BK_SWAP2 };
+// parameter kinds (matrix built on device)
+enum PKind : uint8_t { PK_NONE = 0, PK_RX, PK_RY, PK_RZ, PK_PHASE, PK_ROT, PK_ISINGXX, PK_ISINGYY, PK_ISINGZZ };
+
+static_assert(sizeof(lgpu_bgate_t) == 40, "lgpu_bgate_t layout");
+
+// ---------------------------------------------------------------------------
+// Matrix preparation
+// ---------------------------------------------------------------------------
+__global__ void bprep_kernel(const lgpu_bgate_t *__restrict__ gates, uint64_t ngates, const double *__restrict__ params,
+                             double *__restrict__ pool) {
+    const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
+    for (uint64_t gi = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; gi < ngates; gi += stride) {
+        const lgpu_bgate_t g = gates[gi];
+        double *m = pool + g.mat;
+        const bool adj = (g.flags & 1u) != 0;
+        if (g.pkind != PK_NONE) {
+            const double th0 = params[g.param];
+            const double th = adj ? -th0 : th0;
+            if (g.pkind == PK_RX || g.pkind == PK_RY || g.pkind == PK_RZ || g.pkind == PK_PHASE) {
+                double s, c;
+                if (g.pkind == PK_PHASE) {
+                    sincos(th, &s, &c);
+                    m[0] = 1; m[1] = 0; m[2] = 0; m[3] = 0; m[4] = 0; m[5] = 0; m[6] = c; m[7] = s;
+                } else {
+                    sincos(0.5 * th, &s, &c);
+                    if (g.pkind == PK_RX) {
+                        m[0] = c; m[1] = 0; m[2] = 0; m[3] = -s; m[4] = 0; m[5] = -s; m[6] = c; m[7] = 0;
+                    } else if (g.pkind == PK_RY) {
+                        m[0] = c; m[1] = 0; m[2] = -s; m[3] = 0; m[4] = s; m[5] = 0; m[6] = c; m[7] = 0;
+                    } else {
+                        m[0] = c; m[1] = -s; m[2] = 0; m[3] = 0; m[4] = 0; m[5] = 0; m[6] = c; m[7] = s;
+                    }
+                }
+            } else if (g.pkind == PK_ROT) {
+                // Rot(phi, theta, omega) = RZ(omega) RY(theta) RZ(phi); adjoint = Rot(-omega, -theta, -phi)
+                double phi = params[g.param], theta = params[g.param + 1], omega = params[g.param + 2];
+                if (adj) {
+                    const double t = phi;
+                    phi = -omega;
+                    theta = -theta;
+                    omega = -t;
+                }
+                double cs, sn, cp, sp, cm, sm;
+                sincos(0.5 * theta, &sn, &cs);
+                sincos(0.5 * (phi + omega), &sp, &cp);
+                sincos(0.5 * (phi - omega), &sm, &cm);
+                m[0] = cs * cp; m[1] = -cs * sp;
+                m[2] = -sn * cm; m[3] = -sn * sm;
+                m[4] = sn * cm; m[5] = -sn * sm;
+                m[6] = cs * cp; m[7] = cs * sp;
+            } else {
+                double s, c;
+                sincos(0.5 * th, &s, &c);
+                for (int e = 0; e < 32; e++) m[e] = 0.0;
+                if (g.pkind == PK_ISINGZZ) {
+                    // diag(e^{-i t/2}, e^{i t/2}, e^{i t/2}, e^{-i t/2})
+                    m[0] = c; m[1] = -s; m[10] = c; m[11] = s; m[20] = c; m[21] = s; m[30] = c; m[31] = -s;
+                } else {
+                    const double corner = g.pkind == PK_ISINGXX ? -s : s;  // YY: +i s at (0,3),(3,0)
+                    for (int d = 0; d < 4; d++) m[2 * (d * 4 + d)] = c;
+                    m[2 * (0 * 4 + 3) + 1] = corner;
+                    m[2 * (3 * 4 + 0) + 1] = corner;
+                    m[2 * (1 * 4 + 2) + 1] = -s;
+                    m[2 * (2 * 4 + 1) + 1] = -s;
+                }
+            }
+        }
+        // (fixed matrices arrive from the host already in their final, adjointed form)
+        // integer-pipe multiplier constants for the complex128 structured bodies
+        if (g.kind < BK_DENSE2) {
+            KConst *k = reinterpret_cast<KConst *>(m + 8);
+            if (g.kind == BK_DIAG1) {
+                k[0] = make_kconst(-m[1]); k[1] = make_kconst(m[1]); k[2] = make_kconst(-m[7]); k[3] = make_kconst(m[7]);
+            } else if (g.kind == BK_REAL1) {
+                k[0] = make_kconst(m[2]); k[1] = make_kconst(m[4]); k[2] = make_kconst(0.0); k[3] = make_kconst(0.0);
+            } else if (g.kind == BK_RXLIKE1) {
+                k[0] = make_kconst(-m[3]); k[1] = make_kconst(m[3]); k[2] = make_kconst(-m[5]); k[3] = make_kconst(m[5]);
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// In-shared-memory gate bodies
+// ---------------------------------------------------------------------------
+template <class T, bool EMU>
+__device__ __forceinline__ void apply1(uint8_t kind, const double *m, cplx_t<T> &a0, cplx_t<T> &a1) {
+    using C = cplx_t<T>;
+    const C x = a0, y = a1;
+    if (kind == BK_X1) {
+        a0 = y;
+        a1 = x;
+        return;
+    }
+    if constexpr (EMU && sizeof(T) == 8) {
+        const KConst *k = reinterpret_cast<const KConst *>(m + 8);
+        const double2 xd = reinterpret_cast<const double2 &>(x), yd = reinterpret_cast<const double2 &>(y);
+        double2 r0, r1;
+        if (kind == BK_DIAG1) {
+            r0 = make_double2(__fma_rn(m[0], xd.x, emul(xd.y, k[0])), __fma_rn(m[0], xd.y, emul(xd.x, k[1])));
+            r1 = make_double2(__fma_rn(m[6], yd.x, emul(yd.y, k[2])), __fma_rn(m[6], yd.y, emul(yd.x, k[3])));
+        } else if (kind == BK_REAL1) {
+            r0 = make_double2(__fma_rn(m[0], xd.x, emul(yd.x, k[0])), __fma_rn(m[0], xd.y, emul(yd.y, k[0])));
+            r1 = make_double2(__fma_rn(m[6], yd.x, emul(xd.x, k[1])), __fma_rn(m[6], yd.y, emul(xd.y, k[1])));
+        } else if (kind == BK_RXLIKE1) {
+            r0 = make_double2(__fma_rn(m[0], xd.x, emul(yd.y, k[0])), __fma_rn(m[0], xd.y, emul(yd.x, k[1])));
+            r1 = make_double2(__fma_rn(m[0], yd.x, emul(xd.y, k[2])), __fma_rn(m[0], yd.y, emul(xd.x, k[3])));
+        } else {
+            r0.x = m[0] * xd.x - m[1] * xd.y + m[2] * yd.x - m[3] * yd.y;
+            r0.y = m[0] * xd.y + m[1] * xd.x + m[2] * yd.y + m[3] * yd.x;
+            r1.x = m[4] * xd.x - m[5] * xd.y + m[6] * yd.x - m[7] * yd.y;
+            r1.y = m[4] * xd.y + m[5] * xd.x + m[6] * yd.y + m[7] * yd.x;
+        }
+        a0 = reinterpret_cast<const C &>(r0);
+        a1 = reinterpret_cast<const C &>(r1);
+    } else {
+        const T m0 = T(m[0]), m1 = T(m[1]), m2 = T(m[2]), m3 = T(m[3]), m4 = T(m[4]), m5 = T(m[5]), m6 = T(m[6]),
+                m7 = T(m[7]);
+        if (kind == BK_DIAG1) {
+            a0 = mk<T>(m0 * x.x - m1 * x.y, m0 * x.y + m1 * x.x);
+            a1 = mk<T>(m6 * y.x - m7 * y.y, m6 * y.y + m7 * y.x);
+        } else {
+            a0 = mk<T>(m0 * x.x - m1 * x.y + m2 * y.x - m3 * y.y, m0 * x.y + m1 * x.x + m2 * y.y + m3 * y.x);
+            a1 = mk<T>(m4 * x.x - m5 * x.y + m6 * y.x - m7 * y.y, m4 * x.y + m5 * x.x + m6 * y.y + m7 * y.x);
+        }
+    }
+}
+
+// Apply one gate to the tile in shared memory (all threads).
+template <class T, bool EMU>
+__device__ __forceinline__ void tile_gate(cplx_t<T> *tile, int E, const lgpu_bgate_t &g, const double *pool) {
+    using C = cplx_t<T>;
+    const double *m = pool + g.mat;
+    if (g.kind < BK_DENSE2) {
+        const int q = g.q0;
+        const int lo = (1 << q) - 1;
+        for (int pr = threadIdx.x; pr < (E >> 1); pr += blockDim.x) {
+            const int e0 = ((pr & ~lo) << 1) | (pr & lo);
+            if ((uint32_t(e0) & g.cmask) != g.cval) continue;
+            const int e1 = e0 | (1 << q);
+            C a0 = tile[e0], a1 = tile[e1];
+            apply1<T, EMU>(g.kind, m, a0, a1);
+            tile[e0] = a0;
+            tile[e1] = a1;
+        }
+    } else {
+        const int qa = g.q0, qb = g.q1;
+        const int lo_b = min(qa, qb), hi_b = max(qa, qb);
+        const int lm1 = (1 << lo_b) - 1, lm2 = (1 << hi_b) - 1;
+        for (int pr = threadIdx.x; pr < (E >> 2); pr += blockDim.x) {
+            int e = ((pr & ~lm1) << 1) | (pr & lm1);
+            e = ((e & ~lm2) << 1) | (e & lm2);
+            if ((uint32_t(e) & g.cmask) != g.cval) continue;
+            const int i0 = e, i1 = e | (1 << qb), i2 = e | (1 << qa), i3 = e | (1 << qa) | (1 << qb);
+            if (g.kind == BK_SWAP2) {
+                const C t = tile[i1];
+                tile[i1] = tile[i2];
+                tile[i2] = t;
+                continue;
+            }
+            const C a[4] = {tile[i0], tile[i1], tile[i2], tile[i3]};
+            C r[4];
+#pragma unroll
+            for (int row = 0; row < 4; row++) {
+                double xr = 0, xi = 0;
+#pragma unroll
+                for (int c = 0; c < 4; c++) {
+                    const double mr = m[2 * (row * 4 + c)], mi = m[2 * (row * 4 + c) + 1];
+                    xr += mr * double(a[c].x) - mi * double(a[c].y);
+                    xi += mr * double(a[c].y) + mi * double(a[c].x);
+                }
+                r[row] = mk<T>(T(xr), T(xi));
+            }
+            tile[i0] = r[0];
+            tile[i1] = r[1];
+            tile[i2] = r[2];
+            tile[i3] = r[3];
+        }
+    }
+}
+
+// Observable contribution of one tile: sum over terms of Re(c_t sum_e conj(a_e) sigma_t(g(e^F)) a_{e^F}),
+// flip masks given in tile positions (tflip) and global sign masks.
+template <class T>
+__device__ __forceinline__ double tile_obs(const cplx_t<T> *tile, int E, const lgpu_bterm_t *terms, uint32_t nterms,
+                                           uint64_t base, int m, const uint64_t *hi_off) {
+    double acc = 0.0;
+    const int lowmask = (1 << m) - 1;
+    for (uint32_t t = 0; t < nterms; t++) {
+        const lgpu_bterm_t tm = terms[t];
+        double re = 0.0, im = 0.0;
+        for (int e = threadIdx.x; e < E; e += blockDim.x) {
+            const int f = e ^ int(tm.tflip);
+            const uint64_t gf = base + hi_off[f >> m] + uint64_t(f & lowmask);
+            const double sg = (__popcll(gf & tm.sign) & 1) ? -1.0 : 1.0;
+            const cplx_t<T> a = tile[e], b = tile[f];
+            re += sg * (double(a.x) * b.x + double(a.y) * b.y);
+            im += sg * (double(a.x) * b.y - double(a.y) * b.x);
+        }
+        acc += tm.cr * re - tm.ci * im;
+    }
+    return acc;
+}
+
+__device__ __forceinline__ double block_sum(double v, double *red) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    __syncthreads();
+    if (lane == 0) red[warp] = v;
+    __syncthreads();
+    double s = 0.0;
+    if (threadIdx.x == 0)
+        for (int w = 0; w < int(blockDim.x >> 5); w++) s += red[w];  // fixed order
+    return s;  // valid in thread 0
+}
+
+template <class T, bool EMU>
+__global__ void __launch_bounds__(512, 1) batch_kernel(lgpu_batch_args_t a) {
+    using C = cplx_t<T>;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    C *tile = reinterpret_cast<C *>(smem_raw);
+    __shared__ uint64_t hi_off[64];
+    __shared__ double red[32];
+    __shared__ uint32_t s_idx;
+    C *scratch = reinterpret_cast<C *>(a.scratch) + uint64_t(blockIdx.x) * a.scratch_amps;
+    for (;;) {
+        if (threadIdx.x == 0) s_idx = atomicAdd(a.counter, 1u);
+        __syncthreads();
+        const uint32_t ci = s_idx;
+        __syncthreads();
+        if (ci >= a.ncircuits) break;
+        const lgpu_bcircuit_t cir = a.circuits[a.order ? a.order[ci] : ci];
+        double acc = 0.0;
+        for (uint32_t bi = 0; bi < cir.block_cnt; bi++) {
+            const lgpu_bblock_t blk = a.blocks[cir.block_off + bi];
+            const int k = blk.k, mlow = blk.m;
+            const int E = 1 << k;
+            const bool whole = (k == int(cir.n));  // the tile is the whole state
+            const bool first = bi == 0, last = bi + 1 == cir.block_cnt;
+            // high-bit offset table of this block
+            if (threadIdx.x < 64) {
+                uint64_t o = 0;
+                for (int q = mlow; q < k; q++)
+                    if ((threadIdx.x >> (q - mlow)) & 1) o |= uint64_t(1) << blk.bits[q];
+                hi_off[threadIdx.x] = o;
+            }
+            __syncthreads();
+            const uint64_t ntiles = uint64_t(1) << (cir.n - uint32_t(k));
+            const int lowmask = (1 << mlow) - 1;
+            for (uint64_t tau = 0; tau < ntiles; tau++) {
+                // base = tau with zeros inserted at the tile bits
+                uint64_t base = tau;
+                for (int q = 0; q < k; q++) {
+                    const uint64_t lo = (uint64_t(1) << blk.bits[q]) - 1;
+                    base = ((base & ~lo) << 1) | (base & lo);
+                }
+                if (first) {
+                    for (int e = threadIdx.x; e < E; e += blockDim.x) tile[e] = mk<T>(T(0), T(0));
+                    __syncthreads();
+                    if (threadIdx.x == 0 && base == 0) tile[0] = mk<T>(T(1), T(0));
+                } else {
+                    for (int e = threadIdx.x; e < E; e += blockDim.x)
+                        tile[e] = scratch[base + hi_off[e >> mlow] + uint64_t(e & lowmask)];
+                }
+                __syncthreads();
+                for (uint32_t gi = 0; gi < blk.gate_cnt; gi++) {
+                    const lgpu_bgate_t g = a.gates[blk.gate_off + gi];
+                    if ((base & g.omask) != g.oval) continue;  // tile-uniform controls
+                    tile_gate<T, EMU>(tile, E, g, a.pool);
+                    __syncthreads();
+                }
+                if (last) acc += tile_obs<T>(tile, E, a.terms + cir.obs_off, cir.obs_cnt, base, mlow, hi_off);
+                if (!whole && !last) {
+                    for (int e = threadIdx.x; e < E; e += blockDim.x)
+                        scratch[base + hi_off[e >> mlow] + uint64_t(e & lowmask)] = tile[e];
+                }
+                __syncthreads();
+            }
+            // make this block's stores visible to the next block's loads (same CTA)
+            __threadfence_block();
+            __syncthreads();
+        }
+        const double total = block_sum(acc, red);
+        if (threadIdx.x == 0) a.out[cir.out] = total;
+        __syncthreads();
+    }
+}
+
+template <class T, bool EMU>
+static lgpu_status_t launch_batch(const lgpu_batch_args_t &args, unsigned grid, size_t smem, cudaStream_t s) {
+    cudaError_t e = cudaFuncSetAttribute(batch_kernel<T, EMU>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(batch)");
+    batch_kernel<T, EMU><<<grid, args.threads, smem, s>>>(args);
+    LGPU_CHECK_LAUNCH();
+    return LGPU_OK;
+}
+
+}  // namespace lgpu
+
+using namespace lgpu;
+
+extern "C" {
+
+lgpu_status_t lgpu_batch_prepare(const lgpu_bgate_t *gates, uint64_t ngates, const double *params, double *pool,
+                                 lgpu_stream_t stream) {
+    if (ngates == 0) return LGPU_OK;
+    if (!gates || !pool) return fail(LGPU_ERR_INVALID_ARG, "null gates/pool");
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    bprep_kernel<<<grid_for(ngates, 128, 1, 4), 128, 0, s>>>(gates, ngates, params, pool);
+    LGPU_CHECK_LAUNCH();
+    return LGPU_OK;
+}
+
+lgpu_status_t lgpu_batch_run(const lgpu_batch_args_t *args, lgpu_dtype_t dt, unsigned grid, lgpu_stream_t stream) {
+    if (!args || !args->counter || !args->circuits || !args->out)
+        return fail(LGPU_ERR_INVALID_ARG, "batch: null argument");
+    if (args->kmax < 1 || args->kmax > (dt == LGPU_C128 ? 13u : 14u))
+        return fail(LGPU_ERR_INVALID_ARG, "batch: tile size out of range");
+    if (args->threads != 128 && args->threads != 256 && args->threads != 512)
+        return fail(LGPU_ERR_INVALID_ARG, "batch: threads must be 128, 256 or 512");
+    if (grid == 0) return fail(LGPU_ERR_INVALID_ARG, "batch: empty grid");
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    const size_t smem = (size_t(1) << args->kmax) * (dt == LGPU_C128 ? 16 : 8);
+    if (dt == LGPU_C128)
+        return f64_mode() == 1 ? launch_batch<double, true>(*args, grid, smem, s)
+                               : launch_batch<double, false>(*args, grid, smem, s);
+    return launch_batch<float, false>(*args, grid, smem, s);
+}
+
+}  // extern "C"

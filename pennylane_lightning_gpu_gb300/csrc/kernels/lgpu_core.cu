@@ -373,6 +373,49 @@ lgpu_status_t lgpu_peer_access_all(void) {
     return LGPU_OK;
 }
 
+struct lgpu_graph_s {
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+};
+
+lgpu_status_t lgpu_graph_begin(lgpu_stream_t stream) {
+    LGPU_CUDA_TRY(cudaStreamBeginCapture(reinterpret_cast<cudaStream_t>(stream), cudaStreamCaptureModeThreadLocal));
+    return LGPU_OK;
+}
+
+lgpu_status_t lgpu_graph_end(lgpu_stream_t stream, lgpu_graph_t *graph) {
+    if (!graph) return fail(LGPU_ERR_INVALID_ARG, "graph is null");
+    auto *g = new (std::nothrow) lgpu_graph_s();
+    if (!g) return fail(LGPU_ERR_OOM, "host allocation of graph failed");
+    cudaError_t e = cudaStreamEndCapture(reinterpret_cast<cudaStream_t>(stream), &g->graph);
+    if (e != cudaSuccess) {
+        delete g;
+        return cuda_fail(e, "cudaStreamEndCapture");
+    }
+    e = cudaGraphInstantiate(&g->exec, g->graph, 0);
+    if (e != cudaSuccess) {
+        cudaGraphDestroy(g->graph);
+        delete g;
+        return cuda_fail(e, "cudaGraphInstantiate");
+    }
+    *graph = g;
+    return LGPU_OK;
+}
+
+lgpu_status_t lgpu_graph_launch(lgpu_graph_t graph, lgpu_stream_t stream) {
+    if (!graph) return fail(LGPU_ERR_INVALID_ARG, "graph is null");
+    LGPU_CUDA_TRY(cudaGraphLaunch(graph->exec, reinterpret_cast<cudaStream_t>(stream)));
+    return LGPU_OK;
+}
+
+lgpu_status_t lgpu_graph_destroy(lgpu_graph_t graph) {
+    if (!graph) return LGPU_OK;
+    if (graph->exec) cudaGraphExecDestroy(graph->exec);
+    if (graph->graph) cudaGraphDestroy(graph->graph);
+    delete graph;
+    return LGPU_OK;
+}
+
 lgpu_status_t lgpu_context_create(int device, lgpu_context_t *ctx) {
     if (!ctx) return fail(LGPU_ERR_INVALID_ARG, "ctx is null");
     auto *c = new (std::nothrow) lgpu_context_s();

@@ -62,11 +62,9 @@ struct KConst {
     uint32_t sign;  // 0x80000000 when k < 0
 };
 
-inline KConst make_kconst(double k) {
+LGPU_HD KConst make_kconst(double k) {
     KConst c{};
-    uint64_t b;
-    static_assert(sizeof(b) == sizeof(k), "double is 64-bit");
-    std::memcpy(&b, &k, sizeof(b));
+    const uint64_t b = emu_bits(k);
     const uint32_t hi = uint32_t(b >> 32), lo = uint32_t(b);
     const uint32_t e = (hi >> 20) & 0x7FF;
     c.sign = hi & 0x80000000u;

@@ -80,3 +80,8 @@ def random_state(n, rng, dtype=np.complex128):
     v = rng.normal(size=1 << n) + 1j * rng.normal(size=1 << n)
     v /= np.linalg.norm(v)
     return v.astype(dtype)
+
+
+def sum_z_hamiltonian_terms(n):
+    """sum_i Z_i as (coeff, word, wires) terms."""
+    return [(1.0, "Z", [w]) for w in range(n)]

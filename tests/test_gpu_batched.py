@@ -1,0 +1,76 @@
+"""Batched persistent executor against the oracle and the plain per-circuit loop.
+
+Tolerance: complex128 1e-10, complex64 1e-5 (absolute, per circuit result).
+"""
+import numpy as np
+import pytest
+
+from pennylane_lightning_gpu_gb300 import batched, workloads
+
+pytestmark = pytest.mark.gpu
+
+
+def _oracle_value(oracle, n, ops, obs):
+    psi = oracle.run(n, [(o[0], o[1], o[2], o[3], None) for o in ops])
+    words = [t[1] for t in obs]
+    wires = [t[2] for t in obs]
+    return oracle.expval_pauli_words(psi, words, wires, np.array([t[0] for t in obs], np.complex128))
+
+
+@pytest.mark.parametrize("dtype,tol", [(np.complex128, 1e-10), (np.complex64, 1e-5)])
+def test_batched_matches_oracle_small_and_large(oracle, dtype, tol):
+    rng = np.random.default_rng(11)
+    circuits = []
+    for n in [3, 6, 10, 13, 14, 15, 16]:
+        ops = workloads.random_circuit(n, 3, rng)
+        ops += [("IsingXX", [0, n - 1], [0.4], False), ("SWAP", [1, n - 2], [], False),
+                ("Toffoli", [0, 1, 2], [], False), ("PhaseShift", [n - 1], [0.7], True),
+                ("CRX", [2, 0], [1.1], True), ("Hadamard", [n // 2], [], False), ("S", [1], [], True)]
+        obs = workloads.random_pauli_hamiltonian(n, 6, rng, max_wires=3) + [(0.5, "Z", [n - 1])]
+        circuits.append((n, ops, obs))
+    ex = batched.build_executor(circuits, dtype)
+    got = ex.run()
+    for (n, ops, obs), g in zip(circuits, got):
+        assert abs(g - _oracle_value(oracle, n, ops, obs)) < tol * 10, n
+
+
+@pytest.mark.parametrize("dtype,tol", [(np.complex128, 1e-10), (np.complex64, 1e-5)])
+def test_batched_param_replay(oracle, dtype, tol):
+    circuits = batched.config2_circuits(count=24, nmin=8, nmax=15, seed=5)
+    ex = batched.build_executor(circuits, dtype)
+    first = ex.run()
+    ref_plain = batched.plain_loop(circuits, dtype)
+    assert np.max(np.abs(first - ref_plain)) < tol * 100
+    # new parameters through the captured graph
+    p = ex.params
+    rng = np.random.default_rng(1)
+    newp = rng.uniform(0, 2 * np.pi, p.size)
+    got = ex.run(newp)
+    k = 0
+    for ci, (n, ops, obs) in enumerate(circuits):
+        new_ops = []
+        for o in ops:
+            if o[2]:
+                new_ops.append((o[0], o[1], [float(newp[k])], o[3]))
+                k += 1
+            else:
+                new_ops.append(o)
+        assert abs(got[ci] - _oracle_value(oracle, n, new_ops, obs)) < tol * 10
+
+
+def test_batched_config2_subset_vs_plain():
+    circuits = batched.config2_circuits(count=64, seed=2)
+    ex = batched.build_executor(circuits, np.complex128)
+    got = ex.run()
+    ref = batched.plain_loop(circuits, np.complex128, fusion=True)
+    assert np.max(np.abs(got - ref)) < 1e-9
+
+
+def test_autotune_cache(tmp_path, monkeypatch):
+    monkeypatch.setenv("LGPU_AUTOTUNE_CACHE", str(tmp_path / "tune.json"))
+    circuits = batched.config2_circuits(count=32, nmin=10, nmax=14, seed=3)
+    k, t, rec = batched.autotune(circuits, np.complex64, sample=16, repeats=1,
+                                 candidates=[(12, 256), (14, 256)])
+    assert (k, t) in [(12, 256), (14, 256)]
+    k2, t2, rec2 = batched.autotune(circuits, np.complex64, sample=16, repeats=1)
+    assert (k2, t2) == (k, t)

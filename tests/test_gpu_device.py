@@ -78,7 +78,7 @@ def test_state_prep_and_basis_state(oracle):
     dev.reset()
     dev.apply([Q.BasisState([1, 0, 1], [0, 2, 4])])
     st = dev.state
-    assert st[0b10101] == 1
+    assert st[0b10001] == 1  # wires 0 and 4 set: bits 4 and 0
     with pytest.raises(Exception):
         dev.apply([Q.op("RX", 0, 0.1), Q.BasisState([1], [0])])
 
