@@ -312,8 +312,15 @@ __global__ void __launch_bounds__(512, 1) batch_kernel(lgpu_batch_args_t a) {
 
 template <class T, bool EMU>
 static lgpu_status_t launch_batch(const lgpu_batch_args_t &args, unsigned grid, size_t smem, cudaStream_t s) {
-    cudaError_t e = cudaFuncSetAttribute(batch_kernel<T, EMU>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
-    if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(batch)");
+    // The attribute is set once per size outside any stream capture (the host
+    // runs the batch eagerly once before capturing it).
+    static size_t attr_smem = 0;
+    if (smem > attr_smem) {
+        cudaError_t e =
+            cudaFuncSetAttribute(batch_kernel<T, EMU>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+        if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(batch)");
+        attr_smem = smem;
+    }
     batch_kernel<T, EMU><<<grid, args.threads, smem, s>>>(args);
     LGPU_CHECK_LAUNCH();
     return LGPU_OK;
