@@ -618,6 +618,10 @@ PYBIND11_MODULE(lightning_gpu_qubit_ops, m) {
         .def(py::init([](int device_id, void *stream_id) {
             return new DevTag<int>(device_id, static_cast<cudaStream_t>(stream_id));
         }))
+        .def(py::init([](int device_id, uintptr_t stream_ptr) {
+            // stream given as an integer handle (e.g. torch.cuda.Stream().cuda_stream)
+            return new DevTag<int>(device_id, reinterpret_cast<cudaStream_t>(stream_ptr));
+        }))
         .def(py::init<const DevTag<int> &>())
         .def("getDeviceID", &DevTag<int>::getDeviceID)
         .def("getStreamID", [](DevTag<int> &dev_tag) { return static_cast<void *>(dev_tag.getStreamID()); })

@@ -23,7 +23,7 @@ def test_batched_matches_oracle_small_and_large(oracle, dtype, tol):
     circuits = []
     for n in [3, 6, 10, 13, 14, 15, 16]:
         ops = workloads.random_circuit(n, 3, rng)
-        ops += [("IsingXX", [0, n - 1], [0.4], False), ("SWAP", [1, n - 2], [], False),
+        ops += [("IsingXX", [0, n - 1], [0.4], False), ("SWAP", [1, n - 1], [], False),
                 ("Toffoli", [0, 1, 2], [], False), ("PhaseShift", [n - 1], [0.7], True),
                 ("CRX", [2, 0], [1.1], True), ("Hadamard", [n // 2], [], False), ("S", [1], [], True)]
         obs = workloads.random_pauli_hamiltonian(n, 6, rng, max_wires=3) + [(0.5, "Z", [n - 1])]
