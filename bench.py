@@ -262,7 +262,72 @@ def run_ours(args):
     del sv
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline_sample(n, gates=args.cpu_gates)
+    if not args.no_batched:
+        line["batched"] = bench_batched(args)
+    if not args.no_serving:
+        line["serving"] = bench_serving(args)
     print(json.dumps(line))
+
+
+def bench_batched(args):
+    """Config 2: 4096 circuits (n uniform 10..20, 2..6 layers of the layered
+    ansatz, observable sum_i Z_i) in one persistent graph-captured launch vs
+    the plain per-circuit loop (timed on a seeded subset, scaled)."""
+    import torch
+
+    from pennylane_lightning_gpu_gb300 import batched
+
+    out = {"workload": "%d circuits, n uniform 10..20, 2..6 layers of RX/RY/RZ + CNOT ring, sum_i Z_i"
+                       % args.batch_circuits}
+    circuits = batched.config2_circuits(count=args.batch_circuits, seed=2)
+    rng = np.random.default_rng(0)
+    sub_idx = sorted(rng.choice(len(circuits), size=min(args.batch_plain, len(circuits)), replace=False))
+    sub = [circuits[i] for i in sub_idx]
+    for dt, key in ((np.complex64, "c64"), (np.complex128, "c128")):
+        t0 = time.perf_counter()
+        ex = batched.build_executor(circuits, dt)
+        prep = time.perf_counter() - t0
+        ex.run()
+        ts = []
+        for _ in range(3):
+            torch.cuda.synchronize()
+            a = time.perf_counter()
+            res = ex.run()
+            ts.append(time.perf_counter() - a)
+        run_s = min(ts)
+        a = time.perf_counter()
+        plain = batched.plain_loop(sub, dt)
+        plain_s = (time.perf_counter() - a) * len(circuits) / len(sub)
+        err = float(np.max(np.abs(res[sub_idx] - plain)))
+        out[key] = {"circuits_per_s": round(len(circuits) / run_s, 1), "run_s": round(run_s, 4),
+                    "plain_loop_circuits_per_s": round(len(circuits) / plain_s, 1),
+                    "speedup_vs_plain": round(plain_s / run_s, 2), "prepare_s": round(prep, 3),
+                    "max_abs_diff_vs_plain": err, "plain_sample": len(sub), "stats": ex.stats()}
+        del ex
+    return out
+
+
+def bench_serving(args):
+    """Config 4: Poisson stream of requests (n log-uniform 8..30, depth 2..10,
+    expval / probs / shots), complex64, served with continuous batching vs a
+    sequential loop over the same trace."""
+    from pennylane_lightning_gpu_gb300 import serving
+
+    trace = serving.make_trace(args.serve_requests, rate=args.serve_rate, seed=4)
+    srv = serving.CircuitServer(np.complex64, slots=8)
+    try:
+        done, makespan = serving.replay(srv, trace)
+    finally:
+        srv.close()
+    served = serving.report(done, makespan)
+    seq, seq_makespan = serving.sequential_baseline(serving.make_trace(args.serve_requests, rate=args.serve_rate,
+                                                                       seed=4), np.complex64)
+    base = serving.report(seq, seq_makespan)
+    return {"workload": "%d requests, Poisson rate %.0f/s, n log-uniform 8..30, depth 2..10, complex64"
+                        % (args.serve_requests, args.serve_rate),
+            "served": served, "sequential": base,
+            "throughput_speedup": round(served["circuits_per_s"] / base["circuits_per_s"], 2),
+            "p99_speedup": round(base["p99_ms"] / served["p99_ms"], 2)}
 
 
 def main():
@@ -275,6 +340,12 @@ def main():
     ap.add_argument("--cpu-gates", type=int, default=4)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-variants", action="store_true")
+    ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--no-serving", action="store_true")
+    ap.add_argument("--batch-circuits", type=int, default=4096)
+    ap.add_argument("--batch-plain", type=int, default=256)
+    ap.add_argument("--serve-requests", type=int, default=160)
+    ap.add_argument("--serve-rate", type=float, default=40.0)
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     if args.impl == "reference":

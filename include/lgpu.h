@@ -310,7 +310,8 @@ typedef struct {
     const lgpu_bcircuit_t *circuits;
     const uint32_t *order;   /* processing order (NULL: identity) */
     uint32_t ncircuits;
-    uint32_t kmax;           /* tile bits, <= 13 (C128) / 14 (C64) */
+    uint32_t kmax;           /* circuits of n <= kmax qubits run entirely in shared memory,
+                                kmax <= 13 (C128) / 14 (C64) */
     const lgpu_bblock_t *blocks;
     const lgpu_bgate_t *gates;
     const double *pool;
@@ -320,7 +321,8 @@ typedef struct {
     unsigned *counter;       /* work-queue counter, zero before each launch */
     double *out;             /* one result per circuit */
     uint32_t threads;        /* 128, 256 or 512 */
-    uint32_t pad;
+    uint32_t klarge;         /* tile bits of circuits above kmax qubits, <= 12 (C128) / 13 (C64);
+                                their tiles stream through a 3-stage shared-memory ring */
 } lgpu_batch_args_t;
 
 lgpu_status_t lgpu_batch_prepare(const lgpu_bgate_t *gates, uint64_t ngates, const double *params, double *pool,

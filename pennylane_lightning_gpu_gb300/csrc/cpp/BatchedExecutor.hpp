@@ -73,6 +73,8 @@ template <class Precision> class BatchedExecutor {
     size_t numParams() const { return params_.size(); }
     size_t numCircuits() const { return circuits_.size(); }
     int kmax() const { return kmax_; }
+    // tile bits of circuits above kmax qubits (a 3-stage ring of 64 KB tiles)
+    int klarge() const { return std::is_same_v<Precision, double> ? 12 : 13; }
 
     void prepare() {
         PL_ABORT_IF(prepared_, "prepare() called twice");
@@ -108,7 +110,7 @@ template <class Precision> class BatchedExecutor {
                     d.ctrls = o.ctrls;
                     descs.push_back(d);
                 }
-                const auto plan = Engine::plan_fusion(descs, c.n, kmax_, 5, 1);
+                const auto plan = Engine::plan_fusion(descs, c.n, klarge(), 5, 1);
                 for (const auto &b : plan) {
                     PL_ABORT_IF(b.tile_bits.empty(), "batched execution: an operation does not fit a fused tile");
                     blocks.push_back({b.tile_bits, b.gates});
@@ -128,7 +130,7 @@ template <class Precision> class BatchedExecutor {
                     for (int b = 0; b < int(c.n); b++)
                         if ((flips >> b) & 1) fb.push_back(b);
                     std::vector<int> tile;
-                    PL_ABORT_IF_NOT(Engine::tile_for(fb, kmax_, 5, c.n, tile),
+                    PL_ABORT_IF_NOT(Engine::tile_for(fb, klarge(), 5, c.n, tile),
                                     "batched execution: observable flip bits do not fit one tile");
                     blocks.push_back({tile, {}});
                 }
@@ -217,6 +219,7 @@ template <class Precision> class BatchedExecutor {
         args_.counter = static_cast<unsigned *>(d_counter_);
         args_.out = static_cast<double *>(d_out_);
         args_.threads = uint32_t(threads_);
+        args_.klarge = uint32_t(klarge());
         // one eager run (sets kernel attributes, validates), then capture
         enqueue();
         PL_LGPU_IS_SUCCESS(lgpu_stream_sync(stream_));
@@ -241,6 +244,9 @@ template <class Precision> class BatchedExecutor {
     }
     std::vector<double> wait() {
         PL_LGPU_IS_SUCCESS(lgpu_stream_sync(stream_));
+        int code = 0;
+        PL_LGPU_IS_SUCCESS(lgpu_device_error(&code, 1));
+        PL_ABORT_IF(code != 0, "A batched kernel timed out waiting for a bulk copy; results are invalid");
         std::vector<double> out(circuits_.size());
         std::memcpy(out.data(), h_out_, out.size() * sizeof(double));
         return out;

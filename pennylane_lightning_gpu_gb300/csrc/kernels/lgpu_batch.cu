@@ -238,30 +238,75 @@ __device__ __forceinline__ double block_sum(double v, double *red) {
     return s;  // valid in thread 0
 }
 
+// --- bulk-copy helpers (TMA engine), bounded waits ---------------------------
+__device__ unsigned int g_batch_error = 0;
+constexpr int kRing = 3;
+constexpr uint32_t kBatchWaitLimit = 1u << 24;
+
+__device__ __forceinline__ uint32_t b_smem(const void *p) { return static_cast<uint32_t>(__cvta_generic_to_shared(p)); }
+__device__ __forceinline__ void b_mbar_init(uint64_t *bar) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(b_smem(bar)) : "memory");
+}
+__device__ __forceinline__ void b_expect_tx(uint64_t *bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(b_smem(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool b_try_wait(uint64_t *bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(b_smem(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+__device__ __forceinline__ void b_load(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     b_smem(dst)),
+                 "l"(src), "r"(bytes), "r"(b_smem(bar))
+                 : "memory");
+}
+__device__ __forceinline__ void b_store(void *dst, const void *src, uint32_t bytes) {
+    asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(dst), "r"(b_smem(src)), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void b_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void b_wait_read_2() { asm volatile("cp.async.bulk.wait_group.read 2;" ::: "memory"); }
+__device__ __forceinline__ void b_wait_read_1() { asm volatile("cp.async.bulk.wait_group.read 1;" ::: "memory"); }
+__device__ __forceinline__ void b_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
+__device__ __forceinline__ void b_fence() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
 template <class T, bool EMU>
 __global__ void __launch_bounds__(512, 1) batch_kernel(lgpu_batch_args_t a) {
     using C = cplx_t<T>;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    C *tile = reinterpret_cast<C *>(smem_raw);
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    C *ring = reinterpret_cast<C *>(smem_raw);
     __shared__ uint64_t hi_off[64];
     __shared__ double red[32];
     __shared__ uint32_t s_idx;
+    __shared__ __align__(8) uint64_t full_bar[kRing];
     C *scratch = reinterpret_cast<C *>(a.scratch) + uint64_t(blockIdx.x) * a.scratch_amps;
+    const uint32_t tile_amps = 1u << a.klarge;  // ring stage size (large circuits)
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < kRing; s++) b_mbar_init(&full_bar[s]);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    uint64_t u = 0;            // running count of ring uses by this CTA (stage rotation)
+    uint32_t phase_bits = 0;   // bit s: parity of the next completion of full_bar[s]
+    bool failed = false;
     for (;;) {
         if (threadIdx.x == 0) s_idx = atomicAdd(a.counter, 1u);
         __syncthreads();
         const uint32_t ci = s_idx;
         __syncthreads();
-        if (ci >= a.ncircuits) break;
+        if (ci >= a.ncircuits || failed) break;
         const lgpu_bcircuit_t cir = a.circuits[a.order ? a.order[ci] : ci];
         double acc = 0.0;
-        for (uint32_t bi = 0; bi < cir.block_cnt; bi++) {
+        for (uint32_t bi = 0; bi < cir.block_cnt && !failed; bi++) {
             const lgpu_bblock_t blk = a.blocks[cir.block_off + bi];
             const int k = blk.k, mlow = blk.m;
             const int E = 1 << k;
-            const bool whole = (k == int(cir.n));  // the tile is the whole state
             const bool first = bi == 0, last = bi + 1 == cir.block_cnt;
-            // high-bit offset table of this block
             if (threadIdx.x < 64) {
                 uint64_t o = 0;
                 for (int q = mlow; q < k; q++)
@@ -269,45 +314,121 @@ __global__ void __launch_bounds__(512, 1) batch_kernel(lgpu_batch_args_t a) {
                 hi_off[threadIdx.x] = o;
             }
             __syncthreads();
-            const uint64_t ntiles = uint64_t(1) << (cir.n - uint32_t(k));
-            const int lowmask = (1 << mlow) - 1;
-            for (uint64_t tau = 0; tau < ntiles; tau++) {
-                // base = tau with zeros inserted at the tile bits
+            auto tile_base = [&](uint64_t tau) {
                 uint64_t base = tau;
                 for (int q = 0; q < k; q++) {
                     const uint64_t lo = (uint64_t(1) << blk.bits[q]) - 1;
                     base = ((base & ~lo) << 1) | (base & lo);
                 }
+                return base;
+            };
+            if (k == int(cir.n)) {
+                // ---- whole state in shared memory ----
+                C *tile = ring;
+                for (int e = threadIdx.x; e < E; e += blockDim.x) tile[e] = mk<T>(T(e == 0 ? 1 : 0), T(0));
+                __syncthreads();
+                for (uint32_t gi = 0; gi < blk.gate_cnt; gi++) {
+                    tile_gate<T, EMU>(tile, E, a.gates[blk.gate_off + gi], a.pool);
+                    __syncthreads();
+                }
+                acc += tile_obs<T>(tile, E, a.terms + cir.obs_off, cir.obs_cnt, 0, mlow, hi_off);
+                __syncthreads();
+                continue;
+            }
+            // ---- streamed tiles through the ring (bulk copies) ----
+            const uint64_t ntiles = uint64_t(1) << (cir.n - uint32_t(k));
+            const uint32_t seg_amps = 1u << mlow, nseg = 1u << (k - mlow);
+            const uint32_t seg_bytes = seg_amps * uint32_t(sizeof(C));
+            auto stage_ptr = [&](uint64_t use) { return ring + size_t(use % kRing) * tile_amps; };
+            auto issue_load = [&](uint64_t tau, uint64_t use) {
+                C *buf = stage_ptr(use);
+                uint64_t *bar = &full_bar[use % kRing];
+                const uint64_t base = tile_base(tau);
+                b_expect_tx(bar, nseg * seg_bytes);
+                for (uint32_t sg = 0; sg < nseg; sg++) b_load(buf + sg * seg_amps, scratch + base + hi_off[sg], seg_bytes, bar);
+            };
+            const uint64_t u0 = u;
+            if (!first && threadIdx.x == 0)
+                for (uint64_t j = 0; j < ntiles && j < uint64_t(kRing); j++) issue_load(j, u0 + j);
+            for (uint64_t j = 0; j < ntiles; j++) {
+                const uint64_t use = u0 + j;
+                C *tile = stage_ptr(use);
+                const uint64_t base = tile_base(j);
                 if (first) {
+                    // |0...0> needs no load: wait until the stage's previous store has read it
+                    if (threadIdx.x == 0) b_wait_read_2();
+                    __syncthreads();
                     for (int e = threadIdx.x; e < E; e += blockDim.x) tile[e] = mk<T>(T(0), T(0));
                     __syncthreads();
                     if (threadIdx.x == 0 && base == 0) tile[0] = mk<T>(T(1), T(0));
+                    __syncthreads();
                 } else {
-                    for (int e = threadIdx.x; e < E; e += blockDim.x)
-                        tile[e] = scratch[base + hi_off[e >> mlow] + uint64_t(e & lowmask)];
+                    const int st = int(use % kRing);
+                    const uint32_t parity = (phase_bits >> st) & 1u;
+                    uint32_t spins = 0;
+                    bool timed_out = false;
+                    while (!b_try_wait(&full_bar[st], parity)) {
+                        if (++spins > kBatchWaitLimit) {
+                            timed_out = true;
+                            break;
+                        }
+                    }
+                    if (__syncthreads_or(timed_out)) {
+                        if (threadIdx.x == 0) atomicOr(&g_batch_error, 1u);
+                        failed = true;
+                        break;
+                    }
+                    phase_bits ^= 1u << st;
                 }
-                __syncthreads();
                 for (uint32_t gi = 0; gi < blk.gate_cnt; gi++) {
                     const lgpu_bgate_t g = a.gates[blk.gate_off + gi];
                     if ((base & g.omask) != g.oval) continue;  // tile-uniform controls
                     tile_gate<T, EMU>(tile, E, g, a.pool);
                     __syncthreads();
                 }
-                if (last) acc += tile_obs<T>(tile, E, a.terms + cir.obs_off, cir.obs_cnt, base, mlow, hi_off);
-                if (!whole && !last) {
-                    for (int e = threadIdx.x; e < E; e += blockDim.x)
-                        scratch[base + hi_off[e >> mlow] + uint64_t(e & lowmask)] = tile[e];
+                if (last) {
+                    acc += tile_obs<T>(tile, E, a.terms + cir.obs_off, cir.obs_cnt, base, mlow, hi_off);
+                    __syncthreads();
+                } else {
+                    b_fence();
+                    __syncthreads();
+                    if (threadIdx.x == 0) {
+                        for (uint32_t sg = 0; sg < nseg; sg++)
+                            b_store(scratch + base + hi_off[sg], tile + sg * seg_amps, seg_bytes);
+                        b_commit();
+                    }
                 }
-                __syncthreads();
+                if (!first && threadIdx.x == 0 && j >= 1) {
+                    // refill the previous stage once its store has finished reading it
+                    const uint64_t next = (j - 1) + kRing;
+                    if (next < ntiles) {
+                        if (!last) b_wait_read_1();
+                        issue_load(next, u0 + next);
+                    }
+                }
             }
-            // make this block's stores visible to the next block's loads (same CTA)
-            __threadfence_block();
+            // (every load issued above is for a tile index < ntiles and is consumed)
+            u = u0 + ntiles;
+            // all stores of this block complete before the next block reads
+            if (threadIdx.x == 0) b_wait_all();
+            __threadfence();
             __syncthreads();
         }
+        if (failed) break;
         const double total = block_sum(acc, red);
         if (threadIdx.x == 0) a.out[cir.out] = total;
         __syncthreads();
     }
+    if (threadIdx.x == 0) b_wait_all();
+}
+
+lgpu_status_t batch_error_fetch(unsigned *v, bool reset) {
+    LGPU_CUDA_TRY(cudaMemcpyFromSymbol(v, g_batch_error, sizeof(unsigned)));
+    if (reset && *v) {
+        unsigned z = 0;
+        LGPU_CUDA_TRY(cudaMemcpyToSymbol(g_batch_error, &z, sizeof(z)));
+    }
+    return LGPU_OK;
 }
 
 template <class T, bool EMU>
@@ -347,11 +468,14 @@ lgpu_status_t lgpu_batch_run(const lgpu_batch_args_t *args, lgpu_dtype_t dt, uns
         return fail(LGPU_ERR_INVALID_ARG, "batch: null argument");
     if (args->kmax < 1 || args->kmax > (dt == LGPU_C128 ? 13u : 14u))
         return fail(LGPU_ERR_INVALID_ARG, "batch: tile size out of range");
+    if (args->klarge < 6 || args->klarge > (dt == LGPU_C128 ? 12u : 13u))
+        return fail(LGPU_ERR_INVALID_ARG, "batch: large-circuit tile size out of range");
     if (args->threads != 128 && args->threads != 256 && args->threads != 512)
         return fail(LGPU_ERR_INVALID_ARG, "batch: threads must be 128, 256 or 512");
     if (grid == 0) return fail(LGPU_ERR_INVALID_ARG, "batch: empty grid");
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
-    const size_t smem = (size_t(1) << args->kmax) * (dt == LGPU_C128 ? 16 : 8);
+    const size_t amp = dt == LGPU_C128 ? 16 : 8;
+    const size_t smem = std::max((size_t(1) << args->kmax) * amp, size_t(kRing) * (size_t(1) << args->klarge) * amp);
     if (dt == LGPU_C128)
         return f64_mode() == 1 ? launch_batch<double, true>(*args, grid, smem, s)
                                : launch_batch<double, false>(*args, grid, smem, s);

@@ -1039,9 +1039,10 @@ extern "C" {
 
 lgpu_status_t lgpu_device_error(int *code, int reset) {
     if (!code) return fail(LGPU_ERR_INVALID_ARG, "code is null");
-    unsigned v = 0;
+    unsigned v = 0, vb = 0;
     LGPU_CUDA_TRY(cudaMemcpyFromSymbol(&v, g_lgpu_device_error, sizeof(v)));
-    *code = int(v);
+    LGPU_TRY(batch_error_fetch(&vb, reset != 0));
+    *code = int(v | vb);
     if (reset && v) {
         unsigned z = 0;
         LGPU_CUDA_TRY(cudaMemcpyToSymbol(g_lgpu_device_error, &z, sizeof(z)));

@@ -50,6 +50,8 @@ int f64_mode();
 // Uncontrolled 1-target gates use the bulk-copy pipelined kernel when 1
 // (default); the grid-stride kernel when 0.  See lgpu_set_stream_mode().
 int bulk_enabled();
+// device error flag of the batched kernel's bounded waits (lgpu_batch.cu)
+lgpu_status_t batch_error_fetch(unsigned *v, bool reset);
 
 // ---------------------------------------------------------------------------
 // Scratch context
