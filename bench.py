@@ -342,12 +342,20 @@ def main():
     ap.add_argument("--no-variants", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-serving", action="store_true")
+    ap.add_argument("--only", choices=["batched", "serving"], default=None,
+                    help="run one section alone (profiling runs); the default prints the full line")
     ap.add_argument("--batch-circuits", type=int, default=4096)
     ap.add_argument("--batch-plain", type=int, default=256)
     ap.add_argument("--serve-requests", type=int, default=160)
     ap.add_argument("--serve-rate", type=float, default=40.0)
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
+    if args.only == "batched":
+        print(json.dumps({"batched": bench_batched(args)}))
+        return
+    if args.only == "serving":
+        print(json.dumps({"serving": bench_serving(args)}))
+        return
     if args.impl == "reference":
         if rank == 0:
             run_reference(args)
