@@ -156,7 +156,44 @@ def _apply_gate(sv, g, w):
         sv.RX([w], False, [THETA])
 
 
-def gate_sweep(m, cls, n, steps, warmup, f64_mode=None):
+def _dist():
+    """(rank, world, local_rank); one replica per GPU under torchrun."""
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        if not dist.is_initialized():
+            dist.init_process_group("nccl")
+    return rank, world, local
+
+
+def _barrier():
+    import torch
+
+    torch.cuda.synchronize()
+    if int(os.environ.get("WORLD_SIZE", "1")) > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+        torch.cuda.synchronize()
+
+
+def _max_over_ranks(x):
+    if int(os.environ.get("WORLD_SIZE", "1")) <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([float(x)], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def gate_sweep(m, cls, n, steps, warmup, f64_mode=None, device=0):
     """Device-timed sweep of H and RX over every target; returns
     (GB/s of algorithmic bytes, avg launch ms, per-target GB/s, state)."""
     import torch
@@ -166,12 +203,12 @@ def gate_sweep(m, cls, n, steps, warmup, f64_mode=None):
     amp = 16 if cls.endswith("128") else 8
     S = (1 << n) * amp
     gates = _gate_list(n)
-    sv = getattr(m, cls)(n)
+    sv = getattr(m, cls)(n, m.DevTag(device, 0))
     sv.Hadamard([0], False, [])
     for _ in range(warmup):
         for g, w in gates:
             _apply_gate(sv, g, w)
-    torch.cuda.synchronize()
+    _barrier()
     ev = [[(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in gates]
           for _ in range(steps)]
     start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -182,13 +219,14 @@ def gate_sweep(m, cls, n, steps, warmup, f64_mode=None):
             _apply_gate(sv, g, w)
             ev[s][i][1].record()
     end.record()
-    torch.cuda.synchronize()
-    ms_per_step = start.elapsed_time(end) / steps
+    _barrier()
+    ms_per_step = _max_over_ranks(start.elapsed_time(end) / steps)
     per_launch = np.array([[a.elapsed_time(b) for a, b in row] for row in ev])
     per_target = {}
     for i, (g, w) in enumerate(gates):
         per_target.setdefault(g, []).append(round(2 * S / (float(np.median(per_launch[:, i])) / 1e3) / 1e9, 1))
-    gbs = len(gates) * 2 * S / (ms_per_step / 1e3) / 1e9
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    gbs = world * len(gates) * 2 * S / (ms_per_step / 1e3) / 1e9
     return gbs, float(per_launch.mean()), per_target, ms_per_step, sv
 
 
@@ -198,14 +236,16 @@ def run_ours(args):
     import pennylane_lightning_gpu_gb300 as pkg
 
     m = pkg.native()
+    rank, world, dev = _dist()
     n = args.qubits
     S = (1 << n) * 16
     gates = _gate_list(n)
     default_mode = m.get_f64_mode()
+    single = world == 1  # the side sections and the CPU baseline run at N=1 only
 
     # variants first (each frees its state before the next)
     variants = {}
-    if not args.no_variants:
+    if single and not args.no_variants:
         g, _, _, _, sv = gate_sweep(m, "LightningGPU_C128", n, max(2, args.steps // 2), 2, f64_mode=0)
         variants["c128_native_fp64_gbs"] = round(g, 1)
         del sv
@@ -223,24 +263,24 @@ def run_ours(args):
     clocks.start()
     time.sleep(0.3)
     value, avg_launch_ms, per_target, ms_per_step, sv = gate_sweep(m, "LightningGPU_C128", n, args.steps,
-                                                                   args.warmup, f64_mode=default_mode)
+                                                                   args.warmup, f64_mode=default_mode, device=dev)
     clk = clocks.stop()
     bytes_per_step = len(gates) * 2 * S
 
     # ---- end to end: public API, host params, D2H result read every step ----
-    torch.cuda.synchronize()
+    _barrier()
     t0 = time.perf_counter()
     for _ in range(args.steps):
         for g, w in gates:
             _apply_gate(sv, g, w)
         sv.Probability([0])  # blocking D2H of the step's result
-    e2e_s = (time.perf_counter() - t0) / args.steps
-    e2e_value = (bytes_per_step + S) / e2e_s / 1e9  # + one read pass for the probability
+    e2e_s = _max_over_ranks((time.perf_counter() - t0) / args.steps)
+    e2e_value = world * (bytes_per_step + S) / e2e_s / 1e9  # + one read pass for the probability
 
     peak, peak_kind = _peaks()
     achieved = 2 * S / (avg_launch_ms / 1e3) / 1e9
     line = {
-        "metric": "gate HBM GB/s at 28q", "value": round(value, 1), "unit": "GB/s", "n_gpus": args.gpus,
+        "metric": "gate HBM GB/s at 28q", "value": round(value, 1), "unit": "GB/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_per_step, 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "c128 (f64)", "data": "synthetic",
         "config": {"workload": "dense 1-qubit gates (H and RX) on each target of a 28-qubit complex128 state",
@@ -250,7 +290,7 @@ def run_ours(args):
                    "l2": "state (4 GiB) larger than L2 (129 MB): no flush needed"},
         "e2e": {"value": round(e2e_value, 1), "unit": "GB/s", "h2d_bytes_per_step": 8 * n,
                 "d2h_bytes_per_step": 16},
-        "gpu_launches": len(gates) * args.steps,
+        "gpu_launches": len(gates) * args.steps * world,
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": None, "peak_source": peak_kind,
                      "kernel": "gate1_bulk_kernel" if m.get_stream_mode() == 1 else "gate1_kernel",
@@ -260,13 +300,16 @@ def run_ours(args):
         "clocks": clk,
     }
     del sv
-    if not args.no_cpu_baseline:
+    if world > 1:
+        line["config"]["parallelism"] = "replicas: one independent 28-qubit state per GPU"
+    if single and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline_sample(n, gates=args.cpu_gates)
-    if not args.no_batched:
+    if single and not args.no_batched:
         line["batched"] = bench_batched(args)
-    if not args.no_serving:
+    if single and not args.no_serving:
         line["serving"] = bench_serving(args)
-    print(json.dumps(line))
+    if rank == 0:
+        print(json.dumps(line))
 
 
 def bench_batched(args):

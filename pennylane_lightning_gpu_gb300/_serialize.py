@@ -40,7 +40,8 @@ def _serialize_tensor_ob(ob, wires_map, use_csingle):
 def _serialize_hamiltonian(ob, wires_map, use_csingle, split_terms=True):
     cls = getattr(native(), "HamiltonianGPU_" + _suffix(use_csingle))
     coeffs = np.array(ob.coeffs).astype(_rtype(use_csingle))
-    terms = [_serialize_ob(t, wires_map, use_csingle) for t in ob.ops]
+    # a term that is itself a Hamiltonian (a vjp's sum_k dy_k H_k) stays one observable
+    terms = [_serialize_ob(t, wires_map, use_csingle, split_terms=False) for t in ob.ops]
     if split_terms:
         return [cls(np.array([c], _rtype(use_csingle)), [t]) for c, t in zip(coeffs, terms)]
     return cls(coeffs, terms)
