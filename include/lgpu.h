@@ -217,6 +217,21 @@ lgpu_status_t lgpu_sample(lgpu_context_t ctx, const void *sv, uint32_t n, lgpu_d
 lgpu_status_t lgpu_dot(lgpu_context_t ctx, const void *a, const void *b, uint32_t n,
                        lgpu_dtype_t dt, double *out, int out_on_device, lgpu_stream_t stream);
 
+/* Allocation-free <a|b>: no counterpart in the reference.  Same result bits
+ * as lgpu_dot, but the reduction scratch is a static device array of
+ * lgpu_dot_static_scratch_bytes() (32 KiB) per device and a host `out` is
+ * written by a direct copy, so the call allocates no device or host memory.
+ * For callers that must not allocate: a state that fills the device leaves no
+ * room for a context's scratch, and a context's first use or growth allocates
+ * and synchronises the whole device.  The first call on a device looks up the
+ * array's address (with that device current) and belongs before any stream
+ * capture.  Calls that can overlap on one device share the array and race:
+ * order them.  A reduction whose grid needs more scratch than the array
+ * holds is rejected with LGPU_ERR_INVALID_ARG. */
+lgpu_status_t lgpu_dot_static(const void *a, const void *b, uint32_t n, lgpu_dtype_t dt,
+                              double *out, int out_on_device, lgpu_stream_t stream);
+size_t lgpu_dot_static_scratch_bytes(void);
+
 /* y += alpha * x (cublasZaxpy/Caxpy at cuda_helpers.hpp:512-528). */
 lgpu_status_t lgpu_axpy(double alpha_re, double alpha_im, const void *x, void *y, uint32_t n,
                         lgpu_dtype_t dt, lgpu_stream_t stream);

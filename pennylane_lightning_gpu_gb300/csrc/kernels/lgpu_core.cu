@@ -555,3 +555,101 @@ lgpu_status_t lgpu_dot(lgpu_context_t ctx, const void *a, const void *b, uint32_
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Allocation-free inner product
+// ---------------------------------------------------------------------------
+// lgpu_dot_static runs the same reduction as lgpu_dot (same grid, same fixed
+// summation order, hence the same bits) but takes its scratch from the
+// file-scope device array below instead of a context, and copies a host
+// result straight into the caller's buffer.  It calls no cudaMalloc,
+// cudaMallocHost, cudaFree or other allocating routine.
+//
+// Scratch layout: [arrival counter, 256 B][partials: grid x double2]
+// [result: double2].  Only the counter must start at zero: static device
+// memory is zero when the module loads, and the reduction's last block writes
+// the counter back to zero.  The partials and the result are written before
+// they are read.
+//
+// Set-up: the device address of the array is looked up once per device
+// (cudaGetSymbolAddress with that device current) on the first call made
+// with that device current, and cached.  That lookup may load the module on
+// the device, so the first call on each device belongs before any stream
+// capture.
+//
+// One array per device serves every call: two calls that can run at the same
+// time on one device (different streams, or host threads without ordering)
+// race on it and may return garbage.  Callers order them (one stream, or a
+// synchronisation between calls).
+namespace lgpu {
+
+constexpr size_t kStaticScratchBytes = size_t(32) << 10;  // 32 KiB per device
+__device__ __align__(256) unsigned char g_static_scratch[kStaticScratchBytes];
+
+constexpr int kStaticMaxDevices = 64;
+static std::atomic<void *> g_static_ptr[kStaticMaxDevices];
+static std::mutex g_static_mu;
+
+lgpu_status_t static_scratch(void **out) {
+    int dev = 0;
+    LGPU_CUDA_TRY(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kStaticMaxDevices)
+        return fail(LGPU_ERR_UNSUPPORTED, "lgpu_dot_static: device ordinal " + std::to_string(dev) +
+                                              " is beyond the " + std::to_string(kStaticMaxDevices) +
+                                              " devices it keeps scratch addresses for");
+    void *p = g_static_ptr[dev].load(std::memory_order_acquire);
+    if (!p) {
+        std::lock_guard<std::mutex> lock(g_static_mu);
+        p = g_static_ptr[dev].load(std::memory_order_relaxed);
+        if (!p) {
+            LGPU_CUDA_TRY(cudaGetSymbolAddress(&p, g_static_scratch));
+            g_static_ptr[dev].store(p, std::memory_order_release);
+        }
+    }
+    *out = p;
+    return LGPU_OK;
+}
+
+}  // namespace lgpu
+
+extern "C" {
+
+size_t lgpu_dot_static_scratch_bytes(void) { return kStaticScratchBytes; }
+
+lgpu_status_t lgpu_dot_static(const void *a, const void *b, uint32_t n, lgpu_dtype_t dt, double *out,
+                              int out_on_device, lgpu_stream_t stream) {
+    LGPU_TRY(check_state(a, n, dt));
+    LGPU_TRY(check_state(b, n, dt));
+    if (!out) return fail(LGPU_ERR_INVALID_ARG, "output pointer is null");
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    const uint64_t N = uint64_t(1) << n;
+    const unsigned g = reduce_grid(N);
+    const size_t need = 256 + (size_t(g) + 1) * sizeof(double2);
+    if (need > kStaticScratchBytes)
+        return fail(LGPU_ERR_INVALID_ARG, "lgpu_dot_static: the reduction over 2^" + std::to_string(n) +
+                                              " amplitudes uses " + std::to_string(g) + " blocks and needs " +
+                                              std::to_string(need) + " bytes of scratch; the static scratch holds " +
+                                              std::to_string(kStaticScratchBytes) + " bytes");
+    void *base = nullptr;
+    LGPU_TRY(static_scratch(&base));
+    unsigned *counter = static_cast<unsigned *>(base);
+    double2 *partials = reinterpret_cast<double2 *>(static_cast<char *>(base) + 256);
+    double2 *res = partials + size_t(g);
+    if (dt == LGPU_C128) {
+        DotBody<double> body{static_cast<const double2 *>(a), static_cast<const double2 *>(b)};
+        reduce_kernel<1, uint64_t><<<g, kReduceBlock, 0, s>>>(body, N, partials, counter, res);
+    } else {
+        DotBody<float> body{static_cast<const float2 *>(a), static_cast<const float2 *>(b)};
+        reduce_kernel<1, uint64_t><<<g, kReduceBlock, 0, s>>>(body, N, partials, counter, res);
+    }
+    LGPU_CHECK_LAUNCH();
+    if (out_on_device) {
+        LGPU_CUDA_TRY(cudaMemcpyAsync(out, res, sizeof(double2), cudaMemcpyDeviceToDevice, s));
+        return LGPU_OK;
+    }
+    LGPU_CUDA_TRY(cudaMemcpyAsync(out, res, sizeof(double2), cudaMemcpyDeviceToHost, s));
+    LGPU_CUDA_TRY(cudaStreamSynchronize(s));
+    return LGPU_OK;
+}
+
+}  // extern "C"
