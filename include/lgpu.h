@@ -300,7 +300,8 @@ typedef struct {
     uint32_t cval;
     int32_t param;     /* index of the first parameter (-1: none) */
     uint32_t flags;    /* bit 0: adjoint (parametric gates) */
-    uint32_t mat;      /* offset of the gate's slot in the pool, in doubles (16 for 1q, 32 for 2q) */
+    uint32_t mat;      /* offset of the gate's slot in the pool, in doubles (16 for 1q, 48 for 2q; the
+                          C64 float copy of the matrix is written into the slot by lgpu_batch_prepare) */
     uint64_t omask;    /* controls outside the tile (state bits) and their values */
     uint64_t oval;
 } lgpu_bgate_t;
@@ -341,7 +342,7 @@ typedef struct {
 } lgpu_batch_args_t;
 
 lgpu_status_t lgpu_batch_prepare(const lgpu_bgate_t *gates, uint64_t ngates, const double *params, double *pool,
-                                 lgpu_stream_t stream);
+                                 lgpu_dtype_t dt, lgpu_stream_t stream);
 lgpu_status_t lgpu_batch_run(const lgpu_batch_args_t *args, lgpu_dtype_t dt, unsigned grid, lgpu_stream_t stream);
 
 #ifdef __cplusplus

@@ -24,7 +24,7 @@ def _cls(dtype):
 class BatchedExecutor:
     """Owns one native executor: add circuits, prepare once, run many times."""
 
-    def __init__(self, dtype=np.complex128, kmax=0, threads=256, grid=0):
+    def __init__(self, dtype=np.complex128, kmax=0, threads=512, grid=0):
         self.dtype = np.dtype(dtype)
         self._ex = getattr(native(), _cls(dtype))(int(kmax), int(threads), int(grid))
         self.n_circuits = 0
@@ -54,7 +54,7 @@ class BatchedExecutor:
                 "grid": self._ex.grid(), "kmax": self._ex.kmax(), "scratch_bytes": self._ex.scratch_bytes()}
 
 
-def build_executor(circuits, dtype=np.complex128, kmax=0, threads=256, grid=0):
+def build_executor(circuits, dtype=np.complex128, kmax=0, threads=512, grid=0):
     ex = BatchedExecutor(dtype, kmax, threads, grid)
     for n, ops, obs in circuits:
         ex.add(n, ops, obs)

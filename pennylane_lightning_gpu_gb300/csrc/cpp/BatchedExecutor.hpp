@@ -175,6 +175,9 @@ template <class Precision> class BatchedExecutor {
                 term.ci = cc.imag();
                 ht.push_back(term);
             }
+            // terms sharing a flip mask are adjacent: the kernel transforms each flip group once
+            std::stable_sort(ht.begin() + rec.obs_off, ht.end(),
+                             [](const lgpu_bterm_t &x, const lgpu_bterm_t &y) { return x.tflip < y.tflip; });
             rec.obs_cnt = uint32_t(c.obs.size());
             hc.push_back(rec);
             cost[ci] = work;
@@ -351,7 +354,7 @@ template <class Precision> class BatchedExecutor {
         g.param = o.pkind ? int32_t(param_off) + o.param : -1;
         g.flags = o.adjoint ? 1u : 0u;
         g.mat = uint32_t(pool.size());
-        const size_t slot = o.kind >= 5 ? 32 : 16;
+        const size_t slot = o.kind >= 5 ? 48 : 16;  // matrix, then the C128 multipliers or the C64 float copy
         pool.resize(pool.size() + slot, 0.0);
         for (size_t e = 0; e < o.matrix.size(); e++) {
             pool[g.mat + 2 * e] = o.matrix[e].real();
@@ -365,7 +368,7 @@ template <class Precision> class BatchedExecutor {
                                        LGPU_H2D, 1, stream_));
         PL_LGPU_IS_SUCCESS(lgpu_batch_prepare(static_cast<const lgpu_bgate_t *>(d_gates_), ngates_,
                                               static_cast<const double *>(d_params_), static_cast<double *>(d_pool_),
-                                              stream_));
+                                              dt, stream_));
         PL_LGPU_IS_SUCCESS(lgpu_memset(d_counter_, 0, 256, stream_));
         PL_LGPU_IS_SUCCESS(lgpu_batch_run(&args_, dt, grid_used_, stream_));
         PL_LGPU_IS_SUCCESS(lgpu_memcpy(h_out_, d_out_, circuits_.size() * sizeof(double), LGPU_D2H, 1, stream_));

@@ -293,6 +293,35 @@ inline bool fusable(const GateDesc &d) {
     return d.kind == GateDesc::MATRIX && (d.tgts.size() == 1 || d.tgts.size() == 2) && d.ctrls.size() <= 4;
 }
 
+// Fold each uncontrolled 1-target matrix gate into the previous one on the
+// same bit when no gate touching that bit lies between them (the gates in
+// between act on other bits and commute with both): the earlier gate becomes
+// the 2x2 product and the later one IDENTITY.  Used for complex64 states,
+// where one dense body costs less than several structured ones.
+inline void merge_1q_runs(std::vector<GateDesc> &gates) {
+    std::unordered_map<int, size_t> pending;  // bit -> index of the gate that absorbs the next one
+    for (size_t i = 0; i < gates.size(); i++) {
+        GateDesc &g = gates[i];
+        if (g.kind == GateDesc::IDENTITY) continue;
+        if (g.kind == GateDesc::MATRIX && g.tgts.size() == 1 && g.ctrls.empty() && g.matrix.size() == 4) {
+            const auto it = pending.find(g.tgts[0]);
+            if (it != pending.end()) {
+                GateDesc &a = gates[it->second];
+                const std::vector<cd> &b = g.matrix;
+                const std::vector<cd> m = a.matrix;
+                a.matrix = {b[0] * m[0] + b[1] * m[2], b[0] * m[1] + b[1] * m[3], b[2] * m[0] + b[3] * m[2],
+                            b[2] * m[1] + b[3] * m[3]};
+                g = GateDesc{};
+                continue;
+            }
+            pending[g.tgts[0]] = i;
+            continue;
+        }
+        for (int b : g.tgts) pending.erase(b);
+        for (int b : g.ctrls) pending.erase(b);
+    }
+}
+
 inline std::vector<FusedBlock> plan_fusion(const std::vector<GateDesc> &gates, size_t n, int kmax, int mmin,
                                            size_t min_block = 2) {
     std::vector<FusedBlock> out;

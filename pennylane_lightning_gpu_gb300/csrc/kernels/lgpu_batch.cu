@@ -14,6 +14,7 @@
 //                   observable (a sum of Pauli words) is evaluated on the
 //                   tiles of the last block and reduced inside the CTA, so each
 //                   result is written by exactly one CTA in a fixed order.
+#include "lgpu_bodies.cuh"
 #include "lgpu_f64emu.cuh"
 #include "lgpu_internal.cuh"
 
@@ -30,7 +31,7 @@ static_assert(sizeof(lgpu_bgate_t) == 40, "lgpu_bgate_t layout");
 // Matrix preparation
 // ---------------------------------------------------------------------------
 __global__ void bprep_kernel(const lgpu_bgate_t *__restrict__ gates, uint64_t ngates, const double *__restrict__ params,
-                             double *__restrict__ pool) {
+                             double *__restrict__ pool, int c64) {
     const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
     for (uint64_t gi = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; gi < ngates; gi += stride) {
         const lgpu_bgate_t g = gates[gi];
@@ -89,6 +90,13 @@ __global__ void bprep_kernel(const lgpu_bgate_t *__restrict__ gates, uint64_t ng
             }
         }
         // (fixed matrices arrive from the host already in their final, adjointed form)
+        if (c64) {
+            // complex64: a float copy of the matrix (1q: pool + mat + 8, 2q: pool + mat + 32)
+            float *f = reinterpret_cast<float *>(m + (g.kind < BK_DENSE2 ? 8 : 32));
+            const int cnt = g.kind < BK_DENSE2 ? 8 : 32;
+            for (int e = 0; e < cnt; e++) f[e] = float(m[e]);
+            continue;
+        }
         // integer-pipe multiplier constants for the complex128 structured bodies
         if (g.kind < BK_DENSE2) {
             KConst *k = reinterpret_cast<KConst *>(m + 8);
@@ -104,109 +112,172 @@ __global__ void bprep_kernel(const lgpu_bgate_t *__restrict__ gates, uint64_t ng
 }
 
 // ---------------------------------------------------------------------------
-// In-shared-memory gate bodies
+// In-shared-memory gate application
 // ---------------------------------------------------------------------------
+// Matrix coefficients of a 1-target gate in the state's precision: the
+// complex64 copy (floats at pool + mat + 8) is written by bprep_kernel, so no
+// double->float conversion (an FP64-pipe instruction) runs per amplitude.
 template <class T, bool EMU>
-__device__ __forceinline__ void apply1(uint8_t kind, const double *m, cplx_t<T> &a0, cplx_t<T> &a1) {
-    using C = cplx_t<T>;
-    const C x = a0, y = a1;
-    if (kind == BK_X1) {
-        a0 = y;
-        a1 = x;
-        return;
-    }
-    if constexpr (EMU && sizeof(T) == 8) {
-        const KConst *k = reinterpret_cast<const KConst *>(m + 8);
-        const double2 xd = reinterpret_cast<const double2 &>(x), yd = reinterpret_cast<const double2 &>(y);
-        double2 r0, r1;
-        if (kind == BK_DIAG1) {
-            r0 = make_double2(__fma_rn(m[0], xd.x, emul(xd.y, k[0])), __fma_rn(m[0], xd.y, emul(xd.x, k[1])));
-            r1 = make_double2(__fma_rn(m[6], yd.x, emul(yd.y, k[2])), __fma_rn(m[6], yd.y, emul(yd.x, k[3])));
-        } else if (kind == BK_REAL1) {
-            r0 = make_double2(__fma_rn(m[0], xd.x, emul(yd.x, k[0])), __fma_rn(m[0], xd.y, emul(yd.y, k[0])));
-            r1 = make_double2(__fma_rn(m[6], yd.x, emul(xd.x, k[1])), __fma_rn(m[6], yd.y, emul(xd.y, k[1])));
-        } else if (kind == BK_RXLIKE1) {
-            r0 = make_double2(__fma_rn(m[0], xd.x, emul(yd.y, k[0])), __fma_rn(m[0], xd.y, emul(yd.x, k[1])));
-            r1 = make_double2(__fma_rn(m[0], yd.x, emul(xd.y, k[2])), __fma_rn(m[0], yd.y, emul(xd.x, k[3])));
-        } else {
-            r0.x = m[0] * xd.x - m[1] * xd.y + m[2] * yd.x - m[3] * yd.y;
-            r0.y = m[0] * xd.y + m[1] * xd.x + m[2] * yd.y + m[3] * yd.x;
-            r1.x = m[4] * xd.x - m[5] * xd.y + m[6] * yd.x - m[7] * yd.y;
-            r1.y = m[4] * xd.y + m[5] * xd.x + m[6] * yd.y + m[7] * yd.x;
-        }
-        a0 = reinterpret_cast<const C &>(r0);
-        a1 = reinterpret_cast<const C &>(r1);
+__device__ __forceinline__ void load_coef1(const double *pool, uint32_t mat, T (&m)[8], KConst (&k)[4]) {
+    if constexpr (sizeof(T) == 4) {
+        const float4 *f = reinterpret_cast<const float4 *>(pool + mat + 8);
+        const float4 u = f[0], v = f[1];
+        m[0] = u.x; m[1] = u.y; m[2] = u.z; m[3] = u.w;
+        m[4] = v.x; m[5] = v.y; m[6] = v.z; m[7] = v.w;
+#pragma unroll
+        for (int i = 0; i < 4; i++) k[i] = KConst{};
     } else {
-        const T m0 = T(m[0]), m1 = T(m[1]), m2 = T(m[2]), m3 = T(m[3]), m4 = T(m[4]), m5 = T(m[5]), m6 = T(m[6]),
-                m7 = T(m[7]);
-        if (kind == BK_DIAG1) {
-            a0 = mk<T>(m0 * x.x - m1 * x.y, m0 * x.y + m1 * x.x);
-            a1 = mk<T>(m6 * y.x - m7 * y.y, m6 * y.y + m7 * y.x);
-        } else {
-            a0 = mk<T>(m0 * x.x - m1 * x.y + m2 * y.x - m3 * y.y, m0 * x.y + m1 * x.x + m2 * y.y + m3 * y.x);
-            a1 = mk<T>(m4 * x.x - m5 * x.y + m6 * y.x - m7 * y.y, m4 * x.y + m5 * x.x + m6 * y.y + m7 * y.x);
+        const double2 *d = reinterpret_cast<const double2 *>(pool + mat);
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            const double2 v = d[i];
+            m[2 * i] = v.x;
+            m[2 * i + 1] = v.y;
         }
+        const KConst *kc = reinterpret_cast<const KConst *>(pool + mat + 8);
+#pragma unroll
+        for (int i = 0; i < 4; i++) k[i] = EMU ? kc[i] : KConst{};
     }
 }
 
-// Apply one gate to the tile in shared memory (all threads).
+template <class T, int BODY, bool EMU>
+__device__ __forceinline__ void batch_pairs(cplx_t<T> *tile, int E, int q, uint32_t cmask, uint32_t cval,
+                                            const double *pool, uint32_t mat) {
+    using C = cplx_t<T>;
+    T m[8];
+    KConst k[4];
+    load_coef1<T, EMU>(pool, mat, m, k);
+    const uint32_t holes = cmask | (1u << q);
+    const int nfree = E >> __popc(holes);
+    PairWalk w(holes, threadIdx.x, blockDim.x);
+#pragma unroll 2
+    for (int f = threadIdx.x; f < nfree; f += blockDim.x) {
+        const int e0 = int(w.x | cval);
+        const int e1 = e0 | (1 << q);
+        w.step();
+        C a0 = tile[e0], a1 = tile[e1];
+        body1_sel<T, BODY, EMU>(m, k, a0, a1);
+        tile[e0] = a0;
+        tile[e1] = a1;
+    }
+}
+
+// Apply one gate to the tile in shared memory (all threads; the caller
+// synchronises afterwards).
 template <class T, bool EMU>
 __device__ __forceinline__ void tile_gate(cplx_t<T> *tile, int E, const lgpu_bgate_t &g, const double *pool) {
     using C = cplx_t<T>;
-    const double *m = pool + g.mat;
     if (g.kind < BK_DENSE2) {
         const int q = g.q0;
-        const int lo = (1 << q) - 1;
-        for (int pr = threadIdx.x; pr < (E >> 1); pr += blockDim.x) {
-            const int e0 = ((pr & ~lo) << 1) | (pr & lo);
-            if ((uint32_t(e0) & g.cmask) != g.cval) continue;
-            const int e1 = e0 | (1 << q);
-            C a0 = tile[e0], a1 = tile[e1];
-            apply1<T, EMU>(g.kind, m, a0, a1);
-            tile[e0] = a0;
-            tile[e1] = a1;
+        switch (g.kind) {
+        case BK_DIAG1: batch_pairs<T, B_DIAG, EMU>(tile, E, q, g.cmask, g.cval, pool, g.mat); break;
+        case BK_X1: batch_pairs<T, B_PERM, EMU>(tile, E, q, g.cmask, g.cval, pool, g.mat); break;
+        case BK_REAL1: batch_pairs<T, B_REAL, EMU>(tile, E, q, g.cmask, g.cval, pool, g.mat); break;
+        case BK_RXLIKE1: batch_pairs<T, B_RXLIKE, EMU>(tile, E, q, g.cmask, g.cval, pool, g.mat); break;
+        default: batch_pairs<T, B_DENSE, false>(tile, E, q, g.cmask, g.cval, pool, g.mat); break;
         }
-    } else {
-        const int qa = g.q0, qb = g.q1;
-        const int lo_b = min(qa, qb), hi_b = max(qa, qb);
-        const int lm1 = (1 << lo_b) - 1, lm2 = (1 << hi_b) - 1;
-        for (int pr = threadIdx.x; pr < (E >> 2); pr += blockDim.x) {
-            int e = ((pr & ~lm1) << 1) | (pr & lm1);
-            e = ((e & ~lm2) << 1) | (e & lm2);
-            if ((uint32_t(e) & g.cmask) != g.cval) continue;
-            const int i0 = e, i1 = e | (1 << qb), i2 = e | (1 << qa), i3 = e | (1 << qa) | (1 << qb);
-            if (g.kind == BK_SWAP2) {
-                const C t = tile[i1];
-                tile[i1] = tile[i2];
-                tile[i2] = t;
-                continue;
-            }
-            const C a[4] = {tile[i0], tile[i1], tile[i2], tile[i3]};
-            C r[4];
-#pragma unroll
-            for (int row = 0; row < 4; row++) {
-                double xr = 0, xi = 0;
-#pragma unroll
-                for (int c = 0; c < 4; c++) {
-                    const double mr = m[2 * (row * 4 + c)], mi = m[2 * (row * 4 + c) + 1];
-                    xr += mr * double(a[c].x) - mi * double(a[c].y);
-                    xi += mr * double(a[c].y) + mi * double(a[c].x);
-                }
-                r[row] = mk<T>(T(xr), T(xi));
-            }
-            tile[i0] = r[0];
-            tile[i1] = r[1];
-            tile[i2] = r[2];
-            tile[i3] = r[3];
+        return;
+    }
+    const int qa = g.q0, qb = g.q1;
+    const uint32_t holes = g.cmask | (1u << qa) | (1u << qb);
+    const int nfree = E >> __popc(holes);
+    PairWalk w(holes, threadIdx.x, blockDim.x);
+    // 4x4 coefficients: doubles at pool + mat, the complex64 copy (floats) at pool + mat + 32
+    const T *mm = sizeof(T) == 4 ? reinterpret_cast<const T *>(pool + g.mat + 32)
+                                 : reinterpret_cast<const T *>(pool + g.mat);
+    for (int f = threadIdx.x; f < nfree; f += blockDim.x) {
+        const int e = int(w.x | g.cval);
+        w.step();
+        const int i0 = e, i1 = e | (1 << qb), i2 = e | (1 << qa), i3 = e | (1 << qa) | (1 << qb);
+        if (g.kind == BK_SWAP2) {
+            const C t = tile[i1];
+            tile[i1] = tile[i2];
+            tile[i2] = t;
+            continue;
         }
+        const C a[4] = {tile[i0], tile[i1], tile[i2], tile[i3]};
+        C r[4];
+#pragma unroll
+        for (int row = 0; row < 4; row++) {
+            T xr = 0, xi = 0;
+#pragma unroll
+            for (int c = 0; c < 4; c++) {
+                const T mr = mm[2 * (row * 4 + c)], mi = mm[2 * (row * 4 + c) + 1];
+                xr = fmaT(mr, a[c].x, fmaT(-mi, a[c].y, xr));
+                xi = fmaT(mr, a[c].y, fmaT(mi, a[c].x, xi));
+            }
+            r[row] = mk<T>(xr, xi);
+        }
+        tile[i0] = r[0];
+        tile[i1] = r[1];
+        tile[i2] = r[2];
+        tile[i3] = r[3];
     }
 }
 
-// Observable contribution of one tile: sum over terms of Re(c_t sum_e conj(a_e) sigma_t(g(e^F)) a_{e^F}),
-// flip masks given in tile positions (tflip) and global sign masks.
+// ---------------------------------------------------------------------------
+// Observable on a tile
+// ---------------------------------------------------------------------------
+// Term t contributes Re((cr + i ci) sum_e s_t(e) conj(a_e) a_{e^F}), F its flip
+// mask in tile positions and s_t(e) = (-1)^popc(g(e^F) & sign_t) with g the
+// global index.  With L_t the sign mask in tile positions,
+//   popc(g(e^F) & sign) = popc(base & sign) + popc(F & L_t) + popc(e & L_t)  (mod 2).
+// Thread `slot` owns e = slot + S*i (i = 0..7, S = E/8); the sign over i is
+// (-1)^popc(i & h_t), h_t = L_t >> log2 S, so the eight products of one flip
+// group go through one 8-point Walsh-Hadamard transform and each term then
+// costs a select and one multiply-add instead of a pass over the tile.
+// s_lm[t] = L_t | popc(F & L_t) << 31 and s_c[t] = (cr, ci) are per block.
+constexpr uint32_t kObsTermsCached = 1024;
+
 template <class T>
-__device__ __forceinline__ double tile_obs(const cplx_t<T> *tile, int E, const lgpu_bterm_t *terms, uint32_t nterms,
-                                           uint64_t base, int m, const uint64_t *hi_off) {
+__device__ __forceinline__ double tile_obs(const cplx_t<T> *tile, int k, const lgpu_bterm_t *terms, uint32_t nterms,
+                                           uint64_t base, const uint32_t *s_lm, const cplx_t<T> *s_c) {
+    using A = T;
+    const int lgS = k - 3, S = 1 << lgS;
+    A acc = 0;
+    for (int slot = threadIdx.x; slot < S; slot += blockDim.x) {
+        uint32_t t0 = 0;
+        while (t0 < nterms) {
+            const uint32_t F = terms[t0].tflip;
+            uint32_t t1 = t0 + 1;
+            while (t1 < nterms && terms[t1].tflip == F) t1++;
+            const int fs = int(F) & (S - 1), fh = int(F) >> lgS;
+            A xr[8], xi[8];
+#pragma unroll
+            for (int i = 0; i < 8; i++) {
+                const cplx_t<T> a = tile[slot + S * i];
+                if (F) {
+                    const cplx_t<T> b = tile[(slot ^ fs) + S * (i ^ fh)];
+                    xr[i] = a.x * b.x + a.y * b.y;
+                    xi[i] = a.x * b.y - a.y * b.x;
+                } else {
+                    xr[i] = a.x * a.x + a.y * a.y;
+                    xi[i] = A(0);
+                }
+            }
+            wht8(xr);
+            if (F) wht8(xi);
+            for (uint32_t t = t0; t < t1; t++) {
+                const uint32_t lm = s_lm[t];
+                const uint32_t L = lm & 0x7fffffffu;
+                const int par =
+                    (__popc(uint32_t(slot) & L & uint32_t(S - 1)) + __popcll(base & terms[t].sign) + int(lm >> 31)) & 1;
+                const int h = int(L >> lgS) & 7;
+                const cplx_t<T> c = s_c[t];
+                A v = c.x * sel8(xr, h);
+                if (F) v -= c.y * sel8(xi, h);
+                acc += par ? -v : v;
+            }
+            t0 = t1;
+        }
+    }
+    return double(acc);
+}
+
+// Direct form for tiles of fewer than 8 amplitudes or more terms than cached.
+template <class T>
+__device__ __forceinline__ double tile_obs_direct(const cplx_t<T> *tile, int E, const lgpu_bterm_t *terms,
+                                                  uint32_t nterms, uint64_t base, int m, const uint64_t *hi_off) {
     double acc = 0.0;
     const int lowmask = (1 << m) - 1;
     for (uint32_t t = 0; t < nterms; t++) {
@@ -284,6 +355,8 @@ __global__ void __launch_bounds__(512, 1) batch_kernel(lgpu_batch_args_t a) {
     __shared__ double red[32];
     __shared__ uint32_t s_idx;
     __shared__ __align__(8) uint64_t full_bar[kRing];
+    __shared__ uint32_t s_lm[kObsTermsCached];  // observable terms of the current last block
+    __shared__ C s_c[kObsTermsCached];
     C *scratch = reinterpret_cast<C *>(a.scratch) + uint64_t(blockIdx.x) * a.scratch_amps;
     const uint32_t tile_amps = 1u << a.klarge;  // ring stage size (large circuits)
     if (threadIdx.x == 0) {
@@ -313,6 +386,17 @@ __global__ void __launch_bounds__(512, 1) batch_kernel(lgpu_batch_args_t a) {
                     if ((threadIdx.x >> (q - mlow)) & 1) o |= uint64_t(1) << blk.bits[q];
                 hi_off[threadIdx.x] = o;
             }
+            const bool wht = last && k >= 3 && cir.obs_cnt <= kObsTermsCached;
+            if (wht) {
+                for (uint32_t t = threadIdx.x; t < cir.obs_cnt; t += blockDim.x) {
+                    const lgpu_bterm_t tm = a.terms[cir.obs_off + t];
+                    uint32_t L = 0;
+                    for (int q = 0; q < k; q++)
+                        if ((tm.sign >> blk.bits[q]) & 1u) L |= 1u << q;
+                    s_lm[t] = L | (uint32_t(__popc(uint32_t(tm.tflip) & L) & 1) << 31);
+                    s_c[t] = mk<T>(T(tm.cr), T(tm.ci));
+                }
+            }
             __syncthreads();
             auto tile_base = [&](uint64_t tau) {
                 uint64_t base = tau;
@@ -331,7 +415,8 @@ __global__ void __launch_bounds__(512, 1) batch_kernel(lgpu_batch_args_t a) {
                     tile_gate<T, EMU>(tile, E, a.gates[blk.gate_off + gi], a.pool);
                     __syncthreads();
                 }
-                acc += tile_obs<T>(tile, E, a.terms + cir.obs_off, cir.obs_cnt, 0, mlow, hi_off);
+                acc += wht ? tile_obs<T>(tile, k, a.terms + cir.obs_off, cir.obs_cnt, 0, s_lm, s_c)
+                           : tile_obs_direct<T>(tile, E, a.terms + cir.obs_off, cir.obs_cnt, 0, mlow, hi_off);
                 __syncthreads();
                 continue;
             }
@@ -387,7 +472,8 @@ __global__ void __launch_bounds__(512, 1) batch_kernel(lgpu_batch_args_t a) {
                     __syncthreads();
                 }
                 if (last) {
-                    acc += tile_obs<T>(tile, E, a.terms + cir.obs_off, cir.obs_cnt, base, mlow, hi_off);
+                    acc += wht ? tile_obs<T>(tile, k, a.terms + cir.obs_off, cir.obs_cnt, base, s_lm, s_c)
+                               : tile_obs_direct<T>(tile, E, a.terms + cir.obs_off, cir.obs_cnt, base, mlow, hi_off);
                     __syncthreads();
                 } else {
                     b_fence();
@@ -454,11 +540,12 @@ using namespace lgpu;
 extern "C" {
 
 lgpu_status_t lgpu_batch_prepare(const lgpu_bgate_t *gates, uint64_t ngates, const double *params, double *pool,
-                                 lgpu_stream_t stream) {
+                                 lgpu_dtype_t dt, lgpu_stream_t stream) {
     if (ngates == 0) return LGPU_OK;
     if (!gates || !pool) return fail(LGPU_ERR_INVALID_ARG, "null gates/pool");
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
-    bprep_kernel<<<grid_for(ngates, 128, 1, 4), 128, 0, s>>>(gates, ngates, params, pool);
+    if (dt != LGPU_C64 && dt != LGPU_C128) return fail(LGPU_ERR_INVALID_ARG, "unknown dtype");
+    bprep_kernel<<<grid_for(ngates, 128, 1, 4), 128, 0, s>>>(gates, ngates, params, pool, dt == LGPU_C64 ? 1 : 0);
     LGPU_CHECK_LAUNCH();
     return LGPU_OK;
 }

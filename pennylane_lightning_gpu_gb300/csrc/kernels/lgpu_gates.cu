@@ -14,100 +14,13 @@
 //  * pauli_rot_kernel exp(i angle P) for Pauli words, pairwise (i, i^flip).
 //  * fused_kernel     a block of 1/2-target gates applied to shared-memory
 //                     tiles of 2^k amplitudes: one HBM pass for many gates.
+#include "lgpu_bodies.cuh"
 #include "lgpu_f64emu.cuh"
 #include "lgpu_internal.cuh"
 
 namespace lgpu {
 
 constexpr int kGateBlock = 256;
-
-enum Body1 : int { B_DENSE = 0, B_DIAG = 1, B_PERM = 2, B_ANTIDIAG = 3, B_REAL = 4, B_RXLIKE = 5 };
-
-template <class T, class I> struct G1Params {
-    Holes holes;
-    I tbit;
-    I cset;
-    I ngroups;
-    T m[8];
-    KConst k[4];  // integer-pipe multipliers (complex128 EMU bodies)
-};
-
-template <class T, int BODY>
-__device__ __forceinline__ void body1(const T *m, cplx_t<T> &a0, cplx_t<T> &a1) {
-    using C = cplx_t<T>;
-    const C x = a0, y = a1;
-    if constexpr (BODY == B_PERM) {
-        a0 = y;
-        a1 = x;
-    } else if constexpr (BODY == B_DIAG) {
-        a0 = mk<T>(fmaT(m[0], x.x, -m[1] * x.y), fmaT(m[0], x.y, m[1] * x.x));
-        a1 = mk<T>(fmaT(m[6], y.x, -m[7] * y.y), fmaT(m[6], y.y, m[7] * y.x));
-    } else if constexpr (BODY == B_ANTIDIAG) {
-        a0 = mk<T>(fmaT(m[2], y.x, -m[3] * y.y), fmaT(m[2], y.y, m[3] * y.x));
-        a1 = mk<T>(fmaT(m[4], x.x, -m[5] * x.y), fmaT(m[4], x.y, m[5] * x.x));
-    } else if constexpr (BODY == B_REAL) {
-        a0 = mk<T>(fmaT(m[0], x.x, m[2] * y.x), fmaT(m[0], x.y, m[2] * y.y));
-        a1 = mk<T>(fmaT(m[4], x.x, m[6] * y.x), fmaT(m[4], x.y, m[6] * y.y));
-    } else if constexpr (BODY == B_RXLIKE) {
-        // m00 = m11 = c (real), m01 = i*u, m10 = i*v (u, v real)
-        const T c = m[0], u = m[3], v = m[5];
-        a0 = mk<T>(fmaT(c, x.x, -u * y.y), fmaT(c, x.y, u * y.x));
-        a1 = mk<T>(fmaT(c, y.x, -v * x.y), fmaT(c, y.y, v * x.x));
-    } else {
-        C r0 = mk<T>(m[0] * x.x, m[0] * x.y);
-        r0.x = fmaT(-m[1], x.y, r0.x);
-        r0.y = fmaT(m[1], x.x, r0.y);
-        r0.x = fmaT(m[2], y.x, r0.x);
-        r0.y = fmaT(m[2], y.y, r0.y);
-        r0.x = fmaT(-m[3], y.y, r0.x);
-        r0.y = fmaT(m[3], y.x, r0.y);
-        C r1 = mk<T>(m[4] * x.x, m[4] * x.y);
-        r1.x = fmaT(-m[5], x.y, r1.x);
-        r1.y = fmaT(m[5], x.x, r1.y);
-        r1.x = fmaT(m[6], y.x, r1.x);
-        r1.y = fmaT(m[6], y.y, r1.y);
-        r1.x = fmaT(-m[7], y.y, r1.x);
-        r1.y = fmaT(m[7], y.x, r1.y);
-        a0 = r0;
-        a1 = r1;
-    }
-}
-
-// complex128 bodies with one DFMA + one integer-pipe multiply per output
-// component (half the FP64 issue of body1).  k[] holds the constants the
-// host prepared for the body (see run_gate1).
-template <int BODY>
-__device__ __forceinline__ void body1_emu(const double *m, const KConst *k, double2 &a0, double2 &a1) {
-    const double2 x = a0, y = a1;
-    if constexpr (BODY == B_PERM) {
-        a0 = y;
-        a1 = x;
-    } else if constexpr (BODY == B_DIAG) {  // k = {-m00i, m00i, -m11i, m11i}
-        a0 = make_double2(__fma_rn(m[0], x.x, emul(x.y, k[0])), __fma_rn(m[0], x.y, emul(x.x, k[1])));
-        a1 = make_double2(__fma_rn(m[6], y.x, emul(y.y, k[2])), __fma_rn(m[6], y.y, emul(y.x, k[3])));
-    } else if constexpr (BODY == B_ANTIDIAG) {  // k = {-m01i, m01i, -m10i, m10i}
-        a0 = make_double2(__fma_rn(m[2], y.x, emul(y.y, k[0])), __fma_rn(m[2], y.y, emul(y.x, k[1])));
-        a1 = make_double2(__fma_rn(m[4], x.x, emul(x.y, k[2])), __fma_rn(m[4], x.y, emul(x.x, k[3])));
-    } else if constexpr (BODY == B_REAL) {  // k = {m01r, m10r}
-        a0 = make_double2(__fma_rn(m[0], x.x, emul(y.x, k[0])), __fma_rn(m[0], x.y, emul(y.y, k[0])));
-        a1 = make_double2(__fma_rn(m[6], y.x, emul(x.x, k[1])), __fma_rn(m[6], y.y, emul(x.y, k[1])));
-    } else if constexpr (BODY == B_RXLIKE) {  // k = {-u, u, -v, v}
-        const double c = m[0];
-        a0 = make_double2(__fma_rn(c, x.x, emul(y.y, k[0])), __fma_rn(c, x.y, emul(y.x, k[1])));
-        a1 = make_double2(__fma_rn(c, y.x, emul(x.y, k[2])), __fma_rn(c, y.y, emul(x.x, k[3])));
-    } else {
-        body1<double, B_DENSE>(m, a0, a1);
-    }
-}
-
-template <class T, int BODY, bool EMU>
-__device__ __forceinline__ void body1_sel(const T *m, const KConst *k, cplx_t<T> &a0, cplx_t<T> &a1) {
-    if constexpr (EMU && sizeof(T) == 8)
-        body1_emu<BODY>(reinterpret_cast<const double *>(m), k, reinterpret_cast<double2 &>(a0),
-                        reinterpret_cast<double2 &>(a1));
-    else
-        body1<T, BODY>(m, a0, a1);
-}
 
 // ITEMS pairs per thread in flight: all loads are issued before any math.
 template <class T, class I, int BODY, int ITEMS, bool EMU>
@@ -377,7 +290,7 @@ template <class T, class I, int TT> struct GkParams {
     I cset;
     I ngroups;
     I off[1 << TT];
-    double m[2 * (1 << TT) * (1 << TT)];
+    T m[2 * (1 << TT) * (1 << TT)];  // state precision: no conversions in the loop
 };
 
 template <class T, class I, int TT>
@@ -398,7 +311,7 @@ __global__ void __launch_bounds__(TT >= 4 ? 128 : kGateBlock)
             T xr = 0, xi = 0;
 #pragma unroll
             for (int c = 0; c < D; c++) {
-                const T mr = T(p.m[2 * (r * D + c)]), mi = T(p.m[2 * (r * D + c) + 1]);
+                const T mr = p.m[2 * (r * D + c)], mi = p.m[2 * (r * D + c) + 1];
                 xr = fmaT(mr, a[c].x, xr);
                 xr = fmaT(-mi, a[c].y, xr);
                 xi = fmaT(mr, a[c].y, xi);
@@ -489,17 +402,17 @@ __global__ void __launch_bounds__(kGateBlock)
 // Fused shared-memory tiles
 // ---------------------------------------------------------------------------
 constexpr int kFusedMaxGates = 96;
-constexpr int kFusedMatPool = 3072;  // doubles
+constexpr int kFusedMatPool = 2304;  // matrix elements, in the state's precision
 constexpr int kFusedBlock = 512;
 
 struct FGate {
-    uint8_t ntgt, q0, q1, pad;
-    uint32_t in_mask, in_val;  // controls inside the tile (tile positions)
-    uint32_t mat_off;          // into the matrix pool (doubles)
+    uint8_t ntgt, q0, q1, body;  // q0 = most significant matrix bit; body: Body1 of a 1-target gate
+    uint32_t in_mask, in_val;    // controls inside the tile (tile positions)
+    uint32_t mat_off;            // into the matrix pool
     uint64_t out_mask, out_val;  // controls outside the tile (state bits)
 };
 
-template <class I> struct FusedParams {
+template <class T, class I> struct FusedParams {
     Holes holes;       // tile bits (sorted) as holes: tile base = insert(tau)
     I ntiles;
     int k;             // tile bits
@@ -507,13 +420,37 @@ template <class I> struct FusedParams {
     I hi_off[64];      // offsets of the high tile bits (k - m <= 6 -> 64 entries)
     int ngates;
     FGate gates[kFusedMaxGates];
-    double mats[kFusedMatPool];
+    T mats[kFusedMatPool];
+    KConst kc[kFusedMaxGates][4];  // integer-pipe multipliers (complex128 structured bodies)
 };
 
-static_assert(sizeof(FusedParams<uint64_t>) <= 32000, "fused kernel parameters exceed the 32 KB limit");
+template <class T, int BODY, bool EMU>
+__device__ __forceinline__ void tile_pairs(cplx_t<T> *tile, int E, int q, uint32_t in_mask, uint32_t in_val,
+                                           const T *m, const KConst *k) {
+    using C = cplx_t<T>;
+    const uint32_t holes = in_mask | (1u << q);
+    const int nfree = E >> __popc(holes);
+    T mr[8];
+#pragma unroll
+    for (int i = 0; i < 8; i++) mr[i] = m[i];
+    KConst kr[4];
+#pragma unroll
+    for (int i = 0; i < 4; i++) kr[i] = EMU ? k[i] : KConst{};
+    PairWalk w(holes, threadIdx.x, kFusedBlock);
+#pragma unroll 2
+    for (int f = threadIdx.x; f < nfree; f += kFusedBlock) {
+        const int e0 = int(w.x | in_val);
+        const int e1 = e0 | (1 << q);
+        w.step();
+        C a0 = tile[e0], a1 = tile[e1];
+        body1_sel<T, BODY, EMU>(mr, kr, a0, a1);
+        tile[e0] = a0;
+        tile[e1] = a1;
+    }
+}
 
-template <class T, class I>
-__global__ void __launch_bounds__(kFusedBlock) fused_kernel(cplx_t<T> *__restrict__ sv, const FusedParams<I> p) {
+template <class T, class I, bool EMU>
+__global__ void __launch_bounds__(kFusedBlock, 2) fused_kernel(cplx_t<T> *__restrict__ sv, const FusedParams<T, I> p) {
     using C = cplx_t<T>;
     extern __shared__ unsigned char smem_raw[];
     C *tile = reinterpret_cast<C *>(smem_raw);
@@ -528,34 +465,25 @@ __global__ void __launch_bounds__(kFusedBlock) fused_kernel(cplx_t<T> *__restric
         for (int gi = 0; gi < p.ngates; gi++) {
             const FGate &g = p.gates[gi];
             if ((uint64_t(base) & g.out_mask) != g.out_val) continue;  // tile-uniform
-            const double *mm = p.mats + g.mat_off;
+            const T *mm = p.mats + g.mat_off;
             if (g.ntgt == 1) {
-                const T m0r = T(mm[0]), m0i = T(mm[1]), m1r = T(mm[2]), m1i = T(mm[3]);
-                const T m2r = T(mm[4]), m2i = T(mm[5]), m3r = T(mm[6]), m3i = T(mm[7]);
-                const int q = g.q0;
-                const int lo = (1 << q) - 1;
-                for (int pr = threadIdx.x; pr < (E >> 1); pr += kFusedBlock) {
-                    const int e0 = ((pr & ~lo) << 1) | (pr & lo);
-                    if ((uint32_t(e0) & g.in_mask) != g.in_val) continue;
-                    const int e1 = e0 | (1 << q);
-                    const C x = tile[e0], y = tile[e1];
-                    C r0, r1;
-                    r0.x = m0r * x.x - m0i * x.y + m1r * y.x - m1i * y.y;
-                    r0.y = m0r * x.y + m0i * x.x + m1r * y.y + m1i * y.x;
-                    r1.x = m2r * x.x - m2i * x.y + m3r * y.x - m3i * y.y;
-                    r1.y = m2r * x.y + m2i * x.x + m3r * y.y + m3i * y.x;
-                    tile[e0] = r0;
-                    tile[e1] = r1;
+                const KConst *kk = p.kc[gi];
+                switch (g.body) {
+                case B_DIAG: tile_pairs<T, B_DIAG, EMU>(tile, E, g.q0, g.in_mask, g.in_val, mm, kk); break;
+                case B_PERM: tile_pairs<T, B_PERM, EMU>(tile, E, g.q0, g.in_mask, g.in_val, mm, kk); break;
+                case B_ANTIDIAG: tile_pairs<T, B_ANTIDIAG, EMU>(tile, E, g.q0, g.in_mask, g.in_val, mm, kk); break;
+                case B_REAL: tile_pairs<T, B_REAL, EMU>(tile, E, g.q0, g.in_mask, g.in_val, mm, kk); break;
+                case B_RXLIKE: tile_pairs<T, B_RXLIKE, EMU>(tile, E, g.q0, g.in_mask, g.in_val, mm, kk); break;
+                default: tile_pairs<T, B_DENSE, false>(tile, E, g.q0, g.in_mask, g.in_val, mm, kk); break;
                 }
             } else {
                 const int qa = g.q0, qb = g.q1;  // qa = most significant matrix bit
-                const int lo_b = min(qa, qb), hi_b = max(qa, qb);
-                const int lm1 = (1 << lo_b) - 1;
-                for (int pr = threadIdx.x; pr < (E >> 2); pr += kFusedBlock) {
-                    int e = ((pr & ~lm1) << 1) | (pr & lm1);
-                    const int lm2 = (1 << hi_b) - 1;
-                    e = ((e & ~lm2) << 1) | (e & lm2);
-                    if ((uint32_t(e) & g.in_mask) != g.in_val) continue;
+                const uint32_t holes = g.in_mask | (1u << qa) | (1u << qb);
+                const int nfree = E >> __popc(holes);
+                PairWalk w(holes, threadIdx.x, kFusedBlock);
+                for (int f = threadIdx.x; f < nfree; f += kFusedBlock) {
+                    const int e = int(w.x | g.in_val);
+                    w.step();
                     int idx[4];
                     idx[0] = e;
                     idx[1] = e | (1 << qb);
@@ -569,9 +497,9 @@ __global__ void __launch_bounds__(kFusedBlock) fused_kernel(cplx_t<T> *__restric
                         T xr = 0, xi = 0;
 #pragma unroll
                         for (int c = 0; c < 4; c++) {
-                            const T mr = T(mm[2 * (r * 4 + c)]), mi = T(mm[2 * (r * 4 + c) + 1]);
-                            xr += mr * a[c].x - mi * a[c].y;
-                            xi += mr * a[c].y + mi * a[c].x;
+                            const T mr = mm[2 * (r * 4 + c)], mi = mm[2 * (r * 4 + c) + 1];
+                            xr = fmaT(mr, a[c].x, fmaT(-mi, a[c].y, xr));
+                            xi = fmaT(mr, a[c].y, fmaT(mi, a[c].x, xi));
                         }
                         tile[idx[r]] = mk<T>(xr, xi);
                     }
@@ -779,8 +707,8 @@ static lgpu_status_t run_gatek(cplx_t<T> *sv, unsigned nstates, cplx_t<T> *const
         p->off[r] = I(o);
     }
     for (int e = 0; e < D * D; e++) {
-        p->m[2 * e] = m[size_t(e)].re;
-        p->m[2 * e + 1] = m[size_t(e)].im;
+        p->m[2 * e] = T(m[size_t(e)].re);
+        p->m[2 * e + 1] = T(m[size_t(e)].im);
     }
     const int block = TT >= 4 ? 128 : kGateBlock;
     dim3 grid(grid_for(uint64_t(p->ngroups), block, 1, 8), nstates ? nstates : 1);
@@ -947,9 +875,63 @@ static lgpu_status_t pauli_rot_dispatch(void *sv, void *const *svs, uint32_t nst
     return st;
 }
 
+// Structured body of a 2x2 matrix (m: re/im interleaved, row-major) and the
+// integer-pipe multipliers its complex128 body uses.
+static int body_of_2x2(const double *mm, KConst *kc) {
+    const Cm a{mm[0], mm[1]}, b{mm[2], mm[3]}, c{mm[4], mm[5]}, d{mm[6], mm[7]};
+    for (int i = 0; i < 4; i++) kc[i] = make_kconst(0.0);
+    const bool diag = eq(b, 0, 0) && eq(c, 0, 0);
+    const bool anti = eq(a, 0, 0) && eq(d, 0, 0);
+    const bool real = a.im == 0 && b.im == 0 && c.im == 0 && d.im == 0;
+    const bool rxlike = a.im == 0 && d.im == 0 && a.re == d.re && b.re == 0 && c.re == 0;
+    if (diag) {
+        kc[0] = make_kconst(-a.im); kc[1] = make_kconst(a.im);
+        kc[2] = make_kconst(-d.im); kc[3] = make_kconst(d.im);
+        return B_DIAG;
+    }
+    if (anti && eq(b, 1, 0) && eq(c, 1, 0)) return B_PERM;
+    if (anti) {
+        kc[0] = make_kconst(-b.im); kc[1] = make_kconst(b.im);
+        kc[2] = make_kconst(-c.im); kc[3] = make_kconst(c.im);
+        return B_ANTIDIAG;
+    }
+    if (real) {
+        kc[0] = make_kconst(b.re); kc[1] = make_kconst(c.re);
+        return B_REAL;
+    }
+    if (rxlike) {
+        kc[0] = make_kconst(-b.im); kc[1] = make_kconst(b.im);
+        kc[2] = make_kconst(-c.im); kc[3] = make_kconst(c.im);
+        return B_RXLIKE;
+    }
+    return B_DENSE;
+}
+
+template <class T, class I, bool EMU>
+static lgpu_status_t launch_fused(cplx_t<T> *sv, const FusedParams<T, I> &p, size_t smem, cudaStream_t s) {
+    // dynamic shared memory opted in so far, per device (set outside any
+    // capture: the first launch of a size runs eagerly)
+    static size_t attr[64] = {};
+    int dev = 0;
+    LGPU_CUDA_TRY(cudaGetDevice(&dev));
+    if (smem > 48 * 1024 && (dev >= 64 || smem > attr[dev])) {
+        cudaError_t e =
+            cudaFuncSetAttribute(fused_kernel<T, I, EMU>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+        if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(fused)");
+        if (dev < 64) attr[dev] = smem;
+    }
+    const int per_sm = std::max(1, int((200 * 1024) / smem));
+    const unsigned grid = unsigned(std::min<uint64_t>(uint64_t(p.ntiles), uint64_t(sm_count()) * per_sm));
+    fused_kernel<T, I, EMU><<<grid, kFusedBlock, smem, s>>>(sv, p);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(e, "fused kernel launch");
+    return LGPU_OK;
+}
+
 template <class T, class I>
 static lgpu_status_t fused_t(cplx_t<T> *sv, uint32_t n, const std::vector<int> &tile_bits,
                              uint32_t ngates, const lgpu_fused_gate_t *gates, cudaStream_t s) {
+    static_assert(sizeof(FusedParams<T, I>) <= 32000, "fused kernel parameters exceed the 32 KB limit");
     const int k = int(tile_bits.size());
     // Tile position of each state bit
     std::vector<int> pos(n, -1);
@@ -957,7 +939,7 @@ static lgpu_status_t fused_t(cplx_t<T> *sv, uint32_t n, const std::vector<int> &
     int m = 0;
     while (m < k && tile_bits[size_t(m)] == m) m++;
     if (k - m > 6) return fail(LGPU_ERR_INVALID_ARG, "fused tile: at most 6 tile bits above the contiguous low run");
-    auto *p = new FusedParams<I>();
+    auto *p = new FusedParams<T, I>();
     p->holes = make_holes(tile_bits);
     p->ntiles = I(uint64_t(1) << (n - k));
     p->k = k;
@@ -968,6 +950,7 @@ static lgpu_status_t fused_t(cplx_t<T> *sv, uint32_t n, const std::vector<int> &
             if ((h >> (q - m)) & 1) o |= uint64_t(1) << tile_bits[size_t(q)];
         p->hi_off[h] = I(o);
     }
+    const bool emu = sizeof(T) == 8 && f64_mode() == 1;
     uint32_t done = 0;
     lgpu_status_t st = LGPU_OK;
     while (done < ngates && st == LGPU_OK) {
@@ -997,8 +980,10 @@ static lgpu_status_t fused_t(cplx_t<T> *sv, uint32_t n, const std::vector<int> &
                 if (b < 0 || uint32_t(b) >= n) { st = fail(LGPU_ERR_INVALID_ARG, "fused gate control out of range"); break; }
                 for (int q = 0; q < src.ntgt; q++)
                     if (src.tgt[q] == b) { st = fail(LGPU_ERR_INVALID_ARG, "fused gate: control equals target"); break; }
+                if (st != LGPU_OK) break;
                 const int v = src.ctrl_val[j] ? 1 : 0;
                 if (pos[size_t(b)] >= 0) {
+                    if (dst.in_mask & (1u << pos[size_t(b)])) { st = fail(LGPU_ERR_INVALID_ARG, "fused gate: repeated control"); break; }
                     dst.in_mask |= 1u << pos[size_t(b)];
                     if (v) dst.in_val |= 1u << pos[size_t(b)];
                 } else {
@@ -1008,23 +993,18 @@ static lgpu_status_t fused_t(cplx_t<T> *sv, uint32_t n, const std::vector<int> &
             }
             if (st != LGPU_OK) break;
             dst.mat_off = pool;
-            std::memcpy(p->mats + pool, src.m, need * sizeof(double));
+            for (uint32_t e = 0; e < need; e++) p->mats[pool + e] = T(src.m[e]);
+            dst.body = src.ntgt == 1 ? uint8_t(body_of_2x2(src.m, p->kc[cnt])) : uint8_t(B_DENSE);
             pool += need;
             cnt++;
         }
         if (st != LGPU_OK) break;
         p->ngates = cnt;
         const size_t smem = (size_t(1) << k) * sizeof(cplx_t<T>);
-        if (smem > 48 * 1024) {
-            cudaError_t e = cudaFuncSetAttribute(fused_kernel<T, I>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                 int(smem));
-            if (e != cudaSuccess) { st = cuda_fail(e, "cudaFuncSetAttribute(fused)"); break; }
-        }
-        const int per_sm = std::max(1, int((200 * 1024) / smem));
-        const unsigned grid = unsigned(std::min<uint64_t>(uint64_t(p->ntiles), uint64_t(sm_count()) * per_sm));
-        fused_kernel<T, I><<<grid, kFusedBlock, smem, s>>>(sv, *p);
-        cudaError_t e = cudaGetLastError();
-        if (e != cudaSuccess) st = cuda_fail(e, "fused kernel launch");
+        if constexpr (sizeof(T) == 8)
+            st = emu ? launch_fused<T, I, true>(sv, *p, smem, s) : launch_fused<T, I, false>(sv, *p, smem, s);
+        else
+            st = launch_fused<T, I, false>(sv, *p, smem, s);
         done += uint32_t(cnt);
     }
     delete p;

@@ -191,4 +191,25 @@ __device__ __forceinline__ bool last_block_arrive(unsigned *counter) {
     return is_last;
 }
 
+// 8-point Walsh-Hadamard transform W[h] = sum_j (-1)^popc(j & h) x_j (in
+// place, Sylvester order) and a branch-free pick of W[h] for a runtime h.
+template <class A> __device__ __forceinline__ void wht8(A (&x)[8]) {
+#pragma unroll
+    for (int len = 1; len < 8; len <<= 1)
+#pragma unroll
+        for (int i = 0; i < 8; i++)
+            if (!(i & len)) {
+                const A u = x[i], v = x[i | len];
+                x[i] = u + v;
+                x[i | len] = u - v;
+            }
+}
+
+template <class A> __device__ __forceinline__ A sel8(const A (&x)[8], uint32_t h) {
+    const A s0 = (h & 1u) ? x[1] : x[0], s1 = (h & 1u) ? x[3] : x[2];
+    const A s2 = (h & 1u) ? x[5] : x[4], s3 = (h & 1u) ? x[7] : x[6];
+    const A u0 = (h & 2u) ? s1 : s0, u1 = (h & 2u) ? s3 : s2;
+    return (h & 4u) ? u1 : u0;
+}
+
 }  // namespace lgpu

@@ -2,7 +2,8 @@
 //
 //  * expval of a dense matrix on t bits (FP64 accumulation, deterministic)
 //  * Pauli-word expectations grouped by flip mask: one streaming pass per
-//    distinct flip mask evaluates up to 8 words (bit-parity signs)
+//    distinct flip mask evaluates up to 16 words through an 8-point
+//    Walsh-Hadamard transform of each thread's elements
 //  * marginal probabilities: shared-memory histogram per CTA with register
 //    run-length accumulation, then a fixed-order cross-CTA sum
 //  * sampling: FP64 chunk sums -> single-CTA exclusive scan -> one warp per
@@ -216,6 +217,123 @@ template <class T, class I> struct PauliBody {
     }
 };
 
+// Walsh-Hadamard form of the Pauli-word pass (states of >= 4 qubits).  The
+// items of a pass (all indices, or the indices with the lowest flip bit clear)
+// are split as item = slot + S*j, j = 0..7 in the top three item bits.  A
+// thread loads the eight elements of a slot, forms w_j = conj(a) a^flip (or
+// |a|^2), and takes the 8-point transform W[h] = sum_j (-1)^popc(j & h) w_j.
+// A word with sign mask s then adds (-1)^popc(base & s) W[h_s], h_s the bits
+// of s under the three j bits: per word one popcount, one select and one add
+// per eight elements, instead of a signed FP64 add per element.  complex64
+// transforms in FP32 and flushes chunks of 16 slots into FP64 accumulators.
+constexpr int kWhtWords = 16;
+
+template <class T, class I> struct PauliWhtParams {
+    const cplx_t<T> *sv;
+    Holes holes;  // lowest flip bit (none when flip == 0)
+    I flip;
+    I slots;      // items / 8
+    int lgS;
+    int nt;
+    uint32_t use_im;  // bit t: word t reads the imaginary transform
+    I sgn[kWhtWords];
+    uint32_t hsel[kWhtWords];
+};
+
+template <class T, class I>
+__global__ void __launch_bounds__(kReduceBlock)
+    pauli_wht_kernel(const PauliWhtParams<T, I> p, double2 *partials, unsigned *counter, double2 *out) {
+    using C = cplx_t<T>;
+    constexpr bool kChunk = sizeof(T) == 4;
+    __shared__ double2 sm[kReduceBlock / 32];
+    double acc[kWhtWords];
+    T chunk[kWhtWords];
+#pragma unroll
+    for (int t = 0; t < kWhtWords; t++) {
+        acc[t] = 0.0;
+        chunk[t] = T(0);
+    }
+    I off[8];
+#pragma unroll
+    for (int j = 0; j < 8; j++) off[j] = insert_holes<I>(I(j) << p.lgS, p.holes);
+    int cn = 0;
+    const I stride = I(gridDim.x) * kReduceBlock;
+    for (I slot = I(blockIdx.x) * kReduceBlock + threadIdx.x; slot < p.slots; slot += stride) {
+        const I base = insert_holes<I>(slot, p.holes);
+        T wr[8], wi[8];
+        if (p.flip) {
+            C a[8], b[8];
+#pragma unroll
+            for (int j = 0; j < 8; j++) {
+                a[j] = p.sv[base | off[j]];
+                b[j] = p.sv[(base | off[j]) ^ p.flip];
+            }
+#pragma unroll
+            for (int j = 0; j < 8; j++) {
+                wr[j] = a[j].x * b[j].x + a[j].y * b[j].y;
+                wi[j] = a[j].x * b[j].y - a[j].y * b[j].x;
+            }
+            wht8(wr);
+            wht8(wi);
+        } else {
+            C a[8];
+#pragma unroll
+            for (int j = 0; j < 8; j++) a[j] = p.sv[base | off[j]];
+#pragma unroll
+            for (int j = 0; j < 8; j++) {
+                wr[j] = a[j].x * a[j].x + a[j].y * a[j].y;
+                wi[j] = T(0);
+            }
+            wht8(wr);
+        }
+#pragma unroll
+        for (int t = 0; t < kWhtWords; t++) {
+            if (t < p.nt) {
+                const T v = ((p.use_im >> t) & 1u) ? sel8(wi, p.hsel[t]) : sel8(wr, p.hsel[t]);
+                const T c = (__popcll(uint64_t(base & p.sgn[t])) & 1) ? -v : v;
+                if constexpr (kChunk)
+                    chunk[t] += c;
+                else
+                    acc[t] += c;
+            }
+        }
+        if constexpr (kChunk) {
+            if (++cn == 16) {
+#pragma unroll
+                for (int t = 0; t < kWhtWords; t++) {
+                    acc[t] += double(chunk[t]);
+                    chunk[t] = T(0);
+                }
+                cn = 0;
+            }
+        }
+    }
+    if constexpr (kChunk) {
+#pragma unroll
+        for (int t = 0; t < kWhtWords; t++) acc[t] += double(chunk[t]);
+    }
+#pragma unroll
+    for (int t = 0; t < kWhtWords; t++) {
+        const double2 v = block_reduce_d2<kReduceBlock>(make_double2(acc[t], 0.0), sm);
+        if (threadIdx.x == 0) partials[size_t(blockIdx.x) * kWhtWords + t] = v;
+        __syncthreads();
+    }
+    if (last_block_arrive(counter)) {
+#pragma unroll 1
+        for (int t = 0; t < kWhtWords; t++) {
+            double2 s = make_double2(0.0, 0.0);
+            for (unsigned b = threadIdx.x; b < gridDim.x; b += kReduceBlock) {
+                const double2 q = __ldcg(&partials[size_t(b) * kWhtWords + t]);
+                s.x += q.x;
+            }
+            s = block_reduce_d2<kReduceBlock>(s, sm);
+            if (threadIdx.x == 0) out[t] = s;
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) *counter = 0u;
+    }
+}
+
 template <class T, class I>
 static lgpu_status_t pauli_words_t(lgpu_context_t ctx, const void *sv, uint32_t n, uint32_t nwords,
                                    const uint64_t *flip, const uint64_t *sign, const uint8_t *ny, double *out,
@@ -233,7 +351,94 @@ static lgpu_status_t pauli_words_t(lgpu_context_t ctx, const void *sv, uint32_t 
         }
         groups[gi].push_back(w);
     }
-    // Each pass: up to kWordsPerPass words sharing one flip mask.
+    if (n >= 4) {
+        // Walsh-Hadamard passes: up to kWhtWords words sharing one flip mask.
+        struct WPass {
+            uint64_t flip;
+            std::vector<uint32_t> words;
+        };
+        std::vector<WPass> wp;
+        for (size_t gi = 0; gi < keys.size(); gi++)
+            for (size_t o = 0; o < groups[gi].size(); o += kWhtWords)
+                wp.push_back({keys[gi], std::vector<uint32_t>(groups[gi].begin() + o,
+                                                              groups[gi].begin() + std::min(groups[gi].size(),
+                                                                                            o + kWhtWords))});
+        const uint64_t N = uint64_t(1) << n;
+        const unsigned g = reduce_grid(N / 8);
+        void *p = nullptr;
+        const size_t pbytes = size_t(g) * kWhtWords * sizeof(double2);
+        const size_t rbytes = wp.size() * kWhtWords * sizeof(double2);
+        LGPU_TRY(ctx_scratch(ctx, 256 + pbytes + rbytes, &p));
+        auto *counter = static_cast<unsigned *>(p);
+        auto *partials = reinterpret_cast<double2 *>(static_cast<char *>(p) + 256);
+        auto *results = reinterpret_cast<double2 *>(static_cast<char *>(p) + 256 + pbytes);
+        std::vector<double> coef(wp.size() * kWhtWords, 0.0);
+        for (size_t pi = 0; pi < wp.size(); pi++) {
+            PauliWhtParams<T, I> b{};
+            b.sv = static_cast<const cplx_t<T> *>(sv);
+            b.flip = I(wp[pi].flip);
+            std::vector<int> hole;
+            if (wp[pi].flip) hole.push_back(__builtin_ctzll(wp[pi].flip));
+            b.holes = make_holes(hole);
+            const uint64_t items = wp[pi].flip ? N / 2 : N;
+            b.slots = I(items / 8);
+            b.lgS = __builtin_ctzll(items / 8);
+            b.nt = int(wp[pi].words.size());
+            // element positions of the three j bits
+            int pj[3];
+            for (int q = 0; q < 3; q++) {
+                int pos = b.lgS + q;
+                if (!hole.empty() && pos >= hole[0]) pos++;
+                pj[q] = pos;
+            }
+            for (int t = 0; t < b.nt; t++) {
+                const uint32_t w = wp[pi].words[size_t(t)];
+                b.sgn[t] = I(sign[w]);
+                uint32_t h = 0;
+                for (int q = 0; q < 3; q++) h |= uint32_t((sign[w] >> pj[q]) & 1u) << q;
+                b.hsel[t] = h;
+                const bool kneg = (__builtin_popcountll(flip[w] & sign[w]) & 1) != 0;
+                if (wp[pi].flip && kneg) b.use_im |= 1u << t;
+                // v.x = sum(+-w) (flip 0) or 2 sum(+-Re w); v.y = -2 sum(+-Im w) (odd flip/sign overlap)
+                coef[pi * kWhtWords + size_t(t)] = !wp[pi].flip ? 1.0 : (kneg ? -2.0 : 2.0);
+            }
+            pauli_wht_kernel<T, I><<<g, kReduceBlock, 0, s>>>(b, partials, counter, results + pi * kWhtWords);
+            LGPU_CHECK_LAUNCH();
+        }
+        std::vector<double2> host(wp.size() * kWhtWords);
+        if (!wp.empty()) {
+            void *pin = nullptr;
+            LGPU_TRY(ctx_pinned(ctx, rbytes, &pin));
+            LGPU_CUDA_TRY(cudaMemcpyAsync(pin, results, rbytes, cudaMemcpyDeviceToHost, s));
+            LGPU_CUDA_TRY(cudaStreamSynchronize(s));
+            std::memcpy(host.data(), pin, rbytes);
+        }
+        std::vector<double> vals(nwords, 0.0);
+        for (size_t pi = 0; pi < wp.size(); pi++)
+            for (size_t t = 0; t < wp[pi].words.size(); t++) {
+                const uint32_t w = wp[pi].words[t];
+                const double x = coef[pi * kWhtWords + t] * host[pi * kWhtWords + t].x;
+                const bool im = wp[pi].flip && (__builtin_popcountll(flip[w] & sign[w]) & 1);
+                const double vx = im ? 0.0 : x, vy = im ? x : 0.0;
+                // <P> = Re(i^ny * (vx + i vy))
+                double re = 0;
+                switch (ny[w] & 3) {
+                case 0: re = vx; break;
+                case 1: re = -vy; break;
+                case 2: re = -vx; break;
+                default: re = vy; break;
+                }
+                vals[w] = re;
+            }
+        if (out_on_device) {
+            LGPU_CUDA_TRY(cudaMemcpyAsync(out, vals.data(), nwords * sizeof(double), cudaMemcpyHostToDevice, s));
+            LGPU_CUDA_TRY(cudaStreamSynchronize(s));
+        } else {
+            std::memcpy(out, vals.data(), nwords * sizeof(double));
+        }
+        return LGPU_OK;
+    }
+    // Small states: up to kWordsPerPass words sharing one flip mask per pass.
     struct Pass {
         uint64_t flip;
         std::vector<uint32_t> words;
