@@ -37,6 +37,7 @@ sys.path.insert(0, ROOT)
 N_QUBITS = 28
 THETA = 0.7345
 PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
+TRAFFIC_25Q_BYTES = 1012.9e6
 
 
 def _peaks():
@@ -278,6 +279,9 @@ def run_ours(args):
     e2e_value = world * (bytes_per_step + S) / e2e_s / 1e9  # + one read pass for the probability
 
     peak, peak_kind = _peaks()
+    # DRAM bytes (read + write) of one gate1_bulk_kernel launch, ncu capture of the
+    # same kernel on a 25-qubit state (1013 MB), scaled by the amplitude count
+    traffic = TRAFFIC_25Q_BYTES * (1 << (n - 25)) if m.get_stream_mode() == 1 and n >= 25 else None
     achieved = 2 * S / (avg_launch_ms / 1e3) / 1e9
     line = {
         "metric": "gate HBM GB/s at 28q", "value": round(value, 1), "unit": "GB/s", "n_gpus": world,
@@ -292,7 +296,7 @@ def run_ours(args):
                 "d2h_bytes_per_step": 16},
         "gpu_launches": len(gates) * args.steps * world,
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                     "frac": round(achieved / peak, 4), "traffic": None, "peak_source": peak_kind,
+                     "frac": round(achieved / peak, 4), "traffic": traffic, "peak_source": peak_kind,
                      "kernel": "gate1_bulk_kernel" if m.get_stream_mode() == 1 else "gate1_kernel",
                      "algorithmic_bytes_per_launch": 2 * S},
         "variants": variants,
@@ -304,12 +308,106 @@ def run_ours(args):
         line["config"]["parallelism"] = "replicas: one independent 28-qubit state per GPU"
     if single and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline_sample(n, gates=args.cpu_gates)
+    if single and not args.no_circuits:
+        line["circuits"] = bench_circuits(args)
     if single and not args.no_batched:
         line["batched"] = bench_batched(args)
     if single and not args.no_serving:
         line["serving"] = bench_serving(args)
     if rank == 0:
         print(json.dumps(line))
+
+
+def _timed(fn, reps=2):
+    """Best wall time of `fn` (each call ends with a host read of its result)."""
+    import torch
+
+    fn()
+    best = float("inf")
+    for _ in range(reps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        fn()
+        best = min(best, time.perf_counter() - t0)
+    return best
+
+
+def bench_circuits(args):
+    """Config 1 (28 qubits, 20 layers of random rotations and entanglers; a
+    100-term Pauli Hamiltonian, probs on 10 wires, 1e4 shots), config 3
+    (24-qubit adjoint Jacobian, 384 parameters, 50-term Hamiltonian, through
+    torch.autograd) and config 0 (12-qubit adjoint Jacobian, 144 parameters),
+    end to end through the LightningGPU device with host inputs and results."""
+    from oracle import oracle as O
+    from pennylane_lightning_gpu_gb300 import ops as Q
+    from pennylane_lightning_gpu_gb300 import torch_adjoint as TA
+    from pennylane_lightning_gpu_gb300 import workloads
+    from pennylane_lightning_gpu_gb300.lightning_gpu import LightningGPU
+
+    out = {}
+    n = 28
+    rng = np.random.default_rng(11)
+    raw = workloads.random_circuit(n, 20, rng)
+    terms = workloads.random_pauli_hamiltonian(n, 100, rng, max_wires=6)
+    H = TA.pauli_hamiltonian(terms)
+    ops = [Q.op(o[0], o[1], *o[2]) for o in raw]
+    c1 = {"workload": "28 qubits, 20 layers (28 rotations RX/RY/RZ/Rot + 14 CNOT/CZ/CRY each, %d ops), "
+                      "100-term Pauli Hamiltonian, probs on 10 wires, 1e4 shots" % len(ops)}
+    for dt, key, amp in ((np.complex128, "c128", 16), (np.complex64, "c64", 8)):
+        dev = LightningGPU(n, c_dtype=dt)
+        t_apply = _timed(lambda: (dev.reset(), dev.apply(ops), dev._gpu_state.synchronize()))
+        t_exp = _timed(lambda: dev.expval(H))
+        t_probs = _timed(lambda: dev.probability(wires=list(range(10))))
+        t_shots = _timed(lambda: dev._gpu_state.GenerateSamples(n, 10000))
+        S = (1 << n) * amp
+        c1[key] = {"apply_ms": round(t_apply * 1e3, 2), "expval_ms": round(t_exp * 1e3, 2),
+                   "probs_ms": round(t_probs * 1e3, 2), "shots_ms": round(t_shots * 1e3, 2),
+                   "total_ms": round((t_apply + t_exp + t_probs + t_shots) * 1e3, 2),
+                   "apply_gbs_if_one_pass_per_op": round(len(ops) * 2 * S / t_apply / 1e9, 1)}
+        del dev
+    out["config1"] = c1
+
+    import torch
+
+    n3, layers3 = 24, 8
+    rng = np.random.default_rng(13)
+    terms3 = workloads.random_pauli_hamiltonian(n3, 50, rng, max_wires=6)
+    H3 = TA.pauli_hamiltonian(terms3)
+    template = TA.ry_rz_cz_template(n3, layers3)
+    dev3 = LightningGPU(n3)
+    f = TA.expval_function(template, [H3], dev3)
+    params = torch.tensor(rng.uniform(0, 2 * np.pi, 2 * n3 * layers3), dtype=torch.float64, requires_grad=True)
+
+    def fwd_bwd():
+        params.grad = None
+        y = f(params)
+        y.sum().backward()
+        return params.grad
+
+    t3 = _timed(fwd_bwd, reps=1)
+    out["config3"] = {"workload": "24 qubits complex128, 8 layers RY,RZ + CZ ladder (384 params), 50-term "
+                                  "Pauli Hamiltonian, forward + adjoint backward via torch.autograd",
+                      "forward_backward_ms": round(t3 * 1e3, 1)}
+    del dev3
+
+    n0, layers0 = 12, 4
+    rng = np.random.default_rng(0)
+    raw0 = workloads.layered_ansatz(n0, layers0, rng)
+    ops0 = [Q.op(o[0], o[1], *o[2]) for o in raw0]
+    tape0 = Q.QuantumTape(ops0, [Q.expval(Q.PauliZ(w)) for w in range(n0)])
+    dev0 = LightningGPU(n0)
+    t0g = _timed(lambda: dev0.adjoint_jacobian(tape0), reps=3)
+    oops = [(o[0], o[1], o[2], False, None) for o in raw0]
+    final = O.run(n0, oops)
+    obs = [(False, [(1.0, [("PauliZ", [w], None)])]) for w in range(n0)]
+    a = time.perf_counter()
+    O.adjoint_jacobian(final, oops, obs, list(range(len(raw0))))
+    t0c = time.perf_counter() - a
+    out["config0"] = {"workload": "12 qubits complex128, 4 layers RX,RY,RZ + CNOT ring (144 params), "
+                                  "expval PauliZ on each wire, adjoint Jacobian",
+                      "gpu_ms": round(t0g * 1e3, 2), "cpu_oracle_ms": round(t0c * 1e3, 2),
+                      "cpu_oracle_threads": os.cpu_count()}
+    return out
 
 
 def bench_batched(args):
@@ -383,14 +481,15 @@ def main():
     ap.add_argument("--cpu-gates", type=int, default=4)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-variants", action="store_true")
+    ap.add_argument("--no-circuits", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-serving", action="store_true")
-    ap.add_argument("--only", choices=["batched", "serving"], default=None,
+    ap.add_argument("--only", choices=["batched", "serving", "circuits"], default=None,
                     help="run one section alone (profiling runs); the default prints the full line")
     ap.add_argument("--batch-circuits", type=int, default=4096)
     ap.add_argument("--batch-plain", type=int, default=256)
     ap.add_argument("--serve-requests", type=int, default=160)
-    ap.add_argument("--serve-rate", type=float, default=40.0)
+    ap.add_argument("--serve-rate", type=float, default=100.0)
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     if args.only == "batched":
@@ -398,6 +497,9 @@ def main():
         return
     if args.only == "serving":
         print(json.dumps({"serving": bench_serving(args)}))
+        return
+    if args.only == "circuits":
+        print(json.dumps({"circuits": bench_circuits(args)}))
         return
     if args.impl == "reference":
         if rank == 0:
