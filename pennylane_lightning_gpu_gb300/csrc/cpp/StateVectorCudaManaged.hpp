@@ -501,7 +501,7 @@ class StateVectorCudaManaged : public StateVectorCudaBase<Precision, StateVector
     [[nodiscard]] bool getFusion() const { return fusion_; }
     [[nodiscard]] int fusionTileBits() const {
         if (fusion_tile_bits_ > 0) return fusion_tile_bits_;
-        return std::is_same_v<Precision, double> ? 11 : 12;
+        return 12;  // 32 KB (complex64, double-buffered) / 64 KB (complex128) tiles: three CTAs per SM
     }
 
     void applyDescs(std::vector<Engine::GateDesc> descs) {

@@ -119,4 +119,65 @@ struct PairWalk {
     __device__ __forceinline__ void step() { x = ((x | holes) + inc) & ~holes; }
 };
 
+// Shared-memory tiles are stored swizzled: the 16-byte chunk c of 128-byte
+// row r lives at chunk c ^ (r mod 8) (complex64: element e -> e ^
+// (((e >> 4) & 7) << 1); complex128: e -> e ^ ((e >> 3) & 7)).  A warp
+// reading one element from each of 32 rows (a register group on the lowest
+// tile positions) then spreads over the banks, 16-byte chunks stay whole
+// (so 16-byte asynchronous copies can fill the layout), and accesses within
+// a row are only permuted.
+template <class T> __device__ __forceinline__ int swz(int e) {
+    if constexpr (sizeof(T) == 4)
+        return e ^ (((e >> 4) & 7) << 1);
+    else
+        return e ^ ((e >> 3) & 7);
+}
+
+// Register groups: a run of consecutive 1-target gates whose targets and
+// in-tile controls lie on R tile positions is applied with each thread
+// holding the 2^R amplitudes of one index group in registers (one
+// shared-memory round trip and one barrier per group instead of per gate).
+// A gate is given by its local target LT (0..R-1), the local control mask and
+// values, its body and coefficients.
+template <class T, int R, int LT, int BODY, bool EMU>
+__device__ __forceinline__ void reg_gate(cplx_t<T> (&a)[1 << R], const T *m, const KConst *k, uint32_t lcm,
+                                         uint32_t lcv) {
+    T mr[8];
+#pragma unroll
+    for (int i = 0; i < 8; i++) mr[i] = m[i];
+    KConst kr[4];
+#pragma unroll
+    for (int i = 0; i < 4; i++) kr[i] = EMU ? k[i] : KConst{};
+#pragma unroll
+    for (int j = 0; j < (1 << R); j++) {
+        if (j & (1 << LT)) continue;
+        if ((uint32_t(j) & lcm) != lcv) continue;
+        body1_sel<T, BODY, EMU>(mr, kr, a[j], a[j | (1 << LT)]);
+    }
+}
+
+template <class T, int R, int BODY, bool EMU>
+__device__ __forceinline__ void reg_gate_lt(cplx_t<T> (&a)[1 << R], int lt, const T *m, const KConst *k, uint32_t lcm,
+                                            uint32_t lcv) {
+    switch (lt) {
+    case 0: reg_gate<T, R, 0, BODY, EMU>(a, m, k, lcm, lcv); break;
+    case 1: reg_gate<T, R, 1, BODY, EMU>(a, m, k, lcm, lcv); break;
+    case 2: reg_gate<T, R, 2 % R, BODY, EMU>(a, m, k, lcm, lcv); break;
+    default: reg_gate<T, R, (R - 1), BODY, EMU>(a, m, k, lcm, lcv); break;
+    }
+}
+
+template <class T, int R, bool EMU>
+__device__ __forceinline__ void reg_gate_any(cplx_t<T> (&a)[1 << R], int body, int lt, const T *m, const KConst *k,
+                                             uint32_t lcm, uint32_t lcv) {
+    switch (body) {
+    case B_DIAG: reg_gate_lt<T, R, B_DIAG, EMU>(a, lt, m, k, lcm, lcv); break;
+    case B_PERM: reg_gate_lt<T, R, B_PERM, EMU>(a, lt, m, k, lcm, lcv); break;
+    case B_ANTIDIAG: reg_gate_lt<T, R, B_ANTIDIAG, EMU>(a, lt, m, k, lcm, lcv); break;
+    case B_REAL: reg_gate_lt<T, R, B_REAL, EMU>(a, lt, m, k, lcm, lcv); break;
+    case B_RXLIKE: reg_gate_lt<T, R, B_RXLIKE, EMU>(a, lt, m, k, lcm, lcv); break;
+    default: reg_gate_lt<T, R, B_DENSE, false>(a, lt, m, k, lcm, lcv); break;
+    }
+}
+
 }  // namespace lgpu

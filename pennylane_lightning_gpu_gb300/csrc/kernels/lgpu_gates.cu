@@ -403,13 +403,23 @@ __global__ void __launch_bounds__(kGateBlock)
 // ---------------------------------------------------------------------------
 constexpr int kFusedMaxGates = 96;
 constexpr int kFusedMatPool = 2304;  // matrix elements, in the state's precision
-constexpr int kFusedBlock = 512;
 
 struct FGate {
     uint8_t ntgt, q0, q1, body;  // q0 = most significant matrix bit; body: Body1 of a 1-target gate
+    uint8_t lt, lcm, lcv, pad;   // register group: local target, local control mask and values
     uint32_t in_mask, in_val;    // controls inside the tile (tile positions)
     uint32_t mat_off;            // into the matrix pool
     uint64_t out_mask, out_val;  // controls outside the tile (state bits)
+};
+
+// A run of gates applied between two barriers: kind 0 = a register group on
+// the R tile positions p[] (ascending), kind 1 = one gate through the
+// per-gate shared-memory paths.
+struct FGroup {
+    uint8_t kind;
+    uint8_t p[4];
+    uint8_t pad[3];
+    uint16_t first, count;
 };
 
 template <class T, class I> struct FusedParams {
@@ -419,12 +429,19 @@ template <class T, class I> struct FusedParams {
     int m;             // low bits 0..m-1 are the lowest tile bits (contiguous runs)
     I hi_off[64];      // offsets of the high tile bits (k - m <= 6 -> 64 entries)
     int ngates;
+    int ngroups;
     FGate gates[kFusedMaxGates];
+    FGroup groups[kFusedMaxGates];
     T mats[kFusedMatPool];
     KConst kc[kFusedMaxGates][4];  // integer-pipe multipliers (complex128 structured bodies)
 };
 
-template <class T, int BODY, bool EMU>
+// Amplitudes per thread in a register group: 16 (complex64).  complex128
+// blocks run gate by gate: they are bound by the FP64 pipe, and the register
+// footprint of a group would halve the resident CTAs.
+template <class T> __host__ __device__ constexpr int fused_reg_bits() { return sizeof(T) == 4 ? 4 : 1; }
+
+template <class T, int BODY, bool EMU, int NT>
 __device__ __forceinline__ void tile_pairs(cplx_t<T> *tile, int E, int q, uint32_t in_mask, uint32_t in_val,
                                            const T *m, const KConst *k) {
     using C = cplx_t<T>;
@@ -436,80 +453,192 @@ __device__ __forceinline__ void tile_pairs(cplx_t<T> *tile, int E, int q, uint32
     KConst kr[4];
 #pragma unroll
     for (int i = 0; i < 4; i++) kr[i] = EMU ? k[i] : KConst{};
-    PairWalk w(holes, threadIdx.x, kFusedBlock);
+    PairWalk w(holes, threadIdx.x, NT);
 #pragma unroll 2
-    for (int f = threadIdx.x; f < nfree; f += kFusedBlock) {
+    for (int f = threadIdx.x; f < nfree; f += NT) {
         const int e0 = int(w.x | in_val);
         const int e1 = e0 | (1 << q);
         w.step();
-        C a0 = tile[e0], a1 = tile[e1];
+        C a0 = tile[swz<T>(e0)], a1 = tile[swz<T>(e1)];
         body1_sel<T, BODY, EMU>(mr, kr, a0, a1);
-        tile[e0] = a0;
-        tile[e1] = a1;
+        tile[swz<T>(e0)] = a0;
+        tile[swz<T>(e1)] = a1;
     }
 }
 
-template <class T, class I, bool EMU>
-__global__ void __launch_bounds__(kFusedBlock, 2) fused_kernel(cplx_t<T> *__restrict__ sv, const FusedParams<T, I> p) {
+// All gates of a launch on one tile held in shared memory (all threads; the
+// caller synchronises before and after).
+template <class T, class I, bool EMU, int NT>
+__device__ __forceinline__ void fused_tile(cplx_t<T> *tile, int E, I base, const FusedParams<T, I> &p) {
     using C = cplx_t<T>;
-    extern __shared__ unsigned char smem_raw[];
-    C *tile = reinterpret_cast<C *>(smem_raw);
-    const int E = 1 << p.k;
-    const int lowmask = (1 << p.m) - 1;
-    for (I tau = blockIdx.x; tau < p.ntiles; tau += gridDim.x) {
-        const I base = insert_holes<I>(tau, p.holes);
-        __syncthreads();
-        for (int e = threadIdx.x; e < E; e += kFusedBlock)
-            tile[e] = __ldcs(&sv[base + p.hi_off[e >> p.m] + I(e & lowmask)]);
-        __syncthreads();
-        for (int gi = 0; gi < p.ngates; gi++) {
-            const FGate &g = p.gates[gi];
-            if ((uint64_t(base) & g.out_mask) != g.out_val) continue;  // tile-uniform
-            const T *mm = p.mats + g.mat_off;
-            if (g.ntgt == 1) {
-                const KConst *kk = p.kc[gi];
-                switch (g.body) {
-                case B_DIAG: tile_pairs<T, B_DIAG, EMU>(tile, E, g.q0, g.in_mask, g.in_val, mm, kk); break;
-                case B_PERM: tile_pairs<T, B_PERM, EMU>(tile, E, g.q0, g.in_mask, g.in_val, mm, kk); break;
-                case B_ANTIDIAG: tile_pairs<T, B_ANTIDIAG, EMU>(tile, E, g.q0, g.in_mask, g.in_val, mm, kk); break;
-                case B_REAL: tile_pairs<T, B_REAL, EMU>(tile, E, g.q0, g.in_mask, g.in_val, mm, kk); break;
-                case B_RXLIKE: tile_pairs<T, B_RXLIKE, EMU>(tile, E, g.q0, g.in_mask, g.in_val, mm, kk); break;
-                default: tile_pairs<T, B_DENSE, false>(tile, E, g.q0, g.in_mask, g.in_val, mm, kk); break;
+    constexpr int R = fused_reg_bits<T>();
+    for (int gr = 0; gr < p.ngroups; gr++) {
+        const FGroup &G = p.groups[gr];
+        if constexpr (sizeof(T) == 4) {
+            if (G.kind == 0) {
+                uint32_t M = 0;
+#pragma unroll
+                for (int b = 0; b < R; b++) M |= 1u << G.p[b];
+                // swz is XOR-linear and the slot base and the offsets have
+                // disjoint bits: swz(b0 | off) = swz(b0) ^ swz(off)
+                int soff[1 << R];
+#pragma unroll
+                for (int j = 0; j < (1 << R); j++) {
+                    int o = 0;
+#pragma unroll
+                    for (int b = 0; b < R; b++)
+                        if ((j >> b) & 1) o |= 1 << G.p[b];
+                    soff[j] = swz<T>(o);
                 }
-            } else {
-                const int qa = g.q0, qb = g.q1;  // qa = most significant matrix bit
-                const uint32_t holes = g.in_mask | (1u << qa) | (1u << qb);
-                const int nfree = E >> __popc(holes);
-                PairWalk w(holes, threadIdx.x, kFusedBlock);
-                for (int f = threadIdx.x; f < nfree; f += kFusedBlock) {
-                    const int e = int(w.x | g.in_val);
+                const int nslots = E >> R;
+                PairWalk w(M, threadIdx.x, NT);
+                for (int f = threadIdx.x; f < nslots; f += NT) {
+                    const int sb = swz<T>(int(w.x));
                     w.step();
-                    int idx[4];
-                    idx[0] = e;
-                    idx[1] = e | (1 << qb);
-                    idx[2] = e | (1 << qa);
-                    idx[3] = e | (1 << qa) | (1 << qb);
-                    C a[4];
+                    C a[1 << R];
 #pragma unroll
-                    for (int c = 0; c < 4; c++) a[c] = tile[idx[c]];
-#pragma unroll
-                    for (int r = 0; r < 4; r++) {
-                        T xr = 0, xi = 0;
-#pragma unroll
-                        for (int c = 0; c < 4; c++) {
-                            const T mr = mm[2 * (r * 4 + c)], mi = mm[2 * (r * 4 + c) + 1];
-                            xr = fmaT(mr, a[c].x, fmaT(-mi, a[c].y, xr));
-                            xi = fmaT(mr, a[c].y, fmaT(mi, a[c].x, xi));
-                        }
-                        tile[idx[r]] = mk<T>(xr, xi);
+                    for (int j = 0; j < (1 << R); j++) a[j] = tile[sb ^ soff[j]];
+                    for (int gi = G.first; gi < G.first + G.count; gi++) {
+                        const FGate &g = p.gates[gi];
+                        if ((uint64_t(base) & g.out_mask) != g.out_val) continue;  // tile-uniform
+                        reg_gate_any<T, R, EMU>(a, g.body, g.lt, p.mats + g.mat_off, p.kc[gi], g.lcm, g.lcv);
                     }
+#pragma unroll
+                    for (int j = 0; j < (1 << R); j++) tile[sb ^ soff[j]] = a[j];
+                }
+                __syncthreads();
+                continue;
+            }
+        }
+        // complex128 launches hold one group per gate, in gate order
+        const int gi = sizeof(T) == 4 ? int(G.first) : gr;
+        const FGate &g = p.gates[gi];
+        if ((uint64_t(base) & g.out_mask) != g.out_val) continue;  // tile-uniform
+        const T *mm = p.mats + g.mat_off;
+        if (g.ntgt == 1) {
+            const KConst *kk = p.kc[gi];
+            switch (g.body) {
+            case B_DIAG: tile_pairs<T, B_DIAG, EMU, NT>(tile, E, g.q0, g.in_mask, g.in_val, mm, kk); break;
+            case B_PERM: tile_pairs<T, B_PERM, EMU, NT>(tile, E, g.q0, g.in_mask, g.in_val, mm, kk); break;
+            case B_ANTIDIAG: tile_pairs<T, B_ANTIDIAG, EMU, NT>(tile, E, g.q0, g.in_mask, g.in_val, mm, kk); break;
+            case B_REAL: tile_pairs<T, B_REAL, EMU, NT>(tile, E, g.q0, g.in_mask, g.in_val, mm, kk); break;
+            case B_RXLIKE: tile_pairs<T, B_RXLIKE, EMU, NT>(tile, E, g.q0, g.in_mask, g.in_val, mm, kk); break;
+            default: tile_pairs<T, B_DENSE, false, NT>(tile, E, g.q0, g.in_mask, g.in_val, mm, kk); break;
+            }
+        } else {
+            const int qa = g.q0, qb = g.q1;  // qa = most significant matrix bit
+            const uint32_t holes = g.in_mask | (1u << qa) | (1u << qb);
+            const int nfree = E >> __popc(holes);
+            PairWalk w(holes, threadIdx.x, NT);
+            for (int f = threadIdx.x; f < nfree; f += NT) {
+                const int e = int(w.x | g.in_val);
+                w.step();
+                int idx[4];
+                idx[0] = swz<T>(e);
+                idx[1] = swz<T>(e | (1 << qb));
+                idx[2] = swz<T>(e | (1 << qa));
+                idx[3] = swz<T>(e | (1 << qa) | (1 << qb));
+                C a[4];
+#pragma unroll
+                for (int c = 0; c < 4; c++) a[c] = tile[idx[c]];
+#pragma unroll
+                for (int r = 0; r < 4; r++) {
+                    T xr = 0, xi = 0;
+#pragma unroll
+                    for (int c = 0; c < 4; c++) {
+                        const T mr = mm[2 * (r * 4 + c)], mi = mm[2 * (r * 4 + c) + 1];
+                        xr = fmaT(mr, a[c].x, fmaT(-mi, a[c].y, xr));
+                        xi = fmaT(mr, a[c].y, fmaT(mi, a[c].x, xi));
+                    }
+                    tile[idx[r]] = mk<T>(xr, xi);
                 }
             }
-            __syncthreads();
         }
-        for (int e = threadIdx.x; e < E; e += kFusedBlock)
-            __stcs(&sv[base + p.hi_off[e >> p.m] + I(e & lowmask)], tile[e]);
+        __syncthreads();
     }
+}
+
+__device__ __forceinline__ void cp_async16(void *smem_dst, const void *gsrc) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(static_cast<uint32_t>(__cvta_generic_to_shared(smem_dst))),
+                 "l"(gsrc)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async8(void *smem_dst, const void *gsrc) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(static_cast<uint32_t>(__cvta_generic_to_shared(smem_dst))),
+                 "l"(gsrc)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait0() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+
+// Persistent CTAs, two tile buffers: while the gates run on one tile, the
+// next tile streams into the other buffer through cp.async (16-byte chunks
+// written straight into the swizzled layout); results leave with streaming
+// stores.  The tile = the low run of m state bits (contiguous segments of
+// 2^m amplitudes) times up to 2^6 segments at the high tile bits.
+template <class T, class I, bool EMU, int NT, int STAGES>
+__global__ void __launch_bounds__(NT, NT == 256 ? 3 : 1)
+    fused_kernel(cplx_t<T> *__restrict__ sv, const FusedParams<T, I> p) {
+    using C = cplx_t<T>;
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    const int E = 1 << p.k;
+    C *buf0 = reinterpret_cast<C *>(smem_raw);
+    C *buf1 = STAGES == 2 ? buf0 + E : buf0;
+    const int lowmask = (1 << p.m) - 1;
+    // 16-byte chunks hold 2 complex64 / 1 complex128 amplitudes; complex64
+    // needs an even low run (always, except for a tile without bit 0)
+    constexpr int EPC = sizeof(C) == 8 ? 2 : 1;
+    const bool wide = EPC == 1 || p.m >= 1;
+    auto load = [&](I tau, C *dst) {
+        const I base = insert_holes<I>(tau, p.holes);
+        if (wide) {
+            for (int c = threadIdx.x; c < E / EPC; c += NT) {
+                const int e = c * EPC;
+                cp_async16(&dst[swz<T>(e)], &sv[base + p.hi_off[e >> p.m] + I(e & lowmask)]);
+            }
+        } else {
+            for (int e = threadIdx.x; e < E; e += NT)
+                cp_async8(&dst[swz<T>(e)], &sv[base + p.hi_off[e >> p.m] + I(e & lowmask)]);
+        }
+        cp_async_commit();
+    };
+    I tau = blockIdx.x;
+    if constexpr (STAGES == 2) {
+        if (tau < p.ntiles) load(tau, buf0);
+        else cp_async_commit();
+    }
+    for (int it = 0; tau < p.ntiles; it++, tau += gridDim.x) {
+        C *cur = (it & 1) ? buf1 : buf0;
+        C *nxt = (it & 1) ? buf0 : buf1;
+        if constexpr (STAGES == 2) {
+            const I tn = tau + gridDim.x;
+            if (tn < p.ntiles) load(tn, nxt);
+            else cp_async_commit();
+            cp_async_wait1();  // this thread's copies of `cur` have landed
+        } else {
+            load(tau, cur);
+            cp_async_wait0();
+        }
+        __syncthreads();  // ... and everyone's
+        const I base = insert_holes<I>(tau, p.holes);
+        fused_tile<T, I, EMU, NT>(cur, E, base, p);
+        if (wide) {
+            for (int c = threadIdx.x; c < E / EPC; c += NT) {
+                const int e = c * EPC;
+                C *dst = &sv[base + p.hi_off[e >> p.m] + I(e & lowmask)];
+                if constexpr (EPC == 2)
+                    __stcs(reinterpret_cast<float4 *>(dst), *reinterpret_cast<const float4 *>(&cur[swz<T>(e)]));
+                else
+                    __stcs(dst, cur[swz<T>(e)]);
+            }
+        } else {
+            for (int e = threadIdx.x; e < E; e += NT)
+                __stcs(&sv[base + p.hi_off[e >> p.m] + I(e & lowmask)], cur[swz<T>(e)]);
+        }
+        __syncthreads();  // `cur` is the target of the load issued next iteration
+    }
+    cp_async_wait0();
 }
 
 // ---------------------------------------------------------------------------
@@ -907,8 +1036,60 @@ static int body_of_2x2(const double *mm, KConst *kc) {
     return B_DENSE;
 }
 
-template <class T, class I, bool EMU>
-static lgpu_status_t launch_fused(cplx_t<T> *sv, const FusedParams<T, I> &p, size_t smem, cudaStream_t s) {
+// Split a launch's gates into register groups (consecutive 1-target gates
+// whose targets and in-tile controls span at most R tile positions, padded
+// with the lowest unused positions) and single gates; fills the local target
+// and control fields of grouped gates.  Returns the number of groups.
+static int group_fused_gates(FGate *gates, int cnt, int k, int R, FGroup *groups) {
+    int ng = 0;
+    int i = 0;
+    auto bits_of = [&](const FGate &g) { return g.in_mask | (1u << g.q0); };
+    while (i < cnt) {
+        const FGate &g0 = gates[i];
+        uint32_t set = g0.ntgt == 1 ? bits_of(g0) : 0u;
+        if (k < R || g0.ntgt != 1 || __builtin_popcount(set) > R) {
+            groups[ng++] = FGroup{1, {0, 0, 0, 0}, {0, 0, 0}, uint16_t(i), 1};
+            i++;
+            continue;
+        }
+        int j = i + 1;
+        while (j < cnt && gates[j].ntgt == 1 && __builtin_popcount(set | bits_of(gates[j])) <= R) {
+            set |= bits_of(gates[j]);
+            j++;
+        }
+        if (j - i == 1) {  // a lone gate touches only its own pairs through the per-gate path
+            groups[ng++] = FGroup{1, {0, 0, 0, 0}, {0, 0, 0}, uint16_t(i), 1};
+            i++;
+            continue;
+        }
+        for (int q = 0; q < k && __builtin_popcount(set) < R; q++) set |= 1u << q;
+        FGroup G{0, {0, 0, 0, 0}, {0, 0, 0}, uint16_t(i), uint16_t(j - i)};
+        int loc[32];
+        int nb = 0;
+        for (int q = 0; q < k; q++)
+            if ((set >> q) & 1u) {
+                loc[q] = nb;
+                G.p[nb++] = uint8_t(q);
+            }
+        for (int t = i; t < j; t++) {
+            FGate &g = gates[t];
+            g.lt = uint8_t(loc[g.q0]);
+            g.lcm = 0;
+            g.lcv = 0;
+            for (int q = 0; q < k; q++)
+                if ((g.in_mask >> q) & 1u) {
+                    g.lcm |= uint8_t(1u << loc[q]);
+                    if ((g.in_val >> q) & 1u) g.lcv |= uint8_t(1u << loc[q]);
+                }
+        }
+        groups[ng++] = G;
+        i = j;
+    }
+    return ng;
+}
+
+template <class T, class I, bool EMU, int NT, int STAGES>
+static lgpu_status_t launch_fused_nt(cplx_t<T> *sv, const FusedParams<T, I> &p, size_t smem, cudaStream_t s) {
     // dynamic shared memory opted in so far, per device (set outside any
     // capture: the first launch of a size runs eagerly)
     static size_t attr[64] = {};
@@ -916,16 +1097,29 @@ static lgpu_status_t launch_fused(cplx_t<T> *sv, const FusedParams<T, I> &p, siz
     LGPU_CUDA_TRY(cudaGetDevice(&dev));
     if (smem > 48 * 1024 && (dev >= 64 || smem > attr[dev])) {
         cudaError_t e =
-            cudaFuncSetAttribute(fused_kernel<T, I, EMU>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+            cudaFuncSetAttribute(fused_kernel<T, I, EMU, NT, STAGES>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 int(smem));
         if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(fused)");
         if (dev < 64) attr[dev] = smem;
     }
-    const int per_sm = std::max(1, int((200 * 1024) / smem));
+    const int per_sm = std::max(1, std::min(int((220 * 1024) / smem), 2048 / NT));
     const unsigned grid = unsigned(std::min<uint64_t>(uint64_t(p.ntiles), uint64_t(sm_count()) * per_sm));
-    fused_kernel<T, I, EMU><<<grid, kFusedBlock, smem, s>>>(sv, p);
+    fused_kernel<T, I, EMU, NT, STAGES><<<grid, NT, smem, s>>>(sv, p);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(e, "fused kernel launch");
     return LGPU_OK;
+}
+
+// complex64 (instruction-bound): two tile buffers per CTA, the next tile
+// loading while the current one computes.  complex128 (FP64-bound): one
+// buffer, three CTAs per SM interleave instead.  512 threads when only one
+// CTA fits on an SM.
+template <class T, class I, bool EMU>
+static lgpu_status_t launch_fused(cplx_t<T> *sv, const FusedParams<T, I> &p, size_t tile_bytes, cudaStream_t s) {
+    constexpr int ST = sizeof(T) == 4 ? 2 : 1;
+    const size_t smem = ST * tile_bytes;
+    return smem > 64 * 1024 ? launch_fused_nt<T, I, EMU, 512, ST>(sv, p, smem, s)
+                            : launch_fused_nt<T, I, EMU, 256, ST>(sv, p, smem, s);
 }
 
 template <class T, class I>
@@ -1000,6 +1194,7 @@ static lgpu_status_t fused_t(cplx_t<T> *sv, uint32_t n, const std::vector<int> &
         }
         if (st != LGPU_OK) break;
         p->ngates = cnt;
+        p->ngroups = group_fused_gates(p->gates, cnt, sizeof(T) == 4 ? k : 0, fused_reg_bits<T>(), p->groups);
         const size_t smem = (size_t(1) << k) * sizeof(cplx_t<T>);
         if constexpr (sizeof(T) == 8)
             st = emu ? launch_fused<T, I, true>(sv, *p, smem, s) : launch_fused<T, I, false>(sv, *p, smem, s);
