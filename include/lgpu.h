@@ -273,6 +273,31 @@ lgpu_status_t lgpu_adjoint_step(lgpu_context_t ctx, void *ket, void *const *bras
                                 const double *gen, const double *udag, int apply_udag,
                                 double *out_dev, lgpu_stream_t stream);
 
+/* The whole reverse sweep in one launch for states that fit in shared memory
+ * (n <= lgpu_adjoint_sweep_max_qubits(dt): 12 for C128, 13 for C64): one CTA
+ * per bra keeps lambda (from `ket`) and its bra in shared memory and runs
+ * ops[0..nops) in the given order (the reverse of the circuit), each as
+ *   jac[col * nbras + k] = Im <bra_k| G |lambda>   (when ng > 0)
+ *   lambda <- U^dag lambda ;  bra_k <- U^dag bra_k
+ * `ket` and `bras` are only read.  jac is a device array of at least
+ * (max col + 1) * nbras doubles.  Same results as a sequence of
+ * lgpu_adjoint_step calls; no counterpart in the reference. */
+typedef struct {
+    int32_t nu;       /* bits of U^dag: 1 or 2 (controls folded into the matrix) */
+    int32_t ubits[2]; /* ubits[0] = most significant matrix bit */
+    int32_t ng;       /* bits of the generator: 0 (no gradient), 1 or 2 */
+    int32_t gbits[2];
+    int32_t col;      /* Jacobian column of this operation (ng > 0) */
+    double u[32];     /* U^dag, 2^nu x 2^nu row-major (re, im) */
+    double g[32];     /* generator, 2^ng x 2^ng row-major (re, im) */
+} lgpu_adj_op_t;
+
+uint32_t lgpu_adjoint_sweep_max_qubits(lgpu_dtype_t dt);
+lgpu_status_t lgpu_adjoint_sweep_small(lgpu_context_t ctx, const void *ket, void *const *bras,
+                                       uint32_t nbras, uint32_t n, lgpu_dtype_t dt,
+                                       const lgpu_adj_op_t *ops, uint32_t nops, double *jac_dev,
+                                       lgpu_stream_t stream);
+
 /* ---- CUDA graphs (stream capture) ------------------------------------------
  * Capture everything issued on `stream` between begin and end into an
  * executable graph; launch replays it on any stream. */

@@ -97,6 +97,81 @@ template <class T = double> class AdjointJacobianGPU {
         std::vector<double> col_scale(tp_size, 0.0);
         std::unique_ptr<SV> mu;  // only for operations the fused step cannot take
 
+        // States that fit in shared memory: the whole sweep in one launch
+        // when every operation acts on at most two bits.
+        if (num_observables > 0 && n <= lgpu_adjoint_sweep_max_qubits(SV::dt())) {
+            std::vector<lgpu_adj_op_t> sweep;
+            std::vector<double> scales(tp_size, 0.0);
+            bool ok = true;
+            size_t tpn = tp_size - 1, cpi = num_param_ops - 1;
+            auto it = trainableParams.rbegin();
+            for (int op_idx = static_cast<int>(ops_name.size() - 1); op_idx >= 0 && ok; op_idx--) {
+                PL_ABORT_IF(ops.getOpsParams()[size_t(op_idx)].size() > 1,
+                            "The operation is not supported using the adjoint differentiation method");
+                const std::string &name = ops_name[size_t(op_idx)];
+                if ((name == "QubitStateVector") || (name == "StatePrep") || (name == "BasisState")) continue;
+                if (it == tp_rend) break;
+                const bool inv = ops.getOpsInverses()[size_t(op_idx)];
+                const auto &wires = ops.getOpsWires()[size_t(op_idx)];
+                Engine::GateDesc udag = lower(lambda, ops, size_t(op_idx), !inv);
+                std::vector<int> ubits;
+                std::vector<cd> umat;
+                lgpu_adj_op_t a{};
+                a.col = -1;
+                if (udag.kind == Engine::GateDesc::IDENTITY) {
+                    a.nu = 1;
+                    a.ubits[0] = Engine::bit_of(n, wires.empty() ? 0 : wires[0]);
+                    a.u[0] = a.u[6] = 1.0;
+                } else if (Engine::dense_on_bits(udag, ubits, umat, 2)) {
+                    a.nu = int32_t(ubits.size());
+                    for (size_t q = 0; q < ubits.size(); q++) a.ubits[q] = ubits[q];
+                    for (size_t e = 0; e < umat.size(); e++) {
+                        a.u[2 * e] = umat[e].real();
+                        a.u[2 * e + 1] = umat[e].imag();
+                    }
+                } else {
+                    ok = false;
+                    break;
+                }
+                if (ops.hasParams(size_t(op_idx)) && cpi == *it) {
+                    std::vector<cd> g;
+                    double scale = 0;
+                    PL_ABORT_IF_NOT(Engine::generator_of(name, wires.size(), g, scale),
+                                    ("The operation " + name +
+                                     " is not supported using the adjoint differentiation method")
+                                        .c_str());
+                    if (wires.size() > 2) {
+                        ok = false;
+                        break;
+                    }
+                    a.ng = int32_t(wires.size());
+                    for (size_t q = 0; q < wires.size(); q++) a.gbits[q] = Engine::bit_of(n, wires[q]);
+                    for (size_t e = 0; e < g.size(); e++) {
+                        a.g[2 * e] = g[e].real();
+                        a.g[2 * e + 1] = g[e].imag();
+                    }
+                    a.col = int32_t(tpn);
+                    scales[tpn] = scale * (inv ? -1.0 : 1.0);
+                    tpn--;
+                    ++it;
+                }
+                if (ops.hasParams(size_t(op_idx))) cpi--;
+                sweep.push_back(a);
+            }
+            if (ok) {
+                PL_LGPU_IS_SUCCESS(lgpu_adjoint_sweep_small(lambda.ctx(), lambda.getData(), bra_ptrs.data(),
+                                                            uint32_t(num_observables), n, SV::dt(), sweep.data(),
+                                                            uint32_t(sweep.size()), jac_dev.getData(),
+                                                            lambda.lstream()));
+                std::vector<double> host(tp_size * K);
+                jac_dev.CopyGpuDataToHost(host.data(), host.size(), false);
+                for (size_t p = 0; p < tp_size; p++)
+                    for (size_t k = 0; k < num_observables; k++)
+                        jac[k][p] = static_cast<T>(-2.0 * scales[p] * host[p * K + k]);
+                return;
+            }
+        }
+
         for (int op_idx = static_cast<int>(ops_name.size() - 1); op_idx >= 0; op_idx--) {
             PL_ABORT_IF(ops.getOpsParams()[size_t(op_idx)].size() > 1,
                         "The operation is not supported using the adjoint differentiation method");
@@ -151,15 +226,19 @@ template <class T = double> class AdjointJacobianGPU {
                 trainableParamNumber--;
                 ++tp_it;
             } else {
-                if (fusable) {
+                if (fusable && ubits.size() == 1) {
                     std::vector<int32_t> b32(ubits.begin(), ubits.end());
                     PL_LGPU_IS_SUCCESS(lgpu_adjoint_step(lambda.ctx(), lambda.getData(), bra_ptrs.data(),
                                                          uint32_t(num_observables), n, SV::dt(), uint32_t(b32.size()),
                                                          b32.data(), nullptr, reinterpret_cast<const double *>(umat.data()),
                                                          1, nullptr, lambda.lstream()));
                 } else {
-                    lambda.applyDesc(udag);
-                    for (auto &b : H_lambda) b.applyDesc(udag);
+                    // no gradient here: the gate kernels (structured bodies,
+                    // controls as index holes) update lambda and every bra
+                    // in one launch
+                    std::vector<void *> all(bra_ptrs);
+                    all.push_back(lambda.getData());
+                    lambda.applyDescMulti(udag, all);
                 }
             }
             if (ops.hasParams(size_t(op_idx))) current_param_idx--;

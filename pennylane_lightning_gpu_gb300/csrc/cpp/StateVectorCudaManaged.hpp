@@ -477,6 +477,26 @@ class StateVectorCudaManaged : public StateVectorCudaBase<Precision, StateVector
                                              BaseType::lstream()));
     }
 
+    // The same lowered gate on several states of this size in one launch per
+    // gate (the states share this state's stream).
+    void applyDescMulti(const Engine::GateDesc &d, const std::vector<void *> &states) const {
+        if (states.empty() || d.kind == Engine::GateDesc::IDENTITY) return;
+        std::vector<int32_t> t(d.tgts.begin(), d.tgts.end()), c(d.ctrls.begin(), d.ctrls.end()),
+            v(d.cvals.begin(), d.cvals.end());
+        if (v.empty()) v.assign(c.size(), 1);
+        if (d.kind == Engine::GateDesc::MATRIX) {
+            PL_LGPU_IS_SUCCESS(lgpu_apply_matrix_multi(states.data(), uint32_t(states.size()), nq(), dt(),
+                                                       reinterpret_cast<const double *>(d.matrix.data()),
+                                                       uint32_t(t.size()), t.data(), uint32_t(c.size()), c.data(),
+                                                       v.data(), 0, BaseType::lstream()));
+        } else {
+            PL_LGPU_IS_SUCCESS(lgpu_apply_pauli_rotation_multi(states.data(), uint32_t(states.size()), nq(), dt(),
+                                                               d.angle, uint32_t(t.size()), t.data(),
+                                                               d.paulis.c_str(), uint32_t(c.size()), c.data(),
+                                                               v.data(), BaseType::lstream()));
+        }
+    }
+
     void applyDesc(const Engine::GateDesc &d) {
         switch (d.kind) {
         case Engine::GateDesc::IDENTITY: return;

@@ -8,6 +8,7 @@
 // which replaces the reference's per-op sequence of a D2D copy of lambda,
 // U^dag on lambda, G on mu, K cuBLAS dot products and U^dag on K bras
 // (AdjointDiffGPU.hpp:560-595).
+#include "lgpu_bodies.cuh"
 #include "lgpu_internal.cuh"
 #include "lgpu_reduce.cuh"
 
@@ -88,6 +89,137 @@ template <class T, class I, int W> struct AdjBody {
     }
 };
 
+// One-bit operations (every rotation, PhaseShift and fixed 1-qubit gate):
+// U^dag runs the structured 1-target bodies (integer-pipe multiplies for
+// complex128) and the generator expectation has closed forms for the
+// generators the named gates have, in the state's precision per pair:
+//   Z: Im(b0* k0 - b1* k1)   X: Im(b0* k1 + b1* k0)
+//   Y: Re(b1* k0) - Re(b0* k1)   P1 = |1><1|: Im(b1* k1)
+// instead of two dense FP64 2x2 products per bra and pair.
+enum GenKind : int { G_NONE = 0, G_X, G_Y, G_Z, G_P1, G_DENSE };
+
+template <class T, class I, bool EMU> struct Adj1Body {
+    Holes holes;
+    I tbit;
+    int gk;
+    int ub;  // Body1 of U^dag
+    int apply_u;
+    int update_ket;
+    int nb;
+    T g[8];  // dense generator (G_DENSE)
+    T m[8];  // U^dag
+    KConst k[4];
+    cplx_t<T> *ket;
+    cplx_t<T> *bras[kAdjBras];
+
+    __device__ __forceinline__ T gexp(const cplx_t<T> &b0, const cplx_t<T> &b1, const cplx_t<T> &k0,
+                                      const cplx_t<T> &k1) const {
+        switch (gk) {
+        case G_Z: return (b0.x * k0.y - b0.y * k0.x) - (b1.x * k1.y - b1.y * k1.x);
+        case G_X: return (b0.x * k1.y - b0.y * k1.x) + (b1.x * k0.y - b1.y * k0.x);
+        case G_Y: return (b1.x * k0.x + b1.y * k0.y) - (b0.x * k1.x + b0.y * k1.y);
+        case G_P1: return b1.x * k1.y - b1.y * k1.x;
+        default: {
+            // (G k)_r then Im(b_r* (G k)_r)
+            const T y0r = g[0] * k0.x - g[1] * k0.y + g[2] * k1.x - g[3] * k1.y;
+            const T y0i = g[0] * k0.y + g[1] * k0.x + g[2] * k1.y + g[3] * k1.x;
+            const T y1r = g[4] * k0.x - g[5] * k0.y + g[6] * k1.x - g[7] * k1.y;
+            const T y1i = g[4] * k0.y + g[5] * k0.x + g[6] * k1.y + g[7] * k1.x;
+            return (b0.x * y0i - b0.y * y0r) + (b1.x * y1i - b1.y * y1r);
+        }
+        }
+    }
+
+    __device__ __forceinline__ void udag(cplx_t<T> &a0, cplx_t<T> &a1) const {
+        switch (ub) {
+        case B_DIAG: body1_sel<T, B_DIAG, EMU>(m, k, a0, a1); break;
+        case B_PERM: body1_sel<T, B_PERM, EMU>(m, k, a0, a1); break;
+        case B_ANTIDIAG: body1_sel<T, B_ANTIDIAG, EMU>(m, k, a0, a1); break;
+        case B_REAL: body1_sel<T, B_REAL, EMU>(m, k, a0, a1); break;
+        case B_RXLIKE: body1_sel<T, B_RXLIKE, EMU>(m, k, a0, a1); break;
+        default: body1_sel<T, B_DENSE, false>(m, k, a0, a1); break;
+        }
+    }
+
+    __device__ __forceinline__ void operator()(I gidx, double2 *acc) const {
+        const I i0 = insert_holes<I>(gidx, holes), i1 = i0 | tbit;
+        cplx_t<T> k0 = ket[i0], k1 = ket[i1];
+#pragma unroll 1
+        for (int b = 0; b < nb; b++) {
+            cplx_t<T> *bp = bras[b];
+            cplx_t<T> b0 = bp[i0], b1 = bp[i1];
+            if (gk != G_NONE) {
+                const double im = double(gexp(b0, b1, k0, k1));
+#pragma unroll
+                for (int q = 0; q < kAdjBras; q++)
+                    if (q == b) acc[q].x += im;
+            }
+            if (apply_u) {
+                udag(b0, b1);
+                bp[i0] = b0;
+                bp[i1] = b1;
+            }
+        }
+        if (update_ket) {
+            udag(k0, k1);
+            ket[i0] = k0;
+            ket[i1] = k1;
+        }
+    }
+};
+
+// Exact classification of a 2x2 generator (re/im interleaved).
+static int gen_kind(const double *g) {
+    auto is = [&](int e, double re, double im) { return g[2 * e] == re && g[2 * e + 1] == im; };
+    if (is(0, 1, 0) && is(1, 0, 0) && is(2, 0, 0) && is(3, -1, 0)) return G_Z;
+    if (is(0, 0, 0) && is(1, 1, 0) && is(2, 1, 0) && is(3, 0, 0)) return G_X;
+    if (is(0, 0, 0) && is(1, 0, -1) && is(2, 0, 1) && is(3, 0, 0)) return G_Y;
+    if (is(0, 0, 0) && is(1, 0, 0) && is(2, 0, 0) && is(3, 1, 0)) return G_P1;
+    return G_DENSE;
+}
+
+template <class T, class I, bool EMU>
+static lgpu_status_t adjoint1_t(lgpu_context_t ctx, void *ket, void *const *bras, uint32_t nbras, uint32_t n, int bit,
+                                const double *gen, const double *udag, int apply_udag, double *out_dev, cudaStream_t s) {
+    Adj1Body<T, I, EMU> b{};
+    b.holes = make_holes(std::vector<int>{bit});
+    b.tbit = I(I(1) << bit);
+    b.gk = gen ? gen_kind(gen) : G_NONE;
+    if (gen)
+        for (int e = 0; e < 8; e++) b.g[e] = T(gen[e]);
+    b.ub = B_DENSE;
+    if (udag) {
+        KConst kc[4];
+        b.ub = body_of_2x2_host(udag, kc);
+        for (int e = 0; e < 8; e++) b.m[e] = T(udag[e]);
+        for (int e = 0; e < 4; e++) b.k[e] = kc[e];
+    }
+    b.ket = static_cast<cplx_t<T> *>(ket);
+    const I ngroups = I(uint64_t(1) << (n - 1));
+    // FP64/FP32 work per pair is a few dozen operations per bra: spread the
+    // pairs thinly (one per thread) so small states still use many SMs
+    const unsigned g = grid_for(uint64_t(ngroups), kReduceBlock, 1, 4);
+    ReduceScratch rs;
+    LGPU_TRY(reduce_scratch(ctx, g, kAdjBras, &rs));
+    double2 *res = rs.partials + size_t(g) * kAdjBras;
+    const uint32_t nchunks = nbras == 0 ? 1 : (nbras + kAdjBras - 1) / kAdjBras;
+    for (uint32_t ch = 0; ch < nchunks; ch++) {
+        const uint32_t lo = ch * kAdjBras;
+        const uint32_t cnt = nbras == 0 ? 0 : std::min<uint32_t>(kAdjBras, nbras - lo);
+        b.nb = int(cnt);
+        for (uint32_t q = 0; q < kAdjBras; q++)
+            b.bras[q] = q < cnt ? static_cast<cplx_t<T> *>(bras[lo + q]) : nullptr;
+        b.apply_u = apply_udag && udag ? 1 : 0;
+        b.update_ket = (apply_udag && udag && ch + 1 == nchunks) ? 1 : 0;
+        reduce_kernel<kAdjBras, I><<<g, kReduceBlock, 0, s>>>(b, ngroups, rs.partials, rs.counter, res);
+        LGPU_CHECK_LAUNCH();
+        if (gen && cnt)
+            LGPU_CUDA_TRY(cudaMemcpy2DAsync(out_dev + lo, sizeof(double), res, sizeof(double2), sizeof(double), cnt,
+                                            cudaMemcpyDeviceToDevice, s));
+    }
+    return LGPU_OK;
+}
+
 template <class T, class I, int W>
 static lgpu_status_t adjoint_t(lgpu_context_t ctx, void *ket, void *const *bras, uint32_t nbras, uint32_t n,
                                const std::vector<int> &bits, const double *gen, const double *udag, int apply_udag,
@@ -106,7 +238,8 @@ static lgpu_status_t adjoint_t(lgpu_context_t ctx, void *ket, void *const *bras,
     if (udag) std::memcpy(b->u, udag, sizeof(double) * 2 * D * D);
     b->ket = static_cast<cplx_t<T> *>(ket);
     const I ngroups = I(uint64_t(1) << (n - W));
-    const unsigned g = reduce_grid(uint64_t(ngroups));
+    // dense FP64 products per group: one group per thread
+    const unsigned g = grid_for(uint64_t(ngroups), kReduceBlock, 1, 4);
     ReduceScratch rs;
     lgpu_status_t st = reduce_scratch(ctx, g, kAdjBras, &rs);
     if (st != LGPU_OK) {
@@ -147,12 +280,307 @@ static lgpu_status_t adjoint_dispatch(lgpu_context_t ctx, void *ket, void *const
                                       const std::vector<int> &bits, const double *gen, const double *udag,
                                       int apply_udag, double *out_dev, cudaStream_t s) {
     switch (bits.size()) {
-    case 1: return adjoint_t<T, I, 1>(ctx, ket, bras, nbras, n, bits, gen, udag, apply_udag, out_dev, s);
+    case 1:
+        if constexpr (sizeof(T) == 8)
+            return f64_mode() == 1
+                       ? adjoint1_t<T, I, true>(ctx, ket, bras, nbras, n, bits[0], gen, udag, apply_udag, out_dev, s)
+                       : adjoint1_t<T, I, false>(ctx, ket, bras, nbras, n, bits[0], gen, udag, apply_udag, out_dev, s);
+        else
+            return adjoint1_t<T, I, false>(ctx, ket, bras, nbras, n, bits[0], gen, udag, apply_udag, out_dev, s);
     case 2: return adjoint_t<T, I, 2>(ctx, ket, bras, nbras, n, bits, gen, udag, apply_udag, out_dev, s);
     case 3: return adjoint_t<T, I, 3>(ctx, ket, bras, nbras, n, bits, gen, udag, apply_udag, out_dev, s);
     case 4: return adjoint_t<T, I, 4>(ctx, ket, bras, nbras, n, bits, gen, udag, apply_udag, out_dev, s);
     default: return fail(LGPU_ERR_INVALID_ARG, "adjoint step: 1 to 4 bits");
     }
+}
+
+// ---------------------------------------------------------------------------
+// Whole reverse sweep in shared memory (small states)
+// ---------------------------------------------------------------------------
+// One CTA per bra: lambda and the bra live in shared memory for the whole
+// sweep, so a 12-qubit circuit of a few hundred operations is one launch
+// instead of a few hundred.  U^dag runs as a 1-target structured body under
+// controls (every named 1- and 2-qubit gate but SWAP and the Ising family,
+// which run as dense 4x4), the generator expectation in closed form for
+// X, Y, Z and |1><1| (also under one control, as for CRX/CRY/CRZ/CPhase).
+constexpr int kSweepThreads = 512;
+enum UKind : int { U_NONE = 0, U_ONE = 1, U_DENSE4 = 2 };
+
+struct SweepOp {
+    int ukind, ubody, ut, uq2;  // U_ONE: body on bit ut under (ucm, ucv); U_DENSE4: (ut, uq2), ut = matrix MSB
+    uint32_t ucm, ucv;
+    int gkind, gt, gq2;         // G_X..G_DENSE on gt under (gcm, gcv); G_DENSE4 on (gt, gq2)
+    uint32_t gcm, gcv;
+    int col;
+    double u[32];
+    double g[32];
+    float uf[32];
+    float gf[32];
+    KConst uk[4];
+};
+constexpr int G_DENSE4 = 16;
+
+template <class T> __device__ __forceinline__ const T *op_u(const SweepOp &o) {
+    if constexpr (sizeof(T) == 4) return o.uf;
+    else return o.u;
+}
+template <class T> __device__ __forceinline__ const T *op_g(const SweepOp &o) {
+    if constexpr (sizeof(T) == 4) return o.gf;
+    else return o.g;
+}
+
+template <class T, bool EMU>
+__device__ __forceinline__ void sweep_udag(cplx_t<T> *lam, cplx_t<T> *bra, int E, const SweepOp &o) {
+    using C = cplx_t<T>;
+    const T *m = op_u<T>(o);
+    if (o.ukind == U_ONE) {
+        const uint32_t holes = o.ucm | (1u << o.ut);
+        const int nfree = E >> __popc(holes);
+        PairWalk w(holes, threadIdx.x, kSweepThreads);
+        for (int f = threadIdx.x; f < nfree; f += kSweepThreads) {
+            const int e0 = int(w.x | o.ucv), e1 = e0 | (1 << o.ut);
+            w.step();
+            C l0 = lam[e0], l1 = lam[e1], b0 = bra[e0], b1 = bra[e1];
+            switch (o.ubody) {
+            case B_DIAG: body1_sel<T, B_DIAG, EMU>(m, o.uk, l0, l1); body1_sel<T, B_DIAG, EMU>(m, o.uk, b0, b1); break;
+            case B_PERM: body1_sel<T, B_PERM, EMU>(m, o.uk, l0, l1); body1_sel<T, B_PERM, EMU>(m, o.uk, b0, b1); break;
+            case B_ANTIDIAG:
+                body1_sel<T, B_ANTIDIAG, EMU>(m, o.uk, l0, l1);
+                body1_sel<T, B_ANTIDIAG, EMU>(m, o.uk, b0, b1);
+                break;
+            case B_REAL: body1_sel<T, B_REAL, EMU>(m, o.uk, l0, l1); body1_sel<T, B_REAL, EMU>(m, o.uk, b0, b1); break;
+            case B_RXLIKE:
+                body1_sel<T, B_RXLIKE, EMU>(m, o.uk, l0, l1);
+                body1_sel<T, B_RXLIKE, EMU>(m, o.uk, b0, b1);
+                break;
+            default: body1_sel<T, B_DENSE, false>(m, o.uk, l0, l1); body1_sel<T, B_DENSE, false>(m, o.uk, b0, b1); break;
+            }
+            lam[e0] = l0;
+            lam[e1] = l1;
+            bra[e0] = b0;
+            bra[e1] = b1;
+        }
+    } else if (o.ukind == U_DENSE4) {
+        const int qa = o.ut, qb = o.uq2;
+        const uint32_t holes = (1u << qa) | (1u << qb);
+        const int nfree = E >> 2;
+        PairWalk w(holes, threadIdx.x, kSweepThreads);
+        for (int f = threadIdx.x; f < nfree; f += kSweepThreads) {
+            const int e = int(w.x);
+            w.step();
+            const int idx[4] = {e, e | (1 << qb), e | (1 << qa), e | (1 << qa) | (1 << qb)};
+#pragma unroll
+            for (int s = 0; s < 2; s++) {
+                C *v = s ? bra : lam;
+                C a[4];
+#pragma unroll
+                for (int c = 0; c < 4; c++) a[c] = v[idx[c]];
+#pragma unroll
+                for (int r = 0; r < 4; r++) {
+                    T xr = 0, xi = 0;
+#pragma unroll
+                    for (int c = 0; c < 4; c++) {
+                        const T mr = m[2 * (r * 4 + c)], mi = m[2 * (r * 4 + c) + 1];
+                        xr = fmaT(mr, a[c].x, fmaT(-mi, a[c].y, xr));
+                        xi = fmaT(mr, a[c].y, fmaT(mi, a[c].x, xi));
+                    }
+                    v[idx[r]] = mk<T>(xr, xi);
+                }
+            }
+        }
+    }
+}
+
+// Im <bra| G |lam>, this thread's share (summed over the CTA by the caller).
+template <class T>
+__device__ __forceinline__ double sweep_gen(const cplx_t<T> *lam, const cplx_t<T> *bra, int E, const SweepOp &o) {
+    using C = cplx_t<T>;
+    const T *g = op_g<T>(o);
+    double acc = 0.0;
+    if (o.gkind == G_DENSE4) {
+        const int qa = o.gt, qb = o.gq2;
+        const uint32_t holes = (1u << qa) | (1u << qb);
+        PairWalk w(holes, threadIdx.x, kSweepThreads);
+        for (int f = threadIdx.x; f < (E >> 2); f += kSweepThreads) {
+            const int e = int(w.x);
+            w.step();
+            const int idx[4] = {e, e | (1 << qb), e | (1 << qa), e | (1 << qa) | (1 << qb)};
+            C a[4];
+#pragma unroll
+            for (int c = 0; c < 4; c++) a[c] = lam[idx[c]];
+#pragma unroll
+            for (int r = 0; r < 4; r++) {
+                T yr = 0, yi = 0;
+#pragma unroll
+                for (int c = 0; c < 4; c++) {
+                    const T mr = g[2 * (r * 4 + c)], mi = g[2 * (r * 4 + c) + 1];
+                    yr = fmaT(mr, a[c].x, fmaT(-mi, a[c].y, yr));
+                    yi = fmaT(mr, a[c].y, fmaT(mi, a[c].x, yi));
+                }
+                const C b = bra[idx[r]];
+                acc += double(b.x * yi - b.y * yr);
+            }
+        }
+        return acc;
+    }
+    const uint32_t holes = o.gcm | (1u << o.gt);
+    const int nfree = E >> __popc(holes);
+    PairWalk w(holes, threadIdx.x, kSweepThreads);
+    for (int f = threadIdx.x; f < nfree; f += kSweepThreads) {
+        const int e0 = int(w.x | o.gcv), e1 = e0 | (1 << o.gt);
+        w.step();
+        const C k0 = lam[e0], k1 = lam[e1], b0 = bra[e0], b1 = bra[e1];
+        T v;
+        switch (o.gkind) {
+        case G_Z: v = (b0.x * k0.y - b0.y * k0.x) - (b1.x * k1.y - b1.y * k1.x); break;
+        case G_X: v = (b0.x * k1.y - b0.y * k1.x) + (b1.x * k0.y - b1.y * k0.x); break;
+        case G_Y: v = (b1.x * k0.x + b1.y * k0.y) - (b0.x * k1.x + b0.y * k1.y); break;
+        case G_P1: v = b1.x * k1.y - b1.y * k1.x; break;
+        default: {
+            const T y0r = g[0] * k0.x - g[1] * k0.y + g[2] * k1.x - g[3] * k1.y;
+            const T y0i = g[0] * k0.y + g[1] * k0.x + g[2] * k1.y + g[3] * k1.x;
+            const T y1r = g[4] * k0.x - g[5] * k0.y + g[6] * k1.x - g[7] * k1.y;
+            const T y1i = g[4] * k0.y + g[5] * k0.x + g[6] * k1.y + g[7] * k1.x;
+            v = (b0.x * y0i - b0.y * y0r) + (b1.x * y1i - b1.y * y1r);
+        }
+        }
+        acc += double(v);
+    }
+    return acc;
+}
+
+template <class T, bool EMU>
+__global__ void __launch_bounds__(kSweepThreads, 1)
+    adjoint_sweep_kernel(const cplx_t<T> *__restrict__ ket, cplx_t<T> *const *__restrict__ bras, int n,
+                         const SweepOp *__restrict__ ops, int nops, double *__restrict__ jac, int K) {
+    using C = cplx_t<T>;
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    __shared__ double2 red[kSweepThreads / 32];
+    const int E = 1 << n;
+    C *lam = reinterpret_cast<C *>(smem_raw);
+    C *bra = lam + E;
+    const int k = blockIdx.x;
+    const C *src = bras[k];
+    for (int e = threadIdx.x; e < E; e += kSweepThreads) {
+        lam[e] = ket[e];
+        bra[e] = src[e];
+    }
+    __syncthreads();
+    for (int i = 0; i < nops; i++) {
+        const SweepOp &o = ops[i];
+        if (o.col >= 0 && o.gkind != G_NONE) {
+            const double part = sweep_gen<T>(lam, bra, E, o);
+            const double2 s = block_reduce_d2<kSweepThreads>(make_double2(part, 0.0), red);
+            if (threadIdx.x == 0) jac[size_t(o.col) * K + k] = s.x;
+            __syncthreads();
+        }
+        sweep_udag<T, EMU>(lam, bra, E, o);
+        __syncthreads();
+    }
+}
+
+// Host: classify one operation of the sweep.
+static lgpu_status_t sweep_op_of(const lgpu_adj_op_t &a, uint32_t n, SweepOp *o) {
+    *o = SweepOp{};
+    auto bit_ok = [&](int b) { return b >= 0 && uint32_t(b) < n; };
+    o->col = a.col;
+    // U^dag
+    if (a.nu == 1) {
+        if (!bit_ok(a.ubits[0])) return fail(LGPU_ERR_INVALID_ARG, "adjoint sweep: U bit out of range");
+        o->ukind = U_ONE;
+        o->ut = a.ubits[0];
+        o->ubody = body_of_2x2_host(a.u, o->uk);
+        for (int e = 0; e < 8; e++) o->u[e] = a.u[e];
+    } else if (a.nu == 2) {
+        if (!bit_ok(a.ubits[0]) || !bit_ok(a.ubits[1]) || a.ubits[0] == a.ubits[1])
+            return fail(LGPU_ERR_INVALID_ARG, "adjoint sweep: U bits out of range or repeated");
+        // controlled form [[I, 0], [0, V]] with the control on the most significant matrix bit
+        auto el = [&](int r, int c, int part) { return a.u[2 * (r * 4 + c) + part]; };
+        bool ctrl = true;
+        for (int r = 0; r < 4; r++)
+            for (int c = 0; c < 4; c++) {
+                if (r >= 2 && c >= 2) continue;
+                const double want = (r == c) ? 1.0 : 0.0;
+                if (el(r, c, 0) != want || el(r, c, 1) != 0.0) ctrl = false;
+            }
+        if (ctrl) {
+            double v[8] = {el(2, 2, 0), el(2, 2, 1), el(2, 3, 0), el(2, 3, 1),
+                           el(3, 2, 0), el(3, 2, 1), el(3, 3, 0), el(3, 3, 1)};
+            o->ukind = U_ONE;
+            o->ut = a.ubits[1];
+            o->ucm = o->ucv = 1u << a.ubits[0];
+            o->ubody = body_of_2x2_host(v, o->uk);
+            for (int e = 0; e < 8; e++) o->u[e] = v[e];
+        } else {
+            o->ukind = U_DENSE4;
+            o->ut = a.ubits[0];
+            o->uq2 = a.ubits[1];
+            for (int e = 0; e < 32; e++) o->u[e] = a.u[e];
+        }
+    } else {
+        return fail(LGPU_ERR_INVALID_ARG, "adjoint sweep: U^dag on 1 or 2 bits");
+    }
+    // generator
+    if (a.ng == 1) {
+        if (!bit_ok(a.gbits[0])) return fail(LGPU_ERR_INVALID_ARG, "adjoint sweep: G bit out of range");
+        o->gkind = gen_kind(a.g);
+        o->gt = a.gbits[0];
+        for (int e = 0; e < 8; e++) o->g[e] = a.g[e];
+    } else if (a.ng == 2) {
+        if (!bit_ok(a.gbits[0]) || !bit_ok(a.gbits[1]) || a.gbits[0] == a.gbits[1])
+            return fail(LGPU_ERR_INVALID_ARG, "adjoint sweep: G bits out of range or repeated");
+        // |1><1| (x) P on (gbits[0], gbits[1]): P with a control on gbits[0]
+        auto el = [&](int r, int c, int part) { return a.g[2 * (r * 4 + c) + part]; };
+        bool ctrl = true;
+        for (int r = 0; r < 4; r++)
+            for (int c = 0; c < 4; c++) {
+                if (r >= 2 && c >= 2) continue;
+                if (el(r, c, 0) != 0.0 || el(r, c, 1) != 0.0) ctrl = false;
+            }
+        if (ctrl) {
+            double v[8] = {el(2, 2, 0), el(2, 2, 1), el(2, 3, 0), el(2, 3, 1),
+                           el(3, 2, 0), el(3, 2, 1), el(3, 3, 0), el(3, 3, 1)};
+            o->gkind = gen_kind(v);
+            o->gt = a.gbits[1];
+            o->gcm = o->gcv = 1u << a.gbits[0];
+            for (int e = 0; e < 8; e++) o->g[e] = v[e];
+        } else {
+            o->gkind = G_DENSE4;
+            o->gt = a.gbits[0];
+            o->gq2 = a.gbits[1];
+            for (int e = 0; e < 32; e++) o->g[e] = a.g[e];
+        }
+    } else if (a.ng == 0) {
+        o->gkind = G_NONE;
+        o->col = -1;
+    } else {
+        return fail(LGPU_ERR_INVALID_ARG, "adjoint sweep: generator on 0, 1 or 2 bits");
+    }
+    if (a.ng > 0 && a.col < 0) return fail(LGPU_ERR_INVALID_ARG, "adjoint sweep: negative Jacobian column");
+    for (int e = 0; e < 32; e++) {
+        o->uf[e] = float(o->u[e]);
+        o->gf[e] = float(o->g[e]);
+    }
+    return LGPU_OK;
+}
+
+template <class T, bool EMU>
+static lgpu_status_t sweep_launch(const void *ket, void *const *dbras, uint32_t nbras, uint32_t n, const SweepOp *dops,
+                                  uint32_t nops, double *jac, cudaStream_t s) {
+    const size_t smem = 2 * (size_t(1) << n) * sizeof(cplx_t<T>);
+    static size_t attr[64] = {};
+    int dev = 0;
+    LGPU_CUDA_TRY(cudaGetDevice(&dev));
+    if (smem > 48 * 1024 && (dev >= 64 || smem > attr[dev])) {
+        LGPU_CUDA_TRY(cudaFuncSetAttribute(adjoint_sweep_kernel<T, EMU>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           int(smem)));
+        if (dev < 64) attr[dev] = smem;
+    }
+    adjoint_sweep_kernel<T, EMU><<<nbras, kSweepThreads, smem, s>>>(
+        static_cast<const cplx_t<T> *>(ket), reinterpret_cast<cplx_t<T> *const *>(dbras), int(n), dops, int(nops), jac,
+        int(nbras));
+    LGPU_CHECK_LAUNCH();
+    return LGPU_OK;
 }
 
 }  // namespace lgpu
@@ -182,6 +610,37 @@ lgpu_status_t lgpu_adjoint_step(lgpu_context_t ctx, void *ket, void *const *bras
                        : adjoint_dispatch<double, uint64_t>(ctx, ket, bras, nbras, n, b, gen, udag, apply_udag, out_dev, s);
     return n <= 32 ? adjoint_dispatch<float, uint32_t>(ctx, ket, bras, nbras, n, b, gen, udag, apply_udag, out_dev, s)
                    : adjoint_dispatch<float, uint64_t>(ctx, ket, bras, nbras, n, b, gen, udag, apply_udag, out_dev, s);
+}
+
+
+uint32_t lgpu_adjoint_sweep_max_qubits(lgpu_dtype_t dt) { return dt == LGPU_C128 ? 12u : 13u; }
+
+lgpu_status_t lgpu_adjoint_sweep_small(lgpu_context_t ctx, const void *ket, void *const *bras, uint32_t nbras,
+                                       uint32_t n, lgpu_dtype_t dt, const lgpu_adj_op_t *ops, uint32_t nops,
+                                       double *jac_dev, lgpu_stream_t stream) {
+    LGPU_TRY(check_state(ket, n, dt));
+    if (n > lgpu_adjoint_sweep_max_qubits(dt))
+        return fail(LGPU_ERR_INVALID_ARG, "adjoint sweep: the state does not fit in shared memory");
+    if (nbras == 0) return LGPU_OK;
+    if (!bras || !jac_dev || (nops && !ops)) return fail(LGPU_ERR_INVALID_ARG, "adjoint sweep: null argument");
+    for (uint32_t k = 0; k < nbras; k++) LGPU_TRY(check_state(bras[k], n, dt));
+    std::vector<SweepOp> host(std::max<uint32_t>(nops, 1));
+    for (uint32_t i = 0; i < nops; i++) LGPU_TRY(sweep_op_of(ops[i], n, &host[i]));
+    // scratch: [bra pointers, 256-byte aligned][ops]
+    const size_t pbytes = (sizeof(void *) * nbras + 255) & ~size_t(255);
+    void *p = nullptr;
+    LGPU_TRY(ctx_scratch(ctx, pbytes + sizeof(SweepOp) * host.size(), &p));
+    void **dbras = static_cast<void **>(p);
+    auto *dops = reinterpret_cast<SweepOp *>(static_cast<char *>(p) + pbytes);
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    LGPU_CUDA_TRY(cudaMemcpyAsync(dbras, bras, sizeof(void *) * nbras, cudaMemcpyHostToDevice, s));
+    if (nops) LGPU_CUDA_TRY(cudaMemcpyAsync(dops, host.data(), sizeof(SweepOp) * nops, cudaMemcpyHostToDevice, s));
+    // the pageable source vectors must outlive the copies
+    LGPU_CUDA_TRY(cudaStreamSynchronize(s));
+    if (dt == LGPU_C128)
+        return f64_mode() == 1 ? sweep_launch<double, true>(ket, dbras, nbras, n, dops, nops, jac_dev, s)
+                               : sweep_launch<double, false>(ket, dbras, nbras, n, dops, nops, jac_dev, s);
+    return sweep_launch<float, false>(ket, dbras, nbras, n, dops, nops, jac_dev, s);
 }
 
 }  // extern "C"

@@ -180,4 +180,8 @@ __device__ __forceinline__ void reg_gate_any(cplx_t<T> (&a)[1 << R], int body, i
     }
 }
 
+// Host: structured body of a 2x2 matrix (re/im interleaved, row-major) and
+// the integer-pipe multipliers its complex128 body uses (lgpu_gates.cu).
+int body_of_2x2_host(const double *m, KConst *kc);
+
 }  // namespace lgpu

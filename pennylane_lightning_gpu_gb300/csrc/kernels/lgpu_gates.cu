@@ -1006,7 +1006,7 @@ static lgpu_status_t pauli_rot_dispatch(void *sv, void *const *svs, uint32_t nst
 
 // Structured body of a 2x2 matrix (m: re/im interleaved, row-major) and the
 // integer-pipe multipliers its complex128 body uses.
-static int body_of_2x2(const double *mm, KConst *kc) {
+int body_of_2x2_host(const double *mm, KConst *kc) {
     const Cm a{mm[0], mm[1]}, b{mm[2], mm[3]}, c{mm[4], mm[5]}, d{mm[6], mm[7]};
     for (int i = 0; i < 4; i++) kc[i] = make_kconst(0.0);
     const bool diag = eq(b, 0, 0) && eq(c, 0, 0);
@@ -1188,7 +1188,7 @@ static lgpu_status_t fused_t(cplx_t<T> *sv, uint32_t n, const std::vector<int> &
             if (st != LGPU_OK) break;
             dst.mat_off = pool;
             for (uint32_t e = 0; e < need; e++) p->mats[pool + e] = T(src.m[e]);
-            dst.body = src.ntgt == 1 ? uint8_t(body_of_2x2(src.m, p->kc[cnt])) : uint8_t(B_DENSE);
+            dst.body = src.ntgt == 1 ? uint8_t(body_of_2x2_host(src.m, p->kc[cnt])) : uint8_t(B_DENSE);
             pool += need;
             cnt++;
         }

@@ -336,6 +336,46 @@ def test_adjoint_jacobian_vs_oracle(native, oracle, dtype, seed):
     assert np.max(np.abs(jac - ref)) < tol(dtype) * 50, np.max(np.abs(jac - ref))
 
 
+SMALL_ADJ_OPS = ["RX", "RY", "RZ", "PhaseShift", "CRX", "CRY", "CRZ", "ControlledPhaseShift", "IsingXX", "IsingYY",
+                 "IsingZZ", "SingleExcitation"]
+
+
+@pytest.mark.parametrize("dtype", DTYPES)
+@pytest.mark.parametrize("n", [5, 14])
+def test_adjoint_sweep_and_step_paths(native, oracle, dtype, n):
+    """Operations on at most two wires: n = 5 runs the whole sweep in one
+    launch (state in shared memory), n = 14 the per-operation steps; both
+    agree with the oracle."""
+    rng = np.random.default_rng(900 + n)
+    ops = [("Hadamard", [w], [], False) for w in range(n)]
+    for rep in range(2):
+        for name in SMALL_ADJ_OPS:
+            nw = NW.get(name, 2)
+            wires = [int(x) for x in rng.choice(n, size=nw, replace=False)]
+            ops.append((name, wires, [float(rng.uniform(0, 2 * np.pi))], bool(rng.integers(2))))
+            ops.append(("CNOT", [int(x) for x in rng.choice(n, size=2, replace=False)], [], False))
+    ops.append(("SWAP", [0, n - 1], [], False))
+    nparam = sum(1 for o in ops if o[2])
+    tp = sorted(int(x) for x in rng.choice(nparam, size=16, replace=False))
+    obs_specs = [
+        (False, [(1.0, [("PauliZ", [0], None)])]),
+        (False, [(1.0, [("PauliX", [1], None), ("PauliY", [n - 1], None)])]),
+        (True, [(0.3, [("PauliZ", [2], None)]), (-0.7, [("PauliX", [0], None), ("PauliZ", [3], None)])]),
+    ]
+    sv = getattr(native, cls_name(dtype))(n)
+    apply_ops(sv, ops)
+    adj = getattr(native, "AdjointJacobianGPU_" + ("C128" if dtype == "c128" else "C64"))()
+    rdt = np.float64 if dtype == "c128" else np.float32
+    opsd = adj.create_ops_list([o[0] for o in ops], [np.array(o[2], rdt) for o in ops], [o[1] for o in ops],
+                               [o[3] for o in ops], [np.zeros(0, np_dtype(dtype)) for o in ops])
+    obs = [_obs_native(native, dtype, s) for s in obs_specs]
+    jac = np.asarray(adj.adjoint_jacobian(sv, obs, opsd, tp))
+    final = oracle.run(n, to_oracle_ops(ops))
+    oobs = [(s[0], [(c, [(nm, w, m) for nm, w, m in f]) for c, f in s[1]]) for s in obs_specs]
+    ref = oracle.adjoint_jacobian(final, to_oracle_ops(ops), oobs, tp)
+    assert np.max(np.abs(jac - ref)) < tol(dtype) * 50, np.max(np.abs(jac - ref))
+
+
 @pytest.mark.parametrize("dtype", DTYPES)
 def test_adjoint_rejects_multiparam(native, dtype):
     suf = "C128" if dtype == "c128" else "C64"
