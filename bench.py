@@ -471,6 +471,51 @@ def bench_serving(args):
             "p99_speedup": round(base["p99_ms"] / served["p99_ms"], 2)}
 
 
+def profile_case(name):
+    """One small invocation of a secondary kernel, sized for an ncu capture:
+    fused (25-qubit complex64, one layer of RX/RY/RZ on every wire + CNOT
+    ring), batch (304 circuits of 17 qubits, complex64), pauli (26-qubit
+    complex64, 24 random Pauli words + sum_i Z_i), adjoint (12-qubit
+    complex128, 4 layers, 12 PauliZ observables)."""
+    import pennylane_lightning_gpu_gb300 as pkg
+    from pennylane_lightning_gpu_gb300 import batched, workloads
+
+    m = pkg.native()
+    if name == "fused":
+        n = 25
+        ops = workloads.layered_ansatz(n, 1, np.random.default_rng(1))
+        sv = m.LightningGPU_C64(n)
+        sv.apply([o[0] for o in ops], [list(o[1]) for o in ops], [bool(o[3]) for o in ops], [list(o[2]) for o in ops])
+        sv.synchronize()
+    elif name == "batch":
+        rng = np.random.default_rng(2)
+        circ = []
+        for _ in range(304):
+            circ.append((17, workloads.layered_ansatz(17, int(rng.integers(2, 7)), rng),
+                         workloads.sum_z_hamiltonian_terms(17)))
+        batched.build_executor(circ, np.complex64).run()
+    elif name == "pauli":
+        n = 26
+        sv = m.LightningGPU_C64(n)
+        sv.apply(["Hadamard"] * n, [[w] for w in range(n)], [False] * n, [[]] * n)
+        terms = workloads.random_pauli_hamiltonian(n, 24, np.random.default_rng(5), max_wires=4)
+        terms += workloads.sum_z_hamiltonian_terms(n)
+        sv.ExpectationValue([t[1] for t in terms], [list(t[2]) for t in terms],
+                            np.array([t[0] for t in terms], np.complex64))
+    elif name == "adjoint":
+        n = 12
+        raw = workloads.layered_ansatz(n, 4, np.random.default_rng(0))
+        sv = m.LightningGPU_C128(n)
+        sv.apply([o[0] for o in raw], [list(o[1]) for o in raw], [False] * len(raw), [list(o[2]) for o in raw])
+        adj = m.AdjointJacobianGPU_C128()
+        opsd = adj.create_ops_list([o[0] for o in raw], [np.array(o[2], np.float64) for o in raw],
+                                   [list(o[1]) for o in raw], [False] * len(raw),
+                                   [np.zeros(0, np.complex128) for o in raw])
+        obs = [m.NamedObsGPU_C128("PauliZ", [w]) for w in range(n)]
+        adj.adjoint_jacobian(sv, obs, opsd, list(range(3 * n * 4)))
+    print(json.dumps({"case": name, "ok": True}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -484,6 +529,8 @@ def main():
     ap.add_argument("--no-circuits", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-serving", action="store_true")
+    ap.add_argument("--case", choices=["fused", "batch", "pauli", "adjoint"], default=None,
+                    help="run one small secondary-kernel case (profiling) and exit")
     ap.add_argument("--only", choices=["batched", "serving", "circuits"], default=None,
                     help="run one section alone (profiling runs); the default prints the full line")
     ap.add_argument("--batch-circuits", type=int, default=4096)
@@ -492,6 +539,9 @@ def main():
     ap.add_argument("--serve-rate", type=float, default=100.0)
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
+    if args.case:
+        profile_case(args.case)
+        return
     if args.only == "batched":
         print(json.dumps({"batched": bench_batched(args)}))
         return

@@ -240,11 +240,26 @@ template <class T, class I> struct PauliWhtParams {
     uint32_t hsel[kWhtWords];
 };
 
+__device__ __forceinline__ void wht_cp_async(void *smem_dst, const void *gsrc, int bytes) {
+    const uint32_t d = static_cast<uint32_t>(__cvta_generic_to_shared(smem_dst));
+    if (bytes == 16)
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(gsrc) : "memory");
+    else
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(d), "l"(gsrc) : "memory");
+}
+
+// Each thread streams its slots through a private two-stage ring in shared
+// memory ([stage][a|b][j][thread]): the next slot's loads are in flight while
+// the current slot is transformed (no barrier: a thread reads only its own
+// copies, after cp.async.wait_group).
 template <class T, class I>
 __global__ void __launch_bounds__(kReduceBlock)
     pauli_wht_kernel(const PauliWhtParams<T, I> p, double2 *partials, unsigned *counter, double2 *out) {
     using C = cplx_t<T>;
     constexpr bool kChunk = sizeof(T) == 4;
+    extern __shared__ __align__(16) unsigned char wht_smem[];
+    C *ring = reinterpret_cast<C *>(wht_smem);  // [2][2][8][kReduceBlock]
+    auto at = [&](int st, int ab, int j) -> C * { return ring + ((st * 2 + ab) * 8 + j) * kReduceBlock + threadIdx.x; };
     __shared__ double2 sm[kReduceBlock / 32];
     double acc[kWhtWords];
     T chunk[kWhtWords];
@@ -256,32 +271,41 @@ __global__ void __launch_bounds__(kReduceBlock)
     I off[8];
 #pragma unroll
     for (int j = 0; j < 8; j++) off[j] = insert_holes<I>(I(j) << p.lgS, p.holes);
+    auto prefetch = [&](I slot, int st) {
+        const I base = insert_holes<I>(slot, p.holes);
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+            wht_cp_async(at(st, 0, j), &p.sv[base | off[j]], int(sizeof(C)));
+            if (p.flip) wht_cp_async(at(st, 1, j), &p.sv[(base | off[j]) ^ p.flip], int(sizeof(C)));
+        }
+        asm volatile("cp.async.commit_group;" ::: "memory");
+    };
     int cn = 0;
     const I stride = I(gridDim.x) * kReduceBlock;
-    for (I slot = I(blockIdx.x) * kReduceBlock + threadIdx.x; slot < p.slots; slot += stride) {
+    I slot = I(blockIdx.x) * kReduceBlock + threadIdx.x;
+    if (slot < p.slots) prefetch(slot, 0);
+    else asm volatile("cp.async.commit_group;" ::: "memory");
+    for (int it = 0; slot < p.slots; slot += stride, it++) {
+        const int st = it & 1;
+        if (slot + stride < p.slots) prefetch(slot + stride, st ^ 1);
+        else asm volatile("cp.async.commit_group;" ::: "memory");
+        asm volatile("cp.async.wait_group 1;" ::: "memory");
         const I base = insert_holes<I>(slot, p.holes);
         T wr[8], wi[8];
         if (p.flip) {
-            C a[8], b[8];
 #pragma unroll
             for (int j = 0; j < 8; j++) {
-                a[j] = p.sv[base | off[j]];
-                b[j] = p.sv[(base | off[j]) ^ p.flip];
-            }
-#pragma unroll
-            for (int j = 0; j < 8; j++) {
-                wr[j] = a[j].x * b[j].x + a[j].y * b[j].y;
-                wi[j] = a[j].x * b[j].y - a[j].y * b[j].x;
+                const C a = *at(st, 0, j), b = *at(st, 1, j);
+                wr[j] = a.x * b.x + a.y * b.y;
+                wi[j] = a.x * b.y - a.y * b.x;
             }
             wht8(wr);
             wht8(wi);
         } else {
-            C a[8];
-#pragma unroll
-            for (int j = 0; j < 8; j++) a[j] = p.sv[base | off[j]];
 #pragma unroll
             for (int j = 0; j < 8; j++) {
-                wr[j] = a[j].x * a[j].x + a[j].y * a[j].y;
+                const C a = *at(st, 0, j);
+                wr[j] = a.x * a.x + a.y * a.y;
                 wi[j] = T(0);
             }
             wht8(wr);
@@ -308,6 +332,7 @@ __global__ void __launch_bounds__(kReduceBlock)
             }
         }
     }
+    asm volatile("cp.async.wait_group 0;" ::: "memory");
     if constexpr (kChunk) {
 #pragma unroll
         for (int t = 0; t < kWhtWords; t++) acc[t] += double(chunk[t]);
@@ -332,6 +357,21 @@ __global__ void __launch_bounds__(kReduceBlock)
         }
         if (threadIdx.x == 0) *counter = 0u;
     }
+}
+
+template <class T> constexpr size_t wht_smem_bytes() { return size_t(2) * 2 * 8 * kReduceBlock * sizeof(cplx_t<T>); }
+
+template <class T, class I> static lgpu_status_t wht_smem_attr() {
+    static size_t attr[64] = {};
+    int dev = 0;
+    LGPU_CUDA_TRY(cudaGetDevice(&dev));
+    const size_t smem = wht_smem_bytes<T>();
+    if (smem > 48 * 1024 && (dev >= 64 || smem > attr[dev])) {
+        LGPU_CUDA_TRY(cudaFuncSetAttribute(pauli_wht_kernel<T, I>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           int(smem)));
+        if (dev < 64) attr[dev] = smem;
+    }
+    return LGPU_OK;
 }
 
 template <class T, class I>
@@ -373,6 +413,7 @@ static lgpu_status_t pauli_words_t(lgpu_context_t ctx, const void *sv, uint32_t 
         auto *partials = reinterpret_cast<double2 *>(static_cast<char *>(p) + 256);
         auto *results = reinterpret_cast<double2 *>(static_cast<char *>(p) + 256 + pbytes);
         std::vector<double> coef(wp.size() * kWhtWords, 0.0);
+        LGPU_TRY((wht_smem_attr<T, I>()));
         for (size_t pi = 0; pi < wp.size(); pi++) {
             PauliWhtParams<T, I> b{};
             b.sv = static_cast<const cplx_t<T> *>(sv);
@@ -402,7 +443,8 @@ static lgpu_status_t pauli_words_t(lgpu_context_t ctx, const void *sv, uint32_t 
                 // v.x = sum(+-w) (flip 0) or 2 sum(+-Re w); v.y = -2 sum(+-Im w) (odd flip/sign overlap)
                 coef[pi * kWhtWords + size_t(t)] = !wp[pi].flip ? 1.0 : (kneg ? -2.0 : 2.0);
             }
-            pauli_wht_kernel<T, I><<<g, kReduceBlock, 0, s>>>(b, partials, counter, results + pi * kWhtWords);
+            pauli_wht_kernel<T, I><<<g, kReduceBlock, wht_smem_bytes<T>(), s>>>(b, partials, counter,
+                                                                                 results + pi * kWhtWords);
             LGPU_CHECK_LAUNCH();
         }
         std::vector<double2> host(wp.size() * kWhtWords);
