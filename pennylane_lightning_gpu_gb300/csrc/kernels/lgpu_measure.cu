@@ -236,6 +236,8 @@ template <class T, class I> struct PauliWhtParams {
     int lgS;
     int nt;
     uint32_t use_im;  // bit t: word t reads the imaginary transform
+    int need_re, need_im;  // some word of the pass reads the real / imaginary products
+    int direct;            // few words: each word's one coefficient as a signed 8-term sum
     I sgn[kWhtWords];
     uint32_t hsel[kWhtWords];
 };
@@ -252,8 +254,10 @@ __device__ __forceinline__ void wht_cp_async(void *smem_dst, const void *gsrc, i
 // memory ([stage][a|b][j][thread]): the next slot's loads are in flight while
 // the current slot is transformed (no barrier: a thread reads only its own
 // copies, after cp.async.wait_group).
-template <class T, class I>
-__global__ void __launch_bounds__(kReduceBlock)
+constexpr int kDirectWords = 3;
+
+template <class T, class I, bool DIRECT>
+__global__ void __launch_bounds__(kReduceBlock, 2)
     pauli_wht_kernel(const PauliWhtParams<T, I> p, double2 *partials, unsigned *counter, double2 *out) {
     using C = cplx_t<T>;
     constexpr bool kChunk = sizeof(T) == 4;
@@ -296,11 +300,9 @@ __global__ void __launch_bounds__(kReduceBlock)
 #pragma unroll
             for (int j = 0; j < 8; j++) {
                 const C a = *at(st, 0, j), b = *at(st, 1, j);
-                wr[j] = a.x * b.x + a.y * b.y;
-                wi[j] = a.x * b.y - a.y * b.x;
+                wr[j] = p.need_re ? a.x * b.x + a.y * b.y : T(0);
+                wi[j] = p.need_im ? a.x * b.y - a.y * b.x : T(0);
             }
-            wht8(wr);
-            wht8(wi);
         } else {
 #pragma unroll
             for (int j = 0; j < 8; j++) {
@@ -308,12 +310,28 @@ __global__ void __launch_bounds__(kReduceBlock)
                 wr[j] = a.x * a.x + a.y * a.y;
                 wi[j] = T(0);
             }
-            wht8(wr);
+        }
+        if constexpr (!DIRECT) {
+            if (p.need_re) wht8(wr);
+            if (p.need_im) wht8(wi);
         }
 #pragma unroll
-        for (int t = 0; t < kWhtWords; t++) {
+        for (int t = 0; t < (DIRECT ? kDirectWords : kWhtWords); t++) {
             if (t < p.nt) {
-                const T v = ((p.use_im >> t) & 1u) ? sel8(wi, p.hsel[t]) : sel8(wr, p.hsel[t]);
+                const bool im = (p.use_im >> t) & 1u;
+                T v;
+                if constexpr (DIRECT) {
+                    // W[h] = sum_j (-1)^popc(j & h) x_j for this word's h only
+                    const uint32_t h = p.hsel[t];
+                    v = T(0);
+#pragma unroll
+                    for (int j = 0; j < 8; j++) {
+                        const T x = im ? wi[j] : wr[j];
+                        v += (__popc(uint32_t(j) & h) & 1) ? -x : x;
+                    }
+                } else {
+                    v = im ? sel8(wi, p.hsel[t]) : sel8(wr, p.hsel[t]);
+                }
                 const T c = (__popcll(uint64_t(base & p.sgn[t])) & 1) ? -v : v;
                 if constexpr (kChunk)
                     chunk[t] += c;
@@ -367,7 +385,9 @@ template <class T, class I> static lgpu_status_t wht_smem_attr() {
     LGPU_CUDA_TRY(cudaGetDevice(&dev));
     const size_t smem = wht_smem_bytes<T>();
     if (smem > 48 * 1024 && (dev >= 64 || smem > attr[dev])) {
-        LGPU_CUDA_TRY(cudaFuncSetAttribute(pauli_wht_kernel<T, I>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        LGPU_CUDA_TRY(cudaFuncSetAttribute(pauli_wht_kernel<T, I, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           int(smem)));
+        LGPU_CUDA_TRY(cudaFuncSetAttribute(pauli_wht_kernel<T, I, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            int(smem)));
         if (dev < 64) attr[dev] = smem;
     }
@@ -432,6 +452,8 @@ static lgpu_status_t pauli_words_t(lgpu_context_t ctx, const void *sv, uint32_t 
                 if (!hole.empty() && pos >= hole[0]) pos++;
                 pj[q] = pos;
             }
+            // one word's coefficient directly costs 7 adds, the full transform 24 per product array
+            b.direct = b.nt <= kDirectWords ? 1 : 0;
             for (int t = 0; t < b.nt; t++) {
                 const uint32_t w = wp[pi].words[size_t(t)];
                 b.sgn[t] = I(sign[w]);
@@ -440,11 +462,17 @@ static lgpu_status_t pauli_words_t(lgpu_context_t ctx, const void *sv, uint32_t 
                 b.hsel[t] = h;
                 const bool kneg = (__builtin_popcountll(flip[w] & sign[w]) & 1) != 0;
                 if (wp[pi].flip && kneg) b.use_im |= 1u << t;
+                if (wp[pi].flip && kneg) b.need_im = 1;
+                else b.need_re = 1;
                 // v.x = sum(+-w) (flip 0) or 2 sum(+-Re w); v.y = -2 sum(+-Im w) (odd flip/sign overlap)
                 coef[pi * kWhtWords + size_t(t)] = !wp[pi].flip ? 1.0 : (kneg ? -2.0 : 2.0);
             }
-            pauli_wht_kernel<T, I><<<g, kReduceBlock, wht_smem_bytes<T>(), s>>>(b, partials, counter,
-                                                                                 results + pi * kWhtWords);
+            if (b.direct)
+                pauli_wht_kernel<T, I, true><<<g, kReduceBlock, wht_smem_bytes<T>(), s>>>(b, partials, counter,
+                                                                                       results + pi * kWhtWords);
+            else
+                pauli_wht_kernel<T, I, false><<<g, kReduceBlock, wht_smem_bytes<T>(), s>>>(b, partials, counter,
+                                                                                        results + pi * kWhtWords);
             LGPU_CHECK_LAUNCH();
         }
         std::vector<double2> host(wp.size() * kWhtWords);
