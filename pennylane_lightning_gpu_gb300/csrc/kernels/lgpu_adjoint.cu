@@ -137,7 +137,7 @@ template <class T, class I, bool EMU> struct Adj1Body {
         case B_ANTIDIAG: body1_sel<T, B_ANTIDIAG, EMU>(m, k, a0, a1); break;
         case B_REAL: body1_sel<T, B_REAL, EMU>(m, k, a0, a1); break;
         case B_RXLIKE: body1_sel<T, B_RXLIKE, EMU>(m, k, a0, a1); break;
-        default: body1_sel<T, B_DENSE, false>(m, k, a0, a1); break;
+        default: body1_sel<T, B_DENSE, EMU>(m, k, a0, a1); break;
         }
     }
 
@@ -353,7 +353,7 @@ __device__ __forceinline__ void sweep_udag(cplx_t<T> *lam, cplx_t<T> *bra, int E
                 body1_sel<T, B_RXLIKE, EMU>(m, o.uk, l0, l1);
                 body1_sel<T, B_RXLIKE, EMU>(m, o.uk, b0, b1);
                 break;
-            default: body1_sel<T, B_DENSE, false>(m, o.uk, l0, l1); body1_sel<T, B_DENSE, false>(m, o.uk, b0, b1); break;
+            default: body1_sel<T, B_DENSE, EMU>(m, o.uk, l0, l1); body1_sel<T, B_DENSE, EMU>(m, o.uk, b0, b1); break;
             }
             lam[e0] = l0;
             lam[e1] = l1;

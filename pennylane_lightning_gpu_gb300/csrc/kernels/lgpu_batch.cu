@@ -106,6 +106,8 @@ __global__ void bprep_kernel(const lgpu_bgate_t *__restrict__ gates, uint64_t ng
                 k[0] = make_kconst(m[2]); k[1] = make_kconst(m[4]); k[2] = make_kconst(0.0); k[3] = make_kconst(0.0);
             } else if (g.kind == BK_RXLIKE1) {
                 k[0] = make_kconst(-m[3]); k[1] = make_kconst(m[3]); k[2] = make_kconst(-m[5]); k[3] = make_kconst(m[5]);
+            } else if (g.kind == BK_DENSE1) {
+                k[0] = make_kconst(m[1]); k[1] = make_kconst(m[3]); k[2] = make_kconst(m[5]); k[3] = make_kconst(m[7]);
             }
         }
     }
@@ -174,7 +176,7 @@ __device__ __forceinline__ void tile_gate(cplx_t<T> *tile, int E, const lgpu_bga
         case BK_X1: batch_pairs<T, B_PERM, EMU>(tile, E, q, g.cmask, g.cval, pool, g.mat); break;
         case BK_REAL1: batch_pairs<T, B_REAL, EMU>(tile, E, q, g.cmask, g.cval, pool, g.mat); break;
         case BK_RXLIKE1: batch_pairs<T, B_RXLIKE, EMU>(tile, E, q, g.cmask, g.cval, pool, g.mat); break;
-        default: batch_pairs<T, B_DENSE, false>(tile, E, q, g.cmask, g.cval, pool, g.mat); break;
+        default: batch_pairs<T, B_DENSE, EMU>(tile, E, q, g.cmask, g.cval, pool, g.mat); break;
         }
         return;
     }

@@ -82,8 +82,13 @@ __device__ __forceinline__ void body1_emu(const double *m, const KConst *k, doub
         const double c = m[0];
         a0 = make_double2(__fma_rn(c, x.x, emul(y.y, k[0])), __fma_rn(c, x.y, emul(y.x, k[1])));
         a1 = make_double2(__fma_rn(c, y.x, emul(x.y, k[2])), __fma_rn(c, y.y, emul(x.x, k[3])));
-    } else {
-        body1<double, B_DENSE>(m, a0, a1);
+    } else {  // dense: k = {m00i, m01i, m10i, m11i}; 12 FP64 operations per pair instead of 16
+        const double t0 = emul(x.y, k[0]) + emul(y.y, k[1]);
+        const double t1 = emul(x.x, k[0]) + emul(y.x, k[1]);
+        const double t2 = emul(x.y, k[2]) + emul(y.y, k[3]);
+        const double t3 = emul(x.x, k[2]) + emul(y.x, k[3]);
+        a0 = make_double2(__fma_rn(m[0], x.x, __fma_rn(m[2], y.x, -t0)), __fma_rn(m[0], x.y, __fma_rn(m[2], y.y, t1)));
+        a1 = make_double2(__fma_rn(m[4], x.x, __fma_rn(m[6], y.x, -t2)), __fma_rn(m[4], x.y, __fma_rn(m[6], y.y, t3)));
     }
 }
 

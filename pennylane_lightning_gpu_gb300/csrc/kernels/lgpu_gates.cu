@@ -523,7 +523,7 @@ __device__ __forceinline__ void fused_tile(cplx_t<T> *tile, int E, I base, const
             case B_ANTIDIAG: tile_pairs<T, B_ANTIDIAG, EMU, NT>(tile, E, g.q0, g.in_mask, g.in_val, mm, kk); break;
             case B_REAL: tile_pairs<T, B_REAL, EMU, NT>(tile, E, g.q0, g.in_mask, g.in_val, mm, kk); break;
             case B_RXLIKE: tile_pairs<T, B_RXLIKE, EMU, NT>(tile, E, g.q0, g.in_mask, g.in_val, mm, kk); break;
-            default: tile_pairs<T, B_DENSE, false, NT>(tile, E, g.q0, g.in_mask, g.in_val, mm, kk); break;
+            default: tile_pairs<T, B_DENSE, EMU, NT>(tile, E, g.q0, g.in_mask, g.in_val, mm, kk); break;
             }
         } else {
             const int qa = g.q0, qb = g.q1;  // qa = most significant matrix bit
@@ -716,7 +716,7 @@ static lgpu_status_t launch_bulk_body(cplx_t<T> *sv, const BulkParams<T> &bp, in
     case B_ANTIDIAG: return launch_bulk_t<T, B_ANTIDIAG, EMU>(sv, bp, s);
     case B_REAL: return launch_bulk_t<T, B_REAL, EMU>(sv, bp, s);
     case B_RXLIKE: return launch_bulk_t<T, B_RXLIKE, EMU>(sv, bp, s);
-    default: return launch_bulk_t<T, B_DENSE, false>(sv, bp, s);
+    default: return launch_bulk_t<T, B_DENSE, EMU>(sv, bp, s);
     }
 }
 
@@ -788,6 +788,9 @@ static lgpu_status_t run_gate1(cplx_t<T> *sv, unsigned nstates, cplx_t<T> *const
     } else if (rxlike) {
         p.k[0] = make_kconst(-m[1].im); p.k[1] = make_kconst(m[1].im);
         p.k[2] = make_kconst(-m[2].im); p.k[3] = make_kconst(m[2].im);
+    } else {  // dense
+        p.k[0] = make_kconst(m[0].im); p.k[1] = make_kconst(m[1].im);
+        p.k[2] = make_kconst(m[2].im); p.k[3] = make_kconst(m[3].im);
     }
     if (nstates == 0 && g.ctrls.empty() && bulk_enabled()) {
         const int ch_log2 = sizeof(T) == 8 ? 11 : 12;  // 32 KB halves, 64 KB tiles
@@ -1033,6 +1036,8 @@ int body_of_2x2_host(const double *mm, KConst *kc) {
         kc[2] = make_kconst(-c.im); kc[3] = make_kconst(c.im);
         return B_RXLIKE;
     }
+    kc[0] = make_kconst(a.im); kc[1] = make_kconst(b.im);
+    kc[2] = make_kconst(c.im); kc[3] = make_kconst(d.im);
     return B_DENSE;
 }
 
