@@ -296,8 +296,10 @@ inline bool fusable(const GateDesc &d) {
 // Fold each uncontrolled 1-target matrix gate into the previous one on the
 // same bit when no gate touching that bit lies between them (the gates in
 // between act on other bits and commute with both): the earlier gate becomes
-// the 2x2 product and the later one IDENTITY.  Used for complex64 states,
-// where one dense body costs less than several structured ones.
+// the 2x2 product and the later one IDENTITY.  One dense body costs no more
+// arithmetic than the structured bodies it replaces (complex128: 12 FP64
+// operations per pair either way for RX.RY.RZ) and saves their shared-memory
+// round trips.
 inline void merge_1q_runs(std::vector<GateDesc> &gates) {
     std::unordered_map<int, size_t> pending;  // bit -> index of the gate that absorbs the next one
     for (size_t i = 0; i < gates.size(); i++) {

@@ -540,7 +540,7 @@ class StateVectorCudaManaged : public StateVectorCudaBase<Precision, StateVector
                 }
             }
         }
-        if constexpr (std::is_same_v<Precision, float>) Engine::merge_1q_runs(descs);
+        Engine::merge_1q_runs(descs);
         const int kmax = std::min<int>(fusionTileBits(), int(nq()));
         const auto plan = Engine::plan_fusion(descs, nq(), kmax, std::min<int>(5, kmax));
         for (const auto &blk : plan) {
