@@ -318,13 +318,15 @@ lgpu_status_t lgpu_graph_destroy(lgpu_graph_t graph);
  * new parameters.  No counterpart in the reference (it runs one circuit per
  * device call). */
 typedef struct {
-    uint8_t kind;      /* 0 dense 1q, 1 diagonal 1q, 2 X, 3 real 1q, 4 RX-like 1q, 5 dense 2q, 6 SWAP */
+    uint8_t kind;      /* 0 dense 1q, 1 diagonal 1q, 2 X, 3 real 1q, 4 RX-like 1q, 5 dense 2q, 6 SWAP,
+                          7 folded into the preceding chain head (skipped by the kernel) */
     uint8_t pkind;     /* 0 fixed matrix, 1 RX, 2 RY, 3 RZ, 4 PhaseShift, 5 Rot, 6 IsingXX, 7 IsingYY, 8 IsingZZ */
     uint8_t q0, q1;    /* tile positions of the targets, q0 = most significant matrix bit */
     uint32_t cmask;    /* controls inside the tile (tile positions) and their values */
     uint32_t cval;
     int32_t param;     /* index of the first parameter (-1: none) */
-    uint32_t flags;    /* bit 0: adjoint (parametric gates) */
+    uint32_t flags;    /* bit 0: adjoint (parametric gates); bit 1: chain head, whose matrix is the
+                          product of the q1 gates recorded right after it */
     uint32_t mat;      /* offset of the gate's slot in the pool, in doubles (16 for 1q, 48 for 2q; the
                           C64 float copy of the matrix is written into the slot by lgpu_batch_prepare) */
     uint64_t omask;    /* controls outside the tile (state bits) and their values */

@@ -147,8 +147,41 @@ template <class Precision> class BatchedExecutor {
                 b.gate_off = uint32_t(hg.size());
                 std::vector<int> pos(c.n, -1);
                 for (size_t q = 0; q < blk.first.size(); q++) pos[size_t(blk.first[q])] = int(q);
-                for (size_t gi : blk.second) hg.push_back(record(c.ops[gi], pos, c.param_off, pool));
-                b.gate_cnt = uint32_t(blk.second.size());
+                // runs of uncontrolled 1-target gates on one bit become one
+                // chain head (its matrix is their product, built on the
+                // device) followed by the folded gates, which the kernel skips
+                const auto &gl = blk.second;
+                auto single = [&](size_t gi) {
+                    const Op &o = c.ops[gi];
+                    return o.tgts.size() == 1 && o.ctrls.empty() && o.kind < 5;
+                };
+                for (size_t i = 0; i < gl.size();) {
+                    size_t j = i + 1;
+                    if (single(gl[i]))
+                        while (j < gl.size() && j - i < kMaxChain && single(gl[j]) &&
+                               c.ops[gl[j]].tgts[0] == c.ops[gl[i]].tgts[0])
+                            j++;
+                    if (j - i >= 2) {
+                        lgpu_bgate_t head{};
+                        head.kind = 0;  // dense 1-target
+                        head.q0 = uint8_t(pos[size_t(c.ops[gl[i]].tgts[0])]);
+                        head.q1 = uint8_t(j - i);
+                        head.flags = 2u;
+                        head.param = -1;
+                        head.mat = uint32_t(pool.size());
+                        pool.resize(pool.size() + 16, 0.0);
+                        hg.push_back(head);
+                        for (size_t t = i; t < j; t++) {
+                            lgpu_bgate_t g = record(c.ops[gl[t]], pos, c.param_off, pool);
+                            g.kind = 7;  // folded into the head
+                            hg.push_back(g);
+                        }
+                    } else {
+                        hg.push_back(record(c.ops[gl[i]], pos, c.param_off, pool));
+                    }
+                    i = j;
+                }
+                b.gate_cnt = uint32_t(hg.size() - b.gate_off);
                 hb.push_back(b);
                 work += double(blk.second.size() + 2) * std::ldexp(1.0, int(c.n));
             }
@@ -396,6 +429,7 @@ template <class Precision> class BatchedExecutor {
         h_params_ = h_out_ = nullptr;
     }
 
+    static constexpr size_t kMaxChain = 8;
     int kmax_;
     int threads_;
     int grid_;

@@ -21,7 +21,8 @@
 namespace lgpu {
 
 // body kinds
-enum BKind : uint8_t { BK_DENSE1 = 0, BK_DIAG1, BK_X1, BK_REAL1, BK_RXLIKE1, BK_DENSE2, BK_SWAP2 };
+enum BKind : uint8_t { BK_DENSE1 = 0, BK_DIAG1, BK_X1, BK_REAL1, BK_RXLIKE1, BK_DENSE2, BK_SWAP2, BK_CHAINED };
+constexpr uint32_t kChainHead = 2u;  // flags bit 1: the next q1 gates (BK_CHAINED) fold into this one
 // parameter kinds (matrix built on device)
 enum PKind : uint8_t { PK_NONE = 0, PK_RX, PK_RY, PK_RZ, PK_PHASE, PK_ROT, PK_ISINGXX, PK_ISINGYY, PK_ISINGZZ };
 
@@ -30,64 +31,99 @@ static_assert(sizeof(lgpu_bgate_t) == 40, "lgpu_bgate_t layout");
 // ---------------------------------------------------------------------------
 // Matrix preparation
 // ---------------------------------------------------------------------------
+// Matrix of one gate into m (8 doubles for 1 target, 32 for 2): from the
+// parameters for parametric gates, from the pool for fixed ones.
+__device__ void bgate_matrix(const lgpu_bgate_t &g, const double *__restrict__ params, const double *pool, double *m) {
+    const bool adj = (g.flags & 1u) != 0;
+    if (g.pkind == PK_NONE) {
+        const int cnt = (g.kind == BK_DENSE2 || g.kind == BK_SWAP2) ? 32 : 8;
+        for (int e = 0; e < cnt; e++) m[e] = pool[g.mat + e];
+        return;
+    }
+    const double th0 = params[g.param];
+    const double th = adj ? -th0 : th0;
+    if (g.pkind == PK_RX || g.pkind == PK_RY || g.pkind == PK_RZ || g.pkind == PK_PHASE) {
+        double s, c;
+        if (g.pkind == PK_PHASE) {
+            sincos(th, &s, &c);
+            m[0] = 1; m[1] = 0; m[2] = 0; m[3] = 0; m[4] = 0; m[5] = 0; m[6] = c; m[7] = s;
+        } else {
+            sincos(0.5 * th, &s, &c);
+            if (g.pkind == PK_RX) {
+                m[0] = c; m[1] = 0; m[2] = 0; m[3] = -s; m[4] = 0; m[5] = -s; m[6] = c; m[7] = 0;
+            } else if (g.pkind == PK_RY) {
+                m[0] = c; m[1] = 0; m[2] = -s; m[3] = 0; m[4] = s; m[5] = 0; m[6] = c; m[7] = 0;
+            } else {
+                m[0] = c; m[1] = -s; m[2] = 0; m[3] = 0; m[4] = 0; m[5] = 0; m[6] = c; m[7] = s;
+            }
+        }
+    } else if (g.pkind == PK_ROT) {
+        // Rot(phi, theta, omega) = RZ(omega) RY(theta) RZ(phi); adjoint = Rot(-omega, -theta, -phi)
+        double phi = params[g.param], theta = params[g.param + 1], omega = params[g.param + 2];
+        if (adj) {
+            const double t = phi;
+            phi = -omega;
+            theta = -theta;
+            omega = -t;
+        }
+        double cs, sn, cp, sp, cm, sm;
+        sincos(0.5 * theta, &sn, &cs);
+        sincos(0.5 * (phi + omega), &sp, &cp);
+        sincos(0.5 * (phi - omega), &sm, &cm);
+        m[0] = cs * cp; m[1] = -cs * sp;
+        m[2] = -sn * cm; m[3] = -sn * sm;
+        m[4] = sn * cm; m[5] = -sn * sm;
+        m[6] = cs * cp; m[7] = cs * sp;
+    } else {
+        double s, c;
+        sincos(0.5 * th, &s, &c);
+        for (int e = 0; e < 32; e++) m[e] = 0.0;
+        if (g.pkind == PK_ISINGZZ) {
+            // diag(e^{-i t/2}, e^{i t/2}, e^{i t/2}, e^{-i t/2})
+            m[0] = c; m[1] = -s; m[10] = c; m[11] = s; m[20] = c; m[21] = s; m[30] = c; m[31] = -s;
+        } else {
+            const double corner = g.pkind == PK_ISINGXX ? -s : s;  // YY: +i s at (0,3),(3,0)
+            for (int d = 0; d < 4; d++) m[2 * (d * 4 + d)] = c;
+            m[2 * (0 * 4 + 3) + 1] = corner;
+            m[2 * (3 * 4 + 0) + 1] = corner;
+            m[2 * (1 * 4 + 2) + 1] = -s;
+            m[2 * (2 * 4 + 1) + 1] = -s;
+        }
+    }
+}
+
 __global__ void bprep_kernel(const lgpu_bgate_t *__restrict__ gates, uint64_t ngates, const double *__restrict__ params,
                              double *__restrict__ pool, int c64) {
     const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
     for (uint64_t gi = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; gi < ngates; gi += stride) {
         const lgpu_bgate_t g = gates[gi];
+        if (g.kind == BK_CHAINED) continue;  // folded into its chain head
         double *m = pool + g.mat;
-        const bool adj = (g.flags & 1u) != 0;
-        if (g.pkind != PK_NONE) {
-            const double th0 = params[g.param];
-            const double th = adj ? -th0 : th0;
-            if (g.pkind == PK_RX || g.pkind == PK_RY || g.pkind == PK_RZ || g.pkind == PK_PHASE) {
-                double s, c;
-                if (g.pkind == PK_PHASE) {
-                    sincos(th, &s, &c);
-                    m[0] = 1; m[1] = 0; m[2] = 0; m[3] = 0; m[4] = 0; m[5] = 0; m[6] = c; m[7] = s;
-                } else {
-                    sincos(0.5 * th, &s, &c);
-                    if (g.pkind == PK_RX) {
-                        m[0] = c; m[1] = 0; m[2] = 0; m[3] = -s; m[4] = 0; m[5] = -s; m[6] = c; m[7] = 0;
-                    } else if (g.pkind == PK_RY) {
-                        m[0] = c; m[1] = 0; m[2] = -s; m[3] = 0; m[4] = s; m[5] = 0; m[6] = c; m[7] = 0;
-                    } else {
-                        m[0] = c; m[1] = -s; m[2] = 0; m[3] = 0; m[4] = 0; m[5] = 0; m[6] = c; m[7] = s;
+        if (g.flags & kChainHead) {
+            // product M_q1 ... M_2 M_1 of the run of 1-target gates on one bit
+            // recorded after the head (their own slots stay untouched, so a
+            // replay with new parameters rebuilds it)
+            double a[8] = {1, 0, 0, 0, 0, 0, 1, 0}, b[8];
+            for (uint32_t c = 1; c <= g.q1; c++) {
+                bgate_matrix(gates[gi + c], params, pool, b);
+                double r[8];
+                for (int i = 0; i < 2; i++)
+                    for (int j = 0; j < 2; j++) {
+                        double re = 0, im = 0;
+                        for (int k = 0; k < 2; k++) {
+                            const double br = b[2 * (i * 2 + k)], bi = b[2 * (i * 2 + k) + 1];
+                            const double ar = a[2 * (k * 2 + j)], ai = a[2 * (k * 2 + j) + 1];
+                            re += br * ar - bi * ai;
+                            im += br * ai + bi * ar;
+                        }
+                        r[2 * (i * 2 + j)] = re;
+                        r[2 * (i * 2 + j) + 1] = im;
                     }
-                }
-            } else if (g.pkind == PK_ROT) {
-                // Rot(phi, theta, omega) = RZ(omega) RY(theta) RZ(phi); adjoint = Rot(-omega, -theta, -phi)
-                double phi = params[g.param], theta = params[g.param + 1], omega = params[g.param + 2];
-                if (adj) {
-                    const double t = phi;
-                    phi = -omega;
-                    theta = -theta;
-                    omega = -t;
-                }
-                double cs, sn, cp, sp, cm, sm;
-                sincos(0.5 * theta, &sn, &cs);
-                sincos(0.5 * (phi + omega), &sp, &cp);
-                sincos(0.5 * (phi - omega), &sm, &cm);
-                m[0] = cs * cp; m[1] = -cs * sp;
-                m[2] = -sn * cm; m[3] = -sn * sm;
-                m[4] = sn * cm; m[5] = -sn * sm;
-                m[6] = cs * cp; m[7] = cs * sp;
-            } else {
-                double s, c;
-                sincos(0.5 * th, &s, &c);
-                for (int e = 0; e < 32; e++) m[e] = 0.0;
-                if (g.pkind == PK_ISINGZZ) {
-                    // diag(e^{-i t/2}, e^{i t/2}, e^{i t/2}, e^{-i t/2})
-                    m[0] = c; m[1] = -s; m[10] = c; m[11] = s; m[20] = c; m[21] = s; m[30] = c; m[31] = -s;
-                } else {
-                    const double corner = g.pkind == PK_ISINGXX ? -s : s;  // YY: +i s at (0,3),(3,0)
-                    for (int d = 0; d < 4; d++) m[2 * (d * 4 + d)] = c;
-                    m[2 * (0 * 4 + 3) + 1] = corner;
-                    m[2 * (3 * 4 + 0) + 1] = corner;
-                    m[2 * (1 * 4 + 2) + 1] = -s;
-                    m[2 * (2 * 4 + 1) + 1] = -s;
-                }
+                for (int e = 0; e < 8; e++) a[e] = r[e];
             }
+            for (int e = 0; e < 8; e++) m[e] = a[e];
+        } else if (g.pkind != PK_NONE) {
+            bgate_matrix(g, params, pool, m);
         }
         // (fixed matrices arrive from the host already in their final, adjointed form)
         if (c64) {
@@ -414,7 +450,9 @@ __global__ void __launch_bounds__(512, 1) batch_kernel(lgpu_batch_args_t a) {
                 for (int e = threadIdx.x; e < E; e += blockDim.x) tile[e] = mk<T>(T(e == 0 ? 1 : 0), T(0));
                 __syncthreads();
                 for (uint32_t gi = 0; gi < blk.gate_cnt; gi++) {
-                    tile_gate<T, EMU>(tile, E, a.gates[blk.gate_off + gi], a.pool);
+                    const lgpu_bgate_t g = a.gates[blk.gate_off + gi];
+                    if (g.kind == BK_CHAINED) continue;
+                    tile_gate<T, EMU>(tile, E, g, a.pool);
                     __syncthreads();
                 }
                 acc += wht ? tile_obs<T>(tile, k, a.terms + cir.obs_off, cir.obs_cnt, 0, s_lm, s_c)
@@ -469,7 +507,7 @@ __global__ void __launch_bounds__(512, 1) batch_kernel(lgpu_batch_args_t a) {
                 }
                 for (uint32_t gi = 0; gi < blk.gate_cnt; gi++) {
                     const lgpu_bgate_t g = a.gates[blk.gate_off + gi];
-                    if ((base & g.omask) != g.oval) continue;  // tile-uniform controls
+                    if (g.kind == BK_CHAINED || (base & g.omask) != g.oval) continue;  // tile-uniform
                     tile_gate<T, EMU>(tile, E, g, a.pool);
                     __syncthreads();
                 }
