@@ -98,6 +98,14 @@ lgpu_status_t lgpu_device_reset(void);
 lgpu_status_t lgpu_mem_info(size_t *free_bytes, size_t *total_bytes);
 lgpu_status_t lgpu_malloc(void **ptr, size_t bytes);
 lgpu_status_t lgpu_free(void *ptr);
+/* Stream-ordered allocation from the device's memory pool, which keeps freed
+ * blocks for reuse instead of returning them to the driver: neither call
+ * synchronises the device (cudaFree does), so states created and destroyed on
+ * different streams do not wait for each other's kernels.  The memory is
+ * usable in stream order on `stream`; other streams must order themselves
+ * after it.  No counterpart in the reference. */
+lgpu_status_t lgpu_malloc_async(void **ptr, size_t bytes, lgpu_stream_t stream);
+lgpu_status_t lgpu_free_async(void *ptr, lgpu_stream_t stream);
 lgpu_status_t lgpu_host_alloc_pinned(void **ptr, size_t bytes);
 lgpu_status_t lgpu_host_free_pinned(void *ptr);
 lgpu_status_t lgpu_memcpy(void *dst, const void *src, size_t bytes, lgpu_copy_kind_t kind,
@@ -111,6 +119,12 @@ lgpu_status_t lgpu_peer_access_all(void);
 /* ---- scratch context -------------------------------------------------- */
 lgpu_status_t lgpu_context_create(int device, lgpu_context_t *ctx);
 lgpu_status_t lgpu_context_destroy(lgpu_context_t ctx);
+/* A context from the library's per-device free list (created when the list is
+ * empty); release returns it with its scratch and pinned staging kept.  The
+ * caller must have finished all work that uses the context before releasing
+ * it (e.g. by synchronising the stream it used). */
+lgpu_status_t lgpu_context_acquire(int device, lgpu_context_t *ctx);
+lgpu_status_t lgpu_context_release(lgpu_context_t ctx);
 /* Grow the context's scratch to at least `bytes` now (optional; reductions
  * grow it on first use). */
 lgpu_status_t lgpu_context_reserve(lgpu_context_t ctx, size_t bytes);

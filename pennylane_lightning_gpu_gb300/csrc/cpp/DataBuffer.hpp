@@ -19,7 +19,8 @@ template <class GPUDataT, class DevTagT = int> class DataBuffer {
         : length_{length}, dev_tag_{device_id, stream_id}, gpu_buffer_{nullptr} {
         if (alloc_memory && (length > 0)) {
             dev_tag_.refresh();
-            PL_LGPU_IS_SUCCESS(lgpu_malloc(reinterpret_cast<void **>(&gpu_buffer_), sizeof(GPUDataT) * length));
+            PL_LGPU_IS_SUCCESS(lgpu_malloc_async(reinterpret_cast<void **>(&gpu_buffer_), sizeof(GPUDataT) * length,
+                                                 lstream()));
         }
     }
 
@@ -27,7 +28,8 @@ template <class GPUDataT, class DevTagT = int> class DataBuffer {
         : length_{length}, dev_tag_{dev}, gpu_buffer_{nullptr} {
         if (alloc_memory && (length > 0)) {
             dev_tag_.refresh();
-            PL_LGPU_IS_SUCCESS(lgpu_malloc(reinterpret_cast<void **>(&gpu_buffer_), sizeof(GPUDataT) * length));
+            PL_LGPU_IS_SUCCESS(lgpu_malloc_async(reinterpret_cast<void **>(&gpu_buffer_), sizeof(GPUDataT) * length,
+                                                 lstream()));
         }
     }
 
@@ -35,7 +37,8 @@ template <class GPUDataT, class DevTagT = int> class DataBuffer {
         : length_{length}, dev_tag_{std::move(dev)}, gpu_buffer_{nullptr} {
         if (alloc_memory && (length > 0)) {
             dev_tag_.refresh();
-            PL_LGPU_IS_SUCCESS(lgpu_malloc(reinterpret_cast<void **>(&gpu_buffer_), sizeof(GPUDataT) * length));
+            PL_LGPU_IS_SUCCESS(lgpu_malloc_async(reinterpret_cast<void **>(&gpu_buffer_), sizeof(GPUDataT) * length,
+                                                 lstream()));
         }
     }
 
@@ -50,7 +53,7 @@ template <class GPUDataT, class DevTagT = int> class DataBuffer {
     }
     DataBuffer &operator=(DataBuffer &&other) noexcept {
         if (this != &other) {
-            if (gpu_buffer_) lgpu_free(gpu_buffer_);
+            if (gpu_buffer_) lgpu_free_async(gpu_buffer_, lstream());
             length_ = other.length_;
             dev_tag_ = std::move(other.dev_tag_);
             gpu_buffer_ = other.gpu_buffer_;
@@ -61,13 +64,17 @@ template <class GPUDataT, class DevTagT = int> class DataBuffer {
     }
 
     virtual ~DataBuffer() {
-        if (gpu_buffer_ != nullptr) lgpu_free(gpu_buffer_);
+        if (gpu_buffer_ != nullptr) lgpu_free_async(gpu_buffer_, lstream());
     }
 
     auto zeroInit() {
         PL_LGPU_IS_SUCCESS(lgpu_memset(gpu_buffer_, 0, length_ * sizeof(GPUDataT),
                                        reinterpret_cast<lgpu_stream_t>(dev_tag_.getStreamID())));
     }
+
+    // stream-ordered allocation on this buffer's stream: no device-wide
+    // synchronisation when states come and go (cudaFree would synchronise)
+    lgpu_stream_t lstream() const { return reinterpret_cast<lgpu_stream_t>(dev_tag_.getStreamID()); }
 
     auto getData() -> GPUDataT * { return gpu_buffer_; }
     auto getData() const -> const GPUDataT * { return gpu_buffer_; }

@@ -84,7 +84,9 @@ class StateVectorCudaManaged : public StateVectorCudaBase<Precision, StateVector
         BaseType::CopyGpuDataToGpuIn(other);
     }
 
-    ~StateVectorCudaManaged() = default;
+    // Work queued on this state's stream may still use its scratch context,
+    // which goes back to the library's free list with it.
+    ~StateVectorCudaManaged() { lgpu_stream_sync(BaseType::lstream()); }
 
     // ---- state preparation -------------------------------------------------
     void setBasisState(const std::complex<Precision> &value, const size_t index, const bool async = false) {

@@ -132,8 +132,10 @@ inline SharedCusparseHandle make_shared_cusparse_handle() { return std::make_sha
 // RAII lgpu scratch context (one per state vector / algorithm instance).
 class LgpuContext {
   public:
-    explicit LgpuContext(int device = 0) { PL_LGPU_IS_SUCCESS(lgpu_context_create(device, &ctx_)); }
-    ~LgpuContext() { lgpu_context_destroy(ctx_); }
+    // contexts come from (and return to) the library's per-device free list;
+    // the owner finishes the work that uses the context before it is released
+    explicit LgpuContext(int device = 0) { PL_LGPU_IS_SUCCESS(lgpu_context_acquire(device, &ctx_)); }
+    ~LgpuContext() { lgpu_context_release(ctx_); }
     LgpuContext(const LgpuContext &) = delete;
     LgpuContext &operator=(const LgpuContext &) = delete;
     lgpu_context_t get() const { return ctx_; }

@@ -626,12 +626,12 @@ lgpu_status_t lgpu_adjoint_sweep_small(lgpu_context_t ctx, const void *ket, void
     for (uint32_t k = 0; k < nbras; k++) LGPU_TRY(check_state(bras[k], n, dt));
     std::vector<SweepOp> host(std::max<uint32_t>(nops, 1));
     for (uint32_t i = 0; i < nops; i++) LGPU_TRY(sweep_op_of(ops[i], n, &host[i]));
-    // scratch: [bra pointers, 256-byte aligned][ops]
+    // scratch: [reduction counter, 256 B, left untouched][bra pointers, 256-byte aligned][ops]
     const size_t pbytes = (sizeof(void *) * nbras + 255) & ~size_t(255);
     void *p = nullptr;
-    LGPU_TRY(ctx_scratch(ctx, pbytes + sizeof(SweepOp) * host.size(), &p));
-    void **dbras = static_cast<void **>(p);
-    auto *dops = reinterpret_cast<SweepOp *>(static_cast<char *>(p) + pbytes);
+    LGPU_TRY(ctx_scratch(ctx, 256 + pbytes + sizeof(SweepOp) * host.size(), &p));
+    void **dbras = reinterpret_cast<void **>(static_cast<char *>(p) + 256);
+    auto *dops = reinterpret_cast<SweepOp *>(static_cast<char *>(p) + 256 + pbytes);
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
     LGPU_CUDA_TRY(cudaMemcpyAsync(dbras, bras, sizeof(void *) * nbras, cudaMemcpyHostToDevice, s));
     if (nops) LGPU_CUDA_TRY(cudaMemcpyAsync(dops, host.data(), sizeof(SweepOp) * nops, cudaMemcpyHostToDevice, s));

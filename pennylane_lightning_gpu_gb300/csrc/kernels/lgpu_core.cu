@@ -104,6 +104,10 @@ lgpu_status_t check_bits(uint32_t n, uint32_t count, const int32_t *bits, const 
     return LGPU_OK;
 }
 
+// Scratch of a context.  Bytes 0..127 hold the last-block arrival counter of
+// the reductions: zero at allocation, put back to zero by the last block of
+// every reduction, and never written by anything else (contexts are reused
+// across calls and, through the free list, across states).
 lgpu_status_t ctx_scratch(lgpu_context_t ctx, size_t bytes, void **out) {
     if (!ctx) return fail(LGPU_ERR_INVALID_ARG, "context is null");
     if (bytes > ctx->scratch_bytes) {
@@ -315,6 +319,39 @@ lgpu_status_t lgpu_free(void *ptr) {
     return LGPU_OK;
 }
 
+lgpu_status_t lgpu_malloc_async(void **ptr, size_t bytes, lgpu_stream_t stream) {
+    if (!ptr) return fail(LGPU_ERR_INVALID_ARG, "ptr is null");
+    *ptr = nullptr;
+    if (bytes == 0) return LGPU_OK;
+    int dev = 0;
+    LGPU_CUDA_TRY(cudaGetDevice(&dev));
+    {
+        // the process's default pool keeps freed memory for reuse (set once per device)
+        static std::mutex mu;
+        static bool done[64] = {};
+        std::lock_guard<std::mutex> lock(mu);
+        if (dev >= 0 && dev < 64 && !done[dev]) {
+            cudaMemPool_t pool;
+            LGPU_CUDA_TRY(cudaDeviceGetDefaultMemPool(&pool, dev));
+            uint64_t keep = ~uint64_t(0);
+            LGPU_CUDA_TRY(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep));
+            done[dev] = true;
+        }
+    }
+    cudaError_t e = cudaMallocAsync(ptr, bytes, reinterpret_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        *ptr = nullptr;
+        return cuda_fail(e, "cudaMallocAsync");
+    }
+    return LGPU_OK;
+}
+
+lgpu_status_t lgpu_free_async(void *ptr, lgpu_stream_t stream) {
+    if (ptr) LGPU_CUDA_TRY(cudaFreeAsync(ptr, reinterpret_cast<cudaStream_t>(stream)));
+    return LGPU_OK;
+}
+
 lgpu_status_t lgpu_host_alloc_pinned(void **ptr, size_t bytes) {
     if (!ptr) return fail(LGPU_ERR_INVALID_ARG, "ptr is null");
     LGPU_CUDA_TRY(cudaMallocHost(ptr, bytes));
@@ -432,6 +469,36 @@ lgpu_status_t lgpu_context_destroy(lgpu_context_t ctx) {
     if (ctx->pinned) cudaFreeHost(ctx->pinned);
     delete ctx;
     return LGPU_OK;
+}
+
+static std::mutex g_ctx_pool_mu;
+static std::vector<lgpu_context_t> g_ctx_pool[64];
+
+lgpu_status_t lgpu_context_acquire(int device, lgpu_context_t *ctx) {
+    if (!ctx) return fail(LGPU_ERR_INVALID_ARG, "ctx is null");
+    if (device >= 0 && device < 64) {
+        std::lock_guard<std::mutex> lock(g_ctx_pool_mu);
+        auto &free_list = g_ctx_pool[device];
+        if (!free_list.empty()) {
+            *ctx = free_list.back();
+            free_list.pop_back();
+            return LGPU_OK;
+        }
+    }
+    return lgpu_context_create(device, ctx);
+}
+
+lgpu_status_t lgpu_context_release(lgpu_context_t ctx) {
+    if (!ctx) return LGPU_OK;
+    if (ctx->device >= 0 && ctx->device < 64) {
+        std::lock_guard<std::mutex> lock(g_ctx_pool_mu);
+        auto &free_list = g_ctx_pool[ctx->device];
+        if (free_list.size() < 256) {
+            free_list.push_back(ctx);
+            return LGPU_OK;
+        }
+    }
+    return lgpu_context_destroy(ctx);
 }
 
 lgpu_status_t lgpu_context_reserve(lgpu_context_t ctx, size_t bytes) {

@@ -818,7 +818,7 @@ static lgpu_status_t sample_t(lgpu_context_t ctx, const void *svv, uint32_t n, c
     void *p = nullptr;
     LGPU_TRY(ctx_scratch(ctx, 256 + ((cbytes + 255) & ~size_t(255)) + ((dbytes + 255) & ~size_t(255)) + obytes, &p));
     char *cp = static_cast<char *>(p);
-    auto *total = reinterpret_cast<double *>(cp);
+    auto *total = reinterpret_cast<double *>(cp + 128);  // bytes 0..127: reduction counter, kept zero
     auto *csum = reinterpret_cast<double *>(cp + 256);
     auto *ddraws = reinterpret_cast<double *>(cp + 256 + ((cbytes + 255) & ~size_t(255)));
     auto *dout = reinterpret_cast<uint64_t *>(cp + 256 + ((cbytes + 255) & ~size_t(255)) +

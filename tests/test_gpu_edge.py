@@ -86,3 +86,36 @@ def test_all_wire_probabilities_and_basis_states(native, dtype):
             rev = int(format(idx, "0%db" % n)[::-1], 2)
             want[rev] = 1.0
             assert np.max(np.abs(p - want)) < tol(dtype), (n, idx, p)
+
+
+@pytest.mark.parametrize("dtype", DTYPES)
+def test_reductions_after_sampling_and_adjoint(native, oracle, dtype):
+    """Scratch contexts are reused across calls and, through the library's
+    free list, across states: sampling an unnormalised state (a total that is
+    not 1) and a whole adjoint sweep must leave later reductions intact."""
+    rng = np.random.default_rng(5)
+    psi = 0.7 * random_state(6, rng)
+    sv = make_sv(native, dtype, psi)
+    sv.setSeed(3)
+    idx = np.asarray(sv.GenerateSampleIndices(100, True))
+    assert idx.size == 100
+    p = np.asarray(sv.Probability([0, 1]))
+    ref = oracle.probs(psi.astype(np.complex128), [0, 1])
+    assert np.max(np.abs(p - ref)) < tol(dtype)
+    # adjoint on a small state (whole sweep in one launch), then a fresh state
+    a = getattr(native, cls_name(dtype))(4)
+    a.apply(["RX", "CNOT", "RY"], [[0], [0, 1], [1]], [False] * 3, [[0.3], [], [0.8]])
+    suf = "C128" if dtype == "c128" else "C64"
+    adj = getattr(native, "AdjointJacobianGPU_" + suf)()
+    rdt = np.float64 if dtype == "c128" else np.float32
+    opsd = adj.create_ops_list(["RX", "CNOT", "RY"], [np.array([0.3], rdt), np.zeros(0, rdt), np.array([0.8], rdt)],
+                               [[0], [0, 1], [1]], [False] * 3, [np.zeros(0, np_dtype(dtype))] * 3)
+    adj.adjoint_jacobian(a, [getattr(native, "NamedObsGPU_" + suf)("PauliZ", [1])], opsd, [0, 1])
+    del a
+    for _ in range(3):
+        b = make_sv(native, dtype, random_state(5, rng))
+        st = np.asarray(b.GetState()).astype(np.complex128)
+        z = float(b.ExpectationValue(["Z"], [[0]], np.ones(1, np_dtype(dtype))))
+        want = float(np.sum(np.abs(st[:16]) ** 2) - np.sum(np.abs(st[16:]) ** 2))
+        assert abs(z - want) < tol(dtype) * 10
+        del b
