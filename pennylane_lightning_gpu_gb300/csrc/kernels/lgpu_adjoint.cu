@@ -568,14 +568,8 @@ template <class T, bool EMU>
 static lgpu_status_t sweep_launch(const void *ket, void *const *dbras, uint32_t nbras, uint32_t n, const SweepOp *dops,
                                   uint32_t nops, double *jac, cudaStream_t s) {
     const size_t smem = 2 * (size_t(1) << n) * sizeof(cplx_t<T>);
-    static size_t attr[64] = {};
-    int dev = 0;
-    LGPU_CUDA_TRY(cudaGetDevice(&dev));
-    if (smem > 48 * 1024 && (dev >= 64 || smem > attr[dev])) {
-        LGPU_CUDA_TRY(cudaFuncSetAttribute(adjoint_sweep_kernel<T, EMU>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           int(smem)));
-        if (dev < 64) attr[dev] = smem;
-    }
+    static std::atomic<size_t> attr[64];
+    LGPU_TRY(ensure_smem(reinterpret_cast<const void *>(adjoint_sweep_kernel<T, EMU>), smem, attr));
     adjoint_sweep_kernel<T, EMU><<<nbras, kSweepThreads, smem, s>>>(
         static_cast<const cplx_t<T> *>(ket), reinterpret_cast<cplx_t<T> *const *>(dbras), int(n), dops, int(nops), jac,
         int(nbras));

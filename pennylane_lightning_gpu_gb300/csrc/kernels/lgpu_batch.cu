@@ -561,13 +561,8 @@ template <class T, bool EMU>
 static lgpu_status_t launch_batch(const lgpu_batch_args_t &args, unsigned grid, size_t smem, cudaStream_t s) {
     // The attribute is set once per size outside any stream capture (the host
     // runs the batch eagerly once before capturing it).
-    static size_t attr_smem = 0;
-    if (smem > attr_smem) {
-        cudaError_t e =
-            cudaFuncSetAttribute(batch_kernel<T, EMU>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
-        if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(batch)");
-        attr_smem = smem;
-    }
+    static std::atomic<size_t> attr[64];
+    LGPU_TRY(ensure_smem(reinterpret_cast<const void *>(batch_kernel<T, EMU>), smem, attr));
     batch_kernel<T, EMU><<<grid, args.threads, smem, s>>>(args);
     LGPU_CHECK_LAUNCH();
     return LGPU_OK;

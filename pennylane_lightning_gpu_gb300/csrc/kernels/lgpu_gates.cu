@@ -695,13 +695,8 @@ static void launch_gate1(cplx_t<T> *sv, const G1Params<T, I> &p, unsigned nstate
 template <class T, int BODY, bool EMU>
 static lgpu_status_t launch_bulk_t(cplx_t<T> *sv, const BulkParams<T> &bp, cudaStream_t s) {
     const size_t smem = size_t(kBulkStages) * (size_t(2) << bp.ch_log2) * sizeof(cplx_t<T>);
-    static bool attr_set = false;  // per instantiation; set once (idempotent)
-    if (!attr_set) {
-        cudaError_t e = cudaFuncSetAttribute(gate1_bulk_kernel<T, BODY, EMU>,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
-        if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(gate1_bulk)");
-        attr_set = true;
-    }
+    static std::atomic<size_t> attr[64];
+    LGPU_TRY(ensure_smem(reinterpret_cast<const void *>(gate1_bulk_kernel<T, BODY, EMU>), smem, attr));
     const unsigned grid = unsigned(std::min<uint64_t>(bp.ntiles, uint64_t(sm_count())));
     gate1_bulk_kernel<T, BODY, EMU><<<grid, kBulkThreads, smem, s>>>(sv, bp);
     LGPU_CHECK_LAUNCH();
@@ -882,9 +877,8 @@ static lgpu_status_t run_gatebig(cplx_t<T> *sv, uint32_t n, const std::vector<Cm
     p.off = doff;
     p.mat = dmat;
     const size_t smem = size_t(D) * sizeof(cplx_t<T>);
-    if (smem > 48 * 1024)
-        LGPU_CUDA_TRY(cudaFuncSetAttribute(gatebig_kernel<T, I>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           int(smem)));
+    static std::atomic<size_t> attr[64];
+    LGPU_TRY(ensure_smem(reinterpret_cast<const void *>(gatebig_kernel<T, I>), smem, attr));
     const unsigned grid = unsigned(std::min<uint64_t>(uint64_t(p.ngroups), uint64_t(sm_count()) * 4));
     gatebig_kernel<T, I><<<grid, 256, smem, s>>>(sv, p);
     LGPU_CHECK_LAUNCH();
@@ -1095,18 +1089,8 @@ static int group_fused_gates(FGate *gates, int cnt, int k, int R, FGroup *groups
 
 template <class T, class I, bool EMU, int NT, int STAGES>
 static lgpu_status_t launch_fused_nt(cplx_t<T> *sv, const FusedParams<T, I> &p, size_t smem, cudaStream_t s) {
-    // dynamic shared memory opted in so far, per device (set outside any
-    // capture: the first launch of a size runs eagerly)
-    static size_t attr[64] = {};
-    int dev = 0;
-    LGPU_CUDA_TRY(cudaGetDevice(&dev));
-    if (smem > 48 * 1024 && (dev >= 64 || smem > attr[dev])) {
-        cudaError_t e =
-            cudaFuncSetAttribute(fused_kernel<T, I, EMU, NT, STAGES>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 int(smem));
-        if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(fused)");
-        if (dev < 64) attr[dev] = smem;
-    }
+    static std::atomic<size_t> attr[64];
+    LGPU_TRY(ensure_smem(reinterpret_cast<const void *>(fused_kernel<T, I, EMU, NT, STAGES>), smem, attr));
     const int per_sm = std::max(1, std::min(int((220 * 1024) / smem), 2048 / NT));
     const unsigned grid = unsigned(std::min<uint64_t>(uint64_t(p.ntiles), uint64_t(sm_count()) * per_sm));
     fused_kernel<T, I, EMU, NT, STAGES><<<grid, NT, smem, s>>>(sv, p);

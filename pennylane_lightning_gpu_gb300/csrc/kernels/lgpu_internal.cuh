@@ -1,6 +1,8 @@
 // Internal helpers shared by the liblgpu_gb300 translation units.
 #pragma once
 
+#include <atomic>
+
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -189,6 +191,27 @@ __device__ __forceinline__ bool last_block_arrive(unsigned *counter) {
     }
     __syncthreads();
     return is_last;
+}
+
+// Opt `kernel` in to `smem` bytes of dynamic shared memory on the current
+// device, once per (kernel, device, size).  cudaFuncSetAttribute is not a
+// stream operation: the first launch of each size runs outside any stream
+// capture.  `cache` is the kernel's own array (a static of the caller);
+// concurrent host threads may race to set the same value, which is harmless.
+inline lgpu_status_t ensure_smem(const void *kernel, size_t smem, std::atomic<size_t> (&cache)[64]) {
+    if (smem <= 48 * 1024) return LGPU_OK;
+    int dev = 0;
+    LGPU_CUDA_TRY(cudaGetDevice(&dev));
+    const bool cached = dev >= 0 && dev < 64;
+    if (cached && smem <= cache[dev].load(std::memory_order_acquire)) return LGPU_OK;
+    const cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute");
+    if (cached) {
+        size_t cur = cache[dev].load(std::memory_order_relaxed);
+        while (cur < smem && !cache[dev].compare_exchange_weak(cur, smem, std::memory_order_release)) {
+        }
+    }
+    return LGPU_OK;
 }
 
 // 8-point Walsh-Hadamard transform W[h] = sum_j (-1)^popc(j & h) x_j (in

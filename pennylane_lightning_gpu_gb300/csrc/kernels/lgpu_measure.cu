@@ -153,9 +153,8 @@ static lgpu_status_t expval_big(lgpu_context_t ctx, const cplx_t<T> *sv, uint32_
     LGPU_CUDA_TRY(cudaMemcpyAsync(dmat, matrix, mbytes, cudaMemcpyHostToDevice, s));
     LGPU_CUDA_TRY(cudaMemcpyAsync(doff, off.data(), obytes, cudaMemcpyHostToDevice, s));
     const size_t smem = size_t(D) * sizeof(double2);
-    if (smem > 48 * 1024)
-        LGPU_CUDA_TRY(cudaFuncSetAttribute(expval_big_kernel<T, I>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           int(smem)));
+    static std::atomic<size_t> attr_e[64];
+    LGPU_TRY(ensure_smem(reinterpret_cast<const void *>(expval_big_kernel<T, I>), smem, attr_e));
     expval_big_kernel<T, I><<<g, kReduceBlock, smem, s>>>(sv, make_holes(tg), I(ngroups), t, doff, dmat, partials,
                                                          counter, res);
     LGPU_CHECK_LAUNCH();
@@ -380,17 +379,9 @@ __global__ void __launch_bounds__(kReduceBlock, 2)
 template <class T> constexpr size_t wht_smem_bytes() { return size_t(2) * 2 * 8 * kReduceBlock * sizeof(cplx_t<T>); }
 
 template <class T, class I> static lgpu_status_t wht_smem_attr() {
-    static size_t attr[64] = {};
-    int dev = 0;
-    LGPU_CUDA_TRY(cudaGetDevice(&dev));
-    const size_t smem = wht_smem_bytes<T>();
-    if (smem > 48 * 1024 && (dev >= 64 || smem > attr[dev])) {
-        LGPU_CUDA_TRY(cudaFuncSetAttribute(pauli_wht_kernel<T, I, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           int(smem)));
-        LGPU_CUDA_TRY(cudaFuncSetAttribute(pauli_wht_kernel<T, I, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           int(smem)));
-        if (dev < 64) attr[dev] = smem;
-    }
+    static std::atomic<size_t> attr_w[64], attr_d[64];
+    LGPU_TRY(ensure_smem(reinterpret_cast<const void *>(pauli_wht_kernel<T, I, false>), wht_smem_bytes<T>(), attr_w));
+    LGPU_TRY(ensure_smem(reinterpret_cast<const void *>(pauli_wht_kernel<T, I, true>), wht_smem_bytes<T>(), attr_d));
     return LGPU_OK;
 }
 
@@ -664,9 +655,8 @@ static lgpu_status_t probs_t(lgpu_context_t ctx, const void *svv, uint32_t n, co
         auto *partials = reinterpret_cast<double *>(static_cast<char *>(p) + 256);
         res = partials + size_t(g) * nb;
         const size_t smem = nb * sizeof(double);
-        if (smem > 48 * 1024)
-            LGPU_CUDA_TRY(cudaFuncSetAttribute(probs_hist_kernel<T, I>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                               int(smem)));
+        static std::atomic<size_t> attr_p[64];
+        LGPU_TRY(ensure_smem(reinterpret_cast<const void *>(probs_hist_kernel<T, I>), smem, attr_p));
         if (n < 8) chunk_log2 = int(n);
         probs_hist_kernel<T, I><<<g, 256, smem, s>>>(sv, I(N), chunk_log2, bm, partials, counter, res);
         LGPU_CHECK_LAUNCH();
