@@ -175,23 +175,33 @@ def _dist():
 def _barrier():
     import torch
 
-    torch.cuda.synchronize()
+    if torch.cuda.is_available():
+        torch.cuda.synchronize()
     if int(os.environ.get("WORLD_SIZE", "1")) > 1:
         import torch.distributed as dist
 
         dist.barrier()
-        torch.cuda.synchronize()
+        if torch.cuda.is_available():
+            torch.cuda.synchronize()
 
 
 def _max_over_ranks(x):
+    """Largest value over the ranks (the slowest replica's time)."""
     if int(os.environ.get("WORLD_SIZE", "1")) <= 1:
         return x
     import torch
     import torch.distributed as dist
 
-    t = torch.tensor([float(x)], dtype=torch.float64, device="cuda")
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(x)], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def _replica_value(world, units_per_rank, seconds):
+    """Whole-job throughput of `world` replicas: all units over the slowest
+    replica's time (weak scaling, no data-path collective)."""
+    return world * units_per_rank / seconds
 
 
 def gate_sweep(m, cls, n, steps, warmup, f64_mode=None, device=0):
@@ -227,7 +237,7 @@ def gate_sweep(m, cls, n, steps, warmup, f64_mode=None, device=0):
     for i, (g, w) in enumerate(gates):
         per_target.setdefault(g, []).append(round(2 * S / (float(np.median(per_launch[:, i])) / 1e3) / 1e9, 1))
     world = int(os.environ.get("WORLD_SIZE", "1"))
-    gbs = world * len(gates) * 2 * S / (ms_per_step / 1e3) / 1e9
+    gbs = _replica_value(world, len(gates) * 2 * S, ms_per_step / 1e3) / 1e9
     return gbs, float(per_launch.mean()), per_target, ms_per_step, sv
 
 
@@ -276,7 +286,7 @@ def run_ours(args):
             _apply_gate(sv, g, w)
         sv.Probability([0])  # blocking D2H of the step's result
     e2e_s = _max_over_ranks((time.perf_counter() - t0) / args.steps)
-    e2e_value = world * (bytes_per_step + S) / e2e_s / 1e9  # + one read pass for the probability
+    e2e_value = _replica_value(world, bytes_per_step + S, e2e_s) / 1e9  # + one read pass for the probability
 
     peak, peak_kind = _peaks()
     # DRAM bytes (read + write) of one gate1_bulk_kernel launch, ncu capture of the
