@@ -338,7 +338,15 @@ template <class PrecisionT, class ParamT> void sv_class_bindings(py::module_ &m)
             "Device address of the amplitudes.")
         .def(
             "streamPtr", [](SV &sv) { return reinterpret_cast<uintptr_t>(sv.getStream()); },
-            "The CUDA stream the state works on.");
+            "The CUDA stream the state works on.")
+        .def(
+            "copyFrom",
+            [](SV &sv, const SV &other) {
+                PL_ABORT_IF(other.getNumQubits() != sv.getNumQubits(), "States of different sizes");
+                py::gil_scoped_release r;
+                sv.updateData(other, false);
+            },
+            "Copy the amplitudes of another state of the same size (device to device).");
 
     // ---- observables -------------------------------------------------------
     class_name = "ObservableGPU_C" + bitsize;

@@ -98,7 +98,11 @@ template <class T, class I, int W> struct AdjBody {
 // instead of two dense FP64 2x2 products per bra and pair.
 enum GenKind : int { G_NONE = 0, G_X, G_Y, G_Z, G_P1, G_DENSE };
 
-template <class T, class I, bool EMU> struct Adj1Body {
+// GK / UB fix the generator kind and the U^dag body at compile time for the
+// pairs the named rotations produce; -1 selects them at run time.  (Small
+// run-time switches inside the per-pair loop are if-converted by the
+// compiler, which then issues every case's FP64 work for every pair.)
+template <class T, class I, bool EMU, int GK = -1, int UB = -1> struct Adj1Body {
     Holes holes;
     I tbit;
     int gk;
@@ -114,6 +118,10 @@ template <class T, class I, bool EMU> struct Adj1Body {
 
     __device__ __forceinline__ T gexp(const cplx_t<T> &b0, const cplx_t<T> &b1, const cplx_t<T> &k0,
                                       const cplx_t<T> &k1) const {
+        if constexpr (GK == G_Z) return (b0.x * k0.y - b0.y * k0.x) - (b1.x * k1.y - b1.y * k1.x);
+        if constexpr (GK == G_X) return (b0.x * k1.y - b0.y * k1.x) + (b1.x * k0.y - b1.y * k0.x);
+        if constexpr (GK == G_Y) return (b1.x * k0.x + b1.y * k0.y) - (b0.x * k1.x + b0.y * k1.y);
+        if constexpr (GK == G_P1) return b1.x * k1.y - b1.y * k1.x;
         switch (gk) {
         case G_Z: return (b0.x * k0.y - b0.y * k0.x) - (b1.x * k1.y - b1.y * k1.x);
         case G_X: return (b0.x * k1.y - b0.y * k1.x) + (b1.x * k0.y - b1.y * k0.x);
@@ -131,6 +139,10 @@ template <class T, class I, bool EMU> struct Adj1Body {
     }
 
     __device__ __forceinline__ void udag(cplx_t<T> &a0, cplx_t<T> &a1) const {
+        if constexpr (UB >= 0) {
+            body1_sel<T, (UB >= 0 ? UB : 0), EMU>(m, k, a0, a1);
+            return;
+        }
         switch (ub) {
         case B_DIAG: body1_sel<T, B_DIAG, EMU>(m, k, a0, a1); break;
         case B_PERM: body1_sel<T, B_PERM, EMU>(m, k, a0, a1); break;
@@ -144,16 +156,14 @@ template <class T, class I, bool EMU> struct Adj1Body {
     __device__ __forceinline__ void operator()(I gidx, double2 *acc) const {
         const I i0 = insert_holes<I>(gidx, holes), i1 = i0 | tbit;
         cplx_t<T> k0 = ket[i0], k1 = ket[i1];
-#pragma unroll 1
-        for (int b = 0; b < nb; b++) {
+        // compile-time bra index: acc[b] stays a register (a runtime index
+        // would cost an FP64 add per accumulator slot)
+#pragma unroll
+        for (int b = 0; b < kAdjBras; b++) {
+            if (b >= nb) break;
             cplx_t<T> *bp = bras[b];
             cplx_t<T> b0 = bp[i0], b1 = bp[i1];
-            if (gk != G_NONE) {
-                const double im = double(gexp(b0, b1, k0, k1));
-#pragma unroll
-                for (int q = 0; q < kAdjBras; q++)
-                    if (q == b) acc[q].x += im;
-            }
+            if (GK >= 0 || gk != G_NONE) acc[b].x += double(gexp(b0, b1, k0, k1));
             if (apply_u) {
                 udag(b0, b1);
                 bp[i0] = b0;
@@ -178,10 +188,33 @@ static int gen_kind(const double *g) {
     return G_DENSE;
 }
 
+template <class T, class I, bool EMU, int GK, int UB>
+static lgpu_status_t adjoint1_launch(lgpu_context_t ctx, void *ket, void *const *bras, uint32_t nbras, uint32_t n,
+                                     int bit, const double *gen, const double *udag, int apply_udag, double *out_dev,
+                                     cudaStream_t s);
+
 template <class T, class I, bool EMU>
 static lgpu_status_t adjoint1_t(lgpu_context_t ctx, void *ket, void *const *bras, uint32_t nbras, uint32_t n, int bit,
                                 const double *gen, const double *udag, int apply_udag, double *out_dev, cudaStream_t s) {
-    Adj1Body<T, I, EMU> b{};
+    const int gk = gen ? gen_kind(gen) : G_NONE;
+    KConst kc[4];
+    const int ub = udag ? body_of_2x2_host(udag, kc) : B_DENSE;
+    if (gk == G_X && ub == B_RXLIKE)
+        return adjoint1_launch<T, I, EMU, G_X, B_RXLIKE>(ctx, ket, bras, nbras, n, bit, gen, udag, apply_udag, out_dev, s);
+    if (gk == G_Y && ub == B_REAL)
+        return adjoint1_launch<T, I, EMU, G_Y, B_REAL>(ctx, ket, bras, nbras, n, bit, gen, udag, apply_udag, out_dev, s);
+    if (gk == G_Z && ub == B_DIAG)
+        return adjoint1_launch<T, I, EMU, G_Z, B_DIAG>(ctx, ket, bras, nbras, n, bit, gen, udag, apply_udag, out_dev, s);
+    if (gk == G_P1 && ub == B_DIAG)
+        return adjoint1_launch<T, I, EMU, G_P1, B_DIAG>(ctx, ket, bras, nbras, n, bit, gen, udag, apply_udag, out_dev, s);
+    return adjoint1_launch<T, I, EMU, -1, -1>(ctx, ket, bras, nbras, n, bit, gen, udag, apply_udag, out_dev, s);
+}
+
+template <class T, class I, bool EMU, int GK, int UB>
+static lgpu_status_t adjoint1_launch(lgpu_context_t ctx, void *ket, void *const *bras, uint32_t nbras, uint32_t n,
+                                     int bit, const double *gen, const double *udag, int apply_udag, double *out_dev,
+                                     cudaStream_t s) {
+    Adj1Body<T, I, EMU, GK, UB> b{};
     b.holes = make_holes(std::vector<int>{bit});
     b.tbit = I(I(1) << bit);
     b.gk = gen ? gen_kind(gen) : G_NONE;
@@ -329,36 +362,39 @@ template <class T> __device__ __forceinline__ const T *op_g(const SweepOp &o) {
     else return o.g;
 }
 
+// One 1-target body over lambda and the bra, under (ucm, ucv); the body is a
+// template parameter so that no per-pair switch is if-converted.
+template <class T, int BODY, bool EMU>
+__device__ __forceinline__ void sweep_pairs(cplx_t<T> *lam, cplx_t<T> *bra, int E, const SweepOp &o, const T *m) {
+    using C = cplx_t<T>;
+    const uint32_t holes = o.ucm | (1u << o.ut);
+    const int nfree = E >> __popc(holes);
+    PairWalk w(holes, threadIdx.x, kSweepThreads);
+    for (int f = threadIdx.x; f < nfree; f += kSweepThreads) {
+        const int e0 = int(w.x | o.ucv), e1 = e0 | (1 << o.ut);
+        w.step();
+        C l0 = lam[e0], l1 = lam[e1], b0 = bra[e0], b1 = bra[e1];
+        body1_sel<T, BODY, EMU>(m, o.uk, l0, l1);
+        body1_sel<T, BODY, EMU>(m, o.uk, b0, b1);
+        lam[e0] = l0;
+        lam[e1] = l1;
+        bra[e0] = b0;
+        bra[e1] = b1;
+    }
+}
+
 template <class T, bool EMU>
 __device__ __forceinline__ void sweep_udag(cplx_t<T> *lam, cplx_t<T> *bra, int E, const SweepOp &o) {
     using C = cplx_t<T>;
     const T *m = op_u<T>(o);
     if (o.ukind == U_ONE) {
-        const uint32_t holes = o.ucm | (1u << o.ut);
-        const int nfree = E >> __popc(holes);
-        PairWalk w(holes, threadIdx.x, kSweepThreads);
-        for (int f = threadIdx.x; f < nfree; f += kSweepThreads) {
-            const int e0 = int(w.x | o.ucv), e1 = e0 | (1 << o.ut);
-            w.step();
-            C l0 = lam[e0], l1 = lam[e1], b0 = bra[e0], b1 = bra[e1];
-            switch (o.ubody) {
-            case B_DIAG: body1_sel<T, B_DIAG, EMU>(m, o.uk, l0, l1); body1_sel<T, B_DIAG, EMU>(m, o.uk, b0, b1); break;
-            case B_PERM: body1_sel<T, B_PERM, EMU>(m, o.uk, l0, l1); body1_sel<T, B_PERM, EMU>(m, o.uk, b0, b1); break;
-            case B_ANTIDIAG:
-                body1_sel<T, B_ANTIDIAG, EMU>(m, o.uk, l0, l1);
-                body1_sel<T, B_ANTIDIAG, EMU>(m, o.uk, b0, b1);
-                break;
-            case B_REAL: body1_sel<T, B_REAL, EMU>(m, o.uk, l0, l1); body1_sel<T, B_REAL, EMU>(m, o.uk, b0, b1); break;
-            case B_RXLIKE:
-                body1_sel<T, B_RXLIKE, EMU>(m, o.uk, l0, l1);
-                body1_sel<T, B_RXLIKE, EMU>(m, o.uk, b0, b1);
-                break;
-            default: body1_sel<T, B_DENSE, EMU>(m, o.uk, l0, l1); body1_sel<T, B_DENSE, EMU>(m, o.uk, b0, b1); break;
-            }
-            lam[e0] = l0;
-            lam[e1] = l1;
-            bra[e0] = b0;
-            bra[e1] = b1;
+        switch (o.ubody) {
+        case B_DIAG: sweep_pairs<T, B_DIAG, EMU>(lam, bra, E, o, m); break;
+        case B_PERM: sweep_pairs<T, B_PERM, EMU>(lam, bra, E, o, m); break;
+        case B_ANTIDIAG: sweep_pairs<T, B_ANTIDIAG, EMU>(lam, bra, E, o, m); break;
+        case B_REAL: sweep_pairs<T, B_REAL, EMU>(lam, bra, E, o, m); break;
+        case B_RXLIKE: sweep_pairs<T, B_RXLIKE, EMU>(lam, bra, E, o, m); break;
+        default: sweep_pairs<T, B_DENSE, EMU>(lam, bra, E, o, m); break;
         }
     } else if (o.ukind == U_DENSE4) {
         const int qa = o.ut, qb = o.uq2;
@@ -389,6 +425,40 @@ __device__ __forceinline__ void sweep_udag(cplx_t<T> *lam, cplx_t<T> *bra, int E
             }
         }
     }
+}
+
+// Im <bra| G |lam> over one generator kind (compile time), under (gcm, gcv).
+template <class T, int GKIND>
+__device__ __forceinline__ double sweep_gen1(const cplx_t<T> *lam, const cplx_t<T> *bra, int E, const SweepOp &o,
+                                             const T *g) {
+    using C = cplx_t<T>;
+    double acc = 0.0;
+    const uint32_t holes = o.gcm | (1u << o.gt);
+    const int nfree = E >> __popc(holes);
+    PairWalk w(holes, threadIdx.x, kSweepThreads);
+    for (int f = threadIdx.x; f < nfree; f += kSweepThreads) {
+        const int e0 = int(w.x | o.gcv), e1 = e0 | (1 << o.gt);
+        w.step();
+        const C k0 = lam[e0], k1 = lam[e1], b0 = bra[e0], b1 = bra[e1];
+        T v;
+        if constexpr (GKIND == G_Z) {
+            v = (b0.x * k0.y - b0.y * k0.x) - (b1.x * k1.y - b1.y * k1.x);
+        } else if constexpr (GKIND == G_X) {
+            v = (b0.x * k1.y - b0.y * k1.x) + (b1.x * k0.y - b1.y * k0.x);
+        } else if constexpr (GKIND == G_Y) {
+            v = (b1.x * k0.x + b1.y * k0.y) - (b0.x * k1.x + b0.y * k1.y);
+        } else if constexpr (GKIND == G_P1) {
+            v = b1.x * k1.y - b1.y * k1.x;
+        } else {
+            const T y0r = g[0] * k0.x - g[1] * k0.y + g[2] * k1.x - g[3] * k1.y;
+            const T y0i = g[0] * k0.y + g[1] * k0.x + g[2] * k1.y + g[3] * k1.x;
+            const T y1r = g[4] * k0.x - g[5] * k0.y + g[6] * k1.x - g[7] * k1.y;
+            const T y1i = g[4] * k0.y + g[5] * k0.x + g[6] * k1.y + g[7] * k1.x;
+            v = (b0.x * y0i - b0.y * y0r) + (b1.x * y1i - b1.y * y1r);
+        }
+        acc += double(v);
+    }
+    return acc;
 }
 
 // Im <bra| G |lam>, this thread's share (summed over the CTA by the caller).
@@ -423,30 +493,13 @@ __device__ __forceinline__ double sweep_gen(const cplx_t<T> *lam, const cplx_t<T
         }
         return acc;
     }
-    const uint32_t holes = o.gcm | (1u << o.gt);
-    const int nfree = E >> __popc(holes);
-    PairWalk w(holes, threadIdx.x, kSweepThreads);
-    for (int f = threadIdx.x; f < nfree; f += kSweepThreads) {
-        const int e0 = int(w.x | o.gcv), e1 = e0 | (1 << o.gt);
-        w.step();
-        const C k0 = lam[e0], k1 = lam[e1], b0 = bra[e0], b1 = bra[e1];
-        T v;
-        switch (o.gkind) {
-        case G_Z: v = (b0.x * k0.y - b0.y * k0.x) - (b1.x * k1.y - b1.y * k1.x); break;
-        case G_X: v = (b0.x * k1.y - b0.y * k1.x) + (b1.x * k0.y - b1.y * k0.x); break;
-        case G_Y: v = (b1.x * k0.x + b1.y * k0.y) - (b0.x * k1.x + b0.y * k1.y); break;
-        case G_P1: v = b1.x * k1.y - b1.y * k1.x; break;
-        default: {
-            const T y0r = g[0] * k0.x - g[1] * k0.y + g[2] * k1.x - g[3] * k1.y;
-            const T y0i = g[0] * k0.y + g[1] * k0.x + g[2] * k1.y + g[3] * k1.x;
-            const T y1r = g[4] * k0.x - g[5] * k0.y + g[6] * k1.x - g[7] * k1.y;
-            const T y1i = g[4] * k0.y + g[5] * k0.x + g[6] * k1.y + g[7] * k1.x;
-            v = (b0.x * y0i - b0.y * y0r) + (b1.x * y1i - b1.y * y1r);
-        }
-        }
-        acc += double(v);
+    switch (o.gkind) {
+    case G_Z: return sweep_gen1<T, G_Z>(lam, bra, E, o, g);
+    case G_X: return sweep_gen1<T, G_X>(lam, bra, E, o, g);
+    case G_Y: return sweep_gen1<T, G_Y>(lam, bra, E, o, g);
+    case G_P1: return sweep_gen1<T, G_P1>(lam, bra, E, o, g);
+    default: return sweep_gen1<T, G_DENSE>(lam, bra, E, o, g);
     }
-    return acc;
 }
 
 template <class T, bool EMU>

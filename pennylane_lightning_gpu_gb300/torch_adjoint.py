@@ -26,6 +26,9 @@ class AdjointExpval(torch.autograd.Function):
         ctx.device = device
         ctx.tape = tape
         ctx.nparams = p.size
+        # device copy of the final state: the backward sweep starts from it
+        # instead of applying the circuit again
+        ctx.final = type(device._gpu_state)(device._gpu_state)
         ctx.save_for_backward(params)
         return torch.as_tensor(res, dtype=params.dtype, device=params.device)
 
@@ -33,7 +36,10 @@ class AdjointExpval(torch.autograd.Function):
     def backward(ctx, grad_out):
         (params,) = ctx.saved_tensors
         dy = grad_out.detach().to("cpu", torch.float64).numpy().reshape(-1)
-        vjp = np.asarray(ctx.device.vjp(ctx.tape.measurements, dy)(ctx.tape), dtype=np.float64)
+        ctx.device._gpu_state.copyFrom(ctx.final)
+        ctx.final = None
+        vjp = np.asarray(ctx.device.vjp(ctx.tape.measurements, dy, use_device_state=True)(ctx.tape),
+                         dtype=np.float64)
         if vjp.size != ctx.nparams:
             raise RuntimeError("the template must use each parameter exactly once, in order")
         return torch.as_tensor(vjp, dtype=params.dtype, device=params.device), None, None, None
