@@ -172,17 +172,17 @@ __device__ __forceinline__ void reg_gate_lt(cplx_t<T> (&a)[1 << R], int lt, cons
     }
 }
 
-// Register groups run two bodies only: permutations (X, CNOT) and dense.  The
-// host maps every other body of a grouped gate to dense: a short switch over
-// many small bodies inside the slot loop would be if-converted, issuing every
-// body for every gate.
 template <class T, int R, bool EMU>
 __device__ __forceinline__ void reg_gate_any(cplx_t<T> (&a)[1 << R], int body, int lt, const T *m, const KConst *k,
                                              uint32_t lcm, uint32_t lcv) {
-    if (body == B_PERM)
-        reg_gate_lt<T, R, B_PERM, EMU>(a, lt, m, k, lcm, lcv);
-    else
-        reg_gate_lt<T, R, B_DENSE, false>(a, lt, m, k, lcm, lcv);
+    switch (body) {
+    case B_DIAG: reg_gate_lt<T, R, B_DIAG, EMU>(a, lt, m, k, lcm, lcv); break;
+    case B_PERM: reg_gate_lt<T, R, B_PERM, EMU>(a, lt, m, k, lcm, lcv); break;
+    case B_ANTIDIAG: reg_gate_lt<T, R, B_ANTIDIAG, EMU>(a, lt, m, k, lcm, lcv); break;
+    case B_REAL: reg_gate_lt<T, R, B_REAL, EMU>(a, lt, m, k, lcm, lcv); break;
+    case B_RXLIKE: reg_gate_lt<T, R, B_RXLIKE, EMU>(a, lt, m, k, lcm, lcv); break;
+    default: reg_gate_lt<T, R, B_DENSE, false>(a, lt, m, k, lcm, lcv); break;
+    }
 }
 
 // Host: structured body of a 2x2 matrix (re/im interleaved, row-major) and

@@ -1072,7 +1072,6 @@ static int group_fused_gates(FGate *gates, int cnt, int k, int R, FGroup *groups
             }
         for (int t = i; t < j; t++) {
             FGate &g = gates[t];
-            if (g.body != B_PERM) g.body = B_DENSE;  // register groups run permutation or dense bodies
             g.lt = uint8_t(loc[g.q0]);
             g.lcm = 0;
             g.lcv = 0;

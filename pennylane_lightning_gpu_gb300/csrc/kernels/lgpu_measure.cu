@@ -255,7 +255,8 @@ __device__ __forceinline__ void wht_cp_async(void *smem_dst, const void *gsrc, i
 // copies, after cp.async.wait_group).
 constexpr int kDirectWords = 3;
 
-template <class T, class I, bool DIRECT>
+// NEED (1 real, 2 imaginary, 3 both) selects the products at compile time.
+template <class T, class I, bool DIRECT, int NEED>
 __global__ void __launch_bounds__(kReduceBlock, 2)
     pauli_wht_kernel(const PauliWhtParams<T, I> p, double2 *partials, unsigned *counter, double2 *out) {
     using C = cplx_t<T>;
@@ -299,8 +300,10 @@ __global__ void __launch_bounds__(kReduceBlock, 2)
 #pragma unroll
             for (int j = 0; j < 8; j++) {
                 const C a = *at(st, 0, j), b = *at(st, 1, j);
-                wr[j] = p.need_re ? a.x * b.x + a.y * b.y : T(0);
-                wi[j] = p.need_im ? a.x * b.y - a.y * b.x : T(0);
+                if constexpr ((NEED & 1) != 0) wr[j] = a.x * b.x + a.y * b.y;
+                else wr[j] = T(0);
+                if constexpr ((NEED & 2) != 0) wi[j] = a.x * b.y - a.y * b.x;
+                else wi[j] = T(0);
             }
         } else {
 #pragma unroll
@@ -311,8 +314,8 @@ __global__ void __launch_bounds__(kReduceBlock, 2)
             }
         }
         if constexpr (!DIRECT) {
-            if (p.need_re) wht8(wr);
-            if (p.need_im) wht8(wi);
+            if constexpr ((NEED & 1) != 0) wht8(wr);
+            if constexpr ((NEED & 2) != 0) wht8(wi);
         }
 #pragma unroll
         for (int t = 0; t < (DIRECT ? kDirectWords : kWhtWords); t++) {
@@ -378,11 +381,28 @@ __global__ void __launch_bounds__(kReduceBlock, 2)
 
 template <class T> constexpr size_t wht_smem_bytes() { return size_t(2) * 2 * 8 * kReduceBlock * sizeof(cplx_t<T>); }
 
-template <class T, class I> static lgpu_status_t wht_smem_attr() {
-    static std::atomic<size_t> attr_w[64], attr_d[64];
-    LGPU_TRY(ensure_smem(reinterpret_cast<const void *>(pauli_wht_kernel<T, I, false>), wht_smem_bytes<T>(), attr_w));
-    LGPU_TRY(ensure_smem(reinterpret_cast<const void *>(pauli_wht_kernel<T, I, true>), wht_smem_bytes<T>(), attr_d));
+// Launch one pass with the compile-time product selection (opts the
+// instantiation in to its shared memory first).
+template <class T, class I, bool DIRECT, int NEED>
+static lgpu_status_t wht_launch(const PauliWhtParams<T, I> &b, unsigned g, double2 *partials, unsigned *counter,
+                                double2 *out, cudaStream_t s) {
+    static std::atomic<size_t> attr[64];
+    LGPU_TRY(ensure_smem(reinterpret_cast<const void *>(pauli_wht_kernel<T, I, DIRECT, NEED>), wht_smem_bytes<T>(),
+                         attr));
+    pauli_wht_kernel<T, I, DIRECT, NEED><<<g, kReduceBlock, wht_smem_bytes<T>(), s>>>(b, partials, counter, out);
+    LGPU_CHECK_LAUNCH();
     return LGPU_OK;
+}
+
+template <class T, class I, bool DIRECT>
+static lgpu_status_t wht_dispatch(const PauliWhtParams<T, I> &b, unsigned g, double2 *partials, unsigned *counter,
+                                  double2 *out, cudaStream_t s) {
+    const int need = (b.need_re ? 1 : 0) | (b.need_im ? 2 : 0);
+    switch (need) {
+    case 2: return wht_launch<T, I, DIRECT, 2>(b, g, partials, counter, out, s);
+    case 3: return wht_launch<T, I, DIRECT, 3>(b, g, partials, counter, out, s);
+    default: return wht_launch<T, I, DIRECT, 1>(b, g, partials, counter, out, s);
+    }
 }
 
 template <class T, class I>
@@ -424,7 +444,6 @@ static lgpu_status_t pauli_words_t(lgpu_context_t ctx, const void *sv, uint32_t 
         auto *partials = reinterpret_cast<double2 *>(static_cast<char *>(p) + 256);
         auto *results = reinterpret_cast<double2 *>(static_cast<char *>(p) + 256 + pbytes);
         std::vector<double> coef(wp.size() * kWhtWords, 0.0);
-        LGPU_TRY((wht_smem_attr<T, I>()));
         for (size_t pi = 0; pi < wp.size(); pi++) {
             PauliWhtParams<T, I> b{};
             b.sv = static_cast<const cplx_t<T> *>(sv);
@@ -459,12 +478,9 @@ static lgpu_status_t pauli_words_t(lgpu_context_t ctx, const void *sv, uint32_t 
                 coef[pi * kWhtWords + size_t(t)] = !wp[pi].flip ? 1.0 : (kneg ? -2.0 : 2.0);
             }
             if (b.direct)
-                pauli_wht_kernel<T, I, true><<<g, kReduceBlock, wht_smem_bytes<T>(), s>>>(b, partials, counter,
-                                                                                       results + pi * kWhtWords);
+                LGPU_TRY((wht_dispatch<T, I, true>(b, g, partials, counter, results + pi * kWhtWords, s)));
             else
-                pauli_wht_kernel<T, I, false><<<g, kReduceBlock, wht_smem_bytes<T>(), s>>>(b, partials, counter,
-                                                                                        results + pi * kWhtWords);
-            LGPU_CHECK_LAUNCH();
+                LGPU_TRY((wht_dispatch<T, I, false>(b, g, partials, counter, results + pi * kWhtWords, s)));
         }
         std::vector<double2> host(wp.size() * kWhtWords);
         if (!wp.empty()) {
