@@ -103,6 +103,18 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def headline_config(n, kernel_family=None, f64_mode=None):
+    """The `config` object of the headline line (both arms)."""
+    cfg = {"workload": "dense 1-qubit gates (H and RX) on each target of a %d-qubit complex128 state" % n,
+           "qubits": n, "state_bytes": (1 << n) * 16, "gates_per_step": 2 * n,
+           "l2": "state (%.0f GiB) larger than L2 (129 MB): no flush needed" % ((1 << n) * 16 / 2**30)}
+    if f64_mode is not None:
+        cfg["f64_mode"] = f64_mode
+    if kernel_family is not None:
+        cfg["kernel_family"] = kernel_family
+    return cfg
+
+
 def _gate_list(n):
     return [("Hadamard", w) for w in range(n)] + [("RX", w) for w in range(n)]
 
@@ -142,8 +154,7 @@ def run_reference(args):
     line = {"metric": "gate HBM GB/s at 28q", "value": v, "unit": "GB/s", "impl": "reference", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * wall / max(1, args.steps), 3),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128 (f64)",
-            "data": "synthetic", "config": {"workload": "dense 1-qubit gates on a %d-qubit complex128 state" % n,
-                                            "qubits": n, "l2": "state larger than L2"},
+            "data": "synthetic", "config": headline_config(n),
             "cpu_baseline": {"value": v, "unit": "GB/s", "cores": os.cpu_count(), "kind": "port",
                              "sample": "2 dense 1-qubit gates per step on a %d-qubit complex128 state" % n},
             "e2e": {"value": v, "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -297,11 +308,9 @@ def run_ours(args):
         "metric": "gate HBM GB/s at 28q", "value": round(value, 1), "unit": "GB/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_per_step, 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "c128 (f64)", "data": "synthetic",
-        "config": {"workload": "dense 1-qubit gates (H and RX) on each target of a 28-qubit complex128 state",
-                   "qubits": n, "state_bytes": S, "gates_per_step": len(gates),
-                   "f64_mode": "fp64 fma + integer-pipe multiply" if default_mode == 1 else "native fp64",
-                   "kernel_family": "bulk-copy pipelined tiles" if m.get_stream_mode() == 1 else "grid-stride",
-                   "l2": "state (4 GiB) larger than L2 (129 MB): no flush needed"},
+        "config": headline_config(
+            n, kernel_family="bulk-copy pipelined tiles" if m.get_stream_mode() == 1 else "grid-stride",
+            f64_mode="fp64 fma + integer-pipe multiply" if default_mode == 1 else "native fp64"),
         "e2e": {"value": round(e2e_value, 1), "unit": "GB/s", "h2d_bytes_per_step": 8 * n,
                 "d2h_bytes_per_step": 16},
         "gpu_launches": len(gates) * args.steps * world,
