@@ -87,6 +87,13 @@ int lgpu_get_stream_mode(void);
  * counterpart in the reference. */
 lgpu_status_t lgpu_device_error(int *code, int reset);
 
+/* Diagnostic of the bounded waits: one CTA waits on an mbarrier that expects
+ * bytes no copy will deliver, with the streaming kernels' give-up logic and a
+ * limit of `spin_limit` polls (at most 2^24); the call synchronises `stream`
+ * and leaves the time-out recorded for lgpu_device_error.  No counterpart in
+ * the reference. */
+lgpu_status_t lgpu_selftest_bounded_wait(uint32_t spin_limit, lgpu_stream_t stream);
+
 /* ---- device and memory (DataBuffer.hpp:31-218, cuda_helpers.hpp:796-837,
  *      Bindings.cpp:1736-1748; the C++ layer needs no CUDA runtime of its own) */
 lgpu_status_t lgpu_device_count(int *count);

@@ -102,6 +102,30 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
         : "memory");
     return ok != 0;
 }
+// Self-test of the bounded waits: one CTA arms an mbarrier with a transaction
+// count that no copy will deliver (a flag nothing sets) and waits with the
+// streaming kernels' bounded spin; it gives up after `spin_limit` polls and
+// records the time-out in g_lgpu_device_error, as they do.
+__global__ void wait_selftest_kernel(uint32_t spin_limit) {
+    __shared__ __align__(8) uint64_t bar;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) mbar_expect_tx(&bar, 16);  // 16 bytes that never arrive
+    __syncthreads();
+    uint32_t spins = 0;
+    bool timed_out = false;
+    while (!mbar_try_wait(&bar, 0)) {
+        if (++spins > spin_limit) {
+            timed_out = true;
+            break;
+        }
+    }
+    if (__syncthreads_or(timed_out) && threadIdx.x == 0) atomicOr(&g_lgpu_device_error, 1u);
+}
+
 __device__ __forceinline__ void bulk_load(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
     asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
                      smem_u32(dst)),
@@ -1200,6 +1224,15 @@ static lgpu_status_t fused_t(cplx_t<T> *sv, uint32_t n, const std::vector<int> &
 using namespace lgpu;
 
 extern "C" {
+
+lgpu_status_t lgpu_selftest_bounded_wait(uint32_t spin_limit, lgpu_stream_t stream) {
+    if (spin_limit == 0 || spin_limit > kWaitLimit) return fail(LGPU_ERR_INVALID_ARG, "spin limit out of range");
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    wait_selftest_kernel<<<1, 64, 0, s>>>(spin_limit);
+    LGPU_CHECK_LAUNCH();
+    LGPU_CUDA_TRY(cudaStreamSynchronize(s));
+    return LGPU_OK;
+}
 
 lgpu_status_t lgpu_device_error(int *code, int reset) {
     if (!code) return fail(LGPU_ERR_INVALID_ARG, "code is null");

@@ -114,6 +114,20 @@ class CircuitServer:
             self._waiting.append(req)
             self._lock.notify_all()
 
+    def cancel(self, rid):
+        """Withdraw a request that has not started: it finishes at once with
+        error "cancelled".  Returns False for a running or finished request."""
+        with self._lock:
+            for r in self._waiting:
+                if r.rid == rid:
+                    self._waiting.remove(r)
+                    r.error = "cancelled"
+                    r.finish = time.perf_counter()
+                    self._done.append(r)
+                    self._lock.notify_all()
+                    return True
+        return False
+
     def drain(self, timeout=None):
         """Wait until everything submitted so far has finished."""
         t_end = None if timeout is None else time.perf_counter() + timeout
