@@ -32,16 +32,17 @@ def _serialize_named_ob(o, wires_map, use_csingle):
     return getattr(native(), "NamedObsGPU_" + _suffix(use_csingle))(o.name, wires)
 
 
-def _serialize_tensor_ob(ob, wires_map, use_csingle):
+def _serialize_tensor_ob(ob, wires_map, use_csingle, allow_hermitian=False):
     return getattr(native(), "TensorProdObsGPU_" + _suffix(use_csingle))(
-        [_serialize_ob(o, wires_map, use_csingle) for o in ob.obs])
+        [_serialize_ob(o, wires_map, use_csingle, allow_hermitian=allow_hermitian) for o in ob.obs])
 
 
-def _serialize_hamiltonian(ob, wires_map, use_csingle, split_terms=True):
+def _serialize_hamiltonian(ob, wires_map, use_csingle, split_terms=True, allow_hermitian=False):
     cls = getattr(native(), "HamiltonianGPU_" + _suffix(use_csingle))
     coeffs = np.array(ob.coeffs).astype(_rtype(use_csingle))
     # a term that is itself a Hamiltonian (a vjp's sum_k dy_k H_k) stays one observable
-    terms = [_serialize_ob(t, wires_map, use_csingle, split_terms=False) for t in ob.ops]
+    terms = [_serialize_ob(t, wires_map, use_csingle, split_terms=False, allow_hermitian=allow_hermitian)
+             for t in ob.ops]
     if split_terms:
         return [cls(np.array([c], _rtype(use_csingle)), [t]) for c, t in zip(coeffs, terms)]
     return cls(coeffs, terms)
@@ -62,9 +63,9 @@ def _serialize_hermitian(ob, wires_map, use_csingle):
 
 def _serialize_ob(ob, wires_map, use_csingle, split_terms=True, allow_hermitian=False):
     if isinstance(ob, Tensor):
-        return _serialize_tensor_ob(ob, wires_map, use_csingle)
+        return _serialize_tensor_ob(ob, wires_map, use_csingle, allow_hermitian)
     if isinstance(ob, Hamiltonian):
-        return _serialize_hamiltonian(ob, wires_map, use_csingle, split_terms)
+        return _serialize_hamiltonian(ob, wires_map, use_csingle, split_terms, allow_hermitian)
     if isinstance(ob, SparseHamiltonian):
         return _serialize_sparsehamiltonian(ob, wires_map, use_csingle)
     if ob.name in _PAULI_NAMES:

@@ -49,7 +49,7 @@ class LightningGPU:
                    "SparseHamiltonian"}
 
     def __init__(self, wires, *, c_dtype=np.complex128, shots=None, batch_obs=False, mpi=False, sync=False,
-                 seed=None, fusion=True):
+                 seed=None, fusion=True, adjoint_hermitian=False):
         if mpi:
             raise DeviceError("mpi=True is not supported: the GB300 engine runs one state on one GPU")
         if c_dtype not in (np.complex64, np.complex128):
@@ -70,6 +70,9 @@ class LightningGPU:
         if seed is not None:
             self._gpu_state.setSeed(int(seed))
         self._samples = None
+        # The reference refuses Hermitian observables in adjoint differentiation
+        # (lightning_gpu.py:606-618); the engine supports them when asked.
+        self._adjoint_hermitian = bool(adjoint_hermitian)
 
     # ------------------------------------------------------------------ state
     def reset(self):
@@ -280,7 +283,7 @@ class LightningGPU:
 
     # ---------------------------------------------------------------- adjoint
     @staticmethod
-    def _check_adjdiff_supported_measurements(measurements):
+    def _check_adjdiff_supported_measurements(measurements, allow_hermitian=False):
         if len(measurements) == 0:
             return None
         if len(measurements) == 1 and measurements[0].return_type == "state":
@@ -294,7 +297,7 @@ class LightningGPU:
                 if isinstance(o, Q.Projector):
                     raise QuantumFunctionError("Adjoint differentiation method does not support the Projector "
                                                "observable")
-                if o.name == "Hermitian":
+                if o.name == "Hermitian" and not allow_hermitian:
                     raise QuantumFunctionError("LightningGPU adjoint differentiation method does not currently "
                                                "support the Hermitian observable")
         return "expval"
@@ -316,7 +319,7 @@ class LightningGPU:
         if self.shots is not None:
             warnings.warn("Requested adjoint differentiation to be computed with finite shots. The derivative is "
                           "always exact when using the adjoint differentiation method.", UserWarning)
-        self._check_adjdiff_supported_measurements(tape.measurements)
+        self._check_adjdiff_supported_measurements(tape.measurements, self._adjoint_hermitian)
         if len(tape.trainable_params) == 0:
             return np.array(0)
         self._check_adjdiff_supported_operations(tape.operations)
@@ -328,7 +331,8 @@ class LightningGPU:
         suf = "C64" if self.use_csingle else "C128"
         adj = getattr(self._mod, "AdjointJacobianGPU_" + suf)()
         obs_serialized, obs_offsets = _serialize_observables(tape, self.wire_map, self.use_csingle,
-                                                             split_terms=split_terms)
+                                                             split_terms=split_terms,
+                                                             allow_hermitian=self._adjoint_hermitian)
         ops_serialized, use_sp = _serialize_ops(tape, self.wire_map, self.use_csingle)
         ops_serialized = adj.create_ops_list(*ops_serialized)
         trainable_params = sorted(tape.trainable_params)
@@ -351,7 +355,7 @@ class LightningGPU:
         if self.shots is not None:
             warnings.warn("Requested adjoint differentiation to be computed with finite shots. The derivative is "
                           "always exact when using the adjoint differentiation method.", UserWarning)
-        rtype = self._check_adjdiff_supported_measurements(measurements)
+        rtype = self._check_adjdiff_supported_measurements(measurements, self._adjoint_hermitian)
         dy = np.asarray(dy)
         if np.allclose(dy, 0) or rtype is None:
             return lambda tape: np.zeros(len(tape.trainable_params))

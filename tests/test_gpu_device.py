@@ -168,6 +168,85 @@ def test_adjoint_rejects_unsupported():
         dev.adjoint_jacobian(tape)
 
 
+def _central_differences(dev, ops, measurements, h=1e-4):
+    params = [p for o in ops for p in o.parameters]
+
+    def f(ps):
+        k, new = 0, []
+        for o in ops:
+            m = len(o.parameters)
+            base = Q.Operation(o.name, o.wires, ps[k:k + m], o._matrix)
+            new.append(base.adjoint() if isinstance(o, Q.Adjoint) else base)
+            k += m
+        return np.array(dev.execute(Q.QuantumTape(new, measurements)))
+
+    cols = []
+    for i in range(len(params)):
+        e = np.zeros(len(params))
+        e[i] = h
+        cols.append((f(np.array(params) + e) - f(np.array(params) - e)) / (2 * h))
+    return np.stack(cols, axis=1)
+
+
+@pytest.mark.parametrize("dtype,tol", [(np.complex128, 1e-10), (np.complex64, 1e-5)])
+def test_adjoint_hermitian_opt_in(oracle, dtype, tol):
+    """With adjoint_hermitian=True the adjoint Jacobian of Hermitian
+    observables (alone, inside a tensor product and as a Hamiltonian term)
+    matches the oracle's adjoint; the default keeps the reference's refusal."""
+    from pennylane_lightning_gpu_gb300.lightning_gpu import QuantumFunctionError
+
+    rng = np.random.default_rng(21)
+    n = 5
+    ops = [Q.op("RY", w, rng.uniform(0, 6)) for w in range(n)]
+    ops += [Q.op("CNOT", [0, 1]), Q.op("CRX", [2, 4], 0.6), Q.op("RZ", 3, -0.9), Q.op("IsingXX", [1, 3], 0.4)]
+    h2 = rng.normal(size=(4, 4)) + 1j * rng.normal(size=(4, 4))
+    h2 = h2 + h2.conj().T
+    h1 = rng.normal(size=(2, 2)) + 1j * rng.normal(size=(2, 2))
+    h1 = h1 + h1.conj().T
+    H = Q.Hamiltonian([0.5, -0.7], [Q.Hermitian(h1, [2]), Q.PauliX(0) @ Q.PauliZ(4)])
+    meas = [Q.expval(Q.Hermitian(h2, [3, 1])), Q.expval(Q.Hermitian(h1, [0]) @ Q.PauliY(4)), Q.expval(H)]
+    tape = Q.QuantumTape(ops, meas)
+    with pytest.raises(QuantumFunctionError):
+        _dev(n, dtype).adjoint_jacobian(tape)
+    dev = _dev(n, dtype, adjoint_hermitian=True)
+    jac = dev.adjoint_jacobian(tape)
+    final = oracle.run(n, _oracle_ops(ops))
+    obs = [(False, [(1.0, [("Hermitian", [3, 1], h2)])]),
+           (False, [(1.0, [("Hermitian", [0], h1), ("PauliY", [4], None)])]),
+           (True, [(0.5, [("Hermitian", [2], h1)]), (-0.7, [("PauliX", [0], None), ("PauliZ", [4], None)])])]
+    ntrain = sum(len(o.parameters) for o in ops)
+    ref = oracle.adjoint_jacobian(final, _oracle_ops(ops), obs, list(range(ntrain)))
+    scale = max(1.0, np.max(np.abs(ref)))
+    assert np.max(np.abs(jac - ref)) < tol * 10 * scale
+    # the vjp takes the same opt-in
+    dy = np.array([0.3, -1.1, 0.8])
+    v = dev.vjp(meas, dy)(tape)
+    assert np.max(np.abs(v - dy @ ref)) < tol * 30 * scale
+
+
+def test_adjoint_sparse_hamiltonian_vs_central_differences():
+    """A SparseHamiltonian observable (CSR over all wires) in the adjoint
+    Jacobian agrees with central differences of the device's own expectation
+    (h = 1e-4, 1e-7)."""
+    import scipy.sparse as sp
+
+    rng = np.random.default_rng(22)
+    n = 6
+    dim = 1 << n
+    a = sp.random(dim, dim, density=0.05, random_state=np.random.RandomState(3), format="csr",
+                  dtype=np.float64)
+    a = a + 1j * sp.random(dim, dim, density=0.05, random_state=np.random.RandomState(4), format="csr")
+    herm = (a + a.conj().T).tocsr()
+    ops = [Q.op("RX", w, rng.uniform(0, 6)) for w in range(n)]
+    ops += [Q.op("CNOT", [0, 3]), Q.op("RY", 2, 0.3), Q.op("IsingZZ", [4, 5], 1.1), Q.op("CRZ", [1, 2], -0.5)]
+    meas = [Q.expval(Q.SparseHamiltonian(herm, list(range(n)))), Q.expval(Q.PauliZ(2))]
+    tape = Q.QuantumTape(ops, meas)
+    dev = _dev(n)
+    jac = dev.adjoint_jacobian(tape)
+    fd = _central_differences(dev, ops, meas)
+    assert np.max(np.abs(jac - fd)) < 1e-7
+
+
 def test_mpi_rejected():
     from pennylane_lightning_gpu_gb300.lightning_gpu import DeviceError
 
