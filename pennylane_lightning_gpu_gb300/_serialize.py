@@ -2,7 +2,9 @@
 pennylane_lightning_gpu/_serialize.py:142-336): observables become the
 native ``*ObsGPU_*`` objects, operations become the (names, params, wires,
 inverses, matrices) lists of ``OpsStructGPU``; ``Rot`` is expanded into
-RZ RY RZ; Hamiltonians are split into one-term Hamiltonians (with offsets)
+RZ RY RZ as the reference does (``_serialize.py:311-312``), and, beyond it,
+``CRot`` into CRZ CRY CRZ and inverted ``Rot``/``CRot`` into the inverted
+factors in reverse order; Hamiltonians are split into one-term Hamiltonians (with offsets)
 when ``split_terms`` is set, as the reference does for observable batching.
 """
 import numpy as np
@@ -98,10 +100,33 @@ _BOUND = {"Identity", "PauliX", "PauliY", "PauliZ", "Hadamard", "S", "T", "RX", 
 
 
 def _expand_rot(o):
+    """Rot(phi, theta, omega) = RZ(omega) RY(theta) RZ(phi), and CRot the same
+    product of CRZ/CRY on its (control, target) pair; an inverted one is the
+    inverted factors in reverse order, so its parameters come out as
+    (omega, theta, phi)."""
     from .ops import op
 
     phi, theta, omega = o.parameters
-    return [op("RZ", o.wires, phi), op("RY", o.wires, theta), op("RZ", o.wires, omega)]
+    z, y = ("CRZ", "CRY") if o.name == "CRot" else ("RZ", "RY")
+    if isinstance(o, Adjoint):
+        return [op(z, o.wires, omega).adjoint(), op(y, o.wires, theta).adjoint(), op(z, o.wires, phi).adjoint()]
+    return [op(z, o.wires, phi), op(y, o.wires, theta), op(z, o.wires, omega)]
+
+
+def _expanded_param_positions(tape):
+    """pos[q] = index of tape parameter q among the serialised operations'
+    parameters. Expansion keeps the count, so pos is the identity except in
+    the blocks of inverted Rot/CRot, whose three parameters come out reversed."""
+    pos = []
+    for o in tape.operations:
+        if isinstance(o, (BasisState, StatePrep)):
+            continue
+        base = len(pos)
+        if o.name in ("Rot", "CRot") and isinstance(o, Adjoint):
+            pos.extend([base + 2, base + 1, base])
+        else:
+            pos.extend(range(base, base + len(o.parameters)))
+    return pos
 
 
 def _serialize_ops(tape, wires_map, use_csingle=False):
@@ -111,7 +136,7 @@ def _serialize_ops(tape, wires_map, use_csingle=False):
         if isinstance(o, (BasisState, StatePrep)):
             uses_stateprep = True
             continue
-        if o.name == "Rot" and not isinstance(o, Adjoint):
+        if o.name in ("Rot", "CRot"):
             op_list = _expand_rot(o)
         else:
             op_list = [o]

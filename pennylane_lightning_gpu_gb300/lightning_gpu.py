@@ -23,7 +23,7 @@ import numpy as np
 
 from . import ops as Q
 from ._native import native
-from ._serialize import _serialize_observables, _serialize_ops
+from ._serialize import _expanded_param_positions, _serialize_observables, _serialize_ops
 
 _NAME_MAP = {"PauliX": "X", "PauliY": "Y", "PauliZ": "Z", "Identity": "I"}
 
@@ -304,8 +304,10 @@ class LightningGPU:
 
     @staticmethod
     def _check_adjdiff_supported_operations(operations):
+        # Rot as in the reference (lightning_gpu.py:622-636); CRot and inverted
+        # Rot/CRot too, through their exact expansion into one-parameter gates
         for o in operations:
-            if o.num_params > 1 and o.name != "Rot":
+            if o.num_params > 1 and o.name not in ("Rot", "CRot"):
                 raise QuantumFunctionError('The %s operation is not supported using the "adjoint" '
                                            "differentiation method" % o.name)
 
@@ -343,8 +345,16 @@ class LightningGPU:
                 tp_shift.append(tp)
                 record_tp_rows.append(all_params)
             all_params += 1
-        jac = np.asarray(adj.adjoint_jacobian(self._gpu_state, obs_serialized, ops_serialized, tp_shift))
-        jac = jac.reshape(-1, len(tp_shift))
+        # inverted Rot/CRot serialise their parameters reversed: ask for the
+        # serialised positions in ascending order, then put the columns back
+        pos = _expanded_param_positions(tape)
+        mapped = [pos[t] for t in tp_shift]
+        order = np.argsort(mapped, kind="stable")
+        jac = np.asarray(adj.adjoint_jacobian(self._gpu_state, obs_serialized, ops_serialized,
+                                              [mapped[i] for i in order]))
+        jac_sorted = jac.reshape(-1, len(tp_shift))
+        jac = np.empty_like(jac_sorted)
+        jac[:, order] = jac_sorted
         jac_r = np.zeros((len(tape.observables), all_params))
         for idx in range(len(obs_offsets) - 1):
             jac_r[idx, record_tp_rows] = np.sum(jac[obs_offsets[idx]:obs_offsets[idx + 1], :], axis=0)

@@ -44,3 +44,26 @@ def test_tape_parameter_bookkeeping():
     assert tape.trainable_params == [0, 1, 2, 3]
     o, k, j = tape.get_operation(2)
     assert o.name == "Rot" and j == 1
+
+
+@pytest.mark.parametrize("name,wires", [("Rot", [1]), ("CRot", [2, 0])])
+@pytest.mark.parametrize("inverse", [False, True])
+def test_rot_expansion_is_exact(name, wires, inverse):
+    """The adjoint method's one-parameter expansion of Rot/CRot (and their
+    inverses) multiplies back to the gate, and the parameter positions it
+    reports follow the expanded order."""
+    from pennylane_lightning_gpu_gb300._serialize import _expand_rot, _expanded_param_positions
+
+    o = Q.op(name, wires, 0.3, -1.1, 2.4)
+    if inverse:
+        o = o.adjoint()
+    parts = _expand_rot(o)
+    u = np.eye(1 << len(wires), dtype=complex)
+    for p in parts:
+        u = p.matrix() @ u
+    assert np.allclose(u, o.matrix(), atol=1e-14)
+    tape = Q.QuantumTape([Q.op("RX", 0, 0.1), o, Q.op("RY", 1, 0.2)], [Q.expval(Q.PauliZ(0))])
+    pos = _expanded_param_positions(tape)
+    assert pos == ([0, 3, 2, 1, 4] if inverse else [0, 1, 2, 3, 4])
+    expanded = [pp for p in parts for pp in p.parameters]
+    assert [expanded[pos[q] - 1] for q in (1, 2, 3)] == o.parameters

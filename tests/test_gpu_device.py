@@ -224,6 +224,41 @@ def test_adjoint_hermitian_opt_in(oracle, dtype, tol):
     assert np.max(np.abs(v - dy @ ref)) < tol * 30 * scale
 
 
+@pytest.mark.parametrize("dtype,tol", [(np.complex128, 1e-10), (np.complex64, 1e-5)])
+def test_adjoint_multi_parameter_gates(oracle, dtype, tol):
+    """CRot and inverted Rot/CRot (the reference's adjoint refuses them) through
+    their one-parameter expansion: all parameters and a trainable subset that
+    splits an inverted block, against the oracle adjoint on the expanded ops
+    and (complex128) central differences."""
+    from pennylane_lightning_gpu_gb300._serialize import _expand_rot, _expanded_param_positions
+
+    rng = np.random.default_rng(23)
+    n = 4
+    ops = [Q.op("RY", w, rng.uniform(0, 6)) for w in range(n)]
+    ops += [Q.op("CRot", [0, 2], 0.4, -1.3, 0.8), Q.op("Rot", 1, 1.1, 0.2, -0.6).adjoint(),
+            Q.op("CNOT", [2, 3]), Q.op("CRot", [3, 1], -0.7, 2.1, 0.35).adjoint(), Q.op("Rot", 3, 0.5, 0.9, 1.7)]
+    meas = [Q.expval(Q.PauliZ(1)), Q.expval(Q.PauliX(2) @ Q.PauliY(3))]
+    nparams = sum(len(o.parameters) for o in ops)
+    flat = []
+    for o in ops:
+        flat.extend(_expand_rot(o) if o.name in ("Rot", "CRot") else [o])
+    final = oracle.run(n, _oracle_ops(flat))
+    obs = [(False, [(1.0, [("PauliZ", [1], None)])]),
+           (False, [(1.0, [("PauliX", [2], None), ("PauliY", [3], None)])])]
+    ref_all = oracle.adjoint_jacobian(final, _oracle_ops(flat), obs, list(range(nparams)))
+    pos = _expanded_param_positions(Q.QuantumTape(ops, meas))
+    ref = ref_all[:, pos]  # columns back in tape order
+    dev = _dev(n, dtype)
+    for trainable in (list(range(nparams)), [1, 5, 7, 9, 12, 15]):
+        tape = Q.QuantumTape(ops, meas, trainable)
+        jac = dev.adjoint_jacobian(tape)
+        assert jac.shape == (2, len(trainable))
+        assert np.max(np.abs(jac - ref[:, trainable])) < tol * 10, trainable
+    if dtype == np.complex128:
+        fd = _central_differences(dev, ops, meas)
+        assert np.max(np.abs(dev.adjoint_jacobian(Q.QuantumTape(ops, meas)) - fd)) < 1e-7
+
+
 def test_adjoint_sparse_hamiltonian_vs_central_differences():
     """A SparseHamiltonian observable (CSR over all wires) in the adjoint
     Jacobian agrees with central differences of the device's own expectation
