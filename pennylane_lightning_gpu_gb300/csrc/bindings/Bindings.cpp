@@ -283,8 +283,9 @@ template <class PrecisionT, class ParamT> void sv_class_bindings(py::module_ &m)
     // ---- extensions of this engine (not in the reference module) ----------
     cls.def("setSeed", &SV::setSeed, "Fix the seed of the sampler's std::mt19937 stream.")
         .def("clearSeed", &SV::clearSeed)
-        .def("setFusion", &SV::setFusion, py::arg("on"), py::arg("tile_bits") = 0,
-             "Enable/disable shared-memory gate fusion for multi-op apply().")
+        .def("setFusion", &SV::setFusion, py::arg("on"), py::arg("tile_bits") = 0, py::arg("min_low_bits") = 0,
+             "Enable/disable shared-memory gate fusion for multi-op apply(); optionally set the tile size and "
+             "the shortest contiguous low run of a tile (in bits).")
         .def("getFusion", &SV::getFusion)
         .def(
             "GenerateSampleIndices",

@@ -516,14 +516,23 @@ class StateVectorCudaManaged : public StateVectorCudaBase<Precision, StateVector
 
     // Fusion is on by default for multi-op calls; setFusion(false) applies
     // the ops one kernel each (the plain per-gate path).
-    void setFusion(bool on, int tile_bits = 0) {
+    // tile_bits / min_low_bits (0 = default) set the planner's tile size and
+    // the shortest contiguous low run of a tile.
+    void setFusion(bool on, int tile_bits = 0, int min_low_bits = 0) {
         fusion_ = on;
         if (tile_bits > 0) fusion_tile_bits_ = tile_bits;
+        if (min_low_bits > 0) fusion_min_low_bits_ = min_low_bits;
     }
     [[nodiscard]] bool getFusion() const { return fusion_; }
     [[nodiscard]] int fusionTileBits() const {
         if (fusion_tile_bits_ > 0) return fusion_tile_bits_;
         return 12;  // 32 KB (complex64, double-buffered) / 64 KB (complex128) tiles: three CTAs per SM
+    }
+    // Shortest contiguous low run of a tile: 2^5 amplitudes keep every
+    // segment at least 256 bytes long.
+    [[nodiscard]] int fusionMinLowBits() const {
+        if (fusion_min_low_bits_ > 0) return fusion_min_low_bits_;
+        return 5;
     }
 
     void applyDescs(std::vector<Engine::GateDesc> descs) {
@@ -544,7 +553,7 @@ class StateVectorCudaManaged : public StateVectorCudaBase<Precision, StateVector
         }
         Engine::merge_1q_runs(descs);
         const int kmax = std::min<int>(fusionTileBits(), int(nq()));
-        const auto plan = Engine::plan_fusion(descs, nq(), kmax, std::min<int>(5, kmax));
+        const auto plan = Engine::plan_fusion(descs, nq(), kmax, std::min<int>(fusionMinLowBits(), kmax));
         for (const auto &blk : plan) {
             if (blk.tile_bits.empty()) {
                 for (size_t gi : blk.gates) applyDesc(descs[gi]);
@@ -673,6 +682,7 @@ class StateVectorCudaManaged : public StateVectorCudaBase<Precision, StateVector
     std::map<std::string, std::vector<cd>> user_gate_cache_;
     bool fusion_ = true;
     int fusion_tile_bits_ = 0;
+    int fusion_min_low_bits_ = 0;
 };
 
 } // namespace Pennylane

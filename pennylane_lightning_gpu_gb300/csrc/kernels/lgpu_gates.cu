@@ -14,6 +14,8 @@
 //  * pauli_rot_kernel exp(i angle P) for Pauli words, pairwise (i, i^flip).
 //  * fused_kernel     a block of 1/2-target gates applied to shared-memory
 //                     tiles of 2^k amplitudes: one HBM pass for many gates.
+#include <cstring>
+
 #include "lgpu_bodies.cuh"
 #include "lgpu_f64emu.cuh"
 #include "lgpu_internal.cuh"
@@ -596,19 +598,23 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 __device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait0() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
 
-// Persistent CTAs, two tile buffers: while the gates run on one tile, the
-// next tile streams into the other buffer through cp.async (16-byte chunks
-// written straight into the swizzled layout); results leave with streaming
-// stores.  The tile = the low run of m state bits (contiguous segments of
-// 2^m amplitudes) times up to 2^6 segments at the high tile bits.
-template <class T, class I, bool EMU, int NT, int STAGES>
-__global__ void __launch_bounds__(NT, NT == 256 ? 3 : 1)
+// Persistent CTAs with a ring of STAGES tile buffers: while the gates run on
+// one tile, the next STAGES - 1 tiles stream in through cp.async (16-byte
+// chunks written straight into the swizzled layout); results leave with
+// streaming stores.  STAGES = 1 loads and computes in turn (several CTAs per
+// SM interleave instead).  The tile = the low run of m state bits (contiguous
+// segments of 2^m amplitudes) times up to 2^6 segments at the high tile bits.
+template <int N> __device__ __forceinline__ void cp_async_wait_n() {
+    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
+template <class T, class I, bool EMU, int NT, int STAGES, int MINB>
+__global__ void __launch_bounds__(NT, MINB)
     fused_kernel(cplx_t<T> *__restrict__ sv, const FusedParams<T, I> p) {
     using C = cplx_t<T>;
     extern __shared__ __align__(128) unsigned char smem_raw[];
     const int E = 1 << p.k;
-    C *buf0 = reinterpret_cast<C *>(smem_raw);
-    C *buf1 = STAGES == 2 ? buf0 + E : buf0;
+    C *const ring = reinterpret_cast<C *>(smem_raw);
     const int lowmask = (1 << p.m) - 1;
     // 16-byte chunks hold 2 complex64 / 1 complex128 amplitudes; complex64
     // needs an even low run (always, except for a tile without bit 0)
@@ -627,19 +633,24 @@ __global__ void __launch_bounds__(NT, NT == 256 ? 3 : 1)
         }
         cp_async_commit();
     };
-    I tau = blockIdx.x;
-    if constexpr (STAGES == 2) {
-        if (tau < p.ntiles) load(tau, buf0);
-        else cp_async_commit();
-    }
-    for (int it = 0; tau < p.ntiles; it++, tau += gridDim.x) {
-        C *cur = (it & 1) ? buf1 : buf0;
-        C *nxt = (it & 1) ? buf0 : buf1;
-        if constexpr (STAGES == 2) {
-            const I tn = tau + gridDim.x;
-            if (tn < p.ntiles) load(tn, nxt);
+    const I G = I(gridDim.x);
+    if constexpr (STAGES > 1) {
+#pragma unroll
+        for (int s = 0; s < STAGES - 1; s++) {
+            const I t = I(blockIdx.x) + I(s) * G;
+            if (t < p.ntiles) load(t, ring + size_t(s) * E);
             else cp_async_commit();
-            cp_async_wait1();  // this thread's copies of `cur` have landed
+        }
+    }
+    int it = 0;
+    for (I tau = blockIdx.x; tau < p.ntiles; tau += G, it++) {
+        C *cur = ring + size_t(STAGES > 1 ? it % STAGES : 0) * E;
+        if constexpr (STAGES > 1) {
+            // the buffer of iteration it - 1, freed by its closing barrier
+            const I tn = tau + I(STAGES - 1) * G;
+            if (tn < p.ntiles) load(tn, ring + size_t((it + STAGES - 1) % STAGES) * E);
+            else cp_async_commit();
+            cp_async_wait_n<STAGES - 1>();  // this thread's copies of `cur` have landed
         } else {
             load(tau, cur);
             cp_async_wait0();
@@ -660,7 +671,7 @@ __global__ void __launch_bounds__(NT, NT == 256 ? 3 : 1)
             for (int e = threadIdx.x; e < E; e += NT)
                 __stcs(&sv[base + p.hi_off[e >> p.m] + I(e & lowmask)], cur[swz<T>(e)]);
         }
-        __syncthreads();  // `cur` is the target of the load issued next iteration
+        __syncthreads();  // `cur` is the target of a load issued next iteration
     }
     cp_async_wait0();
 }
@@ -1059,42 +1070,96 @@ int body_of_2x2_host(const double *mm, KConst *kc) {
     return B_DENSE;
 }
 
-// Split a launch's gates into register groups (consecutive 1-target gates
-// whose targets and in-tile controls span at most R tile positions, padded
-// with the lowest unused positions) and single gates; fills the local target
-// and control fields of grouped gates.  Returns the number of groups.
-static int group_fused_gates(FGate *gates, int cnt, int k, int R, FGroup *groups) {
+// Split a launch's gates into register groups (1-target gates whose targets
+// and in-tile controls span at most R tile positions, padded with the lowest
+// unused positions) and single gates, and fill the local target and control
+// fields of grouped gates.  Gates on disjoint tile positions commute, so a
+// group may take any later gate whose earlier conflicting gates are all
+// placed: starting from the first unplaced gate, a group first takes every
+// such gate inside its position set, then grows the set by the gate adding
+// the fewest positions, up to R.  (A layer of 1-qubit gates followed by a CNOT
+// chain becomes two groups instead of one per run of consecutive gates.)
+// The gates and their integer-pipe constants are permuted into group order;
+// returns the number of groups.
+template <class KC>
+static int group_fused_gates(FGate *gates, KC *kc, int cnt, int k, int R, FGroup *groups) {
+    std::vector<uint32_t> P(size_t(cnt) + 1);
+    for (int i = 0; i < cnt; i++) {
+        const FGate &g = gates[i];
+        P[size_t(i)] = g.in_mask | (1u << g.q0) | (g.ntgt == 2 ? (1u << g.q1) : 0u);
+    }
+    auto groupable = [&](int i) { return k >= R && gates[i].ntgt == 1 && __builtin_popcount(P[size_t(i)]) <= R; };
+    std::vector<char> done(size_t(cnt) + 1, 0);
+    auto ready = [&](int i) {
+        for (int h = 0; h < i; h++)
+            if (!done[size_t(h)] && (P[size_t(h)] & P[size_t(i)])) return false;
+        return true;
+    };
+    std::vector<int> order;
+    order.reserve(size_t(cnt));
     int ng = 0;
-    int i = 0;
-    auto bits_of = [&](const FGate &g) { return g.in_mask | (1u << g.q0); };
-    while (i < cnt) {
-        const FGate &g0 = gates[i];
-        uint32_t set = g0.ntgt == 1 ? bits_of(g0) : 0u;
-        if (k < R || g0.ntgt != 1 || __builtin_popcount(set) > R) {
-            groups[ng++] = FGroup{1, {0, 0, 0, 0}, {0, 0, 0}, uint16_t(i), 1};
-            i++;
+    int first = 0;
+    while (true) {
+        while (first < cnt && done[size_t(first)]) first++;
+        if (first >= cnt) break;
+        const int i0 = first;  // every earlier gate is placed
+        const uint16_t start = uint16_t(order.size());
+        done[size_t(i0)] = 1;
+        order.push_back(i0);
+        if (!groupable(i0)) {
+            groups[ng++] = FGroup{1, {0, 0, 0, 0}, {0, 0, 0}, start, 1};
             continue;
         }
-        int j = i + 1;
-        while (j < cnt && gates[j].ntgt == 1 && __builtin_popcount(set | bits_of(gates[j])) <= R) {
-            set |= bits_of(gates[j]);
-            j++;
+        uint32_t set = P[size_t(i0)];
+        for (;;) {
+            bool added = false;
+            for (int i = i0 + 1; i < cnt; i++)
+                if (!done[size_t(i)] && groupable(i) && (P[size_t(i)] & ~set) == 0 && ready(i)) {
+                    done[size_t(i)] = 1;
+                    order.push_back(i);
+                    added = true;
+                }
+            if (added) continue;
+            int best = -1, best_n = R + 1;
+            for (int i = i0 + 1; i < cnt; i++)
+                if (!done[size_t(i)] && groupable(i) && ready(i)) {
+                    const int c = __builtin_popcount(set | P[size_t(i)]);
+                    if (c < best_n) {
+                        best = i;
+                        best_n = c;
+                    }
+                }
+            if (best < 0 || best_n > R) break;
+            set |= P[size_t(best)];
+            done[size_t(best)] = 1;
+            order.push_back(best);
         }
-        if (j - i == 1) {  // a lone gate touches only its own pairs through the per-gate path
-            groups[ng++] = FGroup{1, {0, 0, 0, 0}, {0, 0, 0}, uint16_t(i), 1};
-            i++;
+        const int count = int(order.size()) - int(start);
+        if (count == 1) {  // a lone gate touches only its own pairs through the per-gate path
+            groups[ng++] = FGroup{1, {0, 0, 0, 0}, {0, 0, 0}, start, 1};
             continue;
         }
         for (int q = 0; q < k && __builtin_popcount(set) < R; q++) set |= 1u << q;
-        FGroup G{0, {0, 0, 0, 0}, {0, 0, 0}, uint16_t(i), uint16_t(j - i)};
-        int loc[32];
+        FGroup G{0, {0, 0, 0, 0}, {0, 0, 0}, start, uint16_t(count)};
         int nb = 0;
         for (int q = 0; q < k; q++)
-            if ((set >> q) & 1u) {
-                loc[q] = nb;
-                G.p[nb++] = uint8_t(q);
-            }
-        for (int t = i; t < j; t++) {
+            if ((set >> q) & 1u) G.p[nb++] = uint8_t(q);
+        groups[ng++] = G;
+    }
+    // permute into group order, then fill the local fields of grouped gates
+    std::vector<FGate> g2(gates, gates + cnt);
+    std::vector<unsigned char> k2(sizeof(KC) * size_t(cnt));
+    std::memcpy(k2.data(), kc, k2.size());
+    for (int i = 0; i < cnt; i++) {
+        gates[i] = g2[size_t(order[size_t(i)])];
+        std::memcpy(&kc[i], k2.data() + sizeof(KC) * size_t(order[size_t(i)]), sizeof(KC));
+    }
+    for (int gr = 0; gr < ng; gr++) {
+        const FGroup &G = groups[gr];
+        if (G.kind != 0) continue;
+        int loc[32];
+        for (int b = 0; b < R; b++) loc[G.p[b]] = b;
+        for (int t = G.first; t < G.first + G.count; t++) {
             FGate &g = gates[t];
             g.lt = uint8_t(loc[g.q0]);
             g.lcm = 0;
@@ -1105,19 +1170,17 @@ static int group_fused_gates(FGate *gates, int cnt, int k, int R, FGroup *groups
                     if ((g.in_val >> q) & 1u) g.lcv |= uint8_t(1u << loc[q]);
                 }
         }
-        groups[ng++] = G;
-        i = j;
     }
     return ng;
 }
 
-template <class T, class I, bool EMU, int NT, int STAGES>
+template <class T, class I, bool EMU, int NT, int STAGES, int MINB>
 static lgpu_status_t launch_fused_nt(cplx_t<T> *sv, const FusedParams<T, I> &p, size_t smem, cudaStream_t s) {
     static std::atomic<size_t> attr[64];
-    LGPU_TRY(ensure_smem(reinterpret_cast<const void *>(fused_kernel<T, I, EMU, NT, STAGES>), smem, attr));
+    LGPU_TRY(ensure_smem(reinterpret_cast<const void *>(fused_kernel<T, I, EMU, NT, STAGES, MINB>), smem, attr));
     const int per_sm = std::max(1, std::min(int((220 * 1024) / smem), 2048 / NT));
     const unsigned grid = unsigned(std::min<uint64_t>(uint64_t(p.ntiles), uint64_t(sm_count()) * per_sm));
-    fused_kernel<T, I, EMU, NT, STAGES><<<grid, NT, smem, s>>>(sv, p);
+    fused_kernel<T, I, EMU, NT, STAGES, MINB><<<grid, NT, smem, s>>>(sv, p);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(e, "fused kernel launch");
     return LGPU_OK;
@@ -1126,13 +1189,19 @@ static lgpu_status_t launch_fused_nt(cplx_t<T> *sv, const FusedParams<T, I> &p, 
 // complex64 (instruction-bound): two tile buffers per CTA, the next tile
 // loading while the current one computes.  complex128 (FP64-bound): one
 // buffer, three CTAs per SM interleave instead.  512 threads when only one
-// CTA fits on an SM.
+// CTA fits on an SM.  (Three stages with two CTAs per SM measured slower:
+// the warps of a third CTA hide the tile's barrier and shared-memory
+// latency better than deeper prefetch does.)
 template <class T, class I, bool EMU>
 static lgpu_status_t launch_fused(cplx_t<T> *sv, const FusedParams<T, I> &p, size_t tile_bytes, cudaStream_t s) {
-    constexpr int ST = sizeof(T) == 4 ? 2 : 1;
-    const size_t smem = ST * tile_bytes;
-    return smem > 64 * 1024 ? launch_fused_nt<T, I, EMU, 512, ST>(sv, p, smem, s)
-                            : launch_fused_nt<T, I, EMU, 256, ST>(sv, p, smem, s);
+    if constexpr (sizeof(T) == 4) {
+        const size_t smem = 2 * tile_bytes;
+        return smem > 64 * 1024 ? launch_fused_nt<T, I, EMU, 512, 2, 1>(sv, p, smem, s)
+                                : launch_fused_nt<T, I, EMU, 256, 2, 3>(sv, p, smem, s);
+    } else {
+        return tile_bytes > 64 * 1024 ? launch_fused_nt<T, I, EMU, 512, 1, 1>(sv, p, tile_bytes, s)
+                                      : launch_fused_nt<T, I, EMU, 256, 1, 3>(sv, p, tile_bytes, s);
+    }
 }
 
 template <class T, class I>
@@ -1207,7 +1276,7 @@ static lgpu_status_t fused_t(cplx_t<T> *sv, uint32_t n, const std::vector<int> &
         }
         if (st != LGPU_OK) break;
         p->ngates = cnt;
-        p->ngroups = group_fused_gates(p->gates, cnt, sizeof(T) == 4 ? k : 0, fused_reg_bits<T>(), p->groups);
+        p->ngroups = group_fused_gates(p->gates, p->kc, cnt, sizeof(T) == 4 ? k : 0, fused_reg_bits<T>(), p->groups);
         const size_t smem = (size_t(1) << k) * sizeof(cplx_t<T>);
         if constexpr (sizeof(T) == 8)
             st = emu ? launch_fused<T, I, true>(sv, *p, smem, s) : launch_fused<T, I, false>(sv, *p, smem, s);
