@@ -194,8 +194,9 @@ typedef struct {
     double m[32];      /* row-major 2^ntgt x 2^ntgt complex (interleaved) */
 } lgpu_fused_gate_t;
 
-/* tile_bits: k distinct state bits (k <= 13 for C64, <= 12 for C128); gates
- * must target only tile bits (controls may be anywhere). */
+/* tile_bits: k distinct state bits (k <= 13 for C64, <= 12 for C128); with
+ * 0..m-1 the longest run of lowest state bits among them, at most 8 others.
+ * Gates must target only tile bits (controls may be anywhere). */
 lgpu_status_t lgpu_apply_fused_block(void *sv, uint32_t n, lgpu_dtype_t dt, uint32_t k,
                                      const int32_t *tile_bits, uint32_t ngates,
                                      const lgpu_fused_gate_t *gates, lgpu_stream_t stream);

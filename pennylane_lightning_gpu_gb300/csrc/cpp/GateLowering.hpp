@@ -263,7 +263,8 @@ inline bool dense_on_bits(const GateDesc &d, std::vector<int> &bits, std::vector
 
 // ---------------------------------------------------------------------------
 // Fusion planner: greedy blocks of 1/2-target matrix gates whose targets fit a
-// tile of `kmax` bits made of the low run 0..m-1 plus at most 6 higher bits.
+// tile of `kmax` bits made of the low run 0..m-1 (m >= mmin) plus at most
+// `max_hi` higher bits.
 // A gate may join the current block only if it commutes with every gate the
 // scan has skipped so far (its bits are disjoint from theirs).
 // ---------------------------------------------------------------------------
@@ -272,14 +273,15 @@ struct FusedBlock {
     std::vector<size_t> gates;         // indices into the input list
 };
 
-inline bool tile_for(const std::vector<int> &gate_bits, int kmax, int mmin, size_t n, std::vector<int> &tile) {
+inline bool tile_for(const std::vector<int> &gate_bits, int kmax, int mmin, size_t n, std::vector<int> &tile,
+                     size_t max_hi = 6) {
     for (int m = std::min<int>(kmax, int(n)); m >= std::min<int>(mmin, int(n)); m--) {
         std::vector<int> hi;
         for (int b : gate_bits)
             if (b >= m) hi.push_back(b);
         std::sort(hi.begin(), hi.end());
         hi.erase(std::unique(hi.begin(), hi.end()), hi.end());
-        if (int(hi.size()) <= kmax - m && hi.size() <= 6) {
+        if (int(hi.size()) <= kmax - m && hi.size() <= max_hi) {
             tile.clear();
             for (int b = 0; b < m; b++) tile.push_back(b);
             tile.insert(tile.end(), hi.begin(), hi.end());
@@ -325,7 +327,7 @@ inline void merge_1q_runs(std::vector<GateDesc> &gates) {
 }
 
 inline std::vector<FusedBlock> plan_fusion(const std::vector<GateDesc> &gates, size_t n, int kmax, int mmin,
-                                           size_t min_block = 2) {
+                                           size_t min_block = 2, size_t max_hi = 6) {
     std::vector<FusedBlock> out;
     std::vector<char> done(gates.size(), 0);
     size_t first = 0;
@@ -357,7 +359,7 @@ inline std::vector<FusedBlock> plan_fusion(const std::vector<GateDesc> &gates, s
                 std::vector<int> trial(bits);
                 trial.insert(trial.end(), g.tgts.begin(), g.tgts.end());
                 std::vector<int> t2;
-                if (tile_for(trial, kmax, mmin, n, t2)) {
+                if (tile_for(trial, kmax, mmin, n, t2, max_hi)) {
                     ok = true;
                     bits = trial;
                     tile = t2;

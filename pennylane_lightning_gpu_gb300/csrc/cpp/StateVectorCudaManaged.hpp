@@ -528,6 +528,9 @@ class StateVectorCudaManaged : public StateVectorCudaBase<Precision, StateVector
         if (fusion_tile_bits_ > 0) return fusion_tile_bits_;
         return 12;  // 32 KB (complex64, double-buffered) / 64 KB (complex128) tiles: three CTAs per SM
     }
+    // Tile bits above the contiguous low run (lgpu_apply_fused_block takes up
+    // to 8).
+    static constexpr int kFusionMaxHighBits = 8;
     // Shortest contiguous low run of a tile: 2^5 amplitudes keep every
     // segment at least 256 bytes long.
     [[nodiscard]] int fusionMinLowBits() const {
@@ -553,7 +556,8 @@ class StateVectorCudaManaged : public StateVectorCudaBase<Precision, StateVector
         }
         Engine::merge_1q_runs(descs);
         const int kmax = std::min<int>(fusionTileBits(), int(nq()));
-        const auto plan = Engine::plan_fusion(descs, nq(), kmax, std::min<int>(fusionMinLowBits(), kmax));
+        const auto plan = Engine::plan_fusion(descs, nq(), kmax, std::min<int>(fusionMinLowBits(), kmax), 2,
+                                              size_t(kFusionMaxHighBits));
         for (const auto &blk : plan) {
             if (blk.tile_bits.empty()) {
                 for (size_t gi : blk.gates) applyDesc(descs[gi]);

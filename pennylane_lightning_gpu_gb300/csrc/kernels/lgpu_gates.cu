@@ -453,7 +453,7 @@ template <class T, class I> struct FusedParams {
     I ntiles;
     int k;             // tile bits
     int m;             // low bits 0..m-1 are the lowest tile bits (contiguous runs)
-    I hi_off[64];      // offsets of the high tile bits (k - m <= 6 -> 64 entries)
+    I hi_off[256];     // offsets of the high tile bits (k - m <= 8 -> 256 entries)
     int ngates;
     int ngroups;
     FGate gates[kFusedMaxGates];
@@ -1214,7 +1214,7 @@ static lgpu_status_t fused_t(cplx_t<T> *sv, uint32_t n, const std::vector<int> &
     for (int q = 0; q < k; q++) pos[size_t(tile_bits[size_t(q)])] = q;
     int m = 0;
     while (m < k && tile_bits[size_t(m)] == m) m++;
-    if (k - m > 6) return fail(LGPU_ERR_INVALID_ARG, "fused tile: at most 6 tile bits above the contiguous low run");
+    if (k - m > 8) return fail(LGPU_ERR_INVALID_ARG, "fused tile: at most 8 tile bits above the contiguous low run");
     auto *p = new FusedParams<T, I>();
     p->holes = make_holes(tile_bits);
     p->ntiles = I(uint64_t(1) << (n - k));
