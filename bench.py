@@ -351,6 +351,23 @@ def _timed(fn, reps=2):
     return best
 
 
+# Gates that touch only the amplitudes whose target bit is 1 (one half, or
+# one half of the controlled subspace) and how many control wires a named gate has.
+_HALF_TOUCH = {"PauliZ", "S", "T", "PhaseShift", "CZ", "ControlledPhaseShift"}
+_NCTRL = {"CNOT": 1, "CY": 1, "CZ": 1, "CRX": 1, "CRY": 1, "CRZ": 1, "CRot": 1, "ControlledPhaseShift": 1,
+          "CSWAP": 1, "Toffoli": 2}
+
+
+def gate_bytes(name, S):
+    """Algorithmic HBM bytes of one gate on a state of S bytes: 2S for an
+    uncontrolled gate, 2S / 2^c under c controls, half that when only the
+    amplitudes with the target bit set change (Z, S, T, PhaseShift, CZ,
+    ControlledPhaseShift)."""
+    c = _NCTRL.get(name, 0)
+    b = 2.0 * S / (1 << c)
+    return b / 2 if name in _HALF_TOUCH else b
+
+
 def bench_circuits(args):
     """Config 1 (28 qubits, 20 layers of random rotations and entanglers; a
     100-term Pauli Hamiltonian, probs on 10 wires, 1e4 shots), config 3
@@ -404,9 +421,20 @@ def bench_circuits(args):
         return params.grad
 
     t3 = _timed(fwd_bwd, reps=1)
+    t3f = _timed(lambda: f(params.detach()), reps=1)
+    # algorithmic bytes: forward = the gates + one read per distinct flip mask
+    # of H; adjoint = 4S per operation (undo it on the ket and the one bra),
+    # 2S per trainable parameter (the generator overlap), S (M + 1) for H|psi>
+    S3 = (1 << n3) * 16
+    ops3 = template(np.zeros(2 * n3 * layers3))
+    flips = {sum(1 << w for w, c in zip(t[2], t[1]) if c in "XY") for t in terms3}
+    fwd_bytes = sum(gate_bytes(o.name, S3) for o in ops3) + S3 * len(flips)
+    adj_bytes = (4 * len(ops3) + 2 * len(params) + len(flips) + 1) * S3
     out["config3"] = {"workload": "24 qubits complex128, 8 layers RY,RZ + CZ ladder (384 params), 50-term "
                                   "Pauli Hamiltonian, forward + adjoint backward via torch.autograd",
-                      "forward_backward_ms": round(t3 * 1e3, 1)}
+                      "forward_backward_ms": round(t3 * 1e3, 1), "forward_ms": round(t3f * 1e3, 1),
+                      "algorithmic_gb": {"forward": round(fwd_bytes / 1e9, 1), "adjoint": round(adj_bytes / 1e9, 1)},
+                      "achieved_gbs": round((fwd_bytes + adj_bytes) / t3 / 1e9, 1)}
     del dev3
 
     n0, layers0 = 12, 4
@@ -459,7 +487,10 @@ def bench_batched(args):
         plain = batched.plain_loop(sub, dt)
         plain_s = (time.perf_counter() - a) * len(circuits) / len(sub)
         err = float(np.max(np.abs(res[sub_idx] - plain)))
+        amp = 8 if dt == np.complex64 else 16
+        alg = sum(sum(gate_bytes(o[0], (1 << n) * amp) for o in ops) + (1 << n) * amp for n, ops, _ in circuits)
         out[key] = {"circuits_per_s": round(len(circuits) / run_s, 1), "run_s": round(run_s, 4),
+                    "achieved_gbs": round(alg / run_s / 1e9, 1),
                     "plain_loop_circuits_per_s": round(len(circuits) / plain_s, 1),
                     "speedup_vs_plain": round(plain_s / run_s, 2), "prepare_s": round(prep, 3),
                     "max_abs_diff_vs_plain": err, "plain_sample": len(sub), "stats": ex.stats()}

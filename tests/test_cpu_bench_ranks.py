@@ -51,3 +51,19 @@ def test_replicas_take_the_slowest_rank():
     for rank, t, v in got:
         assert t == 2.0          # max over ranks
         assert v == 2 * 100.0 / 2.0
+
+
+def test_gate_bytes_follow_the_touched_fraction():
+    """Algorithmic bytes per gate: 2S uncontrolled, 2S / 2^c controlled, half
+    of that for gates that change only the target-1 amplitudes."""
+    import bench
+
+    S = 1 << 20
+    assert bench.gate_bytes("RX", S) == 2 * S
+    assert bench.gate_bytes("Rot", S) == 2 * S
+    assert bench.gate_bytes("RZ", S) == 2 * S
+    assert bench.gate_bytes("PhaseShift", S) == S
+    assert bench.gate_bytes("CNOT", S) == S
+    assert bench.gate_bytes("CRY", S) == S
+    assert bench.gate_bytes("CZ", S) == S / 2
+    assert bench.gate_bytes("Toffoli", S) == S / 2
