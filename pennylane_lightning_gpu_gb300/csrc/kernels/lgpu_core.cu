@@ -49,6 +49,18 @@ int bulk_enabled() {
     return m;
 }
 
+static std::atomic<int> g_fused_df_mode{-1};
+
+int fused_df_enabled() {
+    int m = g_fused_df_mode.load(std::memory_order_relaxed);
+    if (m < 0) {
+        const char *e = std::getenv("LGPU_FUSED_DF");
+        m = (e && e[0] == '0') ? 0 : 1;
+        g_fused_df_mode.store(m, std::memory_order_relaxed);
+    }
+    return m;
+}
+
 int current_device() {
     int d = 0;
     cudaGetDevice(&d);

@@ -17,6 +17,7 @@
 #include <cstring>
 
 #include "lgpu_bodies.cuh"
+#include "lgpu_df64.cuh"
 #include "lgpu_f64emu.cuh"
 #include "lgpu_internal.cuh"
 
@@ -492,9 +493,77 @@ __device__ __forceinline__ void tile_pairs(cplx_t<T> *tile, int E, int q, uint32
     }
 }
 
+// complex128 gates on a tile held in float-float form: each amplitude is a
+// float4 (re.hi, re.lo, im.hi, im.lo) in the slot of its double2, so the
+// layout and the swizzle are those of the complex128 tile.
+template <int BODY, int NT>
+__device__ __forceinline__ void tile_pairs_df(float4 *tile, int E, int q, uint32_t in_mask, uint32_t in_val,
+                                              const DF *m) {
+    const uint32_t holes = in_mask | (1u << q);
+    const int nfree = E >> __popc(holes);
+    DF mr[8];
+#pragma unroll
+    for (int i = 0; i < 8; i++) mr[i] = m[i];
+    PairWalk w(holes, threadIdx.x, NT);
+#pragma unroll 2
+    for (int f = threadIdx.x; f < nfree; f += NT) {
+        const int e0 = int(w.x | in_val);
+        const int e1 = e0 | (1 << q);
+        w.step();
+        const float4 a = tile[swz<double>(e0)], b = tile[swz<double>(e1)];
+        DF xr{a.x, a.y}, xi{a.z, a.w}, yr{b.x, b.y}, yi{b.z, b.w};
+        body1_dfv<BODY>(mr, xr, xi, yr, yi);
+        tile[swz<double>(e0)] = make_float4(xr.hi, xr.lo, xi.hi, xi.lo);
+        tile[swz<double>(e1)] = make_float4(yr.hi, yr.lo, yi.hi, yi.lo);
+    }
+}
+
+// Dense 4x4 (2-target) gate on a float-float tile; qa = most significant
+// matrix bit.
+template <int NT>
+__device__ __forceinline__ void tile_quads_df(float4 *tile, int E, int qa, int qb, uint32_t in_mask, uint32_t in_val,
+                                              const DF *m) {
+    const uint32_t holes = in_mask | (1u << qa) | (1u << qb);
+    const int nfree = E >> __popc(holes);
+    PairWalk w(holes, threadIdx.x, NT);
+    for (int f = threadIdx.x; f < nfree; f += NT) {
+        const int e = int(w.x | in_val);
+        w.step();
+        int idx[4];
+        idx[0] = swz<double>(e);
+        idx[1] = swz<double>(e | (1 << qb));
+        idx[2] = swz<double>(e | (1 << qa));
+        idx[3] = swz<double>(e | (1 << qa) | (1 << qb));
+        DF ar[4], ai[4];
+#pragma unroll
+        for (int c = 0; c < 4; c++) {
+            const float4 v = tile[idx[c]];
+            ar[c] = DF{v.x, v.y};
+            ai[c] = DF{v.z, v.w};
+        }
+#pragma unroll
+        for (int r = 0; r < 4; r++) {
+            DF tr[8], ti[8];
+#pragma unroll
+            for (int c = 0; c < 4; c++) {
+                const DF mre = m[2 * (r * 4 + c)], mim = m[2 * (r * 4 + c) + 1];
+                tr[2 * c] = df_mul(mre, ar[c]);
+                tr[2 * c + 1] = df_mul(df_neg(mim), ai[c]);
+                ti[2 * c] = df_mul(mre, ai[c]);
+                ti[2 * c + 1] = df_mul(mim, ar[c]);
+            }
+            const DF xr = df_sum<8>(tr), xi = df_sum<8>(ti);
+            tile[idx[r]] = make_float4(xr.hi, xr.lo, xi.hi, xi.lo);
+        }
+    }
+}
+
 // All gates of a launch on one tile held in shared memory (all threads; the
-// caller synchronises before and after).
-template <class T, class I, bool EMU, int NT>
+// caller synchronises before and after).  DFM (complex128): the tile holds
+// float-float amplitudes (converted once after the load and once at the
+// store) and every gate runs in float-float arithmetic, its coefficients
+// stored as (hi, lo) float pairs in the double slots of the matrix pool.
+template <class T, class I, bool EMU, int NT, bool DFM = false>
 __device__ __forceinline__ void fused_tile(cplx_t<T> *tile, int E, I base, const FusedParams<T, I> &p) {
     using C = cplx_t<T>;
     constexpr int R = fused_reg_bits<T>();
@@ -541,7 +610,22 @@ __device__ __forceinline__ void fused_tile(cplx_t<T> *tile, int E, I base, const
         const FGate &g = p.gates[gi];
         if ((uint64_t(base) & g.out_mask) != g.out_val) continue;  // tile-uniform
         const T *mm = p.mats + g.mat_off;
-        if (g.ntgt == 1) {
+        if constexpr (DFM && sizeof(T) == 8) {
+            float4 *t4 = reinterpret_cast<float4 *>(tile);
+            const DF *md = reinterpret_cast<const DF *>(mm);
+            if (g.ntgt == 1) {
+                switch (g.body) {
+                case B_DIAG: tile_pairs_df<B_DIAG, NT>(t4, E, g.q0, g.in_mask, g.in_val, md); break;
+                case B_PERM: tile_pairs_df<B_PERM, NT>(t4, E, g.q0, g.in_mask, g.in_val, md); break;
+                case B_ANTIDIAG: tile_pairs_df<B_ANTIDIAG, NT>(t4, E, g.q0, g.in_mask, g.in_val, md); break;
+                case B_REAL: tile_pairs_df<B_REAL, NT>(t4, E, g.q0, g.in_mask, g.in_val, md); break;
+                case B_RXLIKE: tile_pairs_df<B_RXLIKE, NT>(t4, E, g.q0, g.in_mask, g.in_val, md); break;
+                default: tile_pairs_df<B_DENSE, NT>(t4, E, g.q0, g.in_mask, g.in_val, md); break;
+                }
+            } else {
+                tile_quads_df<NT>(t4, E, g.q0, g.q1, g.in_mask, g.in_val, md);
+            }
+        } else if (g.ntgt == 1) {
             const KConst *kk = p.kc[gi];
             switch (g.body) {
             case B_DIAG: tile_pairs<T, B_DIAG, EMU, NT>(tile, E, g.q0, g.in_mask, g.in_val, mm, kk); break;
@@ -608,7 +692,7 @@ template <int N> __device__ __forceinline__ void cp_async_wait_n() {
     asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
 }
 
-template <class T, class I, bool EMU, int NT, int STAGES, int MINB>
+template <class T, class I, bool EMU, int NT, int STAGES, int MINB, bool DFM = false>
 __global__ void __launch_bounds__(NT, MINB)
     fused_kernel(cplx_t<T> *__restrict__ sv, const FusedParams<T, I> p) {
     using C = cplx_t<T>;
@@ -656,16 +740,30 @@ __global__ void __launch_bounds__(NT, MINB)
             cp_async_wait0();
         }
         __syncthreads();  // ... and everyone's
+        if constexpr (DFM && sizeof(T) == 8) {
+            // complex128 -> float-float in place (same 16 bytes per amplitude)
+            for (int e = threadIdx.x; e < E; e += NT) {
+                const double2 v = reinterpret_cast<const double2 *>(cur)[e];
+                const DF r = df_from_double(v.x), i = df_from_double(v.y);
+                reinterpret_cast<float4 *>(cur)[e] = make_float4(r.hi, r.lo, i.hi, i.lo);
+            }
+            __syncthreads();
+        }
         const I base = insert_holes<I>(tau, p.holes);
-        fused_tile<T, I, EMU, NT>(cur, E, base, p);
+        fused_tile<T, I, EMU, NT, DFM>(cur, E, base, p);
         if (wide) {
             for (int c = threadIdx.x; c < E / EPC; c += NT) {
                 const int e = c * EPC;
                 C *dst = &sv[base + p.hi_off[e >> p.m] + I(e & lowmask)];
-                if constexpr (EPC == 2)
+                if constexpr (EPC == 2) {
                     __stcs(reinterpret_cast<float4 *>(dst), *reinterpret_cast<const float4 *>(&cur[swz<T>(e)]));
-                else
+                } else if constexpr (DFM && sizeof(T) == 8) {
+                    const float4 v = reinterpret_cast<const float4 *>(cur)[swz<T>(e)];
+                    __stcs(reinterpret_cast<double2 *>(dst),
+                           make_double2(df_to_double(DF{v.x, v.y}), df_to_double(DF{v.z, v.w})));
+                } else {
                     __stcs(dst, cur[swz<T>(e)]);
+                }
             }
         } else {
             for (int e = threadIdx.x; e < E; e += NT)
@@ -1174,13 +1272,13 @@ static int group_fused_gates(FGate *gates, KC *kc, int cnt, int k, int R, FGroup
     return ng;
 }
 
-template <class T, class I, bool EMU, int NT, int STAGES, int MINB>
+template <class T, class I, bool EMU, int NT, int STAGES, int MINB, bool DFM = false>
 static lgpu_status_t launch_fused_nt(cplx_t<T> *sv, const FusedParams<T, I> &p, size_t smem, cudaStream_t s) {
     static std::atomic<size_t> attr[64];
-    LGPU_TRY(ensure_smem(reinterpret_cast<const void *>(fused_kernel<T, I, EMU, NT, STAGES, MINB>), smem, attr));
+    LGPU_TRY(ensure_smem(reinterpret_cast<const void *>(fused_kernel<T, I, EMU, NT, STAGES, MINB, DFM>), smem, attr));
     const int per_sm = std::max(1, std::min(int((220 * 1024) / smem), 2048 / NT));
     const unsigned grid = unsigned(std::min<uint64_t>(uint64_t(p.ntiles), uint64_t(sm_count()) * per_sm));
-    fused_kernel<T, I, EMU, NT, STAGES, MINB><<<grid, NT, smem, s>>>(sv, p);
+    fused_kernel<T, I, EMU, NT, STAGES, MINB, DFM><<<grid, NT, smem, s>>>(sv, p);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(e, "fused kernel launch");
     return LGPU_OK;
@@ -1202,6 +1300,14 @@ static lgpu_status_t launch_fused(cplx_t<T> *sv, const FusedParams<T, I> &p, siz
         return tile_bytes > 64 * 1024 ? launch_fused_nt<T, I, EMU, 512, 1, 1>(sv, p, tile_bytes, s)
                                       : launch_fused_nt<T, I, EMU, 256, 1, 3>(sv, p, tile_bytes, s);
     }
+}
+
+// complex128 blocks with float-float 1-target bodies.
+template <class I>
+static lgpu_status_t launch_fused_df(double2 *sv, const FusedParams<double, I> &p, size_t tile_bytes,
+                                     cudaStream_t s) {
+    return tile_bytes > 64 * 1024 ? launch_fused_nt<double, I, false, 512, 1, 1, true>(sv, p, tile_bytes, s)
+                                  : launch_fused_nt<double, I, false, 256, 1, 3, true>(sv, p, tile_bytes, s);
 }
 
 template <class T, class I>
@@ -1227,6 +1333,7 @@ static lgpu_status_t fused_t(cplx_t<T> *sv, uint32_t n, const std::vector<int> &
         p->hi_off[h] = I(o);
     }
     const bool emu = sizeof(T) == 8 && f64_mode() == 1;
+    const bool dfm = sizeof(T) == 8 && f64_mode() == 1 && fused_df_enabled();
     uint32_t done = 0;
     lgpu_status_t st = LGPU_OK;
     while (done < ngates && st == LGPU_OK) {
@@ -1269,7 +1376,14 @@ static lgpu_status_t fused_t(cplx_t<T> *sv, uint32_t n, const std::vector<int> &
             }
             if (st != LGPU_OK) break;
             dst.mat_off = pool;
-            for (uint32_t e = 0; e < need; e++) p->mats[pool + e] = T(src.m[e]);
+            if (dfm) {  // (hi, lo) float pairs in the double slots
+                for (uint32_t e = 0; e < need; e++) {
+                    const DF d = df_split_host(src.m[e]);
+                    std::memcpy(&p->mats[pool + e], &d, sizeof(DF));
+                }
+            } else {
+                for (uint32_t e = 0; e < need; e++) p->mats[pool + e] = T(src.m[e]);
+            }
             dst.body = src.ntgt == 1 ? uint8_t(body_of_2x2_host(src.m, p->kc[cnt])) : uint8_t(B_DENSE);
             pool += need;
             cnt++;
@@ -1279,7 +1393,8 @@ static lgpu_status_t fused_t(cplx_t<T> *sv, uint32_t n, const std::vector<int> &
         p->ngroups = group_fused_gates(p->gates, p->kc, cnt, sizeof(T) == 4 ? k : 0, fused_reg_bits<T>(), p->groups);
         const size_t smem = (size_t(1) << k) * sizeof(cplx_t<T>);
         if constexpr (sizeof(T) == 8)
-            st = emu ? launch_fused<T, I, true>(sv, *p, smem, s) : launch_fused<T, I, false>(sv, *p, smem, s);
+            st = dfm ? launch_fused_df<I>(sv, *p, smem, s)
+                     : emu ? launch_fused<T, I, true>(sv, *p, smem, s) : launch_fused<T, I, false>(sv, *p, smem, s);
         else
             st = launch_fused<T, I, false>(sv, *p, smem, s);
         done += uint32_t(cnt);

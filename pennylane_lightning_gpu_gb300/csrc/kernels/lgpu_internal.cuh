@@ -49,6 +49,10 @@ int current_device();
 // complex128 arithmetic mode: 0 = native FP64, 1 = FP64 FMA + integer-pipe
 // multiplies (lgpu_f64emu.cuh).  Process-wide; see lgpu_set_f64_mode().
 int f64_mode();
+// complex128 fused blocks run 1-target bodies in float-float arithmetic when 1
+// (default, with f64_mode() == 1); the integer-pipe bodies when 0
+// (environment LGPU_FUSED_DF=0).
+int fused_df_enabled();
 // Uncontrolled 1-target gates use the bulk-copy pipelined kernel when 1
 // (default); the grid-stride kernel when 0.  See lgpu_set_stream_mode().
 int bulk_enabled();
