@@ -15,6 +15,7 @@
 //                   tiles of the last block and reduced inside the CTA, so each
 //                   result is written by exactly one CTA in a fixed order.
 #include "lgpu_bodies.cuh"
+#include "lgpu_df64.cuh"
 #include "lgpu_f64emu.cuh"
 #include "lgpu_internal.cuh"
 
@@ -92,8 +93,14 @@ __device__ void bgate_matrix(const lgpu_bgate_t &g, const double *__restrict__ p
     }
 }
 
+// complex128 batches run in float-float (the same switch as the fused blocks).
+static bool batch_df() { return f64_mode() == 1 && fused_df_enabled() != 0; }
+
+// mode: 0 = complex128 with integer-pipe constants, 1 = complex64 (float
+// copy), 2 = complex128 in float-float (the (hi, lo) pairs of a 1-target
+// matrix at pool + mat + 8).
 __global__ void bprep_kernel(const lgpu_bgate_t *__restrict__ gates, uint64_t ngates, const double *__restrict__ params,
-                             double *__restrict__ pool, int c64) {
+                             double *__restrict__ pool, int mode) {
     const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
     for (uint64_t gi = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; gi < ngates; gi += stride) {
         const lgpu_bgate_t g = gates[gi];
@@ -126,7 +133,14 @@ __global__ void bprep_kernel(const lgpu_bgate_t *__restrict__ gates, uint64_t ng
             bgate_matrix(g, params, pool, m);
         }
         // (fixed matrices arrive from the host already in their final, adjointed form)
-        if (c64) {
+        if (mode == 2) {
+            if (g.kind < BK_DENSE2) {
+                DF *d = reinterpret_cast<DF *>(m + 8);
+                for (int e = 0; e < 8; e++) d[e] = df_from_double(m[e]);
+            }
+            continue;
+        }
+        if (mode == 1) {
             // complex64: a float copy of the matrix (1q: pool + mat + 8, 2q: pool + mat + 32)
             float *f = reinterpret_cast<float *>(m + (g.kind < BK_DENSE2 ? 8 : 32));
             const int cnt = g.kind < BK_DENSE2 ? 8 : 32;
@@ -197,6 +211,98 @@ __device__ __forceinline__ void batch_pairs(cplx_t<T> *tile, int E, int q, uint3
         body1_sel<T, BODY, EMU>(m, k, a0, a1);
         tile[e0] = a0;
         tile[e1] = a1;
+    }
+}
+
+// complex128 in float-float (lgpu_df64.cuh): the tile holds float4
+// (re.hi, re.lo, im.hi, im.lo) per amplitude, in the slot of its double2.
+template <int BODY>
+__device__ __forceinline__ void batch_pairs_df(float4 *tile, int E, int q, uint32_t cmask, uint32_t cval,
+                                               const DF *mp) {
+    DF m[8];
+#pragma unroll
+    for (int i = 0; i < 8; i++) m[i] = mp[i];
+    const uint32_t holes = cmask | (1u << q);
+    const int nfree = E >> __popc(holes);
+    PairWalk w(holes, threadIdx.x, blockDim.x);
+#pragma unroll 2
+    for (int f = threadIdx.x; f < nfree; f += blockDim.x) {
+        const int e0 = int(w.x | cval);
+        const int e1 = e0 | (1 << q);
+        w.step();
+        const float4 a = tile[e0], b = tile[e1];
+        DF xr{a.x, a.y}, xi{a.z, a.w}, yr{b.x, b.y}, yi{b.z, b.w};
+        body1_dfv<BODY>(m, xr, xi, yr, yi);
+        tile[e0] = make_float4(xr.hi, xr.lo, xi.hi, xi.lo);
+        tile[e1] = make_float4(yr.hi, yr.lo, yi.hi, yi.lo);
+    }
+}
+
+__device__ __forceinline__ void tile_gate_df(float4 *tile, int E, const lgpu_bgate_t &g, const double *pool) {
+    if (g.kind < BK_DENSE2) {
+        const int q = g.q0;
+        const DF *m = reinterpret_cast<const DF *>(pool + g.mat + 8);
+        switch (g.kind) {
+        case BK_DIAG1: batch_pairs_df<B_DIAG>(tile, E, q, g.cmask, g.cval, m); break;
+        case BK_X1: batch_pairs_df<B_PERM>(tile, E, q, g.cmask, g.cval, m); break;
+        case BK_REAL1: batch_pairs_df<B_REAL>(tile, E, q, g.cmask, g.cval, m); break;
+        case BK_RXLIKE1: batch_pairs_df<B_RXLIKE>(tile, E, q, g.cmask, g.cval, m); break;
+        default: batch_pairs_df<B_DENSE>(tile, E, q, g.cmask, g.cval, m); break;
+        }
+        return;
+    }
+    const int qa = g.q0, qb = g.q1;
+    const uint32_t holes = g.cmask | (1u << qa) | (1u << qb);
+    const int nfree = E >> __popc(holes);
+    PairWalk w(holes, threadIdx.x, blockDim.x);
+    const double *mm = pool + g.mat;  // 4x4 doubles, split per use (2-target gates are rare)
+    for (int f = threadIdx.x; f < nfree; f += blockDim.x) {
+        const int e = int(w.x | g.cval);
+        w.step();
+        const int idx[4] = {e, e | (1 << qb), e | (1 << qa), e | (1 << qa) | (1 << qb)};
+        if (g.kind == BK_SWAP2) {
+            const float4 t = tile[idx[1]];
+            tile[idx[1]] = tile[idx[2]];
+            tile[idx[2]] = t;
+            continue;
+        }
+        DF ar[4], ai[4];
+#pragma unroll
+        for (int c = 0; c < 4; c++) {
+            const float4 v = tile[idx[c]];
+            ar[c] = DF{v.x, v.y};
+            ai[c] = DF{v.z, v.w};
+        }
+#pragma unroll
+        for (int row = 0; row < 4; row++) {
+            DF tr[8], ti[8];
+#pragma unroll
+            for (int c = 0; c < 4; c++) {
+                const DF mre = df_from_double(mm[2 * (row * 4 + c)]), mim = df_from_double(mm[2 * (row * 4 + c) + 1]);
+                tr[2 * c] = df_mul(mre, ar[c]);
+                tr[2 * c + 1] = df_mul(df_neg(mim), ai[c]);
+                ti[2 * c] = df_mul(mre, ai[c]);
+                ti[2 * c + 1] = df_mul(mim, ar[c]);
+            }
+            const DF xr = df_sum<8>(tr), xi = df_sum<8>(ti);
+            tile[idx[row]] = make_float4(xr.hi, xr.lo, xi.hi, xi.lo);
+        }
+    }
+}
+
+// complex128 tile <-> float-float tile, in place (all threads; the caller
+// synchronises afterwards).
+__device__ __forceinline__ void tile_to_df(void *tile, int E) {
+    for (int e = threadIdx.x; e < E; e += blockDim.x) {
+        const double2 v = reinterpret_cast<const double2 *>(tile)[e];
+        const DF r = df_from_double(v.x), i = df_from_double(v.y);
+        reinterpret_cast<float4 *>(tile)[e] = make_float4(r.hi, r.lo, i.hi, i.lo);
+    }
+}
+__device__ __forceinline__ void tile_from_df(void *tile, int E) {
+    for (int e = threadIdx.x; e < E; e += blockDim.x) {
+        const float4 v = reinterpret_cast<const float4 *>(tile)[e];
+        reinterpret_cast<double2 *>(tile)[e] = make_double2(df_to_double(DF{v.x, v.y}), df_to_double(DF{v.z, v.w}));
     }
 }
 
@@ -384,7 +490,9 @@ __device__ __forceinline__ void b_wait_read_1() { asm volatile("cp.async.bulk.wa
 __device__ __forceinline__ void b_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
 __device__ __forceinline__ void b_fence() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 
-template <class T, bool EMU>
+// DFM (complex128): gates run in float-float on a float-float tile; the tile
+// is converted in place after a load and before a store or the observable.
+template <class T, bool EMU, bool DFM = false>
 __global__ void __launch_bounds__(512, 1) batch_kernel(lgpu_batch_args_t a) {
     using C = cplx_t<T>;
     extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -448,11 +556,22 @@ __global__ void __launch_bounds__(512, 1) batch_kernel(lgpu_batch_args_t a) {
                 // ---- whole state in shared memory ----
                 C *tile = ring;
                 for (int e = threadIdx.x; e < E; e += blockDim.x) tile[e] = mk<T>(T(e == 0 ? 1 : 0), T(0));
+                if constexpr (DFM) {  // (1, 0) and 0 are exact float-float values
+                    __syncthreads();
+                    tile_to_df(tile, E);
+                }
                 __syncthreads();
                 for (uint32_t gi = 0; gi < blk.gate_cnt; gi++) {
                     const lgpu_bgate_t g = a.gates[blk.gate_off + gi];
                     if (g.kind == BK_CHAINED) continue;
-                    tile_gate<T, EMU>(tile, E, g, a.pool);
+                    if constexpr (DFM)
+                        tile_gate_df(reinterpret_cast<float4 *>(tile), E, g, a.pool);
+                    else
+                        tile_gate<T, EMU>(tile, E, g, a.pool);
+                    __syncthreads();
+                }
+                if constexpr (DFM) {
+                    tile_from_df(tile, E);
                     __syncthreads();
                 }
                 acc += wht ? tile_obs<T>(tile, k, a.terms + cir.obs_off, cir.obs_cnt, 0, s_lm, s_c)
@@ -505,10 +624,21 @@ __global__ void __launch_bounds__(512, 1) batch_kernel(lgpu_batch_args_t a) {
                     }
                     phase_bits ^= 1u << st;
                 }
+                if constexpr (DFM) {
+                    tile_to_df(tile, E);
+                    __syncthreads();
+                }
                 for (uint32_t gi = 0; gi < blk.gate_cnt; gi++) {
                     const lgpu_bgate_t g = a.gates[blk.gate_off + gi];
                     if (g.kind == BK_CHAINED || (base & g.omask) != g.oval) continue;  // tile-uniform
-                    tile_gate<T, EMU>(tile, E, g, a.pool);
+                    if constexpr (DFM)
+                        tile_gate_df(reinterpret_cast<float4 *>(tile), E, g, a.pool);
+                    else
+                        tile_gate<T, EMU>(tile, E, g, a.pool);
+                    __syncthreads();
+                }
+                if constexpr (DFM) {
+                    tile_from_df(tile, E);
                     __syncthreads();
                 }
                 if (last) {
@@ -557,13 +687,13 @@ lgpu_status_t batch_error_fetch(unsigned *v, bool reset) {
     return LGPU_OK;
 }
 
-template <class T, bool EMU>
+template <class T, bool EMU, bool DFM = false>
 static lgpu_status_t launch_batch(const lgpu_batch_args_t &args, unsigned grid, size_t smem, cudaStream_t s) {
     // The attribute is set once per size outside any stream capture (the host
     // runs the batch eagerly once before capturing it).
     static std::atomic<size_t> attr[64];
-    LGPU_TRY(ensure_smem(reinterpret_cast<const void *>(batch_kernel<T, EMU>), smem, attr));
-    batch_kernel<T, EMU><<<grid, args.threads, smem, s>>>(args);
+    LGPU_TRY(ensure_smem(reinterpret_cast<const void *>(batch_kernel<T, EMU, DFM>), smem, attr));
+    batch_kernel<T, EMU, DFM><<<grid, args.threads, smem, s>>>(args);
     LGPU_CHECK_LAUNCH();
     return LGPU_OK;
 }
@@ -580,7 +710,8 @@ lgpu_status_t lgpu_batch_prepare(const lgpu_bgate_t *gates, uint64_t ngates, con
     if (!gates || !pool) return fail(LGPU_ERR_INVALID_ARG, "null gates/pool");
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
     if (dt != LGPU_C64 && dt != LGPU_C128) return fail(LGPU_ERR_INVALID_ARG, "unknown dtype");
-    bprep_kernel<<<grid_for(ngates, 128, 1, 4), 128, 0, s>>>(gates, ngates, params, pool, dt == LGPU_C64 ? 1 : 0);
+    const int mode = dt == LGPU_C64 ? 1 : (batch_df() ? 2 : 0);
+    bprep_kernel<<<grid_for(ngates, 128, 1, 4), 128, 0, s>>>(gates, ngates, params, pool, mode);
     LGPU_CHECK_LAUNCH();
     return LGPU_OK;
 }
@@ -599,8 +730,9 @@ lgpu_status_t lgpu_batch_run(const lgpu_batch_args_t *args, lgpu_dtype_t dt, uns
     const size_t amp = dt == LGPU_C128 ? 16 : 8;
     const size_t smem = std::max((size_t(1) << args->kmax) * amp, size_t(kRing) * (size_t(1) << args->klarge) * amp);
     if (dt == LGPU_C128)
-        return f64_mode() == 1 ? launch_batch<double, true>(*args, grid, smem, s)
-                               : launch_batch<double, false>(*args, grid, smem, s);
+        return batch_df()          ? launch_batch<double, false, true>(*args, grid, smem, s)
+               : f64_mode() == 1 ? launch_batch<double, true>(*args, grid, smem, s)
+                                 : launch_batch<double, false>(*args, grid, smem, s);
     return launch_batch<float, false>(*args, grid, smem, s);
 }
 
