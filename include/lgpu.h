@@ -320,6 +320,35 @@ lgpu_status_t lgpu_adjoint_sweep_small(lgpu_context_t ctx, const void *ket, void
                                        const lgpu_adj_op_t *ops, uint32_t nops, double *jac_dev,
                                        lgpu_stream_t stream);
 
+/* Several consecutive operations of the reverse sweep in one pass over the
+ * states (complex128; states too large for lgpu_adjoint_sweep_small).  Each
+ * step is a 1-target U^dag with controls and, when `gen_kind` >= 0, the
+ * generator P1(controls) (x) g on the target:
+ *   jac[col * jac_stride + k] = Im <bra_k| G |lambda>   (G on the pairs the
+ *                                                        controls select)
+ *   lambda <- U^dag lambda ;  bra_k <- U^dag bra_k
+ * in step order.  Every target must be one of the k tile bits: the bits
+ * 0..m-1 plus at most 6 others, k <= 11.  nbras <= 2.  The states are
+ * carried in float-float arithmetic inside the pass (no FP64 instruction per
+ * pair); the sums are deterministic.  Replaces the per-operation
+ * updateJacobian / applyOperationsAdj sequence of AdjointDiffGPU.hpp:560-595
+ * for runs of such operations; no counterpart in the reference. */
+typedef struct {
+    int32_t tgt;         /* state bit */
+    int32_t nctrl;       /* 0..2 */
+    int32_t ctrl[2];     /* state bits */
+    int32_t ctrl_val[2];
+    int32_t gen_kind;    /* -1: no gradient; 0: dense g */
+    int32_t col;         /* Jacobian column (gen_kind >= 0) */
+    double u[8];         /* U^dag, 2x2 row-major (re, im) */
+    double g[8];         /* generator on the target, 2x2 row-major (re, im) */
+} lgpu_adj_block_step_t;
+
+lgpu_status_t lgpu_adjoint_block(lgpu_context_t ctx, void *ket, void *const *bras, uint32_t nbras, uint32_t n,
+                                 lgpu_dtype_t dt, uint32_t k, const int32_t *tile_bits,
+                                 const lgpu_adj_block_step_t *steps, uint32_t nsteps, double *jac_dev,
+                                 uint32_t jac_stride, lgpu_stream_t stream);
+
 /* ---- CUDA graphs (stream capture) ------------------------------------------
  * Capture everything issued on `stream` between begin and end into an
  * executable graph; launch replays it on any stream. */

@@ -11,6 +11,7 @@
 // column stays on the device until one copy at the end.
 #pragma once
 
+#include <cstdlib>
 #include <memory>
 #include <vector>
 
@@ -172,12 +173,63 @@ template <class T = double> class AdjointJacobianGPU {
             }
         }
 
+        const bool blocks = SV::dt() == LGPU_C128 && num_observables >= 1 && num_observables <= 2 && blocks_enabled();
         for (int op_idx = static_cast<int>(ops_name.size() - 1); op_idx >= 0; op_idx--) {
             PL_ABORT_IF(ops.getOpsParams()[size_t(op_idx)].size() > 1,
                         "The operation is not supported using the adjoint differentiation method");
             const std::string &name = ops_name[size_t(op_idx)];
             if ((name == "QubitStateVector") || (name == "StatePrep") || (name == "BasisState")) continue;
             if (tp_it == tp_rend) break;  // All done
+
+            // A run of 1-target operations (with controls) whose targets fit
+            // one tile: one pass over lambda and the bras for the whole run.
+            if (blocks) {
+                std::vector<lgpu_adj_block_step_t> steps;
+                std::vector<int> tbits, tile;
+                std::vector<std::pair<size_t, double>> scales;
+                size_t cpi = current_param_idx, tpn = trainableParamNumber;
+                auto it = tp_it;
+                int j = op_idx;
+                for (; j >= 0 && steps.size() < 48; j--) {
+                    const std::string &nj = ops_name[size_t(j)];
+                    if ((nj == "QubitStateVector") || (nj == "StatePrep") || (nj == "BasisState")) continue;
+                    if (it == tp_rend || ops.getOpsParams()[size_t(j)].size() > 1) break;
+                    const bool invj = ops.getOpsInverses()[size_t(j)];
+                    const bool grad = ops.hasParams(size_t(j)) && cpi == *it;
+                    lgpu_adj_block_step_t st{};
+                    double scale = 0;
+                    if (!block_step(lower(lambda, ops, size_t(j), !invj), nj, ops.getOpsWires()[size_t(j)], n, grad,
+                                    st, scale))
+                        break;
+                    std::vector<int> trial(tbits);
+                    trial.push_back(st.tgt);
+                    std::vector<int> t2;
+                    if (!Engine::tile_for(trial, 11, 5, n, t2, 6)) break;
+                    tbits = trial;
+                    tile = t2;
+                    if (grad) {
+                        st.col = int32_t(tpn);
+                        scales.emplace_back(tpn, scale * (invj ? -1.0 : 1.0));
+                        tpn--;
+                        ++it;
+                    }
+                    if (ops.hasParams(size_t(j))) cpi--;
+                    steps.push_back(st);
+                }
+                if (steps.size() >= 2) {
+                    std::vector<int32_t> tb(tile.begin(), tile.end());
+                    PL_LGPU_IS_SUCCESS(lgpu_adjoint_block(lambda.ctx(), lambda.getData(), bra_ptrs.data(),
+                                                          uint32_t(num_observables), n, SV::dt(), uint32_t(tb.size()),
+                                                          tb.data(), steps.data(), uint32_t(steps.size()),
+                                                          jac_dev.getData(), uint32_t(K), lambda.lstream()));
+                    for (const auto &cs : scales) col_scale[cs.first] = cs.second;
+                    current_param_idx = cpi;
+                    trainableParamNumber = tpn;
+                    tp_it = it;
+                    op_idx = j + 1;  // the loop continues with operation j
+                    continue;
+                }
+            }
 
             const bool inv = ops.getOpsInverses()[size_t(op_idx)];
             const auto &wires = ops.getOpsWires()[size_t(op_idx)];
@@ -260,6 +312,73 @@ template <class T = double> class AdjointJacobianGPU {
     }
 
   private:
+    // Fused adjoint blocks are on unless LGPU_ADJOINT_BLOCKS=0.
+    static bool blocks_enabled() {
+        static const bool on = [] {
+            const char *e = std::getenv("LGPU_ADJOINT_BLOCKS");
+            return !(e && e[0] == '0');
+        }();
+        return on;
+    }
+    // The operation as a step of a fused adjoint block: U^dag a 1-target
+    // gate with at most 2 controls, and (grad) its generator either a 2x2 on
+    // the target of an uncontrolled 1-wire operation, or P11 (x) g on
+    // (control, target) for the controlled rotations and phase.
+    static bool block_step(const Engine::GateDesc &u, const std::string &name, const std::vector<size_t> &wires,
+                           uint32_t n, bool grad, lgpu_adj_block_step_t &st, double &scale) {
+        std::vector<cd> m2;
+        if (u.kind == Engine::GateDesc::IDENTITY) {
+            if (wires.size() != 1) return false;
+            st.tgt = Engine::bit_of(n, wires[0]);
+            m2 = {1.0, 0.0, 0.0, 1.0};
+        } else {
+            if (u.tgts.size() != 1 || u.ctrls.size() > 2) return false;
+            st.tgt = u.tgts[0];
+            if (u.kind == Engine::GateDesc::MATRIX) {
+                if (u.matrix.size() != 4) return false;
+                m2 = u.matrix;
+            } else {
+                Engine::GateDesc bare = u;
+                bare.ctrls.clear();
+                bare.cvals.clear();
+                std::vector<int> bits;
+                if (!Engine::dense_on_bits(bare, bits, m2, 1) || m2.size() != 4) return false;
+            }
+            st.nctrl = int32_t(u.ctrls.size());
+            for (size_t c = 0; c < u.ctrls.size(); c++) {
+                st.ctrl[c] = u.ctrls[c];
+                st.ctrl_val[c] = u.cvals.empty() ? 1 : u.cvals[c];
+            }
+        }
+        for (int e = 0; e < 4; e++) {
+            st.u[2 * e] = m2[size_t(e)].real();
+            st.u[2 * e + 1] = m2[size_t(e)].imag();
+        }
+        st.gen_kind = -1;
+        st.col = -1;
+        if (!grad) return true;
+        std::vector<cd> g;
+        if (!Engine::generator_of(name, wires.size(), g, scale)) return false;
+        std::vector<cd> g1;
+        if (wires.size() == 1 && st.nctrl == 0 && g.size() == 4) {
+            g1 = g;
+        } else if (wires.size() == 2 && g.size() == 16 && st.nctrl == 1 &&
+                   st.ctrl[0] == Engine::bit_of(n, wires[0]) && st.ctrl_val[0] == 1 &&
+                   st.tgt == Engine::bit_of(n, wires[1])) {
+            for (int r = 0; r < 4; r++)
+                for (int c = 0; c < 4; c++)
+                    if ((r < 2 || c < 2) && g[size_t(r * 4 + c)] != cd(0.0)) return false;
+            g1 = {g[10], g[11], g[14], g[15]};
+        } else {
+            return false;
+        }
+        for (int e = 0; e < 4; e++) {
+            st.g[2 * e] = g1[size_t(e)].real();
+            st.g[2 * e + 1] = g1[size_t(e)].imag();
+        }
+        st.gen_kind = 0;
+        return true;
+    }
     double *dot_buf(SV &sv) {
         if (!dot_buf_) dot_buf_ = std::make_unique<CUDA::DataBuffer<double, int>>(2, sv.getDataBuffer().getDevTag(), true);
         return dot_buf_->getData();

@@ -8,7 +8,10 @@
 // which replaces the reference's per-op sequence of a D2D copy of lambda,
 // U^dag on lambda, G on mu, K cuBLAS dot products and U^dag on K bras
 // (AdjointDiffGPU.hpp:560-595).
+#include <memory>
+
 #include "lgpu_bodies.cuh"
+#include "lgpu_df64.cuh"
 #include "lgpu_internal.cuh"
 #include "lgpu_reduce.cuh"
 
@@ -630,6 +633,329 @@ static lgpu_status_t sweep_launch(const void *ket, void *const *dbras, uint32_t 
     return LGPU_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Fused adjoint blocks (complex128): several operations of the reverse sweep
+// per pass.  Each CTA loads a tile of lambda and of each bra (the tile bits =
+// the low run 0..m-1 plus up to 6 high bits, as the fused gate blocks),
+// converts them in place to float-float (lgpu_df64.cuh) and runs the steps in
+// order; a step reads a pair, adds Im <bra| G |lambda> to the thread's
+// float-float sum and applies U^dag to lambda and the bras.  The sums are
+// reduced per warp (shuffles), kept per warp in shared memory across the
+// CTA's tiles, written per CTA and summed over CTAs in a fixed order.
+// ---------------------------------------------------------------------------
+constexpr int kAdjBlockSteps = 48;
+constexpr int kAdjBlockBras = 2;
+constexpr int kAdjBlockThreads = 256;
+
+struct AStep {
+    uint8_t q;      // tile position of the target
+    uint8_t body;   // Body1 of U^dag
+    int8_t gk;      // GenKind, G_NONE: no gradient
+    uint8_t pad;
+    int32_t slot;   // accumulator slot of a gradient step
+    uint32_t in_mask, in_val;    // controls inside the tile
+    uint64_t out_mask, out_val;  // controls outside the tile (state bits)
+    DF u[8];
+    DF g[8];
+};
+
+template <class I> struct AdjBlockParams {
+    Holes holes;
+    I ntiles;
+    int k, m;
+    int nsteps, nslots, nb;
+    I hi_off[64];
+    double2 *ket;
+    double2 *bras[kAdjBlockBras];
+    double *partials;  // [gridDim.x][nslots][nb]
+    AStep steps[kAdjBlockSteps];
+};
+
+__device__ __forceinline__ void adj_cp_async16(void *smem_dst, const void *gsrc) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(static_cast<uint32_t>(__cvta_generic_to_shared(smem_dst))),
+                 "l"(gsrc)
+                 : "memory");
+}
+
+// Im(conj(b) G k) over the pair, G by kind.
+template <int GK>
+__device__ __forceinline__ DF gexp_df(const DF *g, const DF (&b)[4], const DF (&k)[4]) {
+    // b = (b0r, b0i, b1r, b1i), k likewise
+    if constexpr (GK == G_Z)
+        return df_sum<4>({df_mul(b[0], k[1]), df_neg(df_mul(b[1], k[0])), df_neg(df_mul(b[2], k[3])), df_mul(b[3], k[2])});
+    else if constexpr (GK == G_X)
+        return df_sum<4>({df_mul(b[0], k[3]), df_neg(df_mul(b[1], k[2])), df_mul(b[2], k[1]), df_neg(df_mul(b[3], k[0]))});
+    else if constexpr (GK == G_Y)
+        return df_sum<4>({df_mul(b[2], k[0]), df_mul(b[3], k[1]), df_neg(df_mul(b[0], k[2])), df_neg(df_mul(b[1], k[3]))});
+    else if constexpr (GK == G_P1)
+        return df_sum<2>({df_mul(b[2], k[3]), df_neg(df_mul(b[3], k[2]))});
+    else {
+        // y = G k, then Im(conj(b0) y0 + conj(b1) y1)
+        const DF y0r = df_sum<4>({df_mul(g[0], k[0]), df_neg(df_mul(g[1], k[1])), df_mul(g[2], k[2]), df_neg(df_mul(g[3], k[3]))});
+        const DF y0i = df_sum<4>({df_mul(g[0], k[1]), df_mul(g[1], k[0]), df_mul(g[2], k[3]), df_mul(g[3], k[2])});
+        const DF y1r = df_sum<4>({df_mul(g[4], k[0]), df_neg(df_mul(g[5], k[1])), df_mul(g[6], k[2]), df_neg(df_mul(g[7], k[3]))});
+        const DF y1i = df_sum<4>({df_mul(g[4], k[1]), df_mul(g[5], k[0]), df_mul(g[6], k[3]), df_mul(g[7], k[2])});
+        return df_sum<4>({df_mul(b[0], y0i), df_neg(df_mul(b[1], y0r)), df_mul(b[2], y1i), df_neg(df_mul(b[3], y1r))});
+    }
+}
+
+__device__ __forceinline__ DF df_shfl_xor(DF v, int o) {
+    return DF{__shfl_xor_sync(0xffffffffu, v.hi, o), __shfl_xor_sync(0xffffffffu, v.lo, o)};
+}
+
+// One step on the tile: the pairs (e0, e0 | 1 << q) with the in-tile controls
+// set.  BODY / GK at compile time (G_NONE: U^dag only).
+template <int BODY, int GK, int NB>
+__device__ __forceinline__ void adj_block_step(float4 *kt, float4 *const (&bt)[kAdjBlockBras], int E, const AStep &st,
+                                               DF (&acc)[kAdjBlockBras]) {
+    DF u[8], g[8];
+#pragma unroll
+    for (int i = 0; i < 8; i++) u[i] = st.u[i];
+    if constexpr (GK == G_DENSE) {
+#pragma unroll
+        for (int i = 0; i < 8; i++) g[i] = st.g[i];
+    }
+    const uint32_t holes = st.in_mask | (1u << st.q);
+    const int nfree = E >> __popc(holes);
+    PairWalk w(holes, threadIdx.x, kAdjBlockThreads);
+    for (int f = threadIdx.x; f < nfree; f += kAdjBlockThreads) {
+        const int e0 = int(w.x | st.in_val);
+        const int e1 = e0 | (1 << st.q);
+        w.step();
+        const int s0 = swz<double>(e0), s1 = swz<double>(e1);
+        const float4 ka = kt[s0], kb = kt[s1];
+        DF kv[4] = {DF{ka.x, ka.y}, DF{ka.z, ka.w}, DF{kb.x, kb.y}, DF{kb.z, kb.w}};
+#pragma unroll
+        for (int b = 0; b < NB; b++) {
+            const float4 ba = bt[b][s0], bb = bt[b][s1];
+            DF bv[4] = {DF{ba.x, ba.y}, DF{ba.z, ba.w}, DF{bb.x, bb.y}, DF{bb.z, bb.w}};
+            if constexpr (GK != G_NONE) acc[b] = df_sum<2>({acc[b], gexp_df<GK>(g, bv, kv)});
+            body1_dfv<BODY>(u, bv[0], bv[1], bv[2], bv[3]);
+            bt[b][s0] = make_float4(bv[0].hi, bv[0].lo, bv[1].hi, bv[1].lo);
+            bt[b][s1] = make_float4(bv[2].hi, bv[2].lo, bv[3].hi, bv[3].lo);
+        }
+        body1_dfv<BODY>(u, kv[0], kv[1], kv[2], kv[3]);
+        kt[s0] = make_float4(kv[0].hi, kv[0].lo, kv[1].hi, kv[1].lo);
+        kt[s1] = make_float4(kv[2].hi, kv[2].lo, kv[3].hi, kv[3].lo);
+    }
+}
+
+template <int NB>
+__device__ __forceinline__ void adj_block_dispatch(float4 *kt, float4 *const (&bt)[kAdjBlockBras], int E,
+                                                   const AStep &st, DF (&acc)[kAdjBlockBras]) {
+    switch (st.gk) {
+    case G_NONE:
+        switch (st.body) {
+        case B_DIAG: adj_block_step<B_DIAG, G_NONE, NB>(kt, bt, E, st, acc); break;
+        case B_PERM: adj_block_step<B_PERM, G_NONE, NB>(kt, bt, E, st, acc); break;
+        case B_ANTIDIAG: adj_block_step<B_ANTIDIAG, G_NONE, NB>(kt, bt, E, st, acc); break;
+        case B_REAL: adj_block_step<B_REAL, G_NONE, NB>(kt, bt, E, st, acc); break;
+        case B_RXLIKE: adj_block_step<B_RXLIKE, G_NONE, NB>(kt, bt, E, st, acc); break;
+        default: adj_block_step<B_DENSE, G_NONE, NB>(kt, bt, E, st, acc); break;
+        }
+        break;
+    case G_X:  // RX-like rotations
+        if (st.body == B_RXLIKE) adj_block_step<B_RXLIKE, G_X, NB>(kt, bt, E, st, acc);
+        else adj_block_step<B_DENSE, G_X, NB>(kt, bt, E, st, acc);
+        break;
+    case G_Y:  // RY: real rotation
+        if (st.body == B_REAL) adj_block_step<B_REAL, G_Y, NB>(kt, bt, E, st, acc);
+        else adj_block_step<B_DENSE, G_Y, NB>(kt, bt, E, st, acc);
+        break;
+    case G_Z:  // RZ: diagonal
+        if (st.body == B_DIAG) adj_block_step<B_DIAG, G_Z, NB>(kt, bt, E, st, acc);
+        else adj_block_step<B_DENSE, G_Z, NB>(kt, bt, E, st, acc);
+        break;
+    case G_P1:  // PhaseShift: diagonal
+        if (st.body == B_DIAG) adj_block_step<B_DIAG, G_P1, NB>(kt, bt, E, st, acc);
+        else adj_block_step<B_DENSE, G_P1, NB>(kt, bt, E, st, acc);
+        break;
+    default: adj_block_step<B_DENSE, G_DENSE, NB>(kt, bt, E, st, acc); break;
+    }
+}
+
+template <class I, int NB>
+__global__ void __launch_bounds__(kAdjBlockThreads, 2) adjoint_block_kernel(const AdjBlockParams<I> p) {
+    extern __shared__ __align__(128) unsigned char adj_smem[];
+    const int E = 1 << p.k;
+    float4 *kt = reinterpret_cast<float4 *>(adj_smem);
+    float4 *bt[kAdjBlockBras];
+#pragma unroll
+    for (int b = 0; b < kAdjBlockBras; b++) bt[b] = kt + size_t(b + 1) * E;
+    constexpr int W = kAdjBlockThreads / 32;
+    DF *wacc = reinterpret_cast<DF *>(kt + size_t(NB + 1) * E);  // [nslots][NB][W]
+    for (int i = threadIdx.x; i < p.nslots * NB * W; i += kAdjBlockThreads) wacc[i] = DF{0.0f, 0.0f};
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int lowmask = (1 << p.m) - 1;
+    __syncthreads();
+    for (I tau = blockIdx.x; tau < p.ntiles; tau += I(gridDim.x)) {
+        const I base = insert_holes<I>(tau, p.holes);
+        for (int e = threadIdx.x; e < E; e += kAdjBlockThreads) {
+            const I gi = base + p.hi_off[e >> p.m] + I(e & lowmask);
+            adj_cp_async16(&kt[swz<double>(e)], &p.ket[gi]);
+#pragma unroll
+            for (int b = 0; b < NB; b++) adj_cp_async16(&bt[b][swz<double>(e)], &p.bras[b][gi]);
+        }
+        asm volatile("cp.async.commit_group;" ::: "memory");
+        asm volatile("cp.async.wait_group 0;" ::: "memory");
+        __syncthreads();
+        // complex128 -> float-float in place (same 16 bytes per amplitude)
+        for (int e = threadIdx.x; e < E * (NB + 1); e += kAdjBlockThreads) {
+            const double2 v = reinterpret_cast<const double2 *>(kt)[e];
+            const DF r = df_from_double(v.x), i = df_from_double(v.y);
+            kt[e] = make_float4(r.hi, r.lo, i.hi, i.lo);
+        }
+        __syncthreads();
+        for (int si = 0; si < p.nsteps; si++) {
+            const AStep &st = p.steps[si];
+            if ((uint64_t(base) & st.out_mask) != st.out_val) continue;  // tile-uniform
+            DF acc[kAdjBlockBras];
+#pragma unroll
+            for (int b = 0; b < kAdjBlockBras; b++) acc[b] = DF{0.0f, 0.0f};
+            adj_block_dispatch<NB>(kt, bt, E, st, acc);
+            if (st.gk != G_NONE) {
+#pragma unroll
+                for (int b = 0; b < NB; b++) {
+                    DF v = acc[b];
+#pragma unroll
+                    for (int o = 16; o > 0; o >>= 1) v = df_sum<2>({v, df_shfl_xor(v, o)});
+                    if (lane == 0) {
+                        DF &slot = wacc[(st.slot * NB + b) * W + warp];
+                        slot = df_sum<2>({slot, v});
+                    }
+                }
+            }
+            __syncthreads();
+        }
+        // float-float -> complex128, streamed out
+        for (int e = threadIdx.x; e < E; e += kAdjBlockThreads) {
+            const I gi = base + p.hi_off[e >> p.m] + I(e & lowmask);
+            const float4 v = kt[swz<double>(e)];
+            __stcs(&p.ket[gi], make_double2(df_to_double(DF{v.x, v.y}), df_to_double(DF{v.z, v.w})));
+#pragma unroll
+            for (int b = 0; b < NB; b++) {
+                const float4 x = bt[b][swz<double>(e)];
+                __stcs(&p.bras[b][gi], make_double2(df_to_double(DF{x.x, x.y}), df_to_double(DF{x.z, x.w})));
+            }
+        }
+        __syncthreads();
+    }
+    // per CTA: the warps' sums in warp order
+    for (int i = threadIdx.x; i < p.nslots * NB; i += kAdjBlockThreads) {
+        DF t = wacc[i * W];
+        for (int w = 1; w < W; w++) t = df_sum<2>({t, wacc[i * W + w]});
+        p.partials[size_t(blockIdx.x) * p.nslots * NB + i] = df_to_double(t);
+    }
+}
+
+// jac[col[s] * stride + b] = sum over CTAs (in CTA order) of the partials.
+__global__ void adjoint_block_reduce(const double *__restrict__ partials, int nctas, int nslots, int nb,
+                                     const int *__restrict__ cols, double *__restrict__ jac, int stride) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nslots * nb) return;
+    double t = 0.0;
+    for (int c = 0; c < nctas; c++) t += partials[size_t(c) * nslots * nb + i];
+    jac[size_t(cols[i / nb]) * stride + (i % nb)] = t;
+}
+
+template <class I>
+static lgpu_status_t adjoint_block_t(lgpu_context_t ctx, void *ket, void *const *bras, uint32_t nbras, uint32_t n,
+                                     const std::vector<int> &tile_bits, const lgpu_adj_block_step_t *steps,
+                                     uint32_t nsteps, double *jac, uint32_t stride, cudaStream_t s) {
+    const int k = int(tile_bits.size());
+    std::vector<int> pos(n, -1);
+    for (int q = 0; q < k; q++) pos[size_t(tile_bits[size_t(q)])] = q;
+    int m = 0;
+    while (m < k && tile_bits[size_t(m)] == m) m++;
+    if (k - m > 6) return fail(LGPU_ERR_INVALID_ARG, "adjoint block: at most 6 tile bits above the low run");
+    auto *p = new AdjBlockParams<I>();
+    std::unique_ptr<AdjBlockParams<I>> guard(p);
+    p->holes = make_holes(tile_bits);
+    p->ntiles = I(uint64_t(1) << (n - uint32_t(k)));
+    p->k = k;
+    p->m = m;
+    p->nb = int(nbras);
+    for (int h = 0; h < (1 << (k - m)); h++) {
+        uint64_t o = 0;
+        for (int q = m; q < k; q++)
+            if ((h >> (q - m)) & 1) o |= uint64_t(1) << tile_bits[size_t(q)];
+        p->hi_off[h] = I(o);
+    }
+    p->ket = static_cast<double2 *>(ket);
+    for (uint32_t b = 0; b < nbras; b++) p->bras[b] = static_cast<double2 *>(bras[b]);
+    std::vector<int> cols;
+    p->nsteps = int(nsteps);
+    for (uint32_t i = 0; i < nsteps; i++) {
+        const lgpu_adj_block_step_t &a = steps[i];
+        AStep &st = p->steps[i];
+        st = AStep{};
+        if (a.tgt < 0 || uint32_t(a.tgt) >= n || pos[size_t(a.tgt)] < 0)
+            return fail(LGPU_ERR_INVALID_ARG, "adjoint block: target outside the tile");
+        st.q = uint8_t(pos[size_t(a.tgt)]);
+        if (a.nctrl < 0 || a.nctrl > 2) return fail(LGPU_ERR_INVALID_ARG, "adjoint block: at most 2 controls");
+        for (int c = 0; c < a.nctrl; c++) {
+            const int b = a.ctrl[c];
+            if (b < 0 || uint32_t(b) >= n || b == a.tgt) return fail(LGPU_ERR_INVALID_ARG, "adjoint block: bad control");
+            const uint32_t v = a.ctrl_val[c] ? 1u : 0u;
+            if (pos[size_t(b)] >= 0) {
+                st.in_mask |= 1u << pos[size_t(b)];
+                st.in_val |= v << pos[size_t(b)];
+            } else {
+                st.out_mask |= uint64_t(1) << b;
+                st.out_val |= uint64_t(v) << b;
+            }
+        }
+        KConst kc[4];
+        st.body = uint8_t(body_of_2x2_host(a.u, kc));
+        for (int e = 0; e < 8; e++) {
+            st.u[e] = df_split_host(a.u[e]);
+            st.g[e] = df_split_host(a.g[e]);
+        }
+        if (a.gen_kind < 0) {
+            st.gk = int8_t(G_NONE);
+            st.slot = -1;
+        } else {
+            if (a.col < 0) return fail(LGPU_ERR_INVALID_ARG, "adjoint block: negative Jacobian column");
+            const int gkd = gen_kind(a.g);
+            st.gk = int8_t(gkd == G_NONE ? G_DENSE : gkd);
+            st.slot = int32_t(cols.size());
+            cols.push_back(a.col);
+        }
+    }
+    p->nslots = int(cols.size());
+    const size_t tile_bytes = (size_t(1) << k) * 16;
+    const size_t smem = (nbras + 1) * tile_bytes + size_t(std::max(p->nslots, 1)) * nbras * 8 * sizeof(DF);
+    const int per_sm = std::max(1, std::min(2, int((220 * 1024) / smem)));
+    const unsigned grid = unsigned(std::min<uint64_t>(uint64_t(p->ntiles), uint64_t(sm_count()) * per_sm));
+    // scratch: [reduction counter, 256 B, untouched][columns][partials]
+    const size_t cbytes = (sizeof(int) * std::max<size_t>(cols.size(), 1) + 255) & ~size_t(255);
+    const size_t pbytes = sizeof(double) * size_t(grid) * std::max(p->nslots, 1) * nbras;
+    void *scr = nullptr;
+    LGPU_TRY(ctx_scratch(ctx, 256 + cbytes + pbytes, &scr));
+    int *dcols = reinterpret_cast<int *>(static_cast<char *>(scr) + 256);
+    p->partials = reinterpret_cast<double *>(static_cast<char *>(scr) + 256 + cbytes);
+    if (!cols.empty()) {
+        LGPU_CUDA_TRY(cudaMemcpyAsync(dcols, cols.data(), sizeof(int) * cols.size(), cudaMemcpyHostToDevice, s));
+        LGPU_CUDA_TRY(cudaStreamSynchronize(s));  // the pageable source must outlive the copy
+    }
+    static std::atomic<size_t> attr1[64], attr2[64];
+    if (nbras == 1) {
+        LGPU_TRY(ensure_smem(reinterpret_cast<const void *>(adjoint_block_kernel<I, 1>), smem, attr1));
+        adjoint_block_kernel<I, 1><<<grid, kAdjBlockThreads, smem, s>>>(*p);
+    } else {
+        LGPU_TRY(ensure_smem(reinterpret_cast<const void *>(adjoint_block_kernel<I, 2>), smem, attr2));
+        adjoint_block_kernel<I, 2><<<grid, kAdjBlockThreads, smem, s>>>(*p);
+    }
+    LGPU_CHECK_LAUNCH();
+    if (!cols.empty()) {
+        const int total = p->nslots * int(nbras);
+        adjoint_block_reduce<<<(total + 127) / 128, 128, 0, s>>>(p->partials, int(grid), p->nslots, int(nbras), dcols,
+                                                                 jac, int(stride));
+        LGPU_CHECK_LAUNCH();
+    }
+    return LGPU_OK;
+}
+
 }  // namespace lgpu
 
 using namespace lgpu;
@@ -659,6 +985,29 @@ lgpu_status_t lgpu_adjoint_step(lgpu_context_t ctx, void *ket, void *const *bras
                    : adjoint_dispatch<float, uint64_t>(ctx, ket, bras, nbras, n, b, gen, udag, apply_udag, out_dev, s);
 }
 
+
+lgpu_status_t lgpu_adjoint_block(lgpu_context_t ctx, void *ket, void *const *bras, uint32_t nbras, uint32_t n,
+                                 lgpu_dtype_t dt, uint32_t k, const int32_t *tile_bits,
+                                 const lgpu_adj_block_step_t *steps, uint32_t nsteps, double *jac_dev,
+                                 uint32_t jac_stride, lgpu_stream_t stream) {
+    if (dt != LGPU_C128) return fail(LGPU_ERR_INVALID_ARG, "adjoint block: complex128 only");
+    LGPU_TRY(check_state(ket, n, dt));
+    if (nbras < 1 || nbras > uint32_t(kAdjBlockBras) || !bras)
+        return fail(LGPU_ERR_INVALID_ARG, "adjoint block: 1 or 2 bras");
+    for (uint32_t b = 0; b < nbras; b++) LGPU_TRY(check_state(bras[b], n, dt));
+    if (nsteps == 0) return LGPU_OK;
+    if (!steps || nsteps > uint32_t(kAdjBlockSteps)) return fail(LGPU_ERR_INVALID_ARG, "adjoint block: 1 to 48 steps");
+    if (k < 1 || k > 11 || k > n) return fail(LGPU_ERR_INVALID_ARG, "adjoint block: tile of 1 to 11 bits");
+    if (!jac_dev || jac_stride < nbras) return fail(LGPU_ERR_INVALID_ARG, "adjoint block: Jacobian output");
+    std::vector<int> tb;
+    LGPU_TRY(check_bits(n, k, tile_bits, "tile", &tb));
+    std::sort(tb.begin(), tb.end());
+    if (std::adjacent_find(tb.begin(), tb.end()) != tb.end())
+        return fail(LGPU_ERR_INVALID_ARG, "tile bits must be distinct");
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    return n <= 32 ? adjoint_block_t<uint32_t>(ctx, ket, bras, nbras, n, tb, steps, nsteps, jac_dev, jac_stride, s)
+                   : adjoint_block_t<uint64_t>(ctx, ket, bras, nbras, n, tb, steps, nsteps, jac_dev, jac_stride, s);
+}
 
 uint32_t lgpu_adjoint_sweep_max_qubits(lgpu_dtype_t dt) { return dt == LGPU_C128 ? 12u : 13u; }
 

@@ -376,6 +376,44 @@ def test_adjoint_sweep_and_step_paths(native, oracle, dtype, n):
     assert np.max(np.abs(jac - ref)) < tol(dtype) * 50, np.max(np.abs(jac - ref))
 
 
+BLOCK_ADJ_OPS = ["RX", "RY", "RZ", "PhaseShift", "CRX", "CRY", "CRZ", "ControlledPhaseShift", "Hadamard", "S", "T",
+                 "CNOT", "CZ", "Toffoli", "IsingXX", "SingleExcitation"]
+
+
+@pytest.mark.parametrize("n,nobs", [(14, 1), (14, 2), (16, 1)])
+def test_adjoint_fused_blocks(native, oracle, n, nobs):
+    """complex128 states above the shared-memory sweep with one or two
+    observables run runs of 1-target operations (controls allowed) as fused
+    blocks in float-float arithmetic; non-1-target operations (IsingXX,
+    SingleExcitation) end a block and take the per-operation path.  Against
+    the oracle adjoint at 1e-10 x 50, with a trainable subset."""
+    rng = np.random.default_rng(1300 + n + nobs)
+    ops = [("Hadamard", [w], [], False) for w in range(n)]
+    nw = {"CRX": 2, "CRY": 2, "CRZ": 2, "ControlledPhaseShift": 2, "CNOT": 2, "CZ": 2, "Toffoli": 3, "IsingXX": 2,
+          "SingleExcitation": 2}
+    for _ in range(60):
+        name = BLOCK_ADJ_OPS[int(rng.integers(len(BLOCK_ADJ_OPS)))]
+        wires = [int(x) for x in rng.choice(n, size=nw.get(name, 1), replace=False)]
+        params = [float(rng.uniform(0, 2 * np.pi))] if name not in ("Hadamard", "S", "T", "CNOT", "CZ", "Toffoli") else []
+        ops.append((name, wires, params, bool(rng.integers(2)) and bool(params)))
+    nparam = sum(1 for o in ops if o[2])
+    tp = sorted(int(x) for x in rng.choice(nparam, size=min(24, nparam), replace=False))
+    obs_specs = [(True, [(0.6, [("PauliZ", [1], None)]), (-0.4, [("PauliX", [0], None), ("PauliY", [n - 1], None)])]),
+                 (False, [(1.0, [("PauliY", [3], None)])])][:nobs]
+    sv = native.LightningGPU_C128(n)
+    apply_ops(sv, ops)
+    adj = native.AdjointJacobianGPU_C128()
+    opsd = adj.create_ops_list([o[0] for o in ops], [np.array(o[2], np.float64) for o in ops], [o[1] for o in ops],
+                               [o[3] for o in ops], [np.zeros(0, np.complex128) for o in ops])
+    obs = [_obs_native(native, "c128", s) for s in obs_specs]
+    jac = np.asarray(adj.adjoint_jacobian(sv, obs, opsd, tp))
+    final = oracle.run(n, to_oracle_ops(ops))
+    oobs = [(s[0], [(c, [(nm, w, m) for nm, w, m in f]) for c, f in s[1]]) for s in obs_specs]
+    ref = oracle.adjoint_jacobian(final, to_oracle_ops(ops), oobs, tp)
+    assert np.max(np.abs(jac - ref)) < 1e-10 * 50, np.max(np.abs(jac - ref))
+    assert np.max(np.abs(ref)) > 1e-3  # the circuit has gradients to compare
+
+
 @pytest.mark.parametrize("dtype", DTYPES)
 def test_adjoint_rejects_multiparam(native, dtype):
     suf = "C128" if dtype == "c128" else "C64"
