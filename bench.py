@@ -526,7 +526,9 @@ def profile_case(name):
     fused (25-qubit complex64, one layer of RX/RY/RZ on every wire + CNOT
     ring), batch (304 circuits of 17 qubits, complex64), pauli (26-qubit
     complex64, 24 random Pauli words + sum_i Z_i), adjoint (12-qubit
-    complex128, 4 layers, 12 PauliZ observables)."""
+    complex128, 4 layers, 12 PauliZ observables), adjblock (24-qubit
+    complex128, 2 layers of RY, RZ + CZ ladder, one PauliZ observable: the
+    fused adjoint blocks)."""
     import pennylane_lightning_gpu_gb300 as pkg
     from pennylane_lightning_gpu_gb300 import batched, workloads
 
@@ -563,6 +565,17 @@ def profile_case(name):
                                    [np.zeros(0, np.complex128) for o in raw])
         obs = [m.NamedObsGPU_C128("PauliZ", [w]) for w in range(n)]
         adj.adjoint_jacobian(sv, obs, opsd, list(range(3 * n * 4)))
+    elif name == "adjblock":
+        n, layers = 24, 2
+        raw = workloads.ry_rz_cz_ansatz(n, layers, np.random.default_rng(3))
+        sv = m.LightningGPU_C128(n)
+        sv.apply([o[0] for o in raw], [list(o[1]) for o in raw], [False] * len(raw), [list(o[2]) for o in raw])
+        adj = m.AdjointJacobianGPU_C128()
+        opsd = adj.create_ops_list([o[0] for o in raw], [np.array(o[2], np.float64) for o in raw],
+                                   [list(o[1]) for o in raw], [False] * len(raw),
+                                   [np.zeros(0, np.complex128) for o in raw])
+        obs = [m.NamedObsGPU_C128("PauliZ", [1])]
+        adj.adjoint_jacobian(sv, obs, opsd, list(range(2 * n * layers)))
     print(json.dumps({"case": name, "ok": True}))
 
 
@@ -579,7 +592,7 @@ def main():
     ap.add_argument("--no-circuits", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-serving", action="store_true")
-    ap.add_argument("--case", choices=["fused", "batch", "pauli", "adjoint"], default=None,
+    ap.add_argument("--case", choices=["fused", "batch", "pauli", "adjoint", "adjblock"], default=None,
                     help="run one small secondary-kernel case (profiling) and exit")
     ap.add_argument("--only", choices=["batched", "serving", "circuits"], default=None,
                     help="run one section alone (profiling runs); the default prints the full line")
