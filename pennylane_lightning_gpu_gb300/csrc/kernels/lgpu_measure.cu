@@ -9,6 +9,8 @@
 //  * sampling: FP64 chunk sums -> single-CTA exclusive scan -> one warp per
 //    draw searches its chunk with a warp prefix sum
 //  * sum_t c_t P_t |psi> (Hamiltonian apply) and CSR sparse products
+#include "lgpu_bodies.cuh"
+#include "lgpu_df64.cuh"
 #include "lgpu_internal.cuh"
 #include "lgpu_reduce.cuh"
 
@@ -405,10 +407,301 @@ static lgpu_status_t wht_dispatch(const PauliWhtParams<T, I> &b, unsigned g, dou
     }
 }
 
+// ---------------------------------------------------------------------------
+// Tiled Pauli-word passes: words with different flip masks in one pass.
+// A tile is 2^k amplitudes (the low run 0..m-1 of state bits plus up to 6
+// high bits, as the fused gate blocks); every word of the pass flips only
+// tile bits, so each pair (x, x ^ flip) lies in one tile.  A CTA streams
+// tiles through two shared-memory buffers (cp.async); per word each thread
+// sums (-1)^popc(x & sign) * (|a_x|^2, or Re / Im of conj(a_x) a_{x^flip} over
+// the x with the lowest flip bit clear), complex64 in float per tile,
+// complex128 in float-float on the tile converted once after the load (no
+// FP64 instruction per pair).  Warp sums go to per-warp double slots in
+// shared memory; a CTA writes its totals and a second kernel sums the CTAs in
+// a fixed order.  The raw sums equal those of the Walsh-Hadamard pass.
+// ---------------------------------------------------------------------------
+constexpr int kTileWords = 32;
+constexpr int kPauliTileThreads = 256;
+
+template <class I> struct PauliTileParams {
+    const void *sv;
+    Holes holes;
+    I ntiles;
+    int k, m, nw;
+    I hi_off[64];
+    uint32_t tflip[kTileWords];  // flip mask in tile positions (0: diagonal word)
+    uint32_t tsign[kTileWords];  // sign mask in tile positions
+    uint64_t osign[kTileWords];  // sign mask outside the tile (state bits)
+    uint32_t use_im;             // bit t: word t sums Im(conj(a_x) a_{x^flip})
+    double *partials;            // [gridDim.x][nw]
+};
+
+template <class T> struct TileAcc;
+template <> struct TileAcc<float> {
+    float v = 0.0f;
+    __device__ __forceinline__ void add(float x) { v += x; }
+    __device__ __forceinline__ void warp_reduce() {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    }
+    __device__ __forceinline__ double value() const { return double(v); }
+};
+template <> struct TileAcc<double> {
+    DF v{0.0f, 0.0f};
+    __device__ __forceinline__ void add(DF x) { v = df_sum<2>({v, x}); }
+    __device__ __forceinline__ void warp_reduce() {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+            v = df_sum<2>({v, DF{__shfl_xor_sync(0xffffffffu, v.hi, o), __shfl_xor_sync(0xffffffffu, v.lo, o)}});
+    }
+    __device__ __forceinline__ double value() const { return df_to_double(v); }
+};
+
+__device__ __forceinline__ void pt_cp_async16(void *smem_dst, const void *gsrc) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(static_cast<uint32_t>(__cvta_generic_to_shared(smem_dst))),
+                 "l"(gsrc)
+                 : "memory");
+}
+
+template <class T, class I>
+__global__ void __launch_bounds__(kPauliTileThreads, 3) pauli_tile_kernel(const PauliTileParams<I> p) {
+    using C = cplx_t<T>;
+    extern __shared__ __align__(128) unsigned char pt_smem[];
+    const int E = 1 << p.k;
+    C *buf[2] = {reinterpret_cast<C *>(pt_smem), reinterpret_cast<C *>(pt_smem) + E};
+    constexpr int W = kPauliTileThreads / 32;
+    double *slot = reinterpret_cast<double *>(reinterpret_cast<C *>(pt_smem) + 2 * E);  // [nw][W]
+    for (int i = threadIdx.x; i < p.nw * W; i += kPauliTileThreads) slot[i] = 0.0;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int lowmask = (1 << p.m) - 1;
+    const C *sv = static_cast<const C *>(p.sv);
+    constexpr int EPC = sizeof(C) == 8 ? 2 : 1;  // amplitudes per 16-byte chunk (m >= 1)
+    auto load = [&](I tau, C *dst) {
+        const I base = insert_holes<I>(tau, p.holes);
+        for (int c = threadIdx.x; c < E / EPC; c += kPauliTileThreads) {
+            const int e = c * EPC;
+            pt_cp_async16(&dst[swz<T>(e)], &sv[base + p.hi_off[e >> p.m] + I(e & lowmask)]);
+        }
+        asm volatile("cp.async.commit_group;" ::: "memory");
+    };
+    const I G = I(gridDim.x);
+    I tau = blockIdx.x;
+    if (tau < p.ntiles) load(tau, buf[0]);
+    else asm volatile("cp.async.commit_group;" ::: "memory");
+    __syncthreads();
+    for (int it = 0; tau < p.ntiles; tau += G, it++) {
+        C *cur = buf[it & 1];
+        if (tau + G < p.ntiles) load(tau + G, buf[(it + 1) & 1]);
+        else asm volatile("cp.async.commit_group;" ::: "memory");
+        asm volatile("cp.async.wait_group 1;" ::: "memory");
+        __syncthreads();
+        if constexpr (sizeof(T) == 8) {  // complex128 -> float-float in place
+            for (int e = threadIdx.x; e < E; e += kPauliTileThreads) {
+                const double2 v = reinterpret_cast<const double2 *>(cur)[e];
+                const DF r = df_from_double(v.x), im = df_from_double(v.y);
+                reinterpret_cast<float4 *>(cur)[e] = make_float4(r.hi, r.lo, im.hi, im.lo);
+            }
+            __syncthreads();
+        }
+        const I base = insert_holes<I>(tau, p.holes);
+        for (int t = 0; t < p.nw; t++) {
+            const uint32_t f = p.tflip[t], sg = p.tsign[t];
+            const bool neg0 = (__popcll(uint64_t(base) & p.osign[t]) & 1) != 0;
+            const bool im = (p.use_im >> t) & 1u;
+            TileAcc<T> acc;
+            if (f == 0) {
+                for (int e = threadIdx.x; e < E; e += kPauliTileThreads) {
+                    const bool neg = __popc(uint32_t(e) & sg) & 1;
+                    if constexpr (sizeof(T) == 4) {
+                        const C a = cur[swz<T>(e)];
+                        const float q = fmaf(a.x, a.x, a.y * a.y);
+                        acc.add(neg ? -q : q);
+                    } else {
+                        const float4 a = reinterpret_cast<const float4 *>(cur)[swz<T>(e)];
+                        const DF r{a.x, a.y}, i{a.z, a.w};
+                        DF q = df_sum<2>({df_mul(r, r), df_mul(i, i)});
+                        acc.add(neg ? df_neg(q) : q);
+                    }
+                }
+            } else {
+                const uint32_t low = f & (0u - f);  // lowest flip bit: pairs from its clear half
+                PairWalk w(low, threadIdx.x, kPauliTileThreads);
+                for (int c = threadIdx.x; c < (E >> 1); c += kPauliTileThreads) {
+                    const int e0 = int(w.x), e1 = int(w.x ^ f);
+                    w.step();
+                    const bool neg = __popc(uint32_t(e0) & sg) & 1;
+                    if constexpr (sizeof(T) == 4) {
+                        const C a = cur[swz<T>(e0)], b = cur[swz<T>(e1)];
+                        const float q = im ? fmaf(a.x, b.y, -a.y * b.x) : fmaf(a.x, b.x, a.y * b.y);
+                        acc.add(neg ? -q : q);
+                    } else {
+                        const float4 a4 = reinterpret_cast<const float4 *>(cur)[swz<T>(e0)];
+                        const float4 b4 = reinterpret_cast<const float4 *>(cur)[swz<T>(e1)];
+                        const DF ar{a4.x, a4.y}, ai{a4.z, a4.w}, br{b4.x, b4.y}, bi{b4.z, b4.w};
+                        const DF q = im ? df_sum<2>({df_mul(ar, bi), df_neg(df_mul(ai, br))})
+                                        : df_sum<2>({df_mul(ar, br), df_mul(ai, bi)});
+                        acc.add(neg ? df_neg(q) : q);
+                    }
+                }
+            }
+            acc.warp_reduce();
+            if (lane == 0) {
+                const double v = acc.value();
+                slot[t * W + warp] += neg0 ? -v : v;
+            }
+        }
+        __syncthreads();  // `cur` is the target of a load issued next iteration
+    }
+    asm volatile("cp.async.wait_group 0;" ::: "memory");
+    __syncthreads();
+    for (int t = threadIdx.x; t < p.nw; t += kPauliTileThreads) {
+        double v = 0.0;
+        for (int w = 0; w < W; w++) v += slot[t * W + w];
+        p.partials[size_t(blockIdx.x) * p.nw + t] = v;
+    }
+}
+
+// out[t] = sum over CTAs (in CTA order) of the partials.
+__global__ void pauli_tile_reduce(const double *__restrict__ partials, int nctas, int nw, double *__restrict__ out) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nw) return;
+    double v = 0.0;
+    for (int c = 0; c < nctas; c++) v += partials[size_t(c) * nw + t];
+    out[t] = v;
+}
+
+// Group words into tile passes: a word joins the first pass whose tile can
+// also hold its flip bits (low run >= 5 bits, <= 6 high bits, <= kmax bits).
+struct TilePass {
+    std::vector<int> tile;
+    std::vector<uint32_t> words;
+};
+static std::vector<TilePass> plan_tile_passes(uint32_t n, uint32_t nwords, const uint64_t *flip, int kmax) {
+    std::vector<TilePass> passes;
+    std::vector<uint64_t> unions;
+    auto tile_of = [&](uint64_t mask, std::vector<int> &tile) {
+        for (int m = std::min<int>(kmax, int(n)); m >= std::min<int>(5, kmax); m--) {
+            std::vector<int> hi;
+            for (int b = m; b < int(n); b++)
+                if ((mask >> b) & 1u) hi.push_back(b);
+            if (int(hi.size()) <= kmax - m && hi.size() <= 6) {
+                tile.clear();
+                for (int b = 0; b < m; b++) tile.push_back(b);
+                tile.insert(tile.end(), hi.begin(), hi.end());
+                return true;
+            }
+        }
+        return false;
+    };
+    for (uint32_t w = 0; w < nwords; w++) {
+        bool placed = false;
+        for (size_t pi = 0; pi < passes.size() && !placed; pi++) {
+            if (passes[pi].words.size() >= size_t(kTileWords)) continue;
+            std::vector<int> t;
+            if (tile_of(unions[pi] | flip[w], t)) {
+                unions[pi] |= flip[w];
+                passes[pi].tile = t;
+                passes[pi].words.push_back(w);
+                placed = true;
+            }
+        }
+        if (!placed) {
+            TilePass tp;
+            if (!tile_of(flip[w], tp.tile)) continue;  // flips too many bits: left to the caller
+            tp.words.push_back(w);
+            passes.push_back(tp);
+            unions.push_back(flip[w]);
+        }
+    }
+    return passes;
+}
+
+// Raw sums of the words (as the Walsh-Hadamard pass defines them) by tile
+// passes; done[w] = 0 for the words whose flip mask fits no tile.
+template <class T, class I>
+static lgpu_status_t pauli_tile_raw(lgpu_context_t ctx, const void *sv, uint32_t n, uint32_t nwords,
+                                    const uint64_t *flip, const uint64_t *sign, std::vector<double> &raw,
+                                    std::vector<char> &done, cudaStream_t s) {
+    done.assign(nwords, 0);
+    raw.assign(nwords, 0.0);
+    const int kmax = sizeof(T) == 4 ? 12 : 11;  // 32 KB tiles, two per CTA, three CTAs per SM
+    const auto passes = plan_tile_passes(n, nwords, flip, kmax);
+    if (passes.empty()) return LGPU_OK;
+    const unsigned sms = unsigned(sm_count());
+    size_t maxk = 0;
+    for (const auto &tp : passes) maxk = std::max(maxk, tp.tile.size());
+    const unsigned grid_cap = sms * 3;
+    void *scr = nullptr;
+    const size_t pbytes = sizeof(double) * size_t(grid_cap) * kTileWords;
+    const size_t rbytes = sizeof(double) * passes.size() * kTileWords;
+    LGPU_TRY(ctx_scratch(ctx, 256 + pbytes + rbytes, &scr));
+    double *partials = reinterpret_cast<double *>(static_cast<char *>(scr) + 256);
+    double *results = reinterpret_cast<double *>(static_cast<char *>(scr) + 256 + pbytes);
+    static std::atomic<size_t> attr[64];
+    for (size_t pi = 0; pi < passes.size(); pi++) {
+        const TilePass &tp = passes[pi];
+        const int k = int(tp.tile.size());
+        std::vector<int> pos(n, -1);
+        for (int q = 0; q < k; q++) pos[size_t(tp.tile[size_t(q)])] = q;
+        int m = 0;
+        while (m < k && tp.tile[size_t(m)] == m) m++;
+        PauliTileParams<I> b{};
+        b.sv = sv;
+        b.holes = make_holes(tp.tile);
+        b.ntiles = I(uint64_t(1) << (n - uint32_t(k)));
+        b.k = k;
+        b.m = m;
+        b.nw = int(tp.words.size());
+        for (int h = 0; h < (1 << (k - m)); h++) {
+            uint64_t o = 0;
+            for (int q = m; q < k; q++)
+                if ((h >> (q - m)) & 1) o |= uint64_t(1) << tp.tile[size_t(q)];
+            b.hi_off[h] = I(o);
+        }
+        for (int t = 0; t < b.nw; t++) {
+            const uint32_t w = tp.words[size_t(t)];
+            uint32_t tf = 0, ts = 0;
+            uint64_t os = sign[w];
+            for (int q = 0; q < k; q++) {
+                const int bit = tp.tile[size_t(q)];
+                if ((flip[w] >> bit) & 1u) tf |= 1u << q;
+                if ((sign[w] >> bit) & 1u) {
+                    ts |= 1u << q;
+                    os &= ~(uint64_t(1) << bit);
+                }
+            }
+            b.tflip[t] = tf;
+            b.tsign[t] = ts;
+            b.osign[t] = os;
+            if (flip[w] && (__builtin_popcountll(flip[w] & sign[w]) & 1)) b.use_im |= 1u << t;
+        }
+        const size_t smem = 2 * (size_t(1) << k) * sizeof(cplx_t<T>) + sizeof(double) * size_t(b.nw) * 8;
+        const unsigned grid = unsigned(std::min<uint64_t>(uint64_t(b.ntiles), grid_cap));
+        b.partials = partials;
+        LGPU_TRY(ensure_smem(reinterpret_cast<const void *>(pauli_tile_kernel<T, I>), smem, attr));
+        pauli_tile_kernel<T, I><<<grid, kPauliTileThreads, smem, s>>>(b);
+        LGPU_CHECK_LAUNCH();
+        pauli_tile_reduce<<<1, kTileWords, 0, s>>>(partials, int(grid), b.nw, results + pi * kTileWords);
+        LGPU_CHECK_LAUNCH();
+    }
+    std::vector<double> host(passes.size() * kTileWords);
+    void *pin = nullptr;
+    LGPU_TRY(ctx_pinned(ctx, rbytes, &pin));
+    LGPU_CUDA_TRY(cudaMemcpyAsync(pin, results, rbytes, cudaMemcpyDeviceToHost, s));
+    LGPU_CUDA_TRY(cudaStreamSynchronize(s));
+    std::memcpy(host.data(), pin, rbytes);
+    for (size_t pi = 0; pi < passes.size(); pi++)
+        for (size_t t = 0; t < passes[pi].words.size(); t++) {
+            raw[passes[pi].words[t]] = host[pi * kTileWords + t];
+            done[passes[pi].words[t]] = 1;
+        }
+    return LGPU_OK;
+}
+
 template <class T, class I>
 static lgpu_status_t pauli_words_t(lgpu_context_t ctx, const void *sv, uint32_t n, uint32_t nwords,
                                    const uint64_t *flip, const uint64_t *sign, const uint8_t *ny, double *out,
-                                   int out_on_device, cudaStream_t s) {
+                                   int out_on_device, cudaStream_t s, bool tiles = true) {
     // Group words by flip mask (stable order of first appearance).
     std::vector<uint64_t> keys;
     std::vector<std::vector<uint32_t>> groups;
@@ -421,6 +714,53 @@ static lgpu_status_t pauli_words_t(lgpu_context_t ctx, const void *sv, uint32_t 
             groups.emplace_back();
         }
         groups[gi].push_back(w);
+    }
+    // Large states with several flip masks: tile passes hold words with
+    // different flip masks (one read of the state for several masks).
+    if (tiles && n >= 16 && keys.size() >= 2) {
+        std::vector<double> raw;
+        std::vector<char> done;
+        LGPU_TRY((pauli_tile_raw<T, I>(ctx, sv, n, nwords, flip, sign, raw, done, s)));
+        // words whose flips fit no tile: the flip-mask passes, as a subset
+        std::vector<uint32_t> rest;
+        for (uint32_t w = 0; w < nwords; w++)
+            if (!done[w]) rest.push_back(w);
+        {
+            std::vector<double> vals(nwords, 0.0);
+            if (!rest.empty()) {
+                std::vector<uint64_t> rf, rs;
+                std::vector<uint8_t> rn;
+                for (uint32_t w : rest) {
+                    rf.push_back(flip[w]);
+                    rs.push_back(sign[w]);
+                    rn.push_back(ny[w]);
+                }
+                std::vector<double> rv(rest.size());
+                LGPU_TRY((pauli_words_t<T, I>(ctx, sv, n, uint32_t(rest.size()), rf.data(), rs.data(), rn.data(),
+                                              rv.data(), 0, s, false)));
+                for (size_t i = 0; i < rest.size(); i++) vals[rest[i]] = rv[i];
+            }
+            for (uint32_t w = 0; w < nwords; w++) {
+                if (!done[w]) continue;
+                const bool kneg = (__builtin_popcountll(flip[w] & sign[w]) & 1) != 0;
+                const double x = (!flip[w] ? 1.0 : (kneg ? -2.0 : 2.0)) * raw[w];
+                const bool im = flip[w] && kneg;
+                const double vx = im ? 0.0 : x, vy = im ? x : 0.0;
+                switch (ny[w] & 3) {  // <P> = Re(i^ny * (vx + i vy))
+                case 0: vals[w] = vx; break;
+                case 1: vals[w] = -vy; break;
+                case 2: vals[w] = -vx; break;
+                default: vals[w] = vy; break;
+                }
+            }
+            if (out_on_device) {
+                LGPU_CUDA_TRY(cudaMemcpyAsync(out, vals.data(), nwords * sizeof(double), cudaMemcpyHostToDevice, s));
+                LGPU_CUDA_TRY(cudaStreamSynchronize(s));
+            } else {
+                std::memcpy(out, vals.data(), nwords * sizeof(double));
+            }
+            return LGPU_OK;
+        }
     }
     if (n >= 4) {
         // Walsh-Hadamard passes: up to kWhtWords words sharing one flip mask.

@@ -160,8 +160,12 @@ def test_named_observable_expval(native, oracle, dtype):
 
 
 @pytest.mark.parametrize("dtype", DTYPES)
-@pytest.mark.parametrize("n", [4, 9, 14])
+@pytest.mark.parametrize("n", [4, 9, 14, 16, 18])
 def test_pauli_words(native, oracle, dtype, n):
+    """Pauli-word sums and single words against the oracle.  From 16 qubits
+    words with different flip masks share tile passes; words flipping more
+    bits than a tile holds (the 8- and 9-letter X/Y words) take the flip-mask
+    passes in the same call."""
     from pennylane_lightning_gpu_gb300 import workloads
 
     rng = np.random.default_rng(300 + n)
@@ -169,6 +173,8 @@ def test_pauli_words(native, oracle, dtype, n):
     sv = make_sv(native, dtype, psi)
     ham = workloads.random_pauli_hamiltonian(n, 40, rng, max_wires=min(6, n))
     ham += [(0.5, "ZZ", [0, 1]), (-0.25, "ZZ", [1, 2]), (0.1, "XX", [0, 1]), (0.2, "XX", [0, 1]), (0.3, "I", [0])]
+    if n >= 9:
+        ham += [(0.4, "XYXYXYXY", list(range(8))), (-0.3, "YYXXZXYXY", list(range(n - 9, n)))]
     words = [h[1] for h in ham]
     wires = [h[2] for h in ham]
     coeffs = np.array([h[0] for h in ham], np.complex128)
