@@ -414,13 +414,14 @@ static lgpu_status_t wht_dispatch(const PauliWhtParams<T, I> &b, unsigned g, dou
 // tile bits, so each pair (x, x ^ flip) lies in one tile.  A CTA streams
 // tiles through two shared-memory buffers (cp.async); per word each thread
 // sums (-1)^popc(x & sign) * (|a_x|^2, or Re / Im of conj(a_x) a_{x^flip} over
-// the x with the lowest flip bit clear), complex64 in float per tile,
-// complex128 in float-float on the tile converted once after the load (no
-// FP64 instruction per pair).  Warp sums go to per-warp double slots in
-// shared memory; a CTA writes its totals and a second kernel sums the CTAs in
-// a fixed order.  The raw sums equal those of the Walsh-Hadamard pass.
+// the x with the lowest flip bit clear) in registers over all of its CTA's
+// tiles: complex64 in float (each thread's share is small), complex128 in
+// float-float on the tile converted once after the load (no FP64 instruction
+// per pair).  At the end warp sums go to per-warp double slots; a CTA writes
+// its totals and a second kernel sums the CTAs in a fixed order.  The raw
+// sums equal those of the Walsh-Hadamard pass.
 // ---------------------------------------------------------------------------
-constexpr int kTileWords = 32;
+constexpr int kTileWords = 8;  // per-thread accumulators stay in registers
 constexpr int kPauliTileThreads = 256;
 
 template <class I> struct PauliTileParams {
@@ -484,6 +485,7 @@ __global__ void __launch_bounds__(kPauliTileThreads, 3) pauli_tile_kernel(const 
         }
         asm volatile("cp.async.commit_group;" ::: "memory");
     };
+    TileAcc<T> acc[kTileWords];  // per-thread sums over all tiles of this CTA
     const I G = I(gridDim.x);
     I tau = blockIdx.x;
     if (tau < p.ntiles) load(tau, buf[0]);
@@ -504,23 +506,25 @@ __global__ void __launch_bounds__(kPauliTileThreads, 3) pauli_tile_kernel(const 
             __syncthreads();
         }
         const I base = insert_holes<I>(tau, p.holes);
-        for (int t = 0; t < p.nw; t++) {
+        // compile-time word index: acc[t] stays a register
+#pragma unroll
+        for (int t = 0; t < kTileWords; t++) {
+            if (t >= p.nw) break;
             const uint32_t f = p.tflip[t], sg = p.tsign[t];
-            const bool neg0 = (__popcll(uint64_t(base) & p.osign[t]) & 1) != 0;
+            const uint32_t neg0 = uint32_t(__popcll(uint64_t(base) & p.osign[t]) & 1);
             const bool im = (p.use_im >> t) & 1u;
-            TileAcc<T> acc;
             if (f == 0) {
                 for (int e = threadIdx.x; e < E; e += kPauliTileThreads) {
-                    const bool neg = __popc(uint32_t(e) & sg) & 1;
+                    const bool neg = ((__popc(uint32_t(e) & sg) & 1) ^ neg0) != 0;
                     if constexpr (sizeof(T) == 4) {
                         const C a = cur[swz<T>(e)];
                         const float q = fmaf(a.x, a.x, a.y * a.y);
-                        acc.add(neg ? -q : q);
+                        acc[t].add(neg ? -q : q);
                     } else {
                         const float4 a = reinterpret_cast<const float4 *>(cur)[swz<T>(e)];
                         const DF r{a.x, a.y}, i{a.z, a.w};
                         DF q = df_sum<2>({df_mul(r, r), df_mul(i, i)});
-                        acc.add(neg ? df_neg(q) : q);
+                        acc[t].add(neg ? df_neg(q) : q);
                     }
                 }
             } else {
@@ -529,30 +533,31 @@ __global__ void __launch_bounds__(kPauliTileThreads, 3) pauli_tile_kernel(const 
                 for (int c = threadIdx.x; c < (E >> 1); c += kPauliTileThreads) {
                     const int e0 = int(w.x), e1 = int(w.x ^ f);
                     w.step();
-                    const bool neg = __popc(uint32_t(e0) & sg) & 1;
+                    const bool neg = ((__popc(uint32_t(e0) & sg) & 1) ^ neg0) != 0;
                     if constexpr (sizeof(T) == 4) {
                         const C a = cur[swz<T>(e0)], b = cur[swz<T>(e1)];
                         const float q = im ? fmaf(a.x, b.y, -a.y * b.x) : fmaf(a.x, b.x, a.y * b.y);
-                        acc.add(neg ? -q : q);
+                        acc[t].add(neg ? -q : q);
                     } else {
                         const float4 a4 = reinterpret_cast<const float4 *>(cur)[swz<T>(e0)];
                         const float4 b4 = reinterpret_cast<const float4 *>(cur)[swz<T>(e1)];
                         const DF ar{a4.x, a4.y}, ai{a4.z, a4.w}, br{b4.x, b4.y}, bi{b4.z, b4.w};
                         const DF q = im ? df_sum<2>({df_mul(ar, bi), df_neg(df_mul(ai, br))})
                                         : df_sum<2>({df_mul(ar, br), df_mul(ai, bi)});
-                        acc.add(neg ? df_neg(q) : q);
+                        acc[t].add(neg ? df_neg(q) : q);
                     }
                 }
-            }
-            acc.warp_reduce();
-            if (lane == 0) {
-                const double v = acc.value();
-                slot[t * W + warp] += neg0 ? -v : v;
             }
         }
         __syncthreads();  // `cur` is the target of a load issued next iteration
     }
     asm volatile("cp.async.wait_group 0;" ::: "memory");
+#pragma unroll
+    for (int t = 0; t < kTileWords; t++) {
+        if (t >= p.nw) break;
+        acc[t].warp_reduce();
+        if (lane == 0) slot[t * W + warp] = acc[t].value();
+    }
     __syncthreads();
     for (int t = threadIdx.x; t < p.nw; t += kPauliTileThreads) {
         double v = 0.0;
