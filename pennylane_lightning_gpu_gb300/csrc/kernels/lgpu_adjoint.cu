@@ -775,7 +775,7 @@ __device__ __forceinline__ void adj_block_dispatch(float4 *kt, float4 *const (&b
 }
 
 template <class I, int NB>
-__global__ void __launch_bounds__(kAdjBlockThreads, 2) adjoint_block_kernel(const AdjBlockParams<I> p) {
+__global__ void __launch_bounds__(kAdjBlockThreads, 3) adjoint_block_kernel(const AdjBlockParams<I> p) {
     extern __shared__ __align__(128) unsigned char adj_smem[];
     const int E = 1 << p.k;
     float4 *kt = reinterpret_cast<float4 *>(adj_smem);
@@ -925,7 +925,7 @@ static lgpu_status_t adjoint_block_t(lgpu_context_t ctx, void *ket, void *const 
     p->nslots = int(cols.size());
     const size_t tile_bytes = (size_t(1) << k) * 16;
     const size_t smem = (nbras + 1) * tile_bytes + size_t(std::max(p->nslots, 1)) * nbras * 8 * sizeof(DF);
-    const int per_sm = std::max(1, std::min(2, int((220 * 1024) / smem)));
+    const int per_sm = std::max(1, std::min(3, int((220 * 1024) / smem)));
     const unsigned grid = unsigned(std::min<uint64_t>(uint64_t(p->ntiles), uint64_t(sm_count()) * per_sm));
     // scratch: [reduction counter, 256 B, untouched][columns][partials]
     const size_t cbytes = (sizeof(int) * std::max<size_t>(cols.size(), 1) + 255) & ~size_t(255);
