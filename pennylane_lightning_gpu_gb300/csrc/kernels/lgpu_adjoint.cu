@@ -651,7 +651,7 @@ struct AStep {
     uint8_t q;      // tile position of the target
     uint8_t body;   // Body1 of U^dag
     int8_t gk;      // GenKind, G_NONE: no gradient
-    uint8_t pad;
+    uint8_t pad;    // 1: U^dag = diag(+-1, +-1), sign flips
     int32_t slot;   // accumulator slot of a gradient step
     uint32_t in_mask, in_val;    // controls inside the tile
     uint64_t out_mask, out_val;  // controls outside the tile (state bits)
@@ -745,7 +745,8 @@ __device__ __forceinline__ void adj_block_dispatch(float4 *kt, float4 *const (&b
                                                    const AStep &st, DF (&acc)[kAdjBlockBras]) {
     switch (st.gk) {
     case G_NONE:
-        switch (st.body) {
+        switch (st.pad == 1 ? kDfSignDiag : int(st.body)) {
+        case kDfSignDiag: adj_block_step<kDfSignDiag, G_NONE, NB>(kt, bt, E, st, acc); break;
         case B_DIAG: adj_block_step<B_DIAG, G_NONE, NB>(kt, bt, E, st, acc); break;
         case B_PERM: adj_block_step<B_PERM, G_NONE, NB>(kt, bt, E, st, acc); break;
         case B_ANTIDIAG: adj_block_step<B_ANTIDIAG, G_NONE, NB>(kt, bt, E, st, acc); break;
@@ -907,6 +908,7 @@ static lgpu_status_t adjoint_block_t(lgpu_context_t ctx, void *ket, void *const 
         }
         KConst kc[4];
         st.body = uint8_t(body_of_2x2_host(a.u, kc));
+        st.pad = df_sign_diag_host(a.u) ? 1 : 0;  // sign flips instead of products
         for (int e = 0; e < 8; e++) {
             st.u[e] = df_split_host(a.u[e]);
             st.g[e] = df_split_host(a.g[e]);

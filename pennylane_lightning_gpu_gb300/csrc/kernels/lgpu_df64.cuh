@@ -201,13 +201,31 @@ template <int K> LGPU_HD DF df_sum(const DF (&t)[K]) {
 
 LGPU_HD DF df_neg(DF x) { return DF{-x.hi, -x.lo}; }
 
+// Body code of a diagonal with entries exactly +1 or -1 (CZ, Z, their
+// controlled forms): the float-float kernels flip signs instead of
+// multiplying.  Only these kernels know the code; the host sets it.
+constexpr int kDfSignDiag = 6;
+
+// True for a 2x2 (re, im interleaved) that is diag(+-1, +-1).
+inline bool df_sign_diag_host(const double *m) {
+    auto pm1 = [](double v) { return v == 1.0 || v == -1.0; };
+    return pm1(m[0]) && m[1] == 0.0 && m[2] == 0.0 && m[3] == 0.0 && m[4] == 0.0 && m[5] == 0.0 && pm1(m[6]) &&
+           m[7] == 0.0;
+}
+
 // The structured 2x2 bodies (Body1 in lgpu_bodies.cuh) in float-float on
 // float-float amplitudes x = (xr, xi), y = (yr, yi).  m holds the 8 real
 // coefficients (re, im interleaved, row-major) as pairs.  Body codes: 0 dense,
 // 1 diagonal, 2 permutation, 3 antidiagonal, 4 real, 5 RX-like (m00 = m11 = c
 // real, m01 = i u, m10 = i v).
 template <int BODY> LGPU_HD void body1_dfv(const DF *m, DF &xr, DF &xi, DF &yr, DF &yi) {
-    if constexpr (BODY == 2) {
+    if constexpr (BODY == kDfSignDiag) {  // diag(s0, s1), s = +-1 exactly: sign flips, no rounding
+        const float s0 = m[0].hi, s1 = m[6].hi;
+        xr = DF{xr.hi * s0, xr.lo * s0};
+        xi = DF{xi.hi * s0, xi.lo * s0};
+        yr = DF{yr.hi * s1, yr.lo * s1};
+        yi = DF{yi.hi * s1, yi.lo * s1};
+    } else if constexpr (BODY == 2) {
         const DF a = xr, b = xi;
         xr = yr;
         xi = yi;

@@ -433,7 +433,8 @@ constexpr int kFusedMatPool = 2304;  // matrix elements, in the state's precisio
 
 struct FGate {
     uint8_t ntgt, q0, q1, body;  // q0 = most significant matrix bit; body: Body1 of a 1-target gate
-    uint8_t lt, lcm, lcv, pad;   // register group: local target, local control mask and values
+    uint8_t lt, lcm, lcv, pad;   // register group: local target, local control mask and values;
+                                 // pad = 1: diag(+-1, +-1) (complex128 float-float sign flips)
     uint32_t in_mask, in_val;    // controls inside the tile (tile positions)
     uint32_t mat_off;            // into the matrix pool
     uint64_t out_mask, out_val;  // controls outside the tile (state bits)
@@ -614,7 +615,8 @@ __device__ __forceinline__ void fused_tile(cplx_t<T> *tile, int E, I base, const
             float4 *t4 = reinterpret_cast<float4 *>(tile);
             const DF *md = reinterpret_cast<const DF *>(mm);
             if (g.ntgt == 1) {
-                switch (g.body) {
+                switch (g.pad == 1 ? kDfSignDiag : int(g.body)) {
+                case kDfSignDiag: tile_pairs_df<kDfSignDiag, NT>(t4, E, g.q0, g.in_mask, g.in_val, md); break;
                 case B_DIAG: tile_pairs_df<B_DIAG, NT>(t4, E, g.q0, g.in_mask, g.in_val, md); break;
                 case B_PERM: tile_pairs_df<B_PERM, NT>(t4, E, g.q0, g.in_mask, g.in_val, md); break;
                 case B_ANTIDIAG: tile_pairs_df<B_ANTIDIAG, NT>(t4, E, g.q0, g.in_mask, g.in_val, md); break;
@@ -1385,6 +1387,7 @@ static lgpu_status_t fused_t(cplx_t<T> *sv, uint32_t n, const std::vector<int> &
                 for (uint32_t e = 0; e < need; e++) p->mats[pool + e] = T(src.m[e]);
             }
             dst.body = src.ntgt == 1 ? uint8_t(body_of_2x2_host(src.m, p->kc[cnt])) : uint8_t(B_DENSE);
+            dst.pad = (dfm && src.ntgt == 1 && df_sign_diag_host(src.m)) ? 1 : 0;  // float-float sign flips
             pool += need;
             cnt++;
         }
