@@ -361,15 +361,20 @@ class QuantumTape:
     def get_operation(self, idx):
         """Operation owning the idx-th trainable parameter, and its local index."""
         t = self.trainable_params[idx]
-        k = 0
-        for o in self.operations:
-            if isinstance(o, (StatePrep, BasisState)):
-                continue
-            for j in range(len(o.parameters)):
-                if k == t:
-                    return o, k, j
-                k += 1
-        raise IndexError(idx)
+        owners = self._param_owners()
+        if not 0 <= t < len(owners):
+            raise IndexError(idx)
+        o, j = owners[t]
+        return o, t, j
+
+    def _param_owners(self):
+        """(operation, local index) of every parameter, built once per tape."""
+        owners = getattr(self, "_owners", None)
+        if owners is None:
+            owners = [(o, j) for o in self.operations if not isinstance(o, (StatePrep, BasisState))
+                      for j in range(len(o.parameters))]
+            self._owners = owners
+        return owners
 
     def copy(self):
         return QuantumTape(self.operations, self.measurements, self.trainable_params)

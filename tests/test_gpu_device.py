@@ -62,6 +62,31 @@ def test_execute_measurements(oracle, dtype, tol):
     assert abs(res[5] - p23[0b10]) < tol
 
 
+@pytest.mark.parametrize("dtype,tol", [(np.complex128, 1e-10), (np.complex64, 1e-5)])
+def test_var_observables(oracle, dtype, tol):
+    """var = <O^2> - <O>^2 for one-wire Paulis, tensor products (X (x) Y and
+    Z (x) H (x) Y) and a 2-wire Hermitian after rotations, against the oracle
+    (lightning_gpu.py:936-960)."""
+    rng = np.random.default_rng(41)
+    n = 4
+    ops = [Q.op("RX", 0, 0.43), Q.op("RY", 1, -1.2), Q.op("RX", 2, 2.1), Q.op("CNOT", [0, 1]),
+           Q.op("RZ", 2, 0.77), Q.op("RY", 3, 0.35), Q.op("CNOT", [2, 3])]
+    herm = rng.normal(size=(4, 4)) + 1j * rng.normal(size=(4, 4))
+    herm = herm + herm.conj().T
+    observables = [Q.PauliZ(0), Q.PauliX(1) @ Q.PauliY(2), Q.PauliZ(0) @ Q.Hadamard(1) @ Q.PauliY(3),
+                   Q.Hermitian(herm, [3, 1])]
+    dev = _dev(n, dtype)
+    res = dev.execute(Q.QuantumTape(ops, [Q.var(o) for o in observables]))
+    psi = oracle.run(n, _oracle_ops(ops))
+    for got, o in zip(res, observables):
+        m = o.matrix()
+        w = list(o.wires)
+        mean = oracle.expval_matrix(psi, m, w).real
+        sq = oracle.expval_matrix(psi, m.conj().T @ m, w).real
+        scale = max(1.0, float(np.abs(m).max()) ** 2)
+        assert abs(got - (sq - mean ** 2)) < tol * 10 * scale, (o, got, sq - mean ** 2)
+
+
 def test_state_prep_and_basis_state(oracle):
     rng = np.random.default_rng(1)
     n = 5
