@@ -859,6 +859,193 @@ __global__ void adjoint_block_reduce(const double *__restrict__ partials, int nc
     jac[size_t(cols[i / nb]) * stride + (i % nb)] = t;
 }
 
+// ---------------------------------------------------------------------------
+// The whole small-state sweep in float-float (complex128): lambda and the bra
+// are converted once while they are loaded into shared memory, and every
+// operation, generator overlap and block sum runs on the float-float copies
+// (no FP64 instruction).  Same order, operations and results as
+// adjoint_sweep_kernel.
+// ---------------------------------------------------------------------------
+struct SweepDF {
+    DF u[32];
+    DF g[32];
+    int sign_diag;  // U^dag = diag(+-1, +-1) on one bit
+};
+
+template <int BODY>
+__device__ __forceinline__ void sweep_pairs_df(float4 *lam, float4 *bra, int E, const SweepOp &o, const DF *mp) {
+    DF m[8];
+#pragma unroll
+    for (int i = 0; i < 8; i++) m[i] = mp[i];
+    const uint32_t holes = o.ucm | (1u << o.ut);
+    const int nfree = E >> __popc(holes);
+    PairWalk w(holes, threadIdx.x, kSweepThreads);
+    for (int f = threadIdx.x; f < nfree; f += kSweepThreads) {
+        const int e0 = int(w.x | o.ucv), e1 = e0 | (1 << o.ut);
+        w.step();
+#pragma unroll
+        for (int st = 0; st < 2; st++) {
+            float4 *v = st ? bra : lam;
+            const float4 a = v[e0], b = v[e1];
+            DF xr{a.x, a.y}, xi{a.z, a.w}, yr{b.x, b.y}, yi{b.z, b.w};
+            body1_dfv<BODY>(m, xr, xi, yr, yi);
+            v[e0] = make_float4(xr.hi, xr.lo, xi.hi, xi.lo);
+            v[e1] = make_float4(yr.hi, yr.lo, yi.hi, yi.lo);
+        }
+    }
+}
+
+__device__ __forceinline__ void sweep_udag_df(float4 *lam, float4 *bra, int E, const SweepOp &o, const SweepDF &d) {
+    if (o.ukind == U_ONE) {
+        switch (d.sign_diag ? kDfSignDiag : o.ubody) {
+        case kDfSignDiag: sweep_pairs_df<kDfSignDiag>(lam, bra, E, o, d.u); break;
+        case B_DIAG: sweep_pairs_df<B_DIAG>(lam, bra, E, o, d.u); break;
+        case B_PERM: sweep_pairs_df<B_PERM>(lam, bra, E, o, d.u); break;
+        case B_ANTIDIAG: sweep_pairs_df<B_ANTIDIAG>(lam, bra, E, o, d.u); break;
+        case B_REAL: sweep_pairs_df<B_REAL>(lam, bra, E, o, d.u); break;
+        case B_RXLIKE: sweep_pairs_df<B_RXLIKE>(lam, bra, E, o, d.u); break;
+        default: sweep_pairs_df<B_DENSE>(lam, bra, E, o, d.u); break;
+        }
+    } else if (o.ukind == U_DENSE4) {
+        const int qa = o.ut, qb = o.uq2;
+        const uint32_t holes = (1u << qa) | (1u << qb);
+        PairWalk w(holes, threadIdx.x, kSweepThreads);
+        for (int f = threadIdx.x; f < (E >> 2); f += kSweepThreads) {
+            const int e = int(w.x);
+            w.step();
+            const int idx[4] = {e, e | (1 << qb), e | (1 << qa), e | (1 << qa) | (1 << qb)};
+#pragma unroll
+            for (int st = 0; st < 2; st++) {
+                float4 *v = st ? bra : lam;
+                DF ar[4], ai[4];
+#pragma unroll
+                for (int c = 0; c < 4; c++) {
+                    const float4 x = v[idx[c]];
+                    ar[c] = DF{x.x, x.y};
+                    ai[c] = DF{x.z, x.w};
+                }
+#pragma unroll
+                for (int r = 0; r < 4; r++) {
+                    DF tr[8], ti[8];
+#pragma unroll
+                    for (int c = 0; c < 4; c++) {
+                        const DF mre = d.u[2 * (r * 4 + c)], mim = d.u[2 * (r * 4 + c) + 1];
+                        tr[2 * c] = df_mul(mre, ar[c]);
+                        tr[2 * c + 1] = df_mul(df_neg(mim), ai[c]);
+                        ti[2 * c] = df_mul(mre, ai[c]);
+                        ti[2 * c + 1] = df_mul(mim, ar[c]);
+                    }
+                    const DF xr = df_sum<8>(tr), xi = df_sum<8>(ti);
+                    v[idx[r]] = make_float4(xr.hi, xr.lo, xi.hi, xi.lo);
+                }
+            }
+        }
+    }
+}
+
+template <int GK>
+__device__ __forceinline__ DF sweep_gen1_df(const float4 *lam, const float4 *bra, int E, const SweepOp &o,
+                                            const DF *g) {
+    DF acc{0.0f, 0.0f};
+    const uint32_t holes = o.gcm | (1u << o.gt);
+    const int nfree = E >> __popc(holes);
+    PairWalk w(holes, threadIdx.x, kSweepThreads);
+    for (int f = threadIdx.x; f < nfree; f += kSweepThreads) {
+        const int e0 = int(w.x | o.gcv), e1 = e0 | (1 << o.gt);
+        w.step();
+        const float4 ka = lam[e0], kb = lam[e1], ba = bra[e0], bb = bra[e1];
+        const DF kv[4] = {DF{ka.x, ka.y}, DF{ka.z, ka.w}, DF{kb.x, kb.y}, DF{kb.z, kb.w}};
+        const DF bv[4] = {DF{ba.x, ba.y}, DF{ba.z, ba.w}, DF{bb.x, bb.y}, DF{bb.z, bb.w}};
+        acc = df_sum<2>({acc, gexp_df<GK>(g, bv, kv)});
+    }
+    return acc;
+}
+
+__device__ __forceinline__ DF sweep_gen_df(const float4 *lam, const float4 *bra, int E, const SweepOp &o,
+                                           const SweepDF &d) {
+    if (o.gkind == G_DENSE4) {
+        DF acc{0.0f, 0.0f};
+        const int qa = o.gt, qb = o.gq2;
+        const uint32_t holes = (1u << qa) | (1u << qb);
+        PairWalk w(holes, threadIdx.x, kSweepThreads);
+        for (int f = threadIdx.x; f < (E >> 2); f += kSweepThreads) {
+            const int e = int(w.x);
+            w.step();
+            const int idx[4] = {e, e | (1 << qb), e | (1 << qa), e | (1 << qa) | (1 << qb)};
+            DF ar[4], ai[4];
+#pragma unroll
+            for (int c = 0; c < 4; c++) {
+                const float4 x = lam[idx[c]];
+                ar[c] = DF{x.x, x.y};
+                ai[c] = DF{x.z, x.w};
+            }
+#pragma unroll
+            for (int r = 0; r < 4; r++) {
+                DF tr[8], ti[8];
+#pragma unroll
+                for (int c = 0; c < 4; c++) {
+                    const DF gre = d.g[2 * (r * 4 + c)], gim = d.g[2 * (r * 4 + c) + 1];
+                    tr[2 * c] = df_mul(gre, ar[c]);
+                    tr[2 * c + 1] = df_mul(df_neg(gim), ai[c]);
+                    ti[2 * c] = df_mul(gre, ai[c]);
+                    ti[2 * c + 1] = df_mul(gim, ar[c]);
+                }
+                const DF yr = df_sum<8>(tr), yi = df_sum<8>(ti);
+                const float4 b = bra[idx[r]];
+                acc = df_sum<3>({acc, df_mul(DF{b.x, b.y}, yi), df_neg(df_mul(DF{b.z, b.w}, yr))});
+            }
+        }
+        return acc;
+    }
+    switch (o.gkind) {
+    case G_Z: return sweep_gen1_df<G_Z>(lam, bra, E, o, d.g);
+    case G_X: return sweep_gen1_df<G_X>(lam, bra, E, o, d.g);
+    case G_Y: return sweep_gen1_df<G_Y>(lam, bra, E, o, d.g);
+    case G_P1: return sweep_gen1_df<G_P1>(lam, bra, E, o, d.g);
+    default: return sweep_gen1_df<G_DENSE>(lam, bra, E, o, d.g);
+    }
+}
+
+__global__ void __launch_bounds__(kSweepThreads, 1)
+    adjoint_sweep_df_kernel(const double2 *__restrict__ ket, double2 *const *__restrict__ bras, int n,
+                            const SweepOp *__restrict__ ops, const SweepDF *__restrict__ dops, int nops,
+                            double *__restrict__ jac, int K) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    __shared__ DF red[kSweepThreads / 32];
+    const int E = 1 << n;
+    float4 *lam = reinterpret_cast<float4 *>(smem_raw);
+    float4 *bra = lam + E;
+    const int k = blockIdx.x;
+    const double2 *src = bras[k];
+    for (int e = threadIdx.x; e < E; e += kSweepThreads) {
+        const double2 a = ket[e], b = src[e];
+        const DF ar = df_from_double(a.x), ai = df_from_double(a.y), br = df_from_double(b.x), bi = df_from_double(b.y);
+        lam[e] = make_float4(ar.hi, ar.lo, ai.hi, ai.lo);
+        bra[e] = make_float4(br.hi, br.lo, bi.hi, bi.lo);
+    }
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int i = 0; i < nops; i++) {
+        const SweepOp &o = ops[i];
+        const SweepDF &d = dops[i];
+        if (o.col >= 0 && o.gkind != G_NONE) {
+            DF v = sweep_gen_df(lam, bra, E, o, d);
+#pragma unroll
+            for (int s = 16; s > 0; s >>= 1) v = df_sum<2>({v, df_shfl_xor(v, s)});
+            if (lane == 0) red[warp] = v;
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                DF t = red[0];
+                for (int w = 1; w < kSweepThreads / 32; w++) t = df_sum<2>({t, red[w]});
+                jac[size_t(o.col) * K + k] = df_to_double(t);
+            }
+            __syncthreads();
+        }
+        sweep_udag_df(lam, bra, E, o, d);
+        __syncthreads();
+    }
+}
+
 template <class I>
 static lgpu_status_t adjoint_block_t(lgpu_context_t ctx, void *ket, void *const *bras, uint32_t nbras, uint32_t n,
                                      const std::vector<int> &tile_bits, const lgpu_adj_block_step_t *steps,
@@ -1035,6 +1222,36 @@ lgpu_status_t lgpu_adjoint_sweep_small(lgpu_context_t ctx, const void *ket, void
     if (nops) LGPU_CUDA_TRY(cudaMemcpyAsync(dops, host.data(), sizeof(SweepOp) * nops, cudaMemcpyHostToDevice, s));
     // the pageable source vectors must outlive the copies
     LGPU_CUDA_TRY(cudaStreamSynchronize(s));
+    if (dt == LGPU_C128 && f64_mode() == 1 && fused_df_enabled()) {
+        // float-float copies of the coefficients, after the ops in the scratch
+        std::vector<SweepDF> hd(host.size());
+        for (uint32_t i = 0; i < nops; i++) {
+            for (int e = 0; e < 32; e++) {
+                hd[i].u[e] = df_split_host(host[i].u[e]);
+                hd[i].g[e] = df_split_host(host[i].g[e]);
+            }
+            hd[i].sign_diag = host[i].ukind == U_ONE && df_sign_diag_host(host[i].u) ? 1 : 0;
+        }
+        const size_t obytes = (sizeof(SweepOp) * host.size() + 255) & ~size_t(255);
+        LGPU_TRY(ctx_scratch(ctx, 256 + pbytes + obytes + sizeof(SweepDF) * hd.size(), &p));
+        dbras = reinterpret_cast<void **>(static_cast<char *>(p) + 256);
+        dops = reinterpret_cast<SweepOp *>(static_cast<char *>(p) + 256 + pbytes);
+        auto *ddf = reinterpret_cast<SweepDF *>(static_cast<char *>(p) + 256 + pbytes + obytes);
+        LGPU_CUDA_TRY(cudaMemcpyAsync(dbras, bras, sizeof(void *) * nbras, cudaMemcpyHostToDevice, s));
+        if (nops) {
+            LGPU_CUDA_TRY(cudaMemcpyAsync(dops, host.data(), sizeof(SweepOp) * nops, cudaMemcpyHostToDevice, s));
+            LGPU_CUDA_TRY(cudaMemcpyAsync(ddf, hd.data(), sizeof(SweepDF) * nops, cudaMemcpyHostToDevice, s));
+        }
+        LGPU_CUDA_TRY(cudaStreamSynchronize(s));
+        const size_t smem = 2 * (size_t(1) << n) * sizeof(double2);
+        static std::atomic<size_t> attr[64];
+        LGPU_TRY(ensure_smem(reinterpret_cast<const void *>(adjoint_sweep_df_kernel), smem, attr));
+        adjoint_sweep_df_kernel<<<nbras, kSweepThreads, smem, s>>>(static_cast<const double2 *>(ket),
+                                                                   reinterpret_cast<double2 *const *>(dbras), int(n),
+                                                                   dops, ddf, int(nops), jac_dev, int(nbras));
+        LGPU_CHECK_LAUNCH();
+        return LGPU_OK;
+    }
     if (dt == LGPU_C128)
         return f64_mode() == 1 ? sweep_launch<double, true>(ket, dbras, nbras, n, dops, nops, jac_dev, s)
                                : sweep_launch<double, false>(ket, dbras, nbras, n, dops, nops, jac_dev, s);
