@@ -56,11 +56,12 @@ class ClockSampler:
              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
              "clocks_event_reasons.sw_power_cap")
 
-    def __init__(self, period_ms=200):
+    def __init__(self, period_ms=50):
         self.period_ms = period_ms
         self.proc = None
-        self.lines = []
+        self.lines = []  # (host time, csv line)
         self.thread = None
+        self.first = threading.Event()
 
     def start(self):
         try:
@@ -75,9 +76,17 @@ class ClockSampler:
 
     def _read(self):
         for line in self.proc.stdout:
-            self.lines.append(line.strip())
+            self.lines.append((time.perf_counter(), line.strip()))
+            self.first.set()
 
-    def stop(self):
+    def wait_first(self, timeout=3.0):
+        """Block until nvidia-smi has reported once (it is then sampling)."""
+        if self.proc is not None:
+            self.first.wait(timeout)
+
+    def stop(self, t0=None, t1=None):
+        """Summary of the samples taken between host times t0 and t1 (all
+        samples when none falls in that window)."""
         if self.proc is None:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
         self.proc.terminate()
@@ -87,7 +96,12 @@ class ClockSampler:
             self.proc.kill()
         sm, mx, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
+        chosen = self.lines
+        if t0 is not None and t1 is not None:
+            inside = [x for x in self.lines if t0 <= x[0] <= t1]
+            if inside:
+                chosen = inside
+        for _, ln in chosen:
             parts = [p.strip() for p in ln.split(",")]
             if len(parts) < 7:
                 continue
@@ -283,10 +297,12 @@ def run_ours(args):
 
     clocks = ClockSampler()
     clocks.start()
-    time.sleep(0.3)
+    clocks.wait_first()
+    t_load0 = time.perf_counter()
     value, avg_launch_ms, per_target, ms_per_step, sv = gate_sweep(m, "LightningGPU_C128", n, args.steps,
                                                                    args.warmup, f64_mode=default_mode, device=dev)
-    clk = clocks.stop()
+    t_load1 = time.perf_counter()
+    clk = clocks.stop(t_load0, t_load1)  # samples while the warm-up and timed steps run
     bytes_per_step = len(gates) * 2 * S
 
     # ---- end to end: public API, host params, D2H result read every step ----
