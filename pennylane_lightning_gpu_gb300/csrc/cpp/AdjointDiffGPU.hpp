@@ -173,7 +173,8 @@ template <class T = double> class AdjointJacobianGPU {
             }
         }
 
-        const bool blocks = SV::dt() == LGPU_C128 && num_observables >= 1 && num_observables <= 2 && blocks_enabled();
+        const bool blocks = SV::dt() == LGPU_C128 && num_observables >= 1 && blocks_enabled();
+        std::unique_ptr<SV> lam0;  // lambda before a block, when the bras run in pairs
         for (int op_idx = static_cast<int>(ops_name.size() - 1); op_idx >= 0; op_idx--) {
             PL_ABORT_IF(ops.getOpsParams()[size_t(op_idx)].size() > 1,
                         "The operation is not supported using the adjoint differentiation method");
@@ -218,10 +219,20 @@ template <class T = double> class AdjointJacobianGPU {
                 }
                 if (steps.size() >= 2) {
                     std::vector<int32_t> tb(tile.begin(), tile.end());
-                    PL_LGPU_IS_SUCCESS(lgpu_adjoint_block(lambda.ctx(), lambda.getData(), bra_ptrs.data(),
-                                                          uint32_t(num_observables), n, SV::dt(), uint32_t(tb.size()),
-                                                          tb.data(), steps.data(), uint32_t(steps.size()),
-                                                          jac_dev.getData(), uint32_t(K), lambda.lstream()));
+                    // Up to two bras per pass; more run in pairs, each pair
+                    // starting from the same lambda (restored from a copy).
+                    if (num_observables > 2) {
+                        if (!lam0) lam0 = std::make_unique<SV>(lambda.getNumQubits(), dt_local, true);
+                        lam0->updateData(lambda);
+                    }
+                    for (size_t b0 = 0; b0 < num_observables; b0 += 2) {
+                        if (b0 > 0) lambda.updateData(*lam0);
+                        const uint32_t nb = uint32_t(std::min<size_t>(2, num_observables - b0));
+                        PL_LGPU_IS_SUCCESS(lgpu_adjoint_block(lambda.ctx(), lambda.getData(), bra_ptrs.data() + b0, nb,
+                                                              n, SV::dt(), uint32_t(tb.size()), tb.data(), steps.data(),
+                                                              uint32_t(steps.size()), jac_dev.getData() + b0,
+                                                              uint32_t(K), lambda.lstream()));
+                    }
                     for (const auto &cs : scales) col_scale[cs.first] = cs.second;
                     current_param_idx = cpi;
                     trainableParamNumber = tpn;

@@ -386,13 +386,14 @@ BLOCK_ADJ_OPS = ["RX", "RY", "RZ", "PhaseShift", "CRX", "CRY", "CRZ", "Controlle
                  "CNOT", "CZ", "Toffoli", "IsingXX", "SingleExcitation"]
 
 
-@pytest.mark.parametrize("n,nobs", [(14, 1), (14, 2), (16, 1)])
+@pytest.mark.parametrize("n,nobs", [(14, 1), (14, 2), (14, 3), (16, 1)])
 def test_adjoint_fused_blocks(native, oracle, n, nobs):
-    """complex128 states above the shared-memory sweep with one or two
-    observables run runs of 1-target operations (controls allowed) as fused
-    blocks in float-float arithmetic; non-1-target operations (IsingXX,
-    SingleExcitation) end a block and take the per-operation path.  Against
-    the oracle adjoint at 1e-10 x 50, with a trainable subset."""
+    """complex128 states above the shared-memory sweep run runs of 1-target
+    operations (controls allowed) as fused blocks in float-float arithmetic,
+    up to two observables per pass (three: a pair, then the third from the
+    same lambda); non-1-target operations (IsingXX, SingleExcitation) end a
+    block and take the per-operation path.  Against the oracle adjoint at
+    1e-10 x 50, with a trainable subset."""
     rng = np.random.default_rng(1300 + n + nobs)
     ops = [("Hadamard", [w], [], False) for w in range(n)]
     nw = {"CRX": 2, "CRY": 2, "CRZ": 2, "ControlledPhaseShift": 2, "CNOT": 2, "CZ": 2, "Toffoli": 3, "IsingXX": 2,
@@ -405,7 +406,8 @@ def test_adjoint_fused_blocks(native, oracle, n, nobs):
     nparam = sum(1 for o in ops if o[2])
     tp = sorted(int(x) for x in rng.choice(nparam, size=min(24, nparam), replace=False))
     obs_specs = [(True, [(0.6, [("PauliZ", [1], None)]), (-0.4, [("PauliX", [0], None), ("PauliY", [n - 1], None)])]),
-                 (False, [(1.0, [("PauliY", [3], None)])])][:nobs]
+                 (False, [(1.0, [("PauliY", [3], None)])]),
+                 (False, [(1.0, [("PauliX", [n - 2], None), ("PauliZ", [5], None)])])][:nobs]
     sv = native.LightningGPU_C128(n)
     apply_ops(sv, ops)
     adj = native.AdjointJacobianGPU_C128()
