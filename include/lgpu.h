@@ -321,16 +321,17 @@ lgpu_status_t lgpu_adjoint_sweep_small(lgpu_context_t ctx, const void *ket, void
                                        lgpu_stream_t stream);
 
 /* Several consecutive operations of the reverse sweep in one pass over the
- * states (complex128; states too large for lgpu_adjoint_sweep_small).  Each
+ * states (states too large for lgpu_adjoint_sweep_small).  Each
  * step is a 1-target U^dag with controls and, when `gen_kind` >= 0, the
  * generator P1(controls) (x) g on the target:
  *   jac[col * jac_stride + k] = Im <bra_k| G |lambda>   (G on the pairs the
  *                                                        controls select)
  *   lambda <- U^dag lambda ;  bra_k <- U^dag bra_k
  * in step order.  Every target must be one of the k tile bits: the bits
- * 0..m-1 plus at most 6 others, k <= 11.  nbras <= 2.  The states are
- * carried in float-float arithmetic inside the pass (no FP64 instruction per
- * pair); the sums are deterministic.  Replaces the per-operation
+ * 0..m-1 plus at most 6 others, k <= 11 (complex64: m >= 1).  nbras <= 2.
+ * complex128 states are carried in float-float arithmetic inside the pass
+ * (no FP64 instruction per pair), complex64 in FP32; the sums are
+ * deterministic.  Replaces the per-operation
  * updateJacobian / applyOperationsAdj sequence of AdjointDiffGPU.hpp:560-595
  * for runs of such operations; no counterpart in the reference. */
 typedef struct {

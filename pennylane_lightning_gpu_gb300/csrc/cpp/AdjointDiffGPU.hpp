@@ -173,7 +173,7 @@ template <class T = double> class AdjointJacobianGPU {
             }
         }
 
-        const bool blocks = SV::dt() == LGPU_C128 && num_observables >= 1 && blocks_enabled();
+        const bool blocks = num_observables >= 1 && blocks_enabled();
         std::unique_ptr<SV> lam0;  // lambda before a block, when the bras run in pairs
         for (int op_idx = static_cast<int>(ops_name.size() - 1); op_idx >= 0; op_idx--) {
             PL_ABORT_IF(ops.getOpsParams()[size_t(op_idx)].size() > 1,

@@ -849,6 +849,155 @@ __global__ void __launch_bounds__(kAdjBlockThreads, 3) adjoint_block_kernel(cons
     }
 }
 
+// The same blocks for complex64: float2 tiles, FP32 bodies and overlaps
+// (float sums per step and thread, double per-warp slots).
+template <int GK>
+__device__ __forceinline__ float gexp_f32(const float *g, float2 b0, float2 b1, float2 k0, float2 k1) {
+    if constexpr (GK == G_Z) return (b0.x * k0.y - b0.y * k0.x) - (b1.x * k1.y - b1.y * k1.x);
+    else if constexpr (GK == G_X) return (b0.x * k1.y - b0.y * k1.x) + (b1.x * k0.y - b1.y * k0.x);
+    else if constexpr (GK == G_Y) return (b1.x * k0.x + b1.y * k0.y) - (b0.x * k1.x + b0.y * k1.y);
+    else if constexpr (GK == G_P1) return b1.x * k1.y - b1.y * k1.x;
+    else {
+        const float y0r = g[0] * k0.x - g[1] * k0.y + g[2] * k1.x - g[3] * k1.y;
+        const float y0i = g[0] * k0.y + g[1] * k0.x + g[2] * k1.y + g[3] * k1.x;
+        const float y1r = g[4] * k0.x - g[5] * k0.y + g[6] * k1.x - g[7] * k1.y;
+        const float y1i = g[4] * k0.y + g[5] * k0.x + g[6] * k1.y + g[7] * k1.x;
+        return (b0.x * y0i - b0.y * y0r) + (b1.x * y1i - b1.y * y1r);
+    }
+}
+
+template <int BODY, int GK, int NB>
+__device__ __forceinline__ void adj_block_step_f32(float2 *kt, float2 *const (&bt)[kAdjBlockBras], int E,
+                                                   const AStep &st, float (&acc)[kAdjBlockBras]) {
+    float u[8], g[8];
+#pragma unroll
+    for (int i = 0; i < 8; i++) {
+        u[i] = st.u[i].hi;
+        g[i] = st.g[i].hi;
+    }
+    const uint32_t holes = st.in_mask | (1u << st.q);
+    const int nfree = E >> __popc(holes);
+    PairWalk w(holes, threadIdx.x, kAdjBlockThreads);
+    for (int f = threadIdx.x; f < nfree; f += kAdjBlockThreads) {
+        const int e0 = int(w.x | st.in_val);
+        const int e1 = e0 | (1 << st.q);
+        w.step();
+        const int s0 = swz<float>(e0), s1 = swz<float>(e1);
+        float2 k0 = kt[s0], k1 = kt[s1];
+#pragma unroll
+        for (int b = 0; b < NB; b++) {
+            float2 b0 = bt[b][s0], b1 = bt[b][s1];
+            if constexpr (GK != G_NONE) acc[b] += gexp_f32<GK>(g, b0, b1, k0, k1);
+            body1<float, BODY>(u, b0, b1);
+            bt[b][s0] = b0;
+            bt[b][s1] = b1;
+        }
+        body1<float, BODY>(u, k0, k1);
+        kt[s0] = k0;
+        kt[s1] = k1;
+    }
+}
+
+template <int NB>
+__device__ __forceinline__ void adj_block_dispatch_f32(float2 *kt, float2 *const (&bt)[kAdjBlockBras], int E,
+                                                       const AStep &st, float (&acc)[kAdjBlockBras]) {
+    switch (st.gk) {
+    case G_NONE:
+        switch (st.body) {
+        case B_DIAG: adj_block_step_f32<B_DIAG, G_NONE, NB>(kt, bt, E, st, acc); break;
+        case B_PERM: adj_block_step_f32<B_PERM, G_NONE, NB>(kt, bt, E, st, acc); break;
+        case B_ANTIDIAG: adj_block_step_f32<B_ANTIDIAG, G_NONE, NB>(kt, bt, E, st, acc); break;
+        case B_REAL: adj_block_step_f32<B_REAL, G_NONE, NB>(kt, bt, E, st, acc); break;
+        case B_RXLIKE: adj_block_step_f32<B_RXLIKE, G_NONE, NB>(kt, bt, E, st, acc); break;
+        default: adj_block_step_f32<B_DENSE, G_NONE, NB>(kt, bt, E, st, acc); break;
+        }
+        break;
+    case G_X:
+        if (st.body == B_RXLIKE) adj_block_step_f32<B_RXLIKE, G_X, NB>(kt, bt, E, st, acc);
+        else adj_block_step_f32<B_DENSE, G_X, NB>(kt, bt, E, st, acc);
+        break;
+    case G_Y:
+        if (st.body == B_REAL) adj_block_step_f32<B_REAL, G_Y, NB>(kt, bt, E, st, acc);
+        else adj_block_step_f32<B_DENSE, G_Y, NB>(kt, bt, E, st, acc);
+        break;
+    case G_Z:
+        if (st.body == B_DIAG) adj_block_step_f32<B_DIAG, G_Z, NB>(kt, bt, E, st, acc);
+        else adj_block_step_f32<B_DENSE, G_Z, NB>(kt, bt, E, st, acc);
+        break;
+    case G_P1:
+        if (st.body == B_DIAG) adj_block_step_f32<B_DIAG, G_P1, NB>(kt, bt, E, st, acc);
+        else adj_block_step_f32<B_DENSE, G_P1, NB>(kt, bt, E, st, acc);
+        break;
+    default: adj_block_step_f32<B_DENSE, G_DENSE, NB>(kt, bt, E, st, acc); break;
+    }
+}
+
+template <class I, int NB>
+__global__ void __launch_bounds__(kAdjBlockThreads, 3) adjoint_block_f32_kernel(const AdjBlockParams<I> p) {
+    extern __shared__ __align__(128) unsigned char adj_smem[];
+    const int E = 1 << p.k;
+    float2 *kt = reinterpret_cast<float2 *>(adj_smem);
+    float2 *bt[kAdjBlockBras];
+#pragma unroll
+    for (int b = 0; b < kAdjBlockBras; b++) bt[b] = kt + size_t(b + 1) * E;
+    constexpr int W = kAdjBlockThreads / 32;
+    double *wacc = reinterpret_cast<double *>(kt + size_t(NB + 1) * E);  // [nslots][NB][W]
+    for (int i = threadIdx.x; i < p.nslots * NB * W; i += kAdjBlockThreads) wacc[i] = 0.0;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int lowmask = (1 << p.m) - 1;
+    float2 *ket = reinterpret_cast<float2 *>(p.ket);
+    float2 *bras[kAdjBlockBras];
+#pragma unroll
+    for (int b = 0; b < kAdjBlockBras; b++) bras[b] = reinterpret_cast<float2 *>(p.bras[b]);
+    __syncthreads();
+    for (I tau = blockIdx.x; tau < p.ntiles; tau += I(gridDim.x)) {
+        const I base = insert_holes<I>(tau, p.holes);
+        // 16-byte chunks = 2 amplitudes of the low run (m >= 1)
+        for (int c = threadIdx.x; c < E / 2; c += kAdjBlockThreads) {
+            const int e = 2 * c;
+            const I gi = base + p.hi_off[e >> p.m] + I(e & lowmask);
+            adj_cp_async16(&kt[swz<float>(e)], &ket[gi]);
+#pragma unroll
+            for (int b = 0; b < NB; b++) adj_cp_async16(&bt[b][swz<float>(e)], &bras[b][gi]);
+        }
+        asm volatile("cp.async.commit_group;" ::: "memory");
+        asm volatile("cp.async.wait_group 0;" ::: "memory");
+        __syncthreads();
+        for (int si = 0; si < p.nsteps; si++) {
+            const AStep &st = p.steps[si];
+            if ((uint64_t(base) & st.out_mask) != st.out_val) continue;  // tile-uniform
+            float acc[kAdjBlockBras];
+#pragma unroll
+            for (int b = 0; b < kAdjBlockBras; b++) acc[b] = 0.0f;
+            adj_block_dispatch_f32<NB>(kt, bt, E, st, acc);
+            if (st.gk != G_NONE) {
+#pragma unroll
+                for (int b = 0; b < NB; b++) {
+                    float v = acc[b];
+#pragma unroll
+                    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+                    if (lane == 0) wacc[(st.slot * NB + b) * W + warp] += double(v);
+                }
+            }
+            __syncthreads();
+        }
+        for (int c = threadIdx.x; c < E / 2; c += kAdjBlockThreads) {
+            const int e = 2 * c;
+            const I gi = base + p.hi_off[e >> p.m] + I(e & lowmask);
+            __stcs(reinterpret_cast<float4 *>(&ket[gi]), *reinterpret_cast<const float4 *>(&kt[swz<float>(e)]));
+#pragma unroll
+            for (int b = 0; b < NB; b++)
+                __stcs(reinterpret_cast<float4 *>(&bras[b][gi]), *reinterpret_cast<const float4 *>(&bt[b][swz<float>(e)]));
+        }
+        __syncthreads();
+    }
+    for (int i = threadIdx.x; i < p.nslots * NB; i += kAdjBlockThreads) {
+        double t = 0.0;
+        for (int w = 0; w < W; w++) t += wacc[i * W + w];
+        p.partials[size_t(blockIdx.x) * p.nslots * NB + i] = t;
+    }
+}
+
 // jac[col[s] * stride + b] = sum over CTAs (in CTA order) of the partials.
 __global__ void adjoint_block_reduce(const double *__restrict__ partials, int nctas, int nslots, int nb,
                                      const int *__restrict__ cols, double *__restrict__ jac, int stride) {
@@ -1049,7 +1198,7 @@ __global__ void __launch_bounds__(kSweepThreads, 1)
 template <class I>
 static lgpu_status_t adjoint_block_t(lgpu_context_t ctx, void *ket, void *const *bras, uint32_t nbras, uint32_t n,
                                      const std::vector<int> &tile_bits, const lgpu_adj_block_step_t *steps,
-                                     uint32_t nsteps, double *jac, uint32_t stride, cudaStream_t s) {
+                                     uint32_t nsteps, double *jac, uint32_t stride, bool c64, cudaStream_t s) {
     const int k = int(tile_bits.size());
     std::vector<int> pos(n, -1);
     for (int q = 0; q < k; q++) pos[size_t(tile_bits[size_t(q)])] = q;
@@ -1112,7 +1261,8 @@ static lgpu_status_t adjoint_block_t(lgpu_context_t ctx, void *ket, void *const 
         }
     }
     p->nslots = int(cols.size());
-    const size_t tile_bytes = (size_t(1) << k) * 16;
+    if (c64 && m < 1) return fail(LGPU_ERR_INVALID_ARG, "adjoint block: complex64 tiles need bit 0");
+    const size_t tile_bytes = (size_t(1) << k) * (c64 ? 8 : 16);
     const size_t smem = (nbras + 1) * tile_bytes + size_t(std::max(p->nslots, 1)) * nbras * 8 * sizeof(DF);
     const int per_sm = std::max(1, std::min(3, int((220 * 1024) / smem)));
     const unsigned grid = unsigned(std::min<uint64_t>(uint64_t(p->ntiles), uint64_t(sm_count()) * per_sm));
@@ -1127,8 +1277,14 @@ static lgpu_status_t adjoint_block_t(lgpu_context_t ctx, void *ket, void *const 
         LGPU_CUDA_TRY(cudaMemcpyAsync(dcols, cols.data(), sizeof(int) * cols.size(), cudaMemcpyHostToDevice, s));
         LGPU_CUDA_TRY(cudaStreamSynchronize(s));  // the pageable source must outlive the copy
     }
-    static std::atomic<size_t> attr1[64], attr2[64];
-    if (nbras == 1) {
+    static std::atomic<size_t> attr1[64], attr2[64], attr3[64], attr4[64];
+    if (c64 && nbras == 1) {
+        LGPU_TRY(ensure_smem(reinterpret_cast<const void *>(adjoint_block_f32_kernel<I, 1>), smem, attr3));
+        adjoint_block_f32_kernel<I, 1><<<grid, kAdjBlockThreads, smem, s>>>(*p);
+    } else if (c64) {
+        LGPU_TRY(ensure_smem(reinterpret_cast<const void *>(adjoint_block_f32_kernel<I, 2>), smem, attr4));
+        adjoint_block_f32_kernel<I, 2><<<grid, kAdjBlockThreads, smem, s>>>(*p);
+    } else if (nbras == 1) {
         LGPU_TRY(ensure_smem(reinterpret_cast<const void *>(adjoint_block_kernel<I, 1>), smem, attr1));
         adjoint_block_kernel<I, 1><<<grid, kAdjBlockThreads, smem, s>>>(*p);
     } else {
@@ -1179,7 +1335,6 @@ lgpu_status_t lgpu_adjoint_block(lgpu_context_t ctx, void *ket, void *const *bra
                                  lgpu_dtype_t dt, uint32_t k, const int32_t *tile_bits,
                                  const lgpu_adj_block_step_t *steps, uint32_t nsteps, double *jac_dev,
                                  uint32_t jac_stride, lgpu_stream_t stream) {
-    if (dt != LGPU_C128) return fail(LGPU_ERR_INVALID_ARG, "adjoint block: complex128 only");
     LGPU_TRY(check_state(ket, n, dt));
     if (nbras < 1 || nbras > uint32_t(kAdjBlockBras) || !bras)
         return fail(LGPU_ERR_INVALID_ARG, "adjoint block: 1 or 2 bras");
@@ -1194,8 +1349,9 @@ lgpu_status_t lgpu_adjoint_block(lgpu_context_t ctx, void *ket, void *const *bra
     if (std::adjacent_find(tb.begin(), tb.end()) != tb.end())
         return fail(LGPU_ERR_INVALID_ARG, "tile bits must be distinct");
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
-    return n <= 32 ? adjoint_block_t<uint32_t>(ctx, ket, bras, nbras, n, tb, steps, nsteps, jac_dev, jac_stride, s)
-                   : adjoint_block_t<uint64_t>(ctx, ket, bras, nbras, n, tb, steps, nsteps, jac_dev, jac_stride, s);
+    const bool c64 = dt == LGPU_C64;
+    return n <= 32 ? adjoint_block_t<uint32_t>(ctx, ket, bras, nbras, n, tb, steps, nsteps, jac_dev, jac_stride, c64, s)
+                   : adjoint_block_t<uint64_t>(ctx, ket, bras, nbras, n, tb, steps, nsteps, jac_dev, jac_stride, c64, s);
 }
 
 uint32_t lgpu_adjoint_sweep_max_qubits(lgpu_dtype_t dt) { return dt == LGPU_C128 ? 12u : 13u; }

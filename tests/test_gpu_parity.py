@@ -386,14 +386,16 @@ BLOCK_ADJ_OPS = ["RX", "RY", "RZ", "PhaseShift", "CRX", "CRY", "CRZ", "Controlle
                  "CNOT", "CZ", "Toffoli", "IsingXX", "SingleExcitation"]
 
 
-@pytest.mark.parametrize("n,nobs", [(14, 1), (14, 2), (14, 3), (16, 1)])
-def test_adjoint_fused_blocks(native, oracle, n, nobs):
-    """complex128 states above the shared-memory sweep run runs of 1-target
-    operations (controls allowed) as fused blocks in float-float arithmetic,
-    up to two observables per pass (three: a pair, then the third from the
-    same lambda); non-1-target operations (IsingXX, SingleExcitation) end a
-    block and take the per-operation path.  Against the oracle adjoint at
-    1e-10 x 50, with a trainable subset."""
+@pytest.mark.parametrize("n,nobs,dtype", [(14, 1, "c128"), (14, 2, "c128"), (14, 3, "c128"), (16, 1, "c128"),
+                                          (14, 1, "c64"), (14, 3, "c64")])
+def test_adjoint_fused_blocks(native, oracle, n, nobs, dtype):
+    """States above the shared-memory sweep run runs of 1-target operations
+    (controls allowed) as fused blocks (complex128 in float-float arithmetic,
+    complex64 in FP32), up to two observables per pass (three: a pair, then
+    the third from the same lambda); non-1-target operations (IsingXX,
+    SingleExcitation) end a block and take the per-operation path.  Against
+    the oracle adjoint at 50 x the dtype tolerance (1e-10 / 1e-5), with a
+    trainable subset."""
     rng = np.random.default_rng(1300 + n + nobs)
     ops = [("Hadamard", [w], [], False) for w in range(n)]
     nw = {"CRX": 2, "CRY": 2, "CRZ": 2, "ControlledPhaseShift": 2, "CNOT": 2, "CZ": 2, "Toffoli": 3, "IsingXX": 2,
@@ -408,17 +410,19 @@ def test_adjoint_fused_blocks(native, oracle, n, nobs):
     obs_specs = [(True, [(0.6, [("PauliZ", [1], None)]), (-0.4, [("PauliX", [0], None), ("PauliY", [n - 1], None)])]),
                  (False, [(1.0, [("PauliY", [3], None)])]),
                  (False, [(1.0, [("PauliX", [n - 2], None), ("PauliZ", [5], None)])])][:nobs]
-    sv = native.LightningGPU_C128(n)
+    suf = "C128" if dtype == "c128" else "C64"
+    rdt = np.float64 if dtype == "c128" else np.float32
+    sv = getattr(native, cls_name(dtype))(n)
     apply_ops(sv, ops)
-    adj = native.AdjointJacobianGPU_C128()
-    opsd = adj.create_ops_list([o[0] for o in ops], [np.array(o[2], np.float64) for o in ops], [o[1] for o in ops],
-                               [o[3] for o in ops], [np.zeros(0, np.complex128) for o in ops])
-    obs = [_obs_native(native, "c128", s) for s in obs_specs]
+    adj = getattr(native, "AdjointJacobianGPU_" + suf)()
+    opsd = adj.create_ops_list([o[0] for o in ops], [np.array(o[2], rdt) for o in ops], [o[1] for o in ops],
+                               [o[3] for o in ops], [np.zeros(0, np_dtype(dtype)) for o in ops])
+    obs = [_obs_native(native, dtype, s) for s in obs_specs]
     jac = np.asarray(adj.adjoint_jacobian(sv, obs, opsd, tp))
     final = oracle.run(n, to_oracle_ops(ops))
     oobs = [(s[0], [(c, [(nm, w, m) for nm, w, m in f]) for c, f in s[1]]) for s in obs_specs]
     ref = oracle.adjoint_jacobian(final, to_oracle_ops(ops), oobs, tp)
-    assert np.max(np.abs(jac - ref)) < 1e-10 * 50, np.max(np.abs(jac - ref))
+    assert np.max(np.abs(jac - ref)) < tol(dtype) * 50, np.max(np.abs(jac - ref))
     assert np.max(np.abs(ref)) > 1e-3  # the circuit has gradients to compare
 
 
