@@ -2,7 +2,7 @@
 test files (run in the build container, where the reference checkout is
 mounted; the GPU machine never reads the reference).
 
-Two sources:
+Sources:
   1. C++ Catch2 known answers: the numeric literals are read from the cited
      line ranges of the reference test files; the circuit around them is
      restated here (initial state, operation, wires, parameters).
@@ -10,6 +10,15 @@ Two sources:
      (operation, input state, expected state) tuples), evaluated from the
      reference source with a stub namespace in which ``qml.<Op>`` is the
      operation's name; no reference code runs.
+  3. The closed forms of tests/test_expval.py and tests/test_var.py: each
+     test body (its assignments, ``dev.apply`` and ``assert np.allclose``
+     statements) is evaluated against recording stubs of ``qml`` and the
+     device at the module's THETA / PHI / VARPHI rows.
+  4. The parametrize tables of tests/test_probs.py and
+     tests/test_hamiltonian_sparse.py, and the closed-form gradients of
+     tests/test_adjoint_jacobian.py (test_ry_gradient, test_rx_gradient,
+     test_multiple_rx_gradient), with the short circuits restated and
+     checked against the test source text.
 
 Usage:  python tests/golden/make_golden.py [/path/to/reference]
 """
@@ -169,8 +178,298 @@ def python_cases():
     return cases
 
 
+class _Obs:
+    """An operation or observable of a reference test, recorded by name:
+    ``name`` (or a list of names for a tensor product), wires, parameters and
+    an explicit matrix for Hermitian factors."""
+
+    def __init__(self, name, params, wires, matrix=None):
+        self.factors = [(name, [int(w) for w in np.atleast_1d(wires)], [float(p) for p in params], matrix)]
+
+    def __matmul__(self, other):
+        out = _Obs.__new__(_Obs)
+        out.factors = self.factors + other.factors
+        return out
+
+    def diagonalizing_gates(self):
+        return []  # the reference device ignores rotations in apply()
+
+    def as_op(self):
+        (name, wires, params, _), = self.factors
+        return [name, wires, params, False]
+
+    def as_obs(self):
+        return [[f[0], f[1]] + ([[[float(np.real(x)), float(np.imag(x))] for x in np.ravel(f[3])]]
+                                if f[3] is not None else []) for f in self.factors]
+
+
+class _Ham:
+    def __init__(self, coeffs, obs):
+        self.coeffs, self.obs = [float(c) for c in coeffs], obs
+
+    def sparse_matrix(self):
+        return self
+
+
+class _QmlObs:
+    """Stub of the ``qml`` namespace: constructors record operations and
+    observables; ``qml.device`` returns a recording device."""
+
+    def __getattr__(self, name):
+        def make(*args, wires=None, **kw):
+            if name == "SparseHamiltonian":
+                return args[0]
+            if name == "Hermitian":
+                return _Obs(name, [], wires, np.asarray(args[0], complex))
+            if wires is None:
+                args, wires = args[:-1], args[-1]
+            return _Obs(name, args, wires)
+        return make
+
+    def Hamiltonian(self, coeffs, obs):  # noqa: N802 (the reference's name)
+        return _Ham(coeffs, obs)
+
+    def device(self, *a, **kw):
+        return _RecDev()
+
+
+class _RecDev:
+    def __init__(self):
+        self.ops = []
+
+    def apply(self, ops, **kw):
+        self.ops.extend(o.as_op() for o in ops)
+
+    def syncH2D(self, state):
+        self.state = np.asarray(state)
+
+    def expval(self, obs):
+        if isinstance(obs, _Ham):
+            return _Meas("expval", obs)
+        return _Meas("expval", obs.as_obs())
+
+    def var(self, obs):
+        return _Meas("var", obs.as_obs())
+
+
+class _Meas:
+    """A recorded measurement (kept opaque so that ``np.array([...])`` of
+    several measurements stays a one-dimensional object array)."""
+
+    def __init__(self, kind, obs):
+        self.rec = [kind, obs]
+
+
+def _decorator_params(node, ns):
+    """(names, rows) of a ``pytest.mark.parametrize(names, rows)`` decorator."""
+    for d in node.decorator_list:
+        if isinstance(d, ast.Call) and getattr(d.func, "attr", "") == "parametrize":
+            names = [s.strip() for s in ast.literal_eval(d.args[0]).split(",")]
+            rows = eval(compile(ast.Expression(d.args[1]), "<param>", "eval"), ns)
+            if len(names) == 1:
+                return names, [(r,) for r in rows]
+            return names, [tuple(r) for r in rows]
+    return None, None
+
+
+def _run_body(fn, rel, ns):
+    """Evaluate a reference test body against the stubs; every
+    ``assert np.allclose(res, expected, ...)`` becomes a recorded pair."""
+    recorded = []
+
+    def record(res, expected, *a, **kw):
+        recorded.append((res, expected))
+        return True
+
+    body = []
+    for st in fn.body:
+        if isinstance(st, ast.Assert) and isinstance(st.test, ast.Call) and \
+                getattr(st.test.func, "attr", "") == "allclose":
+            st = ast.Expr(ast.Call(ast.Name("_record", ast.Load()), st.test.args, st.test.keywords))
+        if isinstance(st, (ast.Assign, ast.Expr)):
+            body.append(st)
+    mod = ast.fix_missing_locations(ast.Module(body, []))
+    local = dict(ns, _record=record)
+    exec(compile(mod, rel, "exec"), local)
+    return recorded, local
+
+
+def python_measure_cases():
+    """Closed-form expectation values and variances of the reference's
+    tests/test_expval.py and tests/test_var.py (TestExpval, TestTensorExpval,
+    TestVar, TestTensorVar): each test body is evaluated with the recording
+    stubs at the module's THETA / PHI / VARPHI rows; the expected values are
+    the reference's own expressions."""
+    cases = []
+    for rel in ("tests/test_expval.py", "tests/test_var.py"):
+        with open(os.path.join(REF, rel)) as f:
+            tree = ast.parse(f.read())
+        ns = {"np": np, "qml": _QmlObs(), "math": math}
+        for node in tree.body:
+            if isinstance(node, ast.Assign) and isinstance(node.targets[0], ast.Name) and \
+                    node.targets[0].id in ("THETA", "PHI", "VARPHI"):
+                ns[node.targets[0].id] = eval(compile(ast.Expression(node.value), rel, "eval"), ns)
+        for cls in tree.body:
+            if not isinstance(cls, ast.ClassDef):
+                continue
+            names, rows = _decorator_params(cls, ns)
+            if names is None:
+                continue
+            for fn in cls.body:
+                if not (isinstance(fn, ast.FunctionDef) and fn.name.startswith("test_")):
+                    continue
+                for row in rows:
+                    dev = _RecDev()
+                    env = dict(ns, tol=1e-4, qubit_device_3_wires=dev, dev=dev, **dict(zip(names, row)))
+                    recorded, local = _run_body(fn, rel, env)
+                    dev = local["dev"]
+                    for res, expected in recorded:
+                        meas = [r.rec for r in (res if isinstance(res, (list, np.ndarray)) else [res])]
+                        exp = np.atleast_1d(np.asarray(expected, float)).tolist()
+                        if len(exp) == 1 and len(meas) > 1:
+                            exp = exp * len(meas)
+                        cases.append({"kind": "measure", "source": "%s:%d (%s.%s)" % (rel, fn.lineno, cls.name,
+                                                                                     fn.name),
+                                      "n": 3, "init": None, "ops": dev.ops, "measure": meas, "expected": exp})
+    return cases
+
+
+def python_probs_sparse_cases():
+    """Known answers of tests/test_probs.py (probabilities of fixed 2-wire
+    circuits, PennyLane order) and tests/test_hamiltonian_sparse.py (sparse
+    Hamiltonian expectation values): the numbers are the reference's
+    parametrize tables; the circuits are restated from the test bodies."""
+    cases = []
+    rel = "tests/test_probs.py"
+    with open(os.path.join(REF, rel)) as f:
+        tree = ast.parse(f.read())
+    circuits = {
+        # test_probs_tape_wire0: RX(0.4), Rot(0.5, 0.3, -0.7), RY(-0.2) on wire 0
+        "test_probs_tape_wire0": [["RX", [0], [0.4], False], ["Rot", [0], [0.5, 0.3, -0.7], False],
+                                  ["RY", [0], [-0.2], False]],
+        # test_probs_tape_wire01: RX(0.5) on wire 0, RY(0.3) on wire 1
+        "test_probs_tape_wire01": [["RX", [0], [0.5], False], ["RY", [1], [0.3], False]],
+    }
+    for cls in [c for c in tree.body if isinstance(c, ast.ClassDef)]:
+        for fn in cls.body:
+            if isinstance(fn, ast.FunctionDef) and fn.name in circuits:
+                src = ast.get_source_segment(open(os.path.join(REF, rel)).read(), fn)
+                for op in circuits[fn.name]:
+                    assert "qml.%s(" % op[0] in src, (fn.name, op)
+                _, rows = _decorator_params(fn, {"np": np})
+                for (row,) in rows:
+                    wires, expected = row
+                    cases.append({"kind": "probs", "source": "%s:%d (%s)" % (rel, fn.lineno, fn.name), "n": 2,
+                                  "init": None, "ops": circuits[fn.name], "wires": [int(w) for w in np.atleast_1d(wires)],
+                                  "expected": [float(x) for x in expected]})
+    rel = "tests/test_hamiltonian_sparse.py"
+    with open(os.path.join(REF, rel)) as f:
+        text = f.read()
+    tree = ast.parse(text)
+    ns = {"np": np, "qml": _QmlObs()}
+    for cls in [c for c in tree.body if isinstance(c, ast.ClassDef)]:
+        for fn in cls.body:
+            if not isinstance(fn, ast.FunctionDef):
+                continue
+            src = ast.get_source_segment(text, fn)
+            if fn.name in ("test_sparse_Pauli_words", "test_sparse_arbitrary"):
+                assert "qml.RX(0.4, wires=[0])" in src and "qml.RY(-0.2, wires=[1])" in src
+                _, rows = _decorator_params(fn, ns)
+                for (row,) in rows:
+                    obs, expected = row
+                    cases.append({"kind": "expval_sparse", "source": "%s:%d (%s)" % (rel, fn.lineno, fn.name),
+                                  "n": 2, "init": None,
+                                  "ops": [["RX", [0], [0.4], False], ["RY", [1], [-0.2], False]],
+                                  **_csr([1.0], [obs], 2), "expected": [float(expected)]})
+            elif fn.name == "test_hamiltonian_expectation":
+                recorded, local = _run_body(fn, rel, dict(ns, qubit_device_3_wires=_RecDev(), tol=1e-4,
+                                                          _record=None))
+                sv = local["state_vector"]
+                ham = local["Hmat"]
+                cases.append({"kind": "expval_sparse", "source": "%s:%d (%s)" % (rel, fn.lineno, fn.name),
+                              "n": 3, "init": [[float(np.real(x)), float(np.imag(x))] for x in sv],
+                              **_csr(ham.coeffs, ham.obs, 3), "expected": [float(local["expected"])],
+                              # the test's state is complex64 (norm 1 to 4e-8), checked by np.allclose
+                              "tol": 1e-6})
+    return cases
+
+
+_PAULI = {"Identity": np.eye(2), "PauliX": np.array([[0, 1], [1, 0]]), "PauliY": np.array([[0, -1j], [1j, 0]]),
+          "PauliZ": np.diag([1, -1])}
+
+
+def _csr(coeffs, obs_list, n):
+    """CSR of sum_k c_k O_k on n wires (wire 0 the most significant bit), the
+    matrix that ``qml.Hamiltonian(...).sparse_matrix()`` builds."""
+    h = np.zeros((1 << n, 1 << n), complex)
+    for c, o in zip(coeffs, obs_list):
+        per = [np.eye(2)] * n
+        for name, wires, _, mat in o.factors:
+            assert len(wires) == 1
+            per[wires[0]] = mat if mat is not None else _PAULI[name]
+        m = np.array([[1.0]])
+        for p in per:
+            m = np.kron(m, p)
+        h += c * m
+    indptr, indices, data = [0], [], []
+    for r in range(1 << n):
+        for col in np.nonzero(h[r])[0]:
+            indices.append(int(col))
+            data.append([float(h[r, col].real), float(h[r, col].imag)])
+        indptr.append(len(indices))
+    return {"indptr": indptr, "indices": indices, "data": data}
+
+
+def python_adjoint_cases():
+    """Closed-form adjoint Jacobians of tests/test_adjoint_jacobian.py:
+    test_ry_gradient (d<X>/d par = cos par over its parametrize list),
+    test_rx_gradient (-sin a) and test_multiple_rx_gradient (-diag(sin p));
+    the parameters and expected expressions are evaluated from the test
+    bodies, the one-gate circuits are restated."""
+    rel = "tests/test_adjoint_jacobian.py"
+    with open(os.path.join(REF, rel)) as f:
+        text = f.read()
+    tree = ast.parse(text)
+    cases = []
+    fns = {fn.name: fn for fn in ast.walk(tree) if isinstance(fn, ast.FunctionDef)}
+
+    def assigned(fn, env, names):
+        for st in fn.body:
+            if isinstance(st, ast.Assign) and isinstance(st.targets[0], ast.Name) and st.targets[0].id in names:
+                env[st.targets[0].id] = eval(compile(ast.Expression(st.value), rel, "eval"), env)
+        return env
+
+    fn = fns["test_ry_gradient"]
+    src = ast.get_source_segment(text, fn)
+    assert "qml.RY(par, wires=[0])" in src and "qml.PauliX(0)" in src
+    _, rows = _decorator_params(fn, {"np": np})
+    for (par,) in rows:
+        env = assigned(fn, {"np": np, "par": par}, {"exact"})
+        cases.append({"kind": "adjoint", "source": "%s:%d (test_ry_gradient)" % (rel, fn.lineno), "n": 1,
+                      "ops": [["RY", [0], [float(par)], False]], "obs": [[False, [[1.0, [["PauliX", [0]]]]]]],
+                      "tp": [0], "expected": [[float(env["exact"])]]})
+    fn = fns["test_rx_gradient"]
+    src = ast.get_source_segment(text, fn)
+    assert "qml.RX(a, wires=0)" in src and "qml.PauliZ(0)" in src
+    env = assigned(fn, {"np": np}, {"a", "expected_jacobian"})
+    cases.append({"kind": "adjoint", "source": "%s:%d (test_rx_gradient)" % (rel, fn.lineno), "n": 1,
+                  "ops": [["RX", [0], [float(env["a"])], False]], "obs": [[False, [[1.0, [["PauliZ", [0]]]]]]],
+                  "tp": [0], "expected": [[float(env["expected_jacobian"])]]})
+    fn = fns["test_multiple_rx_gradient"]
+    src = ast.get_source_segment(text, fn)
+    assert "qml.RX(params[2], wires=2)" in src and "qml.expval(qml.PauliZ(idx))" in src
+    env = assigned(fn, {"np": np}, {"params", "expected_jacobian"})
+    p = [float(x) for x in env["params"]]
+    cases.append({"kind": "adjoint", "source": "%s:%d (test_multiple_rx_gradient)" % (rel, fn.lineno), "n": 3,
+                  "ops": [["RX", [w], [p[w]], False] for w in range(3)],
+                  "obs": [[False, [[1.0, [["PauliZ", [w]]]]]] for w in range(3)], "tp": [0, 1, 2],
+                  "expected": np.asarray(env["expected_jacobian"], float).tolist()})
+    return cases
+
+
 def main():
-    cases = cpp_cases() + python_cases()
+    cases = cpp_cases() + python_cases() + python_measure_cases() + python_probs_sparse_cases() + \
+        python_adjoint_cases()
     with open(OUT, "w") as f:
         json.dump({"reference": "PennyLane-Lightning-GPU 0.33.0-dev", "cases": cases}, f, indent=1)
     print("wrote %d cases to %s" % (len(cases), OUT))

@@ -123,6 +123,29 @@ def test_samples_and_shot_expval():
     assert abs(r[1]) < 0.03
 
 
+@pytest.mark.parametrize("dtype", [np.complex64, np.complex128])
+def test_sample_dimensions_and_values(dtype):
+    """The scenarios of the reference's tests/test_sample.py:43-100: the
+    shot count may change between draws, samples of PauliZ and of a tensor
+    product have one entry per shot, and every sample is +1 or -1."""
+    dev = _dev(2, dtype, shots=1000, seed=5)
+    dev.apply([Q.op("RX", 0, 1.5708), Q.op("RX", 1, 1.5708)])
+    for shots, obs in ((10, Q.PauliZ(0)), (12, Q.PauliZ(1)), (17, Q.PauliX(0) @ Q.PauliZ(1))):
+        dev.reset()
+        dev.apply([Q.op("RX", 0, 1.5708), Q.op("RX", 1, 1.5708)])
+        dev.shots = shots
+        dev._samples = dev.generate_samples()
+        s = dev.sample(obs)
+        assert s.shape == (shots,)
+        assert np.allclose(s ** 2, 1)
+    dev.reset()
+    dev.shots = 1000
+    dev.apply([Q.op("RX", 0, 1.5708)])
+    dev._samples = dev.generate_samples()
+    s = dev.sample(Q.PauliZ(0))
+    assert np.allclose(s ** 2, 1) and abs(np.mean(s)) < 0.15
+
+
 @pytest.mark.parametrize("split", [False, True])
 def test_adjoint_jacobian_vs_oracle_and_fd(oracle, split):
     rng = np.random.default_rng(2)

@@ -13,6 +13,8 @@ CASES = G.load()
 @pytest.mark.parametrize("case", CASES, ids=[G.case_id(c) for c in CASES])
 def test_gpu_matches_reference_golden(native, case, dtype):
     tol = max(G.tolerance(case), 1e-10 if dtype == "c128" else 1e-5)
+    if case["kind"] in ("measure", "probs"):
+        return _device_case(case, dtype, tol)
     psi = G.init_state(case)
     sv = getattr(native, cls_name(dtype))(np.ascontiguousarray(psi, np_dtype(dtype)))
     ops = case.get("ops") or []
@@ -43,3 +45,25 @@ def test_gpu_matches_reference_golden(native, case, dtype):
             obs.append(named[0] if len(named) == 1 else getattr(native, "TensorProdObsGPU_" + suf)(named))
         jac = np.asarray(adj.adjoint_jacobian(sv, obs, opsd, case["tp"]))
         assert np.max(np.abs(jac - np.array(case["expected"]))) < tol * 10
+
+
+def _device_case(case, dtype, tol):
+    """Expectation values, variances and probabilities through the Python
+    device, the path the reference's tests/test_expval.py, test_var.py and
+    test_probs.py drive (apply, then expval / var / probability)."""
+    from pennylane_lightning_gpu_gb300 import ops as Q
+    from pennylane_lightning_gpu_gb300.lightning_gpu import LightningGPU
+
+    dev = LightningGPU(case["n"], c_dtype=np_dtype(dtype))
+    dev.apply([Q.op(o[0], o[1], *o[2]) for o in case["ops"]])
+    if case["kind"] == "probs":
+        got = dev.probability(wires=case["wires"])
+        assert np.max(np.abs(got - np.array(case["expected"]))) < tol
+        return
+    for (kind, factors), want in zip(case["measure"], case["expected"]):
+        obs = None
+        for f in factors:
+            o = Q.Hermitian(G.cplx(f[2]).reshape(2, 2), f[1]) if len(f) > 2 else getattr(Q, f[0])(f[1][0])
+            obs = o if obs is None else obs @ o
+        got = dev.expval(obs) if kind == "expval" else dev.var(obs)
+        assert abs(got - want) < tol * 10, (kind, factors, got, want)
