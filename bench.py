@@ -540,7 +540,8 @@ def bench_serving(args):
 def profile_case(name):
     """One small invocation of a secondary kernel, sized for an ncu capture:
     fused (25-qubit complex64, one layer of RX/RY/RZ on every wire + CNOT
-    ring), batch (304 circuits of 17 qubits, complex64), pauli (26-qubit
+    ring), fused128 (25-qubit complex128, two layers of random rotations and
+    CNOT/CZ/CRY: the float-float fused blocks), batch (304 circuits of 17 qubits, complex64), pauli (26-qubit
     complex64, 24 random Pauli words + sum_i Z_i), adjoint (12-qubit
     complex128, 4 layers, 12 PauliZ observables), adjblock (24-qubit
     complex128, 2 layers of RY, RZ + CZ ladder, one PauliZ observable: the
@@ -553,6 +554,12 @@ def profile_case(name):
         n = 25
         ops = workloads.layered_ansatz(n, 1, np.random.default_rng(1))
         sv = m.LightningGPU_C64(n)
+        sv.apply([o[0] for o in ops], [list(o[1]) for o in ops], [bool(o[3]) for o in ops], [list(o[2]) for o in ops])
+        sv.synchronize()
+    elif name == "fused128":
+        n = 25
+        ops = workloads.random_circuit(n, 2, np.random.default_rng(11))
+        sv = m.LightningGPU_C128(n)
         sv.apply([o[0] for o in ops], [list(o[1]) for o in ops], [bool(o[3]) for o in ops], [list(o[2]) for o in ops])
         sv.synchronize()
     elif name == "batch":
@@ -608,7 +615,7 @@ def main():
     ap.add_argument("--no-circuits", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-serving", action="store_true")
-    ap.add_argument("--case", choices=["fused", "batch", "pauli", "adjoint", "adjblock"], default=None,
+    ap.add_argument("--case", choices=["fused", "fused128", "batch", "pauli", "adjoint", "adjblock"], default=None,
                     help="run one small secondary-kernel case (profiling) and exit")
     ap.add_argument("--only", choices=["batched", "serving", "circuits"], default=None,
                     help="run one section alone (profiling runs); the default prints the full line")
