@@ -60,6 +60,9 @@ typedef enum { LGPU_H2D = 0, LGPU_D2H = 1, LGPU_D2D = 2 } lgpu_copy_kind_t;
 typedef struct lgpu_context_s *lgpu_context_t;
 
 /* ---- library / errors ------------------------------------------------ */
+/* Errors: the reference raises LightningException from PL_CUDA_IS_SUCCESS /
+ * PL_CUSTATEVEC_IS_SUCCESS (cuda_helpers.hpp:48-80); here every call returns a
+ * status and lgpu_last_error_string() holds the message (thread-local). */
 int lgpu_abi_version(void);
 const char *lgpu_last_error_string(void);
 
@@ -94,8 +97,9 @@ lgpu_status_t lgpu_device_error(int *code, int reset);
  * the reference. */
 lgpu_status_t lgpu_selftest_bounded_wait(uint32_t spin_limit, lgpu_stream_t stream);
 
-/* ---- device and memory (DataBuffer.hpp:31-218, cuda_helpers.hpp:796-837,
- *      Bindings.cpp:1736-1748; the C++ layer needs no CUDA runtime of its own) */
+/* ---- device and memory (DataBuffer.hpp:31-218; cuda_helpers.hpp:600-650,
+ *      getGPUCount / getGPUIdx / deviceReset / getGPUArch; Bindings.cpp:1736-1748;
+ *      the C++ layer needs no CUDA runtime of its own) */
 lgpu_status_t lgpu_device_count(int *count);
 lgpu_status_t lgpu_get_device(int *device);
 lgpu_status_t lgpu_set_device(int device);
@@ -123,7 +127,17 @@ lgpu_status_t lgpu_stream_destroy(lgpu_stream_t stream);
 lgpu_status_t lgpu_stream_sync(lgpu_stream_t stream);
 lgpu_status_t lgpu_peer_access_all(void);
 
-/* ---- scratch context -------------------------------------------------- */
+/* ---- scratch context ----------------------------------------------------
+ * Replaces the per-state library handles and their workspaces: the
+ * cuStateVec / cuBLAS / cuSPARSE handles of StateVectorCudaManaged
+ * (StateVectorCudaManaged.hpp:83-134, the SharedCusvHandle / CublasCaller /
+ * SharedCusparseHandle arguments), the per-call workspace queries and
+ * cudaMalloc/cudaFree around custatevecApplyMatrix and
+ * custatevecComputeExpectation (:1433-1471, :1602-1639), and CublasCaller's
+ * mutex-guarded handle (cuda_helpers.hpp:433-440), all made by
+ * make_shared_cublas_caller / make_shared_cusv_handle /
+ * make_shared_cusparse_handle (cuda_helpers.hpp:817-839).  A context holds the
+ * reduction scratch and pinned staging of one device. */
 lgpu_status_t lgpu_context_create(int device, lgpu_context_t *ctx);
 lgpu_status_t lgpu_context_destroy(lgpu_context_t ctx);
 /* A context from the library's per-device free list (created when the list is
@@ -180,6 +194,10 @@ lgpu_status_t lgpu_apply_pauli_rotation_multi(void *const *svs, uint32_t nstates
                                               lgpu_stream_t stream);
 
 /* ---- fused gate blocks (shared-memory tiles) -------------------------------
+ * Replaces the per-gate loop of the batched applyOperation overloads
+ * (StateVectorCudaManaged.hpp:270-315), which issue one custatevecApplyMatrix
+ * or custatevecApplyPauliRotation per operation; the C++ layer plans the
+ * blocks (GateLowering.hpp).  No single reference call corresponds.
  * A block is a list of 1- and 2-target gates (controls allowed) whose target
  * bits all lie in the tile bit set.  One launch streams the state once:
  * each CTA loads a tile of 2^k amplitudes (the tile bits vary, every other bit
@@ -352,7 +370,8 @@ lgpu_status_t lgpu_adjoint_block(lgpu_context_t ctx, void *ket, void *const *bra
 
 /* ---- CUDA graphs (stream capture) ------------------------------------------
  * Capture everything issued on `stream` between begin and end into an
- * executable graph; launch replays it on any stream. */
+ * executable graph; launch replays it on any stream.  No counterpart in the
+ * reference (used by the batched-circuit executor and the serving loop). */
 typedef struct lgpu_graph_s *lgpu_graph_t;
 lgpu_status_t lgpu_graph_begin(lgpu_stream_t stream);
 lgpu_status_t lgpu_graph_end(lgpu_stream_t stream, lgpu_graph_t *graph);
