@@ -352,7 +352,15 @@ template <class PrecisionT, class ParamT> void sv_class_bindings(py::module_ &m)
     // ---- observables -------------------------------------------------------
     class_name = "ObservableGPU_C" + bitsize;
     py::class_<ObservableGPU<PrecisionT>, std::shared_ptr<ObservableGPU<PrecisionT>>>(m, class_name.c_str(),
-                                                                                      py::module_local());
+                                                                                      py::module_local())
+        .def(
+            "applyInPlace",
+            [](const ObservableGPU<PrecisionT> &obs, SV &sv) {
+                py::gil_scoped_release r;
+                obs.applyInPlace(sv);
+                sv.sync();
+            },
+            "O|psi> in place (ObservableGPU::applyInPlace; not bound by the reference module).");
 
     class_name = "NamedObsGPU_C" + bitsize;
     py::class_<NamedObsGPU<PrecisionT>, std::shared_ptr<NamedObsGPU<PrecisionT>>, ObservableGPU<PrecisionT>>(

@@ -14,7 +14,9 @@ Sources:
      test body (its assignments, ``dev.apply`` and ``assert np.allclose``
      statements) is evaluated against recording stubs of ``qml`` and the
      device at the module's THETA / PHI / VARPHI rows.
-  4. The parametrize tables of tests/test_probs.py and
+  4. The ObservableGPU applyInPlace states of Test_ObservablesGPU.cpp
+     (named, Hermitian, tensor-product and Hamiltonian observables).
+  5. The parametrize tables of tests/test_probs.py and
      tests/test_hamiltonian_sparse.py, and the closed-form gradients of
      tests/test_adjoint_jacobian.py (test_ry_gradient, test_rx_gradient,
      test_multiple_rx_gradient), with the short circuits restated and
@@ -141,6 +143,68 @@ def cpp_cases():
     cases.append({"kind": "adjoint", "source": "%s:339-407" % A, "n": 2, "ops": ops,
                   "obs": [[False, [[1.0, [["PauliX", [0]], ["PauliZ", [1]]]]]]], "tp": [1, 2, 3],
                   "expected": [exp]})
+    return cases
+
+
+CPAIR = re.compile(r"\{\s*(-?[0-9.]+(?:[eE][-+]?\d+)?)\s*,\s*(-?[0-9.]+(?:[eE][-+]?\d+)?)\s*\}")
+
+
+def cpairs(rel, a, b):
+    """The {re, im} literals on lines a..b of a reference file, in order."""
+    return [[float(x), float(y)] for x, y in CPAIR.findall(lines(rel, a, b))]
+
+
+def observable_cases():
+    """ObservableGPU::applyInPlace known answers (Test_ObservablesGPU.cpp):
+    a 4-qubit state, optional Hadamards, then observables applied in turn,
+    the state checked after each.  Amplitudes are read from the cited lines;
+    the observables are restated (a named observable with a parameter, RX
+    on wire 1 at 0.245, is given as its matrix, as is the test's rotation
+    matrix passed as a Hermitian)."""
+    O = CPP_TESTS + "/Test_ObservablesGPU.cpp"
+    h = cpairs(O, 93, 96)
+    assert len(h) == 4 and abs(h[0][0] - 0.7071067811865475) < 1e-16
+    assert "std::cos(0.1234)" in lines(O, 97, 97) and "-std::sin(0.1234)" in lines(O, 98, 98)
+    c, s_ = math.cos(0.1234), math.sin(0.1234)
+    ry = [[c, 0.0], [-s_, 0.0], [s_, 0.0], [c, 0.0]]  # lines 97-100, row-major
+    assert '"RX", {1}, {0.245}' in lines(O, 35, 35)
+    c2, s2 = math.cos(0.245 / 2), math.sin(0.245 / 2)
+    rx = [[c2, 0.0], [0.0, -s2], [0.0, -s2], [c2, 0.0]]  # RX(0.245)
+
+    def named(name, w):
+        return [name, [w], None]
+
+    def mat(m, w):
+        return ["Hermitian", [w], m]
+
+    def single(*factors):
+        return [False, [[1.0, list(factors)]]]
+
+    had = lambda ws: [["Hadamard", [w], [], False] for w in ws]
+    cases = []
+    r1, r2 = cpairs(O, 58, 59), cpairs(O, 61, 63)
+    assert len(r1) == 16 and len(r2) == 16
+    cases.append({"kind": "observable", "source": "%s:52-81" % O, "n": 4, "init": None, "ops": [],
+                  "steps": [{"ops": [], "obs": single(named("PauliX", 3)), "expected": r1},
+                            {"ops": [], "obs": single(mat(rx, 1)), "expected": r2}]})
+    r1, r2 = cpairs(O, 119, 134), cpairs(O, 136, 139)
+    assert len(r1) == 16 and len(r2) == 16
+    assert "applyHadamard({1}" in lines(O, 148, 148) and "applyHadamard({2}" in lines(O, 149, 149)
+    cases.append({"kind": "observable", "source": "%s:114-158" % O, "n": 4, "init": None, "ops": [],
+                  "steps": [{"ops": [], "obs": single(mat(h, 0)), "expected": r1},
+                            {"ops": had([1, 2]), "obs": single(mat(ry, 2)), "expected": r2}]})
+    r1, r2 = cpairs(O, 221, 224), cpairs(O, 235, 242)
+    assert len(r1) == 16 and len(r2) == 16
+    cases.append({"kind": "observable", "source": "%s:189-250" % O, "n": 4, "init": None, "ops": had([1, 2]),
+                  "steps": [{"ops": [], "obs": single(mat(h, 0), mat(ry, 2)), "expected": r1},
+                            {"ops": [], "obs": single(named("PauliX", 3), mat(rx, 1)), "expected": r2}]})
+    assert "{0.165, 0.13, 0.5423}" in lines(O, 281, 281) and "{0.8545, 0.3222}" in lines(O, 285, 285)
+    r1, r2 = cpairs(O, 324, 327), cpairs(O, 338, 342)
+    assert len(r1) == 16 and len(r2) == 16
+    ham1 = [True, [[0.165, [mat(h, 0)]], [0.13, [named("PauliX", 2)]], [0.5423, [named("PauliX", 2)]]]]
+    ham2 = [True, [[0.8545, [mat(h, 0), named("PauliX", 2)]], [0.3222, [named("PauliX", 2), named("PauliX", 3)]]]]
+    cases.append({"kind": "observable", "source": "%s:258-352" % O, "n": 4, "init": None, "ops": had([0, 1, 2]),
+                  "steps": [{"ops": [], "obs": ham1, "expected": r1}, {"ops": [], "obs": ham2, "expected": r2}]})
     return cases
 
 
@@ -469,7 +533,7 @@ def python_adjoint_cases():
 
 def main():
     cases = cpp_cases() + python_cases() + python_measure_cases() + python_probs_sparse_cases() + \
-        python_adjoint_cases()
+        python_adjoint_cases() + observable_cases()
     with open(OUT, "w") as f:
         json.dump({"reference": "PennyLane-Lightning-GPU 0.33.0-dev", "cases": cases}, f, indent=1)
     print("wrote %d cases to %s" % (len(cases), OUT))

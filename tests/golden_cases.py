@@ -43,6 +43,14 @@ def observable_matrix(factors):
     return m, wires
 
 
+def oracle_observable(obs):
+    """A fixture observable [is_hamiltonian, [[coeff, [[name, wires, matrix_or_None], ...]], ...]]
+    in the oracle's form."""
+    is_h, terms = obs
+    return (is_h, [(c, [(f[0], f[1], None if f[2] is None else cplx(f[2]).reshape(2, 2)) for f in fs])
+                   for c, fs in terms])
+
+
 def pennylane_order(p, k):
     """Probabilities of the engine's order (bit j of the index is wires[j])
     in PennyLane's order (wires[0] most significant), as the device returns them."""

@@ -33,6 +33,13 @@ def test_oracle_matches_reference_golden(oracle, case):
             mean = oracle.expval_matrix(psi, m, wires).real
             got = mean if kind == "expval" else oracle.expval_matrix(psi, m @ m, wires).real - mean ** 2
             assert abs(got - want) < tol, (kind, factors, got, want)
+    elif case["kind"] == "observable":
+        psi = oracle.apply_ops(psi, ops) if ops else psi
+        for step in case["steps"]:
+            if step["ops"]:
+                psi = oracle.apply_ops(psi, [(o[0], o[1], o[2], o[3], None) for o in step["ops"]])
+            psi = oracle.apply_observable(psi, G.oracle_observable(step["obs"]))
+            assert np.max(np.abs(psi - G.cplx(step["expected"]))) < tol
     elif case["kind"] == "probs":
         psi = oracle.apply_ops(psi, ops)
         k = len(case["wires"])
@@ -47,7 +54,7 @@ def test_oracle_matches_reference_golden(oracle, case):
 
 def test_fixture_covers_reference_tests():
     kinds = {c["kind"] for c in CASES}
-    assert kinds == {"state", "expval_matrix", "expval_sparse", "adjoint", "measure", "probs"}
+    assert kinds == {"state", "expval_matrix", "expval_sparse", "adjoint", "measure", "probs", "observable"}
     assert len(CASES) >= 150
     sources = {c["source"].split(":")[0] for c in CASES}
     for rel in ("tests/test_apply.py", "tests/test_expval.py", "tests/test_var.py", "tests/test_probs.py",

@@ -32,6 +32,13 @@ def test_gpu_matches_reference_golden(native, case, dtype):
         r = sv.ExpectationValue(np.array(case["indptr"], itype), np.array(case["indices"], itype),
                                 G.cplx(case["data"]).astype(np_dtype(dtype)))
         assert abs(r - case["expected"][0]) < tol * 10
+    elif case["kind"] == "observable":
+        suf = "C128" if dtype == "c128" else "C64"
+        for step in case["steps"]:
+            for o in step["ops"]:
+                sv.apply(o[0], o[1], bool(o[3]), o[2], np.zeros(0, np_dtype(dtype)))
+            _native_observable(native, suf, np_dtype(dtype), step["obs"]).applyInPlace(sv)
+            assert np.max(np.abs(sv.GetState() - G.cplx(step["expected"]))) < tol
     elif case["kind"] == "adjoint":
         suf = "C128" if dtype == "c128" else "C64"
         rdt = np.float64 if dtype == "c128" else np.float32
@@ -45,6 +52,26 @@ def test_gpu_matches_reference_golden(native, case, dtype):
             obs.append(named[0] if len(named) == 1 else getattr(native, "TensorProdObsGPU_" + suf)(named))
         jac = np.asarray(adj.adjoint_jacobian(sv, obs, opsd, case["tp"]))
         assert np.max(np.abs(jac - np.array(case["expected"]))) < tol * 10
+
+
+def _native_observable(native, suf, cdt, obs):
+    """ObservableGPU objects of the bindings for a fixture observable."""
+    def factor(f):
+        if f[2] is not None:
+            return getattr(native, "HermitianObsGPU_" + suf)(G.cplx(f[2]).astype(cdt), f[1])
+        return getattr(native, "NamedObsGPU_" + suf)(f[0], f[1])
+
+    def term(fs):
+        parts = [factor(f) for f in fs]
+        return parts[0] if len(parts) == 1 else getattr(native, "TensorProdObsGPU_" + suf)(parts)
+
+    is_h, terms = obs
+    if not is_h:
+        assert len(terms) == 1
+        return term(terms[0][1])
+    rdt = np.float64 if suf == "C128" else np.float32
+    return getattr(native, "HamiltonianGPU_" + suf)(np.array([c for c, _ in terms], rdt),
+                                                    [term(fs) for _, fs in terms])
 
 
 def _device_case(case, dtype, tol):
