@@ -415,6 +415,8 @@ def bench_circuits(args):
         c1[key] = {"apply_ms": round(t_apply * 1e3, 2), "expval_ms": round(t_exp * 1e3, 2),
                    "probs_ms": round(t_probs * 1e3, 2), "shots_ms": round(t_shots * 1e3, 2),
                    "total_ms": round((t_apply + t_exp + t_probs + t_shots) * 1e3, 2),
+                   # one read of the state each, through the Python device (host overhead included)
+                   "probs_gbs": round(S / t_probs / 1e9, 1), "shots_gbs": round(S / t_shots / 1e9, 1),
                    "apply_gbs_if_one_pass_per_op": round(len(ops) * 2 * S / t_apply / 1e9, 1)}
         del dev
     out["config1"] = c1

@@ -931,6 +931,49 @@ static lgpu_status_t pauli_words_t(lgpu_context_t ctx, const void *sv, uint32_t 
 }
 
 // ---------------------------------------------------------------------------
+// |a|^2 without FP64 instructions (GB300 issues about 2 FP64 operations per
+// clock per SM, so one DFMA + DMUL + DADD per amplitude would bound these
+// single-read passes at a third of HBM bandwidth): the square is formed in
+// float-float (exact for complex64; complex128 is split to float-float
+// first), short runs are summed in float-float and each run's sum is added
+// to a double.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ DF prob_df(const float2 a) {
+    const float px = df_mul_rn(a.x, a.x), py = df_mul_rn(a.y, a.y);
+    return df_sum<2>({DF{px, df_fma(a.x, a.x, -px)}, DF{py, df_fma(a.y, a.y, -py)}});
+}
+__device__ __forceinline__ DF prob_df(const double2 a) {
+    const DF x = df_from_double(a.x), y = df_from_double(a.y);
+    return df_sum<2>({df_mul(x, x), df_mul(y, y)});
+}
+
+// Sum of |a_i|^2 over i = start + STRIDE j < len (one thread's share of a
+// slice): eight loads in flight per thread.
+template <class T, class I, int STRIDE>
+__device__ __forceinline__ double strided_prob_sum(const cplx_t<T> *__restrict__ a, I len, int start) {
+    double acc = 0.0;
+    for (I o = I(start); o < len; o += I(STRIDE * 8)) {
+        cplx_t<T> v[8];
+#pragma unroll
+        for (int u = 0; u < 8; u++) {
+            const I i = o + I(STRIDE * u);
+            v[u] = i < len ? a[i] : cplx_t<T>{};
+        }
+        DF run = prob_df(v[0]);
+#pragma unroll
+        for (int u = 1; u < 8; u++) run = df_sum<2>({run, prob_df(v[u])});
+        acc += df_to_double(run);
+    }
+    return acc;
+}
+
+__device__ __forceinline__ double warp_sum_d(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// ---------------------------------------------------------------------------
 // Probabilities
 // ---------------------------------------------------------------------------
 struct BinMap {
@@ -945,6 +988,11 @@ template <class I> __device__ __forceinline__ uint32_t bin_of(I i, const BinMap 
     return b;
 }
 
+// Marginal histogram over chunks of 2^chunk_log2 amplitudes.  Bins are split
+// into the probed bits at or above chunk_log2 (constant over a chunk) and
+// those below it.  Without low bits a chunk feeds one bin: each warp sums a
+// slice and adds it to the CTA's histogram once.  With low bits every thread
+// accumulates runs of equal bin over its strided amplitudes.
 template <class T, class I>
 __global__ void __launch_bounds__(256)
     probs_hist_kernel(const cplx_t<T> *__restrict__ sv, I N, int chunk_log2, BinMap bm, double *partials,
@@ -952,27 +1000,53 @@ __global__ void __launch_bounds__(256)
     extern __shared__ double hist[];
     const int nb = 1 << bm.k;
     for (int b = threadIdx.x; b < nb; b += 256) hist[b] = 0.0;
+    uint32_t lowsel = 0;  // probed bits below chunk_log2 (output bit positions)
+    for (int q = 0; q < bm.k; q++)
+        if (bm.bits[q] < chunk_log2) lowsel |= 1u << q;
     __syncthreads();
     const I chunk = I(1) << chunk_log2;
     const I nchunks = N >> chunk_log2;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (I c = blockIdx.x; c < nchunks; c += gridDim.x) {
         const I base = c * chunk;
+        uint32_t hb = 0;
+        for (int q = 0; q < bm.k; q++)
+            if (!((lowsel >> q) & 1u)) hb |= uint32_t((base >> bm.bits[q]) & 1) << q;
+        if (lowsel == 0 && chunk_log2 >= 8) {
+            const I per = chunk >> 3;  // eight warps, one slice each (>= 32 amplitudes)
+            const double v = warp_sum_d(strided_prob_sum<T, I, 32>(sv + base + I(warp) * per, per, lane));
+            if (lane == 0) atomicAdd(&hist[hb], v);
+            continue;
+        }
+        // A thread visits offsets threadIdx.x + 256 j: probed bits below 8
+        // are fixed for it, so without probed bits in [8, chunk_log2) its
+        // whole share of the chunk feeds one bin.
+        uint32_t tb = hb, midsel = 0;
+        for (int q = 0; q < bm.k; q++)
+            if ((lowsel >> q) & 1u) {
+                if (bm.bits[q] < 8) tb |= uint32_t((threadIdx.x >> bm.bits[q]) & 1) << q;
+                else midsel |= 1u << q;
+            }
+        if (midsel == 0) {
+            if (I(threadIdx.x) < chunk) atomicAdd(&hist[tb], strided_prob_sum<T, I, 256>(sv + base, chunk, threadIdx.x));
+            continue;
+        }
         uint32_t cur = 0xffffffffu;
-        double run = 0.0;
+        DF run{0.0f, 0.0f};
         for (I o = threadIdx.x; o < chunk; o += 256) {
-            const I i = base + o;
-            const cplx_t<T> a = sv[i];
-            const double p = fma(double(a.x), double(a.x), double(a.y) * double(a.y));
-            const uint32_t b = bin_of<I>(i, bm);
+            const DF pr = prob_df(sv[base + o]);
+            uint32_t b = hb;
+            for (int q = 0; q < bm.k; q++)
+                if ((lowsel >> q) & 1u) b |= uint32_t((o >> bm.bits[q]) & 1) << q;
             if (b != cur) {
-                if (cur != 0xffffffffu) atomicAdd(&hist[cur], run);
+                if (cur != 0xffffffffu) atomicAdd(&hist[cur], df_to_double(run));
                 cur = b;
-                run = p;
+                run = pr;
             } else {
-                run += p;
+                run = df_sum<2>({run, pr});
             }
         }
-        if (cur != 0xffffffffu) atomicAdd(&hist[cur], run);
+        if (cur != 0xffffffffu) atomicAdd(&hist[cur], df_to_double(run));
     }
     __syncthreads();
     for (int b = threadIdx.x; b < nb; b += 256) partials[size_t(blockIdx.x) * nb + b] = hist[b];
@@ -990,10 +1064,40 @@ template <class T, class I>
 __global__ void probs_atomic_kernel(const cplx_t<T> *__restrict__ sv, I N, BinMap bm, double *out) {
     const I stride = I(gridDim.x) * blockDim.x;
     for (I i = I(blockIdx.x) * blockDim.x + threadIdx.x; i < N; i += stride) {
-        const cplx_t<T> a = sv[i];
-        atomicAdd(&out[bin_of<I>(i, bm)], fma(double(a.x), double(a.x), double(a.y) * double(a.y)));
+        atomicAdd(&out[bin_of<I>(i, bm)], df_to_double(prob_df(sv[i])));
     }
 }
+
+// Marginal probabilities when every probed bit is at or above chunk_log2:
+// each chunk feeds one bin.  One CTA per bin sums the chunk sums csum[c] of
+// that bin in a fixed order.  The chunk index has m = n - chunk_log2 bits;
+// the probed ones are fixed by the bin, the others enumerate the bin's chunks.
+__global__ void __launch_bounds__(256)
+    probs_from_chunks_kernel(const double *__restrict__ csum, int m, int chunk_log2, BinMap bm, double *out) {
+    __shared__ double2 sm[8];
+    const uint32_t b = blockIdx.x;
+    uint64_t fixed = 0, probed = 0;
+    for (int q = 0; q < bm.k; q++) {
+        const int cb = bm.bits[q] - chunk_log2;
+        probed |= uint64_t(1) << cb;
+        if ((b >> q) & 1u) fixed |= uint64_t(1) << cb;
+    }
+    const uint64_t freemask = ((uint64_t(1) << m) - 1) & ~probed;
+    const uint64_t per_bin = uint64_t(1) << (m - bm.k);
+    double acc = 0.0;
+    for (uint64_t j = threadIdx.x; j < per_bin; j += 256) {
+        uint64_t c = fixed, jj = j;
+        for (uint64_t fm = freemask; fm && jj; fm &= fm - 1, jj >>= 1)
+            if (jj & 1) c |= fm & (0 - fm);
+        acc += csum[c];
+    }
+    const double2 v = block_reduce_d2<256>(make_double2(acc, 0.0), sm);
+    if (threadIdx.x == 0) out[b] = v.x;
+}
+
+template <class T>
+__global__ void __launch_bounds__(256)
+    chunk_sums_kernel(const cplx_t<T> *__restrict__ sv, uint64_t nchunks, int chunk_log2, double *csum);
 
 template <class T, class I>
 static lgpu_status_t probs_t(lgpu_context_t ctx, const void *svv, uint32_t n, const std::vector<int> &bits,
@@ -1006,11 +1110,28 @@ static lgpu_status_t probs_t(lgpu_context_t ctx, const void *svv, uint32_t n, co
     const size_t nb = size_t(1) << bm.k;
     void *p = nullptr;
     double *res = nullptr;
-    if (bm.k <= 12) {
+    int minbit = int(n);
+    for (int b : bits) minbit = std::min(minbit, b);
+    // chunks of >= 1024 amplitudes, at most 2^20 of them, each inside one bin
+    const int cl_fast = std::min(minbit, std::max(10, int(n) - 14));
+    if (bm.k >= 1 && bm.k <= 12 && cl_fast >= 10 && int(n) - cl_fast <= 20) {
+        const uint64_t nchunks = N >> cl_fast;
+        LGPU_TRY(ctx_scratch(ctx, 256 + nchunks * sizeof(double) + nb * sizeof(double), &p));
+        auto *csum = reinterpret_cast<double *>(static_cast<char *>(p) + 256);
+        res = csum + nchunks;
+        const unsigned g1 =
+            unsigned(std::max<uint64_t>(1, std::min<uint64_t>((nchunks + 7) / 8, uint64_t(sm_count()) * 8)));
+        chunk_sums_kernel<T><<<g1, 256, 0, s>>>(sv, nchunks, cl_fast, csum);
+        LGPU_CHECK_LAUNCH();
+        probs_from_chunks_kernel<<<unsigned(nb), 256, 0, s>>>(csum, int(n) - cl_fast, cl_fast, bm, res);
+        LGPU_CHECK_LAUNCH();
+    } else if (bm.k <= 12) {
         int chunk_log2 = std::max(8, int(n) - 12);
         if (chunk_log2 > int(n)) chunk_log2 = int(n);
         const uint64_t nchunks = N >> chunk_log2;
-        const unsigned g = unsigned(std::min<uint64_t>(nchunks, uint64_t(sm_count()) * 4));
+        // two CTAs per SM (eight loads in flight per thread are enough for
+        // HBM) keep the last CTA's sum over the per-CTA histograms short
+        const unsigned g = unsigned(std::min<uint64_t>(nchunks, uint64_t(sm_count()) * 2));
         LGPU_TRY(ctx_scratch(ctx, 256 + size_t(g) * nb * sizeof(double) + nb * sizeof(double), &p));
         auto *counter = static_cast<unsigned *>(p);
         auto *partials = reinterpret_cast<double *>(static_cast<char *>(p) + 256);
@@ -1040,55 +1161,74 @@ static lgpu_status_t probs_t(lgpu_context_t ctx, const void *svv, uint32_t n, co
 // ---------------------------------------------------------------------------
 // Sampling
 // ---------------------------------------------------------------------------
+// csum[c] = sum of |a_i|^2 over chunk c: one warp per chunk.
 template <class T>
 __global__ void __launch_bounds__(256)
     chunk_sums_kernel(const cplx_t<T> *__restrict__ sv, uint64_t nchunks, int chunk_log2, double *csum) {
-    __shared__ double2 sm[8];
+    const int lane = threadIdx.x & 31;
+    const uint64_t warp = (uint64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    const uint64_t nwarps = (uint64_t(gridDim.x) * blockDim.x) >> 5;
     const uint64_t chunk = uint64_t(1) << chunk_log2;
-    for (uint64_t c = blockIdx.x; c < nchunks; c += gridDim.x) {
-        double acc = 0.0;
-        for (uint64_t o = threadIdx.x; o < chunk; o += 256) {
-            const cplx_t<T> a = sv[c * chunk + o];
-            acc += fma(double(a.x), double(a.x), double(a.y) * double(a.y));
-        }
-        double2 v = block_reduce_d2<256>(make_double2(acc, 0.0), sm);
-        if (threadIdx.x == 0) csum[c] = v.x;
-        __syncthreads();
+    for (uint64_t c = warp; c < nchunks; c += nwarps) {
+        const double v = warp_sum_d(strided_prob_sum<T, uint64_t, 32>(sv + c * chunk, chunk, lane));
+        if (lane == 0) csum[c] = v;
     }
 }
 
-// Exclusive scan of csum (in place) by one CTA; writes the total to *total.
-__global__ void __launch_bounds__(1024) scan_kernel(double *csum, uint64_t nchunks, double *total) {
-    __shared__ double part[1024];
-    const uint64_t per = (nchunks + 1023) / 1024;
-    const uint64_t lo = threadIdx.x * per, hi = min(nchunks, lo + per);
-    double s = 0.0;
-    for (uint64_t i = lo; i < hi; i++) s += csum[i];
-    part[threadIdx.x] = s;
+// Exclusive scan of csum within blocks of 1024 chunks (one CTA each, in
+// place); each block's total goes to btot[block].
+__global__ void __launch_bounds__(1024) scan_blocks_kernel(double *csum, uint64_t nchunks, double *btot) {
+    __shared__ double wsum[32];
+    const uint64_t i = uint64_t(blockIdx.x) * 1024 + threadIdx.x;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const double v = i < nchunks ? csum[i] : 0.0;
+    double x = v;  // inclusive warp scan
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const double y = __shfl_up_sync(0xffffffffu, x, d);
+        if (lane >= d) x += y;
+    }
+    if (lane == 31) wsum[w] = x;
     __syncthreads();
-    if (threadIdx.x == 0) {
-        double run = 0.0;
-        for (int t = 0; t < 1024; t++) {
-            const double v = part[t];
-            part[t] = run;
-            run += v;
+    if (w == 0) {
+        const double t = wsum[lane];
+        double z = t;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const double y = __shfl_up_sync(0xffffffffu, z, d);
+            if (lane >= d) z += y;
         }
-        *total = run;
+        wsum[lane] = z - t;
+        if (lane == 31) btot[blockIdx.x] = z;
     }
     __syncthreads();
-    double run = part[threadIdx.x];
-    for (uint64_t i = lo; i < hi; i++) {
-        const double v = csum[i];
-        csum[i] = run;
+    if (i < nchunks) csum[i] = wsum[w] + (x - v);
+}
+
+// Exclusive scan of the (at most 256) block totals by one thread; the sum
+// of all probabilities goes to *total.
+__global__ void scan_tops_kernel(double *btot, uint32_t nblocks, double *total) {
+    if (threadIdx.x != 0) return;
+    double run = 0.0;
+    for (uint32_t b = 0; b < nblocks; b++) {
+        const double v = btot[b];
+        btot[b] = run;
         run += v;
     }
+    *total = run;
+}
+
+// Cumulative probability before chunk c.
+__device__ __forceinline__ double chunk_start(const double *csum, const double *boff, uint64_t c) {
+    return boff[c >> 10] + csum[c];
 }
 
 // One warp per draw.
 template <class T>
 __global__ void __launch_bounds__(256)
-    search_kernel(const cplx_t<T> *__restrict__ sv, const double *__restrict__ cstart, uint64_t nchunks,
-                  int chunk_log2, const double *total_p, const double *draws, uint64_t shots, uint64_t *out) {
+    search_kernel(const cplx_t<T> *__restrict__ sv, const double *__restrict__ cstart,
+                  const double *__restrict__ boff, uint64_t nchunks, int chunk_log2, const double *total_p,
+                  const double *draws, uint64_t shots, uint64_t *out) {
     const int lane = threadIdx.x & 31;
     const uint64_t warp = (uint64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
     const uint64_t nwarps = (uint64_t(gridDim.x) * blockDim.x) >> 5;
@@ -1096,11 +1236,11 @@ __global__ void __launch_bounds__(256)
     const uint64_t chunk = uint64_t(1) << chunk_log2;
     for (uint64_t sidx = warp; sidx < shots; sidx += nwarps) {
         const double target = draws[sidx] * total;
-        // chunk: last c with cstart[c] <= target (binary search)
+        // chunk: last c whose start is <= target (binary search)
         uint64_t lo = 0, hi = nchunks;  // invariant: answer in [lo, hi)
         while (hi - lo > 1) {
             const uint64_t mid = (lo + hi) >> 1;
-            if (cstart[mid] <= target)
+            if (chunk_start(cstart, boff, mid) <= target)
                 lo = mid;
             else
                 hi = mid;
@@ -1110,7 +1250,7 @@ __global__ void __launch_bounds__(256)
         // non-zero probability of a later chunk).
         uint64_t found = ~uint64_t(0), last_nz = ~uint64_t(0);
         for (uint64_t c = lo; c < nchunks && found == ~uint64_t(0); c++) {
-            double run = cstart[c];
+            double run = chunk_start(cstart, boff, c);
             for (uint64_t o = 0; o < chunk; o += 32) {
                 double p = 0.0;
                 if (o + lane < chunk) {
@@ -1162,8 +1302,9 @@ static lgpu_status_t sample_t(lgpu_context_t ctx, const void *svv, uint32_t n, c
     if (chunk_log2 > int(n)) chunk_log2 = int(n);
     if (chunk_log2 < 5 && n >= 5) chunk_log2 = 5;
     const uint64_t nchunks = (uint64_t(1) << n) >> chunk_log2;
-    // scratch: total(256) | csum | draws | out
-    const size_t cbytes = nchunks * sizeof(double);
+    // scratch: total (bytes 128..255) | csum, then the block offsets | draws | out
+    const uint64_t nblocks = (nchunks + 1023) / 1024;  // <= 256 (nchunks <= 2^18)
+    const size_t cbytes = (nchunks + nblocks) * sizeof(double);
     const size_t dbytes = shots * sizeof(double);
     const size_t obytes = shots * sizeof(uint64_t);
     void *p = nullptr;
@@ -1178,7 +1319,8 @@ static lgpu_status_t sample_t(lgpu_context_t ctx, const void *svv, uint32_t n, c
     LGPU_TRY(ctx_pinned(ctx, std::max(dbytes, obytes), &pin));
     std::memcpy(pin, draws, dbytes);
     LGPU_CUDA_TRY(cudaMemcpyAsync(ddraws, pin, dbytes, cudaMemcpyHostToDevice, s));
-    const unsigned g1 = unsigned(std::min<uint64_t>(nchunks, uint64_t(sm_count()) * 8));
+    const unsigned g1 =
+        unsigned(std::max<uint64_t>(1, std::min<uint64_t>((nchunks + 7) / 8, uint64_t(sm_count()) * 8)));
     if (n < 5) {
         // tiny states: a single chunk
         chunk_sums_kernel<T><<<1, 256, 0, s>>>(sv, 1, int(n), csum);
@@ -1188,10 +1330,14 @@ static lgpu_status_t sample_t(lgpu_context_t ctx, const void *svv, uint32_t n, c
     LGPU_CHECK_LAUNCH();
     const uint64_t nch = n < 5 ? 1 : nchunks;
     const int clog = n < 5 ? int(n) : chunk_log2;
-    scan_kernel<<<1, 1024, 0, s>>>(csum, nch, total);
+    double *boff = csum + nchunks;
+    const uint64_t nbl = (nch + 1023) / 1024;
+    scan_blocks_kernel<<<unsigned(nbl), 1024, 0, s>>>(csum, nch, boff);
+    LGPU_CHECK_LAUNCH();
+    scan_tops_kernel<<<1, 32, 0, s>>>(boff, uint32_t(nbl), total);
     LGPU_CHECK_LAUNCH();
     const unsigned g2 = unsigned(std::max<uint64_t>(1, std::min<uint64_t>((shots + 7) / 8, uint64_t(sm_count()) * 8)));
-    search_kernel<T><<<g2, 256, 0, s>>>(sv, csum, nch, clog, total, ddraws, shots, dout);
+    search_kernel<T><<<g2, 256, 0, s>>>(sv, csum, boff, nch, clog, total, ddraws, shots, dout);
     LGPU_CHECK_LAUNCH();
     // Copy back through the pinned buffer; the draws have already been consumed
     // by the H2D copy that precedes this D2H copy in stream order.

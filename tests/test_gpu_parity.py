@@ -204,7 +204,27 @@ def test_probabilities(native, oracle, dtype, n):
 
 
 @pytest.mark.parametrize("dtype", DTYPES)
-@pytest.mark.parametrize("n", [1, 4, 10, 16])
+@pytest.mark.parametrize("n", [18, 22])
+def test_probability_kernel_paths(native, oracle, dtype, n):
+    """Every reduction path of lgpu_probs against the oracle: all probed state
+    bits >= 10 (per-chunk sums, then one CTA per bin), bits below 8 (a fixed
+    bin per thread), bits between 8 and the chunk size (runs of equal bin,
+    n = 22), mixed sets, wires in any order, and more than 12 wires (global
+    atomics)."""
+    rng = np.random.default_rng(900 + n)
+    psi = random_state(n, rng)
+    sv = make_sv(native, dtype, psi)
+    cases = [[0], [2, 0, 1], list(range(n - 10)), [n - 1], [n - 2, n - 3], [n - 9, n - 10], [n - 12, 1],
+             [n - 1, 0, n // 2], list(range(n - 8, n)), list(range(13))]
+    for wires in cases:
+        got = np.asarray(sv.Probability(wires))
+        ref = oracle.probs(psi, wires)
+        assert got.shape == ref.shape
+        assert np.max(np.abs(got - ref)) < tol(dtype), (wires,)
+
+
+@pytest.mark.parametrize("dtype", DTYPES)
+@pytest.mark.parametrize("n", [1, 4, 10, 16, 24])
 def test_sampling_bit_exact(native, oracle, dtype, n):
     rng = np.random.default_rng(500 + n)
     psi = random_state(n, rng)
