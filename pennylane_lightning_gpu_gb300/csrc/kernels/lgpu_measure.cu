@@ -1129,9 +1129,10 @@ static lgpu_status_t probs_t(lgpu_context_t ctx, const void *svv, uint32_t n, co
         int chunk_log2 = std::max(8, int(n) - 12);
         if (chunk_log2 > int(n)) chunk_log2 = int(n);
         const uint64_t nchunks = N >> chunk_log2;
-        // two CTAs per SM (eight loads in flight per thread are enough for
-        // HBM) keep the last CTA's sum over the per-CTA histograms short
-        const unsigned g = unsigned(std::min<uint64_t>(nchunks, uint64_t(sm_count()) * 2));
+        // eight loads in flight per thread; with many bins, two CTAs per SM
+        // keep the last CTA's sum over the per-CTA histograms short
+        const uint64_t per_sm = nb <= 64 ? 8 : 2;
+        const unsigned g = unsigned(std::min<uint64_t>(nchunks, uint64_t(sm_count()) * per_sm));
         LGPU_TRY(ctx_scratch(ctx, 256 + size_t(g) * nb * sizeof(double) + nb * sizeof(double), &p));
         auto *counter = static_cast<unsigned *>(p);
         auto *partials = reinterpret_cast<double *>(static_cast<char *>(p) + 256);
