@@ -163,13 +163,146 @@ static lgpu_status_t expval_big(lgpu_context_t ctx, const cplx_t<T> *sv, uint32_
     return deliver(ctx, res, 1, out, out_on_device, s);
 }
 
+// ---------------------------------------------------------------------------
+// Dense matrix expectation, t <= 2, without FP64 work per amplitude:
+// <a|M|a> = sum_rc M_rc G_rc with the Gram sums G_rc = sum_g conj(a_gr) a_gc
+// (Hermitian: D real diagonal sums and D(D-1)/2 complex ones).  Each thread
+// forms the products in float-float (complex128 amplitudes are split first),
+// sums runs of UB groups in float-float and adds each run to a double; the
+// last CTA contracts the reduced G with M in double.
+// ---------------------------------------------------------------------------
+template <class T, class I, int TT> struct GramParams {
+    Holes holes;
+    I off[1 << TT];
+    I ngroups;
+    double m[2 * (1 << TT) * (1 << TT)];
+    const cplx_t<T> *sv;
+};
+
+__device__ __forceinline__ DF to_df(float x) { return DF{x, 0.0f}; }
+__device__ __forceinline__ DF to_df(double x) { return df_from_double(x); }
+
+template <class T, class I, int TT>
+__global__ void __launch_bounds__(kReduceBlock)
+    gram_expval_kernel(const GramParams<T, I, TT> p, double2 *partials, unsigned *counter, double2 *out) {
+    constexpr int D = 1 << TT, NA = D * D, N2 = NA / 2, UB = TT == 1 ? 4 : 2;
+    __shared__ double2 sm[kReduceBlock / 32];
+    __shared__ double gsum[NA];
+    double accd[NA];
+#pragma unroll
+    for (int j = 0; j < NA; j++) accd[j] = 0.0;
+    const I stride = I(gridDim.x) * kReduceBlock;
+    for (I g0 = I(blockIdx.x) * kReduceBlock + threadIdx.x; g0 < p.ngroups; g0 += I(UB) * stride) {
+        cplx_t<T> v[UB][D];
+#pragma unroll
+        for (int u = 0; u < UB; u++) {
+            const I g = g0 + I(u) * stride;
+            const bool ok = g < p.ngroups;
+            const I base = insert_holes<I>(ok ? g : I(0), p.holes);
+#pragma unroll
+            for (int c = 0; c < D; c++) v[u][c] = ok ? p.sv[base | p.off[c]] : cplx_t<T>{};
+        }
+        DF acc[NA];
+#pragma unroll
+        for (int j = 0; j < NA; j++) acc[j] = DF{0.0f, 0.0f};
+#pragma unroll
+        for (int u = 0; u < UB; u++) {
+            DF ar[D], ai[D];
+#pragma unroll
+            for (int c = 0; c < D; c++) {
+                ar[c] = to_df(v[u][c].x);
+                ai[c] = to_df(v[u][c].y);
+            }
+#pragma unroll
+            for (int r = 0; r < D; r++) acc[r] = df_sum<3>({acc[r], df_mul(ar[r], ar[r]), df_mul(ai[r], ai[r])});
+            int k = D;
+#pragma unroll
+            for (int r = 0; r < D; r++)
+#pragma unroll
+                for (int c = r + 1; c < D; c++) {
+                    acc[k] = df_sum<3>({acc[k], df_mul(ar[r], ar[c]), df_mul(ai[r], ai[c])});
+                    acc[k + 1] = df_sum<3>({acc[k + 1], df_mul(ar[r], ai[c]), df_neg(df_mul(ai[r], ar[c]))});
+                    k += 2;
+                }
+        }
+#pragma unroll
+        for (int j = 0; j < NA; j++) accd[j] += df_to_double(acc[j]);
+    }
+#pragma unroll
+    for (int k = 0; k < N2; k++) {
+        const double2 v = block_reduce_d2<kReduceBlock>(make_double2(accd[2 * k], accd[2 * k + 1]), sm);
+        if (threadIdx.x == 0) partials[size_t(blockIdx.x) * N2 + k] = v;
+        __syncthreads();
+    }
+    if (last_block_arrive(counter)) {
+#pragma unroll
+        for (int k = 0; k < N2; k++) {
+            double2 s = make_double2(0.0, 0.0);
+            for (unsigned b = threadIdx.x; b < gridDim.x; b += kReduceBlock) {
+                const double2 q = __ldcg(&partials[size_t(b) * N2 + k]);
+                s.x += q.x;
+                s.y += q.y;
+            }
+            s = block_reduce_d2<kReduceBlock>(s, sm);
+            if (threadIdx.x == 0) {
+                gsum[2 * k] = s.x;
+                gsum[2 * k + 1] = s.y;
+            }
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) {
+            double re = 0.0, im = 0.0;
+            for (int r = 0; r < D; r++) {  // M_rr G_rr
+                re += p.m[2 * (r * D + r)] * gsum[r];
+                im += p.m[2 * (r * D + r) + 1] * gsum[r];
+            }
+            int k = D;
+            for (int r = 0; r < D; r++)
+                for (int c = r + 1; c < D; c++) {  // M_rc G_rc + M_cr conj(G_rc)
+                    const double gr = gsum[k], gi = gsum[k + 1];
+                    const double ar = p.m[2 * (r * D + c)], ai = p.m[2 * (r * D + c) + 1];
+                    const double br = p.m[2 * (c * D + r)], bi = p.m[2 * (c * D + r) + 1];
+                    re += ar * gr - ai * gi + br * gr + bi * gi;
+                    im += ar * gi + ai * gr + bi * gr - br * gi;
+                    k += 2;
+                }
+            *out = make_double2(re, im);
+            *counter = 0u;
+        }
+    }
+}
+
+template <class T, class I, int TT>
+static lgpu_status_t expval_gram(lgpu_context_t ctx, const cplx_t<T> *sv, uint32_t n, const double *matrix,
+                                 const std::vector<int> &tg, double *out, int out_on_device, cudaStream_t s) {
+    constexpr int D = 1 << TT, N2 = D * D / 2;
+    GramParams<T, I, TT> p{};
+    p.holes = make_holes(tg);
+    for (int r = 0; r < D; r++) {
+        uint64_t o = 0;
+        for (int k = 0; k < TT; k++)
+            if ((r >> (TT - 1 - k)) & 1) o |= uint64_t(1) << tg[size_t(k)];
+        p.off[r] = I(o);
+    }
+    p.ngroups = I(uint64_t(1) << (n - TT));
+    std::memcpy(p.m, matrix, sizeof(double) * 2 * D * D);
+    p.sv = sv;
+    const unsigned g = reduce_grid(uint64_t(p.ngroups));
+    ReduceScratch rs;
+    LGPU_TRY(reduce_scratch(ctx, g, N2, &rs));
+    double2 *res = rs.partials + size_t(g) * N2;
+    gram_expval_kernel<T, I, TT><<<g, kReduceBlock, 0, s>>>(p, rs.partials, rs.counter, res);
+    LGPU_CHECK_LAUNCH();
+    return deliver(ctx, res, 1, out, out_on_device, s);
+}
+
 template <class T, class I>
 static lgpu_status_t expval_dispatch(lgpu_context_t ctx, const void *sv, uint32_t n, const double *matrix,
                                      const std::vector<int> &tg, double *out, int od, cudaStream_t s) {
     const auto *p = static_cast<const cplx_t<T> *>(sv);
     switch (tg.size()) {
-    case 1: return expval_small<T, I, 1>(ctx, p, n, matrix, tg, out, od, s);
-    case 2: return expval_small<T, I, 2>(ctx, p, n, matrix, tg, out, od, s);
+    case 1: return expval_gram<T, I, 1>(ctx, p, n, matrix, tg, out, od, s);
+    case 2: return expval_gram<T, I, 2>(ctx, p, n, matrix, tg, out, od, s);
     case 3: return expval_small<T, I, 3>(ctx, p, n, matrix, tg, out, od, s);
     case 4: return expval_small<T, I, 4>(ctx, p, n, matrix, tg, out, od, s);
     default: return expval_big<T, I>(ctx, p, n, matrix, tg, out, od, s);

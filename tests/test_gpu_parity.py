@@ -141,7 +141,43 @@ def test_expval_matrix(native, oracle, dtype, k):
 
 
 @pytest.mark.parametrize("dtype", DTYPES)
-def test_named_observable_expval(native, oracle, dtype):
+@pytest.mark.parametrize("k", [1, 2])
+def test_expval_matrix_gram_sums(native, oracle, dtype, k):
+    """1- and 2-target expectations go through Gram sums (G_rc = sum conj(a_r)
+    a_c, contracted with M at the end): Hermitian and general complex
+    matrices, both parts of the complex result (through the C ABI), targets
+    low, high and mixed, on a 20-qubit state so that many CTAs take part."""
+    import ctypes
+
+    import pennylane_lightning_gpu_gb300 as pkg
+
+    rng = np.random.default_rng(250 + k)
+    n = 20
+    psi = random_state(n, rng)
+    sv = make_sv(native, dtype, psi)
+    lib = ctypes.CDLL(pkg.library_path())
+    dp = ctypes.POINTER(ctypes.c_double)
+    ctx = ctypes.c_void_p()
+    assert lib.lgpu_context_create(0, ctypes.byref(ctx)) == 0
+    try:
+        for wires in (list(range(k)), list(range(n - k, n)), [int(x) for x in rng.choice(n, k, replace=False)]):
+            for m in (random_hermitian(1 << k, rng), random_unitary(1 << k, rng)):
+                ref = oracle.expval_matrix(psi, m, wires)
+                got = sv.ExpectationValue(wires, m.ravel())
+                assert abs(got - ref.real) < tol(dtype) * 10, (wires, got, ref)
+                # both parts through the C ABI (targets as state bits, first = most significant matrix bit)
+                mat = np.ascontiguousarray(m, np.complex128).view(np.float64)
+                bits = np.array([n - 1 - w for w in wires], np.int32)
+                out = np.zeros(2)
+                rc = lib.lgpu_expval_matrix(ctx, ctypes.c_void_p(sv.dataPtr()), ctypes.c_uint32(n),
+                                            ctypes.c_int(1 if dtype == "c128" else 0), mat.ctypes.data_as(dp),
+                                            ctypes.c_uint32(k), bits.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
+                                            out.ctypes.data_as(dp), ctypes.c_int(0), ctypes.c_void_p(sv.streamPtr()))
+                assert rc == 0
+                assert abs(complex(out[0], out[1]) - ref) < tol(dtype) * 10, (wires, out, ref)
+    finally:
+        lib.lgpu_context_destroy(ctx)
+
     rng = np.random.default_rng(11)
     n = 6
     psi = random_state(n, rng)
