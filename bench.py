@@ -543,7 +543,8 @@ def profile_case(name):
     """One small invocation of a secondary kernel, sized for an ncu capture:
     fused (25-qubit complex64, one layer of RX/RY/RZ on every wire + CNOT
     ring), fused128 (25-qubit complex128, two layers of random rotations and
-    CNOT/CZ/CRY: the float-float fused blocks), batch (304 circuits of 17 qubits, complex64), pauli (26-qubit
+    CNOT/CZ/CRY: the float-float fused blocks), gram (26-qubit complex64,
+    expectations of 1- and 2-target matrices: the Gram-sum kernel), batch (304 circuits of 17 qubits, complex64), pauli (26-qubit
     complex64, 24 random Pauli words + sum_i Z_i), adjoint (12-qubit
     complex128, 4 layers, 12 PauliZ observables), adjblock (24-qubit
     complex128, 2 layers of RY, RZ + CZ ladder, one PauliZ observable: the
@@ -564,6 +565,13 @@ def profile_case(name):
         sv = m.LightningGPU_C128(n)
         sv.apply([o[0] for o in ops], [list(o[1]) for o in ops], [bool(o[3]) for o in ops], [list(o[2]) for o in ops])
         sv.synchronize()
+    elif name == "gram":
+        n = 26
+        sv = m.LightningGPU_C64(n)
+        sv.apply(["Hadamard"] * n, [[w] for w in range(n)], [False] * n, [[]] * n)
+        z = np.array([[1, 0], [0, -1]], np.complex64)
+        sv.ExpectationValue([0], z.ravel())
+        sv.ExpectationValue([3, 17], np.kron(z, z).ravel())
     elif name == "batch":
         rng = np.random.default_rng(2)
         circ = []
@@ -617,7 +625,7 @@ def main():
     ap.add_argument("--no-circuits", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-serving", action="store_true")
-    ap.add_argument("--case", choices=["fused", "fused128", "batch", "pauli", "adjoint", "adjblock"], default=None,
+    ap.add_argument("--case", choices=["fused", "fused128", "gram", "batch", "pauli", "adjoint", "adjblock"], default=None,
                     help="run one small secondary-kernel case (profiling) and exit")
     ap.add_argument("--only", choices=["batched", "serving", "circuits"], default=None,
                     help="run one section alone (profiling runs); the default prints the full line")

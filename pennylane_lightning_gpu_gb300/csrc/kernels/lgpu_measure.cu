@@ -168,7 +168,7 @@ static lgpu_status_t expval_big(lgpu_context_t ctx, const cplx_t<T> *sv, uint32_
 // <a|M|a> = sum_rc M_rc G_rc with the Gram sums G_rc = sum_g conj(a_gr) a_gc
 // (Hermitian: D real diagonal sums and D(D-1)/2 complex ones).  Each thread
 // forms the products in float-float (complex128 amplitudes are split first),
-// sums runs of UB groups in float-float and adds each run to a double; the
+// sums 16 runs of UB groups in float-float, then adds them to a double; the
 // last CTA contracts the reduced G with M in double.
 // ---------------------------------------------------------------------------
 template <class T, class I, int TT> struct GramParams {
@@ -192,6 +192,10 @@ __global__ void __launch_bounds__(kReduceBlock)
 #pragma unroll
     for (int j = 0; j < NA; j++) accd[j] = 0.0;
     const I stride = I(gridDim.x) * kReduceBlock;
+    DF acc[NA];
+#pragma unroll
+    for (int j = 0; j < NA; j++) acc[j] = DF{0.0f, 0.0f};
+    int runs = 0;
     for (I g0 = I(blockIdx.x) * kReduceBlock + threadIdx.x; g0 < p.ngroups; g0 += I(UB) * stride) {
         cplx_t<T> v[UB][D];
 #pragma unroll
@@ -202,9 +206,6 @@ __global__ void __launch_bounds__(kReduceBlock)
 #pragma unroll
             for (int c = 0; c < D; c++) v[u][c] = ok ? p.sv[base | p.off[c]] : cplx_t<T>{};
         }
-        DF acc[NA];
-#pragma unroll
-        for (int j = 0; j < NA; j++) acc[j] = DF{0.0f, 0.0f};
 #pragma unroll
         for (int u = 0; u < UB; u++) {
             DF ar[D], ai[D];
@@ -225,9 +226,17 @@ __global__ void __launch_bounds__(kReduceBlock)
                     k += 2;
                 }
         }
+        if (++runs == 16) {  // 16 runs of UB groups in float-float, then into the doubles
+            runs = 0;
 #pragma unroll
-        for (int j = 0; j < NA; j++) accd[j] += df_to_double(acc[j]);
+            for (int j = 0; j < NA; j++) {
+                accd[j] += df_to_double(acc[j]);
+                acc[j] = DF{0.0f, 0.0f};
+            }
+        }
     }
+#pragma unroll
+    for (int j = 0; j < NA; j++) accd[j] += df_to_double(acc[j]);
 #pragma unroll
     for (int k = 0; k < N2; k++) {
         const double2 v = block_reduce_d2<kReduceBlock>(make_double2(accd[2 * k], accd[2 * k + 1]), sm);
