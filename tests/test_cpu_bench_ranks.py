@@ -67,3 +67,13 @@ def test_gate_bytes_follow_the_touched_fraction():
     assert bench.gate_bytes("CRY", S) == S
     assert bench.gate_bytes("CZ", S) == S / 2
     assert bench.gate_bytes("Toffoli", S) == S / 2
+
+
+def test_distinct_flip_masks():
+    import bench
+
+    terms = [(0.5, "ZZ", [0, 1]), (1.0, "Z", [3]), (0.2, "XZ", [2, 0]), (0.1, "YX", [2, 5]),
+             (0.3, "XY", [5, 2]), (0.4, "X", [2])]
+    # {} (diagonal), {2}, {2, 5}
+    assert bench.distinct_flip_masks(terms) == 3
+    assert bench.distinct_flip_masks([]) == 0
