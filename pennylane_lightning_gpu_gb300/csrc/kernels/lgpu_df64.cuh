@@ -201,6 +201,35 @@ template <int K> LGPU_HD DF df_sum(const DF (&t)[K]) {
 
 LGPU_HD DF df_neg(DF x) { return DF{-x.hi, -x.lo}; }
 
+// conj(a) . (M a) over one group of D amplitudes, added to (re, im).  m holds
+// M row-major as (re, im) float-float pairs; a = ar + i ai.  Each row
+// x_r = sum_c M_rc a_c is formed in float-float, then re += Re(conj(a_r) x_r)
+// and im += Im(conj(a_r) x_r).  The row loop stays rolled (the columns are
+// unrolled); a_r is picked from the arrays by compile-time selects, so the
+// arrays stay in registers.
+template <int D, class MAT>
+LGPU_HD void df_expval_group(const MAT &m, const DF (&ar)[D], const DF (&ai)[D], DF &re, DF &im) {
+#pragma unroll 1
+    for (int r = 0; r < D; r++) {
+        DF xr{0.0f, 0.0f}, xi{0.0f, 0.0f};
+#pragma unroll
+        for (int c = 0; c < D; c++) {
+            const DF mr = m[2 * (r * D + c)], mi = m[2 * (r * D + c) + 1];
+            xr = df_sum<3>({xr, df_mul(mr, ar[c]), df_neg(df_mul(mi, ai[c]))});
+            xi = df_sum<3>({xi, df_mul(mr, ai[c]), df_mul(mi, ar[c])});
+        }
+        DF pr = ar[0], pi = ai[0];
+#pragma unroll
+        for (int k = 1; k < D; k++)
+            if (k == r) {
+                pr = ar[k];
+                pi = ai[k];
+            }
+        re = df_sum<3>({re, df_mul(pr, xr), df_mul(pi, xi)});
+        im = df_sum<3>({im, df_mul(pr, xi), df_neg(df_mul(pi, xr))});
+    }
+}
+
 // Body code of a diagonal with entries exactly +1 or -1 (CZ, Z, their
 // controlled forms): the float-float kernels flip signs instead of
 // multiplying.  Only these kernels know the code; the host sets it.

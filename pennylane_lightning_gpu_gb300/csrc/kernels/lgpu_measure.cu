@@ -305,6 +305,94 @@ static lgpu_status_t expval_gram(lgpu_context_t ctx, const cplx_t<T> *sv, uint32
     return deliver(ctx, res, 1, out, out_on_device, s);
 }
 
+// Dense matrix expectation on 3 targets in float-float: per group of 8
+// amplitudes conj(a) . (M a) (df_expval_group), 16 groups per thread summed
+// in float-float before each double flush, fixed-order reduction.
+template <class T, class I, int TT> struct DfExpvalParams {
+    Holes holes;
+    I off[1 << TT];
+    I ngroups;
+    DF m[2 * (1 << TT) * (1 << TT)];  // (re, im) of M_rc, row-major
+    const cplx_t<T> *sv;
+};
+
+template <class T, class I, int TT>
+__global__ void __launch_bounds__(kReduceBlock)
+    expval_df_kernel(const __grid_constant__ DfExpvalParams<T, I, TT> p, double2 *partials, unsigned *counter,
+                     double2 *out) {
+    constexpr int D = 1 << TT;
+    __shared__ double2 sm[kReduceBlock / 32];
+    double2 accd = make_double2(0.0, 0.0);
+    DF re{0.0f, 0.0f}, im{0.0f, 0.0f};
+    int runs = 0;
+    const I stride = I(gridDim.x) * kReduceBlock;
+    for (I g = I(blockIdx.x) * kReduceBlock + threadIdx.x; g < p.ngroups; g += stride) {
+        const I base = insert_holes<I>(g, p.holes);
+        DF ar[D], ai[D];
+#pragma unroll
+        for (int c = 0; c < D; c++) {
+            const cplx_t<T> v = p.sv[base | p.off[c]];
+            ar[c] = to_df(v.x);
+            ai[c] = to_df(v.y);
+        }
+        df_expval_group<D>(p.m, ar, ai, re, im);
+        if (++runs == 16) {
+            runs = 0;
+            accd.x += df_to_double(re);
+            accd.y += df_to_double(im);
+            re = DF{0.0f, 0.0f};
+            im = DF{0.0f, 0.0f};
+        }
+    }
+    accd.x += df_to_double(re);
+    accd.y += df_to_double(im);
+    const double2 v = block_reduce_d2<kReduceBlock>(accd, sm);
+    if (threadIdx.x == 0) partials[blockIdx.x] = v;
+    __syncthreads();
+    if (last_block_arrive(counter)) {
+        double2 t = make_double2(0.0, 0.0);
+        for (unsigned b = threadIdx.x; b < gridDim.x; b += kReduceBlock) {
+            const double2 q = __ldcg(&partials[b]);
+            t.x += q.x;
+            t.y += q.y;
+        }
+        t = block_reduce_d2<kReduceBlock>(t, sm);
+        if (threadIdx.x == 0) {
+            *out = t;
+            *counter = 0u;
+        }
+    }
+}
+
+template <class T, class I, int TT>
+static lgpu_status_t expval_df(lgpu_context_t ctx, const cplx_t<T> *sv, uint32_t n, const double *matrix,
+                               const std::vector<int> &tg, double *out, int out_on_device, cudaStream_t s) {
+    constexpr int D = 1 << TT;
+    auto *p = new DfExpvalParams<T, I, TT>();
+    p->holes = make_holes(tg);
+    for (int r = 0; r < D; r++) {
+        uint64_t o = 0;
+        for (int k = 0; k < TT; k++)
+            if ((r >> (TT - 1 - k)) & 1) o |= uint64_t(1) << tg[size_t(k)];
+        p->off[r] = I(o);
+    }
+    p->ngroups = I(uint64_t(1) << (n - TT));
+    for (int i = 0; i < 2 * D * D; i++) p->m[i] = df_split_host(matrix[i]);
+    p->sv = sv;
+    const unsigned g = reduce_grid(uint64_t(p->ngroups));
+    ReduceScratch rs;
+    lgpu_status_t st = reduce_scratch(ctx, g, 1, &rs);
+    if (st != LGPU_OK) {
+        delete p;
+        return st;
+    }
+    double2 *res = rs.partials + size_t(g);
+    expval_df_kernel<T, I, TT><<<g, kReduceBlock, 0, s>>>(*p, rs.partials, rs.counter, res);
+    delete p;
+    LGPU_CHECK_LAUNCH();
+    return deliver(ctx, res, 1, out, out_on_device, s);
+}
+
 template <class T, class I>
 static lgpu_status_t expval_dispatch(lgpu_context_t ctx, const void *sv, uint32_t n, const double *matrix,
                                      const std::vector<int> &tg, double *out, int od, cudaStream_t s) {
@@ -312,7 +400,7 @@ static lgpu_status_t expval_dispatch(lgpu_context_t ctx, const void *sv, uint32_
     switch (tg.size()) {
     case 1: return expval_gram<T, I, 1>(ctx, p, n, matrix, tg, out, od, s);
     case 2: return expval_gram<T, I, 2>(ctx, p, n, matrix, tg, out, od, s);
-    case 3: return expval_small<T, I, 3>(ctx, p, n, matrix, tg, out, od, s);
+    case 3: return expval_df<T, I, 3>(ctx, p, n, matrix, tg, out, od, s);
     case 4: return expval_small<T, I, 4>(ctx, p, n, matrix, tg, out, od, s);
     default: return expval_big<T, I>(ctx, p, n, matrix, tg, out, od, s);
     }

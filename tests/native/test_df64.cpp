@@ -5,7 +5,9 @@
 //    otherwise;
 //  * every structured body agrees with a long-double evaluation of the same
 //    2x2 product within 4e-14 of the largest input magnitude;
-//  * NaN inputs give NaN outputs.
+//  * NaN inputs give NaN outputs;
+//  * df_expval_group (3-target expectations) agrees with long double.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <random>
@@ -136,6 +138,53 @@ int main() {
         lgpu::body1_df<0>(mdf, a, b, c, d);
         if (!std::isnan(a)) fail("nan", a, a);
     }
-    std::printf("split %ld rebuild %ld body %ld bad %ld\n", n_split, n_rebuild, n_body, bad);
+    // conj(a) . (M a) over groups of 8 amplitudes (3-target expectations):
+    // general complex M and amplitudes of mixed magnitudes, summed over 16
+    // groups as the kernel does, against long double within 1e-13 of the
+    // sum of |a|^2 |M|.
+    long n_expval = 0;
+    {
+        std::uniform_int_distribution<int> aex(-14, 0);
+        for (int trial = 0; trial < 2000; trial++) {
+            double mm[128];
+            DF mdf[128];
+            double mscale = 0;
+            for (int k = 0; k < 128; k++) {
+                mm[k] = u(gen);
+                mdf[k] = lgpu::df_from_double(mm[k]);
+                mscale = std::max(mscale, std::fabs(mm[k]));
+            }
+            DF re{0.0f, 0.0f}, im{0.0f, 0.0f};
+            long double rre = 0, rim = 0, norm = 0;
+            for (int g = 0; g < 16; g++) {
+                double a[16];
+                DF ar[8], ai[8];
+                for (int c = 0; c < 8; c++) {
+                    const double sc = std::ldexp(1.0, aex(gen));
+                    a[2 * c] = sc * u(gen);
+                    a[2 * c + 1] = sc * u(gen);
+                    ar[c] = lgpu::df_from_double(a[2 * c]);
+                    ai[c] = lgpu::df_from_double(a[2 * c + 1]);
+                    norm += (long double)a[2 * c] * a[2 * c] + (long double)a[2 * c + 1] * a[2 * c + 1];
+                }
+                lgpu::df_expval_group<8>(mdf, ar, ai, re, im);
+                for (int r = 0; r < 8; r++) {
+                    long double xr = 0, xi = 0;
+                    for (int c = 0; c < 8; c++) {
+                        const long double mr = mm[2 * (r * 8 + c)], mi = mm[2 * (r * 8 + c) + 1];
+                        xr += mr * a[2 * c] - mi * a[2 * c + 1];
+                        xi += mr * a[2 * c + 1] + mi * a[2 * c];
+                    }
+                    rre += a[2 * r] * xr + a[2 * r + 1] * xi;
+                    rim += a[2 * r] * xi - a[2 * r + 1] * xr;
+                }
+            }
+            const double bound = 1e-13 * double(norm) * mscale * 8;
+            n_expval++;
+            if (std::fabs(lgpu::df_to_double(re) - double(rre)) > bound) fail("expval re", lgpu::df_to_double(re), double(rre));
+            if (std::fabs(lgpu::df_to_double(im) - double(rim)) > bound) fail("expval im", lgpu::df_to_double(im), double(rim));
+        }
+    }
+    std::printf("split %ld rebuild %ld body %ld expval %ld bad %ld\n", n_split, n_rebuild, n_body, n_expval, bad);
     return bad == 0 ? 0 : 1;
 }

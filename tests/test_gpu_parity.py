@@ -141,12 +141,13 @@ def test_expval_matrix(native, oracle, dtype, k):
 
 
 @pytest.mark.parametrize("dtype", DTYPES)
-@pytest.mark.parametrize("k", [1, 2])
-def test_expval_matrix_gram_sums(native, oracle, dtype, k):
+@pytest.mark.parametrize("k", [1, 2, 3])
+def test_expval_matrix_float_float_paths(native, oracle, dtype, k):
     """1- and 2-target expectations go through Gram sums (G_rc = sum conj(a_r)
-    a_c, contracted with M at the end): Hermitian and general complex
-    matrices, both parts of the complex result (through the C ABI), targets
-    low, high and mixed, on a 20-qubit state so that many CTAs take part."""
+    a_c, contracted with M at the end), 3-target ones through conj(a).(M a)
+    per group in float-float: Hermitian and general complex matrices, both
+    parts of the complex result (through the C ABI), targets low, high and
+    mixed, on a 20-qubit state so that many CTAs take part."""
     import ctypes
 
     import pennylane_lightning_gpu_gb300 as pkg
