@@ -17,7 +17,8 @@
 namespace lgpu {
 
 // ---------------------------------------------------------------------------
-// Dense matrix expectation, t <= 5 (matrix in the parameter bank)
+// Dense matrix expectation in FP64, 4 targets (matrix in the parameter bank;
+// 1-3 targets take the float-float kernels below)
 // ---------------------------------------------------------------------------
 template <class T, class I, int TT> struct ExpvalBody {
     Holes holes;
