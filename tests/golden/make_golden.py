@@ -93,6 +93,61 @@ def cpp_cases():
                     e[int(idx)] = [float(re_), float(im_)]
             cases.append({"kind": "state", "source": "%s:437-528" % P, "n": 3, "init": None,
                           "ops": [["IsingXX", wires, [ang[k % 2]], adj]], "expected": e})
+    # --- IsingYY on |000>: angles 536, expected 541-551, adjoint 556-566 (same layout as IsingXX)
+    ang = numbers(P, 536, 536)
+    for (a, b), adj in (((541, 551), False), ((556, 566), True)):
+        entries = ISING.findall(lines(P, a, b))
+        assert len(entries) == 8
+        for k in range(4):
+            wires = [0, 1] if k < 2 else [0, 2]
+            e = [[0.0, 0.0] for _ in range(8)]
+            for kk, idx, re_, im_ in entries:
+                if int(kk) == k:
+                    e[int(idx)] = [float(re_), float(im_)]
+            cases.append({"kind": "state", "source": "%s:530-621" % P, "n": 3, "init": None,
+                          "ops": [["IsingYY", wires, [ang[k % 2]], adj]], "expected": e})
+    # --- IsingZZ on |000>: angles 629, expected 634-635, adjoint 639-640, wires {0,1} and {0,2}
+    ang = numbers(P, 629, 629)
+    for (a, b), adj in (((634, 635), False), ((639, 640), True)):
+        entries = ISING.findall(lines(P, a, b))
+        assert len(entries) == 2
+        for kk, idx, re_, im_ in entries:
+            for wires in ([0, 1], [0, 2]):
+                e = [[0.0, 0.0] for _ in range(8)]
+                e[int(idx)] = [float(re_), float(im_)]
+                cases.append({"kind": "state", "source": "%s:623-694" % P, "n": 3, "init": None,
+                              "ops": [["IsingZZ", wires, [ang[int(kk)]], adj]], "expected": e})
+    # --- excitations and MultiRZ on |0...0>: every apply<Gate>({wires}, adjoint, angles[index])
+    # call of the test block, checked against expected_results[_adj][index] (phases of |0...0>
+    # for the Minus/Plus forms and MultiRZ) or against the unchanged |0...0> (SingleExcitation,
+    # DoubleExcitation)
+    for name, a, b in (("SingleExcitation", 695, 740), ("SingleExcitationMinus", 741, 815),
+                       ("SingleExcitationPlus", 816, 890), ("DoubleExcitation", 891, 926),
+                       ("DoubleExcitationMinus", 927, 981), ("DoubleExcitationPlus", 982, 1036),
+                       ("MultiRZ", 1037, 1108)):
+        text = lines(P, a, b)
+        assert ("LightningGPU::apply%s\"" % name) in text
+        nq = int(re.search(r"num_qubits = (\d+);", text).group(1))
+        ang = [float(x) for x in re.search(r"angles\{([^}]*)\}", text).group(1).split(",")]
+        table = {False: {}, True: {}}
+        for m in re.finditer(r"expected_results(_adj)?\[(\d+)\]\[(\d+)\] = \{([^,]+), ([^}]+)\}", text):
+            table[m.group(1) is not None].setdefault(int(m.group(2)), {})[int(m.group(3))] = [float(m.group(4)),
+                                                                                            float(m.group(5))]
+        calls = re.findall(r"apply%s\(\s*\{([0-9, ]+)\},\s*(true|false),\s*angles\[index\]" % name, text)
+        assert calls, name
+        for wires_s, adj_s in calls:
+            wires = [int(x) for x in wires_s.split(",")]
+            adj = adj_s == "true"
+            for k, theta in enumerate(ang):
+                e = [[0.0, 0.0] for _ in range(1 << nq)]
+                if table[adj]:
+                    for idx, v in table[adj][k].items():
+                        e[idx] = v
+                else:
+                    assert re.search(r"expected_results\[0\] = \{1\.0, 0\.0\}", text)
+                    e[0] = [1.0, 0.0]
+                cases.append({"kind": "state", "source": "%s:%d-%d" % (P, a, b), "n": nq, "init": None,
+                              "ops": [[name, wires, [theta], adj]], "expected": e})
     # --- dense expval (1.263 - 1.011i) with a non-normalised state: NonParam 866-889
     init = pairs(numbers(N, 867, 869))
     mat = pairs(numbers(N, 874, 886))
