@@ -1,0 +1,37 @@
+"""Host unit test of the gate lowering and the shared-memory fusion planner
+(GateLowering.hpp): block invariants and state equivalence of the planned
+order on random circuits (compiled with the host compiler; no GPU needed)."""
+import os
+import shutil
+import subprocess
+import tempfile
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _cuda_include():
+    for cand in (os.environ.get("CUDA_HOME"), os.environ.get("CUDA_PATH"), "/usr/local/cuda"):
+        if cand and os.path.exists(os.path.join(cand, "include", "cuComplex.h")):
+            return os.path.join(cand, "include")
+    nvcc = shutil.which("nvcc")
+    if nvcc:
+        inc = os.path.join(os.path.dirname(os.path.dirname(nvcc)), "include")
+        if os.path.exists(os.path.join(inc, "cuComplex.h")):
+            return inc
+    return None
+
+
+def test_fusion_plan_keeps_the_state():
+    inc = _cuda_include()
+    if inc is None:
+        pytest.skip("cuComplex.h not found")
+    with tempfile.TemporaryDirectory() as d:
+        exe = os.path.join(d, "test_planner")
+        subprocess.run(["g++", "-O2", "-std=c++17", "-I" + os.path.join(ROOT, "include"),
+                        "-I" + os.path.join(ROOT, "pennylane_lightning_gpu_gb300", "csrc", "cpp"), "-I" + inc,
+                        os.path.join(ROOT, "tests", "native", "test_planner.cpp"), "-o", exe], check=True)
+        r = subprocess.run([exe], capture_output=True, text=True)
+        assert r.returncode == 0, r.stdout + r.stderr
+        assert "bad 0" in r.stdout
