@@ -19,6 +19,7 @@
 #include "lgpu_bodies.cuh"
 #include "lgpu_df64.cuh"
 #include "lgpu_f64emu.cuh"
+#include "lgpu_fused_plan.h"
 #include "lgpu_internal.cuh"
 
 namespace lgpu {
@@ -428,28 +429,6 @@ __global__ void __launch_bounds__(kGateBlock)
 // ---------------------------------------------------------------------------
 // Fused shared-memory tiles
 // ---------------------------------------------------------------------------
-constexpr int kFusedMaxGates = 96;
-constexpr int kFusedMatPool = 2304;  // matrix elements, in the state's precision
-
-struct FGate {
-    uint8_t ntgt, q0, q1, body;  // q0 = most significant matrix bit; body: Body1 of a 1-target gate
-    uint8_t lt, lcm, lcv, pad;   // register group: local target, local control mask and values;
-                                 // pad = 1: diag(+-1, +-1) (complex128 float-float sign flips)
-    uint32_t in_mask, in_val;    // controls inside the tile (tile positions)
-    uint32_t mat_off;            // into the matrix pool
-    uint64_t out_mask, out_val;  // controls outside the tile (state bits)
-};
-
-// A run of gates applied between two barriers: kind 0 = a register group on
-// the R tile positions p[] (ascending), kind 1 = one gate through the
-// per-gate shared-memory paths.
-struct FGroup {
-    uint8_t kind;
-    uint8_t p[4];
-    uint8_t pad[3];
-    uint16_t first, count;
-};
-
 template <class T, class I> struct FusedParams {
     Holes holes;       // tile bits (sorted) as holes: tile base = insert(tau)
     I ntiles;
@@ -1168,110 +1147,6 @@ int body_of_2x2_host(const double *mm, KConst *kc) {
     kc[0] = make_kconst(a.im); kc[1] = make_kconst(b.im);
     kc[2] = make_kconst(c.im); kc[3] = make_kconst(d.im);
     return B_DENSE;
-}
-
-// Split a launch's gates into register groups (1-target gates whose targets
-// and in-tile controls span at most R tile positions, padded with the lowest
-// unused positions) and single gates, and fill the local target and control
-// fields of grouped gates.  Gates on disjoint tile positions commute, so a
-// group may take any later gate whose earlier conflicting gates are all
-// placed: starting from the first unplaced gate, a group first takes every
-// such gate inside its position set, then grows the set by the gate adding
-// the fewest positions, up to R.  (A layer of 1-qubit gates followed by a CNOT
-// chain becomes two groups instead of one per run of consecutive gates.)
-// The gates and their integer-pipe constants are permuted into group order;
-// returns the number of groups.
-template <class KC>
-static int group_fused_gates(FGate *gates, KC *kc, int cnt, int k, int R, FGroup *groups) {
-    std::vector<uint32_t> P(size_t(cnt) + 1);
-    for (int i = 0; i < cnt; i++) {
-        const FGate &g = gates[i];
-        P[size_t(i)] = g.in_mask | (1u << g.q0) | (g.ntgt == 2 ? (1u << g.q1) : 0u);
-    }
-    auto groupable = [&](int i) { return k >= R && gates[i].ntgt == 1 && __builtin_popcount(P[size_t(i)]) <= R; };
-    std::vector<char> done(size_t(cnt) + 1, 0);
-    auto ready = [&](int i) {
-        for (int h = 0; h < i; h++)
-            if (!done[size_t(h)] && (P[size_t(h)] & P[size_t(i)])) return false;
-        return true;
-    };
-    std::vector<int> order;
-    order.reserve(size_t(cnt));
-    int ng = 0;
-    int first = 0;
-    while (true) {
-        while (first < cnt && done[size_t(first)]) first++;
-        if (first >= cnt) break;
-        const int i0 = first;  // every earlier gate is placed
-        const uint16_t start = uint16_t(order.size());
-        done[size_t(i0)] = 1;
-        order.push_back(i0);
-        if (!groupable(i0)) {
-            groups[ng++] = FGroup{1, {0, 0, 0, 0}, {0, 0, 0}, start, 1};
-            continue;
-        }
-        uint32_t set = P[size_t(i0)];
-        for (;;) {
-            bool added = false;
-            for (int i = i0 + 1; i < cnt; i++)
-                if (!done[size_t(i)] && groupable(i) && (P[size_t(i)] & ~set) == 0 && ready(i)) {
-                    done[size_t(i)] = 1;
-                    order.push_back(i);
-                    added = true;
-                }
-            if (added) continue;
-            int best = -1, best_n = R + 1;
-            for (int i = i0 + 1; i < cnt; i++)
-                if (!done[size_t(i)] && groupable(i) && ready(i)) {
-                    const int c = __builtin_popcount(set | P[size_t(i)]);
-                    if (c < best_n) {
-                        best = i;
-                        best_n = c;
-                    }
-                }
-            if (best < 0 || best_n > R) break;
-            set |= P[size_t(best)];
-            done[size_t(best)] = 1;
-            order.push_back(best);
-        }
-        const int count = int(order.size()) - int(start);
-        if (count == 1) {  // a lone gate touches only its own pairs through the per-gate path
-            groups[ng++] = FGroup{1, {0, 0, 0, 0}, {0, 0, 0}, start, 1};
-            continue;
-        }
-        for (int q = 0; q < k && __builtin_popcount(set) < R; q++) set |= 1u << q;
-        FGroup G{0, {0, 0, 0, 0}, {0, 0, 0}, start, uint16_t(count)};
-        int nb = 0;
-        for (int q = 0; q < k; q++)
-            if ((set >> q) & 1u) G.p[nb++] = uint8_t(q);
-        groups[ng++] = G;
-    }
-    // permute into group order, then fill the local fields of grouped gates
-    std::vector<FGate> g2(gates, gates + cnt);
-    std::vector<unsigned char> k2(sizeof(KC) * size_t(cnt));
-    std::memcpy(k2.data(), kc, k2.size());
-    for (int i = 0; i < cnt; i++) {
-        gates[i] = g2[size_t(order[size_t(i)])];
-        std::memcpy(&kc[i], k2.data() + sizeof(KC) * size_t(order[size_t(i)]), sizeof(KC));
-    }
-    for (int gr = 0; gr < ng; gr++) {
-        const FGroup &G = groups[gr];
-        if (G.kind != 0) continue;
-        int loc[32];
-        for (int b = 0; b < R; b++) loc[G.p[b]] = b;
-        for (int t = G.first; t < G.first + G.count; t++) {
-            FGate &g = gates[t];
-            g.lt = uint8_t(loc[g.q0]);
-            g.lcm = 0;
-            g.lcv = 0;
-            for (int q = 0; q < k; q++)
-                if ((g.in_mask >> q) & 1u) {
-                    g.lcm |= uint8_t(1u << loc[q]);
-                    if ((g.in_val >> q) & 1u) g.lcv |= uint8_t(1u << loc[q]);
-                }
-        }
-    }
-    return ng;
 }
 
 template <class T, class I, bool EMU, int NT, int STAGES, int MINB, bool DFM = false>
