@@ -1,7 +1,8 @@
 """Host unit tests of the gate lowering and the shared-memory fusion planner
-(GateLowering.hpp), and of the register-group split of a fused block
-(lgpu_fused_plan.h): invariants and state equivalence of the reordered
-gates on random inputs (compiled with the host compiler; no GPU needed)."""
+(GateLowering.hpp), of the register-group split of a fused block
+(lgpu_fused_plan.h) and of the Pauli-word tile pass plan
+(lgpu_pauli_plan.h): invariants, and state equivalence of the reordered
+gates, on random inputs (compiled with the host compiler; no GPU needed)."""
 import os
 import shutil
 import subprocess
@@ -44,6 +45,17 @@ def test_register_groups_keep_the_state():
         subprocess.run(["g++", "-O2", "-std=c++17",
                         "-I" + os.path.join(ROOT, "pennylane_lightning_gpu_gb300", "csrc", "kernels"),
                         os.path.join(ROOT, "tests", "native", "test_fused_groups.cpp"), "-o", exe], check=True)
+        r = subprocess.run([exe], capture_output=True, text=True)
+        assert r.returncode == 0, r.stdout + r.stderr
+        assert "bad 0" in r.stdout
+
+
+def test_pauli_tile_pass_plan():
+    with tempfile.TemporaryDirectory() as d:
+        exe = os.path.join(d, "test_pauli_plan")
+        subprocess.run(["g++", "-O2", "-std=c++17",
+                        "-I" + os.path.join(ROOT, "pennylane_lightning_gpu_gb300", "csrc", "kernels"),
+                        os.path.join(ROOT, "tests", "native", "test_pauli_plan.cpp"), "-o", exe], check=True)
         r = subprocess.run([exe], capture_output=True, text=True)
         assert r.returncode == 0, r.stdout + r.stderr
         assert "bad 0" in r.stdout
