@@ -274,7 +274,8 @@ class Hamiltonian(Observable):
         self.ops = list(observables)
         if len(self.coeffs) != len(self.ops):
             raise ValueError("number of coefficients and observables differ")
-        wires = sorted({w for o in self.ops for w in o.wires})
+        # PennyLane's order: wires in order of first appearance (any hashable labels)
+        wires = list(dict.fromkeys(w for o in self.ops for w in o.wires))
         super().__init__("Hamiltonian", wires)
 
     def matrix(self, wire_order=None):
