@@ -148,6 +148,25 @@ def cpp_cases():
                     e[0] = [1.0, 0.0]
                 cases.append({"kind": "state", "source": "%s:%d-%d" % (P, a, b), "n": nq, "init": None,
                               "ops": [[name, wires, [theta], adj]], "expected": e})
+    # --- PauliY / PauliZ / S / T on |+++> (NonParam): the expected_results rows are tables of
+    # two symbols per target wire; the symbols' values are restated from their definitions
+    s2 = 1.0 / math.sqrt(2.0)
+    for name, (da, db), (ra, rb), sym, must in (
+            ("PauliY", (193, 197), (199, 202), {"p": 0.5j * s2, "m": -0.5j * s2}, "IMAG"),
+            ("PauliZ", (238, 240), (242, 245), {"p": 0.5 * s2, "m": -0.5 * s2}, "INVSQRT2"),
+            ("S", (279, 281), (283, 286), {"r": 0.5 * s2, "i": 0.5j * s2}, "IMAG"),
+            ("T", (321, 322), (324, 327), {"r": 1.0 / (2.0 * math.sqrt(2.0)), "i": 0.25 + 0.25j}, "1.0 / 4")):
+        assert must in lines(N, da, db), name
+        rows = re.findall(r"\{([a-z, ]+)\}", lines(N, ra, rb))
+        assert len(rows) == 3, (name, rows)
+        for index, row in enumerate(rows):
+            vals = [sym[x.strip()] for x in row.split(",")]
+            assert len(vals) == 8
+            block = {"PauliY": "182-226", "PauliZ": "228-268", "S": "270-309", "T": "311-352"}[name]
+            cases.append({"kind": "state", "source": "%s:%s" % (N, block), "n": 3, "init": None,
+                          "ops": [["Hadamard", [0], [], False], ["Hadamard", [1], [], False],
+                                  ["Hadamard", [2], [], False], [name, [index], [], False]],
+                          "expected": [[float(np.real(v)), float(np.imag(v))] for v in vals]})
     # --- dense expval (1.263 - 1.011i) with a non-normalised state: NonParam 866-889
     init = pairs(numbers(N, 867, 869))
     mat = pairs(numbers(N, 874, 886))
