@@ -80,7 +80,8 @@ def build(verbose=False, jobs=None):
     os.makedirs(BUILD, exist_ok=True)
     os.makedirs(LIBDIR, exist_ok=True)
     cu = sorted(glob.glob(os.path.join(KERNELS, "*.cu")))
-    headers = glob.glob(os.path.join(KERNELS, "*.cuh")) + [os.path.join(INCLUDE, "lgpu.h")]
+    headers = (glob.glob(os.path.join(KERNELS, "*.cuh")) + glob.glob(os.path.join(KERNELS, "*.h")) +
+               [os.path.join(INCLUDE, "lgpu.h")])
     objs = [os.path.join(BUILD, os.path.basename(f)[:-3] + ".o") for f in cu]
     todo = [(src, obj) for src, obj in zip(cu, objs) if _newer(obj, [src] + headers)]
 
