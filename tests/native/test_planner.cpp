@@ -18,64 +18,17 @@
 #include <string>
 #include <vector>
 
-#include "GateLowering.hpp"
+#include "desc_apply.hpp"
 
 using namespace Pennylane::Engine;
-using cdv = std::vector<std::complex<double>>;
+using hosttest::apply_desc;
+using hosttest::cdv;
 
 static long bad = 0;
 
 static void fail(const char *what, int trial, double v) {
     if (bad < 20) std::printf("bad %s (trial %d): %g\n", what, trial, v);
     bad++;
-}
-
-// Dense 2^t x 2^t matrix on target bits tg (tg[0] = most significant matrix
-// bit) under controls ct with values cv.
-static void apply_dense(cdv &sv, const std::vector<int> &tg, const std::vector<int> &ct, const std::vector<int> &cv,
-                        const cdv &m) {
-    const size_t t = tg.size(), D = size_t(1) << t;
-    uint64_t tmask = 0;
-    for (int b : tg) tmask |= uint64_t(1) << b;
-    std::vector<size_t> off(D);
-    for (size_t r = 0; r < D; r++) {
-        size_t o = 0;
-        for (size_t k = 0; k < t; k++)
-            if ((r >> (t - 1 - k)) & 1) o |= size_t(1) << tg[k];
-        off[r] = o;
-    }
-    cdv a(D), y(D);
-    for (size_t i = 0; i < sv.size(); i++) {
-        if (i & tmask) continue;
-        bool on = true;
-        for (size_t k = 0; k < ct.size(); k++)
-            if (int((i >> ct[k]) & 1) != cv[k]) on = false;
-        if (!on) continue;
-        for (size_t c = 0; c < D; c++) a[c] = sv[i | off[c]];
-        for (size_t r = 0; r < D; r++) {
-            std::complex<double> s = 0;
-            for (size_t c = 0; c < D; c++) s += m[r * D + c] * a[c];
-            y[r] = s;
-        }
-        for (size_t r = 0; r < D; r++) sv[i | off[r]] = y[r];
-    }
-}
-
-static void apply_desc(cdv &sv, const GateDesc &d) {
-    if (d.kind == GateDesc::IDENTITY) return;
-    if (d.kind == GateDesc::MATRIX) {
-        std::vector<int> cv = d.cvals;
-        if (cv.empty()) cv.assign(d.ctrls.size(), 1);
-        apply_dense(sv, d.tgts, d.ctrls, cv, d.matrix);
-        return;
-    }
-    std::vector<int> bits;
-    cdv m;
-    if (!dense_on_bits(d, bits, m, 12)) {
-        fail("pauli rotation not expandable", -1, 0);
-        return;
-    }
-    apply_dense(sv, bits, {}, {}, m);
 }
 
 struct Spec {
@@ -135,7 +88,8 @@ int main() {
             cdv psi(size_t(1) << n);
             for (auto &x : psi) x = {nrm(gen), nrm(gen)};
             cdv ref = psi;
-            for (const auto &d : descs) apply_desc(ref, d);
+            for (const auto &d : descs)
+                if (!apply_desc(ref, d)) fail("gate not expandable", trial, 0);
             std::vector<GateDesc> merged = descs;
             merge_1q_runs(merged);
             for (const Shape &sh : shapes) {
@@ -151,7 +105,7 @@ int main() {
                             continue;
                         }
                         seen[gi]++;
-                        apply_desc(out, merged[gi]);
+                        if (!apply_desc(out, merged[gi])) fail("gate not expandable", trial, double(gi));
                     }
                     if (blk.tile_bits.empty()) {
                         if (blk.gates.size() != 1) fail("single block with several gates", trial, blk.gates.size());

@@ -31,7 +31,8 @@ def test_fusion_plan_keeps_the_state():
         pytest.skip("cuComplex.h not found")
     with tempfile.TemporaryDirectory() as d:
         exe = os.path.join(d, "test_planner")
-        subprocess.run(["g++", "-O2", "-std=c++17", "-I" + os.path.join(ROOT, "include"),
+        subprocess.run(["g++", "-O2", "-std=c++17", "-I" + os.path.join(ROOT, "tests", "native"),
+                        "-I" + os.path.join(ROOT, "include"),
                         "-I" + os.path.join(ROOT, "pennylane_lightning_gpu_gb300", "csrc", "cpp"), "-I" + inc,
                         os.path.join(ROOT, "tests", "native", "test_planner.cpp"), "-o", exe], check=True)
         r = subprocess.run([exe], capture_output=True, text=True)
@@ -56,6 +57,21 @@ def test_pauli_tile_pass_plan():
         subprocess.run(["g++", "-O2", "-std=c++17",
                         "-I" + os.path.join(ROOT, "pennylane_lightning_gpu_gb300", "csrc", "kernels"),
                         os.path.join(ROOT, "tests", "native", "test_pauli_plan.cpp"), "-o", exe], check=True)
+        r = subprocess.run([exe], capture_output=True, text=True)
+        assert r.returncode == 0, r.stdout + r.stderr
+        assert "bad 0" in r.stdout
+
+
+def test_lowering_matches_the_oracle():
+    inc = _cuda_include()
+    if inc is None:
+        pytest.skip("cuComplex.h not found")
+    with tempfile.TemporaryDirectory() as d:
+        exe = os.path.join(d, "test_lowering_vs_oracle")
+        subprocess.run(["g++", "-O2", "-std=c++17", "-I" + os.path.join(ROOT, "tests", "native"),
+                        "-I" + os.path.join(ROOT, "oracle"), "-I" + os.path.join(ROOT, "include"),
+                        "-I" + os.path.join(ROOT, "pennylane_lightning_gpu_gb300", "csrc", "cpp"), "-I" + inc,
+                        os.path.join(ROOT, "tests", "native", "test_lowering_vs_oracle.cpp"), "-o", exe], check=True)
         r = subprocess.run([exe], capture_output=True, text=True)
         assert r.returncode == 0, r.stdout + r.stderr
         assert "bad 0" in r.stdout
