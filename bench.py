@@ -117,60 +117,81 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def headline_config(n, kernel_family=None, f64_mode=None):
-    """The `config` object of the headline line (both arms)."""
-    cfg = {"workload": "dense 1-qubit gates (H and RX) on each target of a %d-qubit complex128 state" % n,
-           "qubits": n, "state_bytes": (1 << n) * 16, "gates_per_step": 2 * n,
-           "l2": "state (%.0f GiB) larger than L2 (129 MB): no flush needed" % ((1 << n) * 16 / 2**30)}
-    if f64_mode is not None:
-        cfg["f64_mode"] = f64_mode
-    if kernel_family is not None:
-        cfg["kernel_family"] = kernel_family
-    return cfg
+def headline_config(n):
+    """The `config` object of the headline line, identical in both arms: one
+    step applies H, then RX(theta), to each of the n targets of an n-qubit
+    complex128 state."""
+    return {"workload": "dense 1-qubit gates (H and RX) on each target of a %d-qubit complex128 state" % n,
+            "qubits": n, "state_bytes": (1 << n) * 16, "gates_per_step": 2 * n,
+            "l2": "state (%.0f GiB) larger than L2 (129 MB): no flush needed" % ((1 << n) * 16 / 2**30)}
 
 
 def _gate_list(n):
     return [("Hadamard", w) for w in range(n)] + [("RX", w) for w in range(n)]
 
 
-def cpu_baseline_sample(n, gates=2):
-    """Oracle (CPU) single-gate GB/s on the host cores: a bounded sample of
-    `gates` dense 1-qubit gates on an n-qubit complex128 state."""
-    from oracle import oracle as O
+def _host_cores():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:  # pragma: no cover
+        return os.cpu_count()
 
-    state = np.zeros(1 << n, np.complex128)
-    state[0] = 1.0
-    c, s = np.cos(THETA / 2), np.sin(THETA / 2)
-    rx = np.array([[c, -1j * s], [-1j * s, c]])
-    h = np.array([[1, 1], [1, -1]]) / np.sqrt(2)
-    O.apply_1q_inplace(state, 0, h)  # warm the pages and the thread pool
-    t0 = time.perf_counter()
-    for k in range(gates):
-        O.apply_1q_inplace(state, (k * 7) % n, rx if k % 2 else h)
-    dt = time.perf_counter() - t0
-    S = state.nbytes
-    return {"value": round(gates * 2 * S / dt / 1e9, 2), "unit": "GB/s", "cores": os.cpu_count(),
-            "kind": "port", "sample": "%d dense 1-qubit gates on a %d-qubit complex128 state (%.1f GiB)" % (
-                gates, n, S / 2**30)}
+
+class CpuSweep:
+    """The headline step on the host cores through the oracle port: H, then
+    RX(theta), on each target of an n-qubit complex128 state (OpenMP, all
+    host threads)."""
+
+    def __init__(self, n):
+        from oracle import oracle as O
+
+        self.O = O
+        self.n = n
+        self.state = np.zeros(1 << n, np.complex128)
+        self.state[0] = 1.0
+        c, s = np.cos(THETA / 2), np.sin(THETA / 2)
+        self.rx = np.array([[c, -1j * s], [-1j * s, c]])
+        self.h = np.array([[1, 1], [1, -1]]) / np.sqrt(2)
+
+    def step(self):
+        """Seconds for one step (2 n gates)."""
+        t0 = time.perf_counter()
+        for g, w in _gate_list(self.n):
+            self.O.apply_1q_inplace(self.state, w, self.h if g == "Hadamard" else self.rx)
+        return time.perf_counter() - t0
+
+    def gbs(self, seconds):
+        return 2 * self.n * 2 * self.state.nbytes / seconds / 1e9
+
+
+def cpu_baseline_sample(n, steps=1):
+    """Oracle (CPU) GB/s of the headline step on the host cores: `steps`
+    full steps after one warm-up step."""
+    sweep = CpuSweep(n)
+    sweep.step()  # first touch of the pages and the thread pool
+    best = min(sweep.step() for _ in range(steps))
+    return {"value": round(sweep.gbs(best), 2), "unit": "GB/s", "cores": _host_cores(), "kind": "port",
+            "sample": "%d full step(s): H and RX on each of the %d targets of a %d-qubit complex128 state "
+                      "(%.1f GiB), best step" % (steps, n, n, sweep.state.nbytes / 2**30)}
 
 
 def run_reference(args):
-    """CPU reference arm: the oracle port on all host threads, same metric."""
+    """CPU reference arm: the oracle port of the reference's gate application
+    on all host threads, timing the same step as the GPU arm (H and RX on
+    every target of the 28-qubit complex128 state)."""
     n = args.qubits
-    vals = []
-    for _ in range(args.warmup):
-        cpu_baseline_sample(n, gates=1)
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        vals.append(cpu_baseline_sample(n, gates=2)["value"])
-    wall = time.perf_counter() - t0
-    v = statistics.median(vals)
+    sweep = CpuSweep(n)
+    for _ in range(max(1, args.warmup)):
+        sweep.step()
+    times = [sweep.step() for _ in range(args.steps)]
+    v = round(sweep.gbs(statistics.median(times)), 2)
     line = {"metric": "gate HBM GB/s at 28q", "value": v, "unit": "GB/s", "impl": "reference", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * wall / max(1, args.steps), 3),
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * statistics.mean(times), 3),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128 (f64)",
             "data": "synthetic", "config": headline_config(n),
-            "cpu_baseline": {"value": v, "unit": "GB/s", "cores": os.cpu_count(), "kind": "port",
-                             "sample": "2 dense 1-qubit gates per step on a %d-qubit complex128 state" % n},
+            "cpu_baseline": {"value": v, "unit": "GB/s", "cores": _host_cores(), "kind": "port",
+                             "sample": "every step in full: %d dense 1-qubit gates on a %d-qubit complex128 state"
+                                       % (2 * n, n)},
             "e2e": {"value": v, "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
@@ -324,9 +345,9 @@ def run_ours(args):
         "metric": "gate HBM GB/s at 28q", "value": round(value, 1), "unit": "GB/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_per_step, 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "c128 (f64)", "data": "synthetic",
-        "config": headline_config(
-            n, kernel_family="bulk-copy pipelined tiles" if m.get_stream_mode() == 1 else "grid-stride",
-            f64_mode="fp64 fma + integer-pipe multiply" if default_mode == 1 else "native fp64"),
+        "config": headline_config(n),
+        "impl_detail": {"kernel_family": "bulk-copy pipelined tiles" if m.get_stream_mode() == 1 else "grid-stride",
+                        "f64_mode": "fp64 fma + integer-pipe multiply" if default_mode == 1 else "native fp64"},
         "e2e": {"value": round(e2e_value, 1), "unit": "GB/s", "h2d_bytes_per_step": 8 * n,
                 "d2h_bytes_per_step": 16},
         "gpu_launches": len(gates) * args.steps * world,
@@ -342,7 +363,8 @@ def run_ours(args):
     if world > 1:
         line["config"]["parallelism"] = "replicas: one independent 28-qubit state per GPU"
     if single and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline_sample(n, gates=args.cpu_gates)
+        line["cpu_baseline"] = cpu_baseline_sample(n, steps=args.cpu_steps)
+        line["lightning_qubit"] = lightning_qubit_probe()
     if single and not args.no_circuits:
         line["circuits"] = bench_circuits(args)
     if single and not args.no_batched:
@@ -391,57 +413,141 @@ def distinct_flip_masks(terms):
     return len({frozenset(w for ch, w in zip(word, wires) if ch in "XY") for _, word, wires in terms})
 
 
-def bench_circuits(args):
-    """Config 1 (28 qubits, 20 layers of random rotations and entanglers; a
-    100-term Pauli Hamiltonian, probs on 10 wires, 1e4 shots), config 3
-    (24-qubit adjoint Jacobian, 384 parameters, 50-term Hamiltonian, through
-    torch.autograd) and config 0 (12-qubit adjoint Jacobian, 144 parameters),
-    end to end through the LightningGPU device with host inputs and results."""
-    from oracle import oracle as O
+def lightning_qubit_probe():
+    """The reference's CPU device (lightning.qubit, the sibling of
+    lightning_gpu.py) timed on the 12-qubit adjoint workload when PennyLane
+    and pennylane_lightning import on this host; otherwise the reason."""
+    try:
+        import pennylane as qml
+
+        qml.device("lightning.qubit", wires=1)
+    except Exception as e:  # not installed on this image
+        msg = (str(e).splitlines() or [type(e).__name__])[0]
+        return {"available": False, "note": "unavailable on this box: %s: %s" % (type(e).__name__, msg)}
+    try:
+        from pennylane_lightning_gpu_gb300 import workloads
+
+        n, layers = 12, 4
+        raw = workloads.layered_ansatz(n, layers, np.random.default_rng(0))
+        dev = qml.device("lightning.qubit", wires=n)
+
+        @qml.qnode(dev, diff_method="adjoint")
+        def circuit(p):
+            k = 0
+            for name, wires, params, _ in raw:
+                if params:
+                    getattr(qml, name)(p[k], wires=wires)
+                    k += 1
+                else:
+                    getattr(qml, name)(wires=wires)
+            return [qml.expval(qml.PauliZ(w)) for w in range(n)]
+
+        p = qml.numpy.array([o[2][0] for o in raw if o[2]], requires_grad=True)
+        jac = qml.jacobian(lambda x: qml.math.stack(circuit(x)))
+        jac(p)
+        t0 = time.perf_counter()
+        jac(p)
+        return {"available": True, "config0_adjoint_ms": round(1e3 * (time.perf_counter() - t0), 2),
+                "threads": os.environ.get("OMP_NUM_THREADS", "default"), "cores": _host_cores()}
+    except Exception as e:
+        return {"available": False, "note": "imported but failed: %s" % e}
+
+
+def _pauli_terms_args(terms):
+    return [t[1] for t in terms], [list(t[2]) for t in terms], np.array([t[0] for t in terms], np.complex128)
+
+
+def _wall(fn):
+    t0 = time.perf_counter()
+    out = fn()
+    return out, time.perf_counter() - t0
+
+
+def bench_config1(O):
+    """28 qubits, 20 layers (28 rotations RX/RY/RZ/Rot + 14 CNOT/CZ/CRY each,
+    840 operations), a 100-term Pauli Hamiltonian, probabilities on 10 wires
+    and 1e4 shots, through the LightningGPU device with host inputs and
+    results; the same workload on the host through the oracle (timed, and
+    the reference values for the error of each result)."""
     from pennylane_lightning_gpu_gb300 import ops as Q
     from pennylane_lightning_gpu_gb300 import torch_adjoint as TA
     from pennylane_lightning_gpu_gb300 import workloads
     from pennylane_lightning_gpu_gb300.lightning_gpu import LightningGPU
 
-    out = {}
-    n = 28
-    rng = np.random.default_rng(11)
-    raw = workloads.random_circuit(n, 20, rng)
-    terms = workloads.random_pauli_hamiltonian(n, 100, rng, max_wires=6)
+    n, shots, seed = 28, 10000, 77
+    raw, terms = workloads.circuit_28q_workload(n)
     H = TA.pauli_hamiltonian(terms)
     ops = [Q.op(o[0], o[1], *o[2]) for o in raw]
     masks = distinct_flip_masks(terms)
-    c1 = {"workload": "28 qubits, 20 layers (28 rotations RX/RY/RZ/Rot + 14 CNOT/CZ/CRY each, %d ops), "
-                      "100-term Pauli Hamiltonian, probs on 10 wires, 1e4 shots" % len(ops)}
+    words, wires, coeffs = _pauli_terms_args(terms)
+    out = {"workload": "28 qubits, 20 layers (28 rotations RX/RY/RZ/Rot + 14 CNOT/CZ/CRY each, %d ops), "
+                       "100-term Pauli Hamiltonian, probs on 10 wires, 1e4 shots" % len(ops)}
+
+    # the oracle on the host cores: CPU baseline and reference values
+    psi, t_apply = _wall(lambda: O.run(n, [(o[0], o[1], o[2], False, None) for o in raw]))
+    e_ref, t_exp = _wall(lambda: O.expval_pauli_words(psi, words, wires, coeffs))
+    p_ref, t_probs = _wall(lambda: O.probs(psi, list(range(10))))
+    _, t_shots = _wall(lambda: O.sample_indices(psi, seed, shots))
+    out["cpu_baseline"] = {"kind": "port", "cores": _host_cores(), "unit": "ms",
+                           "sample": "the whole workload once (complex128)",
+                           "apply_ms": round(t_apply * 1e3, 1), "expval_ms": round(t_exp * 1e3, 1),
+                           "probs_ms": round(t_probs * 1e3, 1), "shots_ms": round(t_shots * 1e3, 1),
+                           "value": round((t_apply + t_exp + t_probs + t_shots) * 1e3, 1)}
+    p_ref_pl = p_ref.reshape([2] * 10).transpose().reshape(-1)  # PennyLane order, as the device returns
+    scale = sum(abs(t[0]) for t in terms)
     for dt, key, amp in ((np.complex128, "c128", 16), (np.complex64, "c64", 8)):
         dev = LightningGPU(n, c_dtype=dt)
         t_apply = _timed(lambda: (dev.reset(), dev.apply(ops), dev._gpu_state.synchronize()))
         t_exp = _timed(lambda: dev.expval(H))
         t_probs = _timed(lambda: dev.probability(wires=list(range(10))))
-        t_shots = _timed(lambda: dev._gpu_state.GenerateSamples(n, 10000))
+        t_shots = _timed(lambda: dev._gpu_state.GenerateSamples(n, shots))
         S = (1 << n) * amp
-        c1[key] = {"apply_ms": round(t_apply * 1e3, 2), "expval_ms": round(t_exp * 1e3, 2),
-                   "probs_ms": round(t_probs * 1e3, 2), "shots_ms": round(t_shots * 1e3, 2),
-                   "total_ms": round((t_apply + t_exp + t_probs + t_shots) * 1e3, 2),
-                   # one read of the state each, through the Python device (host overhead included)
-                   "probs_gbs": round(S / t_probs / 1e9, 1), "shots_gbs": round(S / t_shots / 1e9, 1),
-                   # S per distinct flip mask; tile passes serve several masks per read
-                   "expval_algorithmic_gb": round(S * masks / 1e9, 1),
-                   "expval_gbs": round(S * masks / t_exp / 1e9, 1),
-                   "apply_gbs_if_one_pass_per_op": round(len(ops) * 2 * S / t_apply / 1e9, 1)}
-        del dev
-    out["config1"] = c1
+        r = {"apply_ms": round(t_apply * 1e3, 2), "expval_ms": round(t_exp * 1e3, 2),
+             "probs_ms": round(t_probs * 1e3, 2), "shots_ms": round(t_shots * 1e3, 2),
+             "total_ms": round((t_apply + t_exp + t_probs + t_shots) * 1e3, 2),
+             # one read of the state each, through the Python device (host overhead included)
+             "probs_gbs": round(S / t_probs / 1e9, 1), "shots_gbs": round(S / t_shots / 1e9, 1),
+             # S per distinct flip mask; tile passes serve several masks per read
+             "expval_algorithmic_gb": round(S * masks / 1e9, 1),
+             "expval_gbs": round(S * masks / t_exp / 1e9, 1),
+             "apply_gbs_if_one_pass_per_op": round(len(ops) * 2 * S / t_apply / 1e9, 1)}
+        # error of every result against the FP64 oracle
+        held = dev.state.astype(np.complex128)
+        e_gpu = float(dev.expval(H))
+        p_gpu = np.asarray(dev.probability(wires=list(range(10))))
+        dev._gpu_state.setSeed(seed)
+        idx = np.asarray(dev._gpu_state.GenerateSampleIndices(shots, True))
+        ref_idx = O.sample_indices(held, seed, shots, float_draws=(dt == np.complex64))
+        r["max_abs_err_vs_oracle"] = {
+            "state": float(np.max(np.abs(held - psi))), "expval": abs(e_gpu - e_ref),
+            "expval_bound": (1e-10 if key == "c128" else 1e-5) * scale,
+            "probs": float(np.max(np.abs(p_gpu - p_ref_pl))),
+            "shots_index_mismatches": int(np.sum(idx != ref_idx))}
+        r["cpu_speedup"] = round(out["cpu_baseline"]["value"] / r["total_ms"], 1)
+        out[key] = r
+        del dev, held
+    del psi
+    return out
 
+
+def bench_config3(O):
+    """24-qubit complex128 ansatz, 8 layers of RY, RZ + CZ ladder (384
+    parameters), 50-term Pauli Hamiltonian: forward + adjoint backward through
+    torch.autograd; the oracle's forward + adjoint on the host (timed, and
+    the reference Jacobian)."""
     import torch
 
+    from pennylane_lightning_gpu_gb300 import torch_adjoint as TA
+    from pennylane_lightning_gpu_gb300 import workloads
+    from pennylane_lightning_gpu_gb300.lightning_gpu import LightningGPU
+
     n3, layers3 = 24, 8
-    rng = np.random.default_rng(13)
-    terms3 = workloads.random_pauli_hamiltonian(n3, 50, rng, max_wires=6)
+    terms3, pvals = workloads.adjoint_24q_workload(n3, layers3)
     H3 = TA.pauli_hamiltonian(terms3)
     template = TA.ry_rz_cz_template(n3, layers3)
     dev3 = LightningGPU(n3)
     f = TA.expval_function(template, [H3], dev3)
-    params = torch.tensor(rng.uniform(0, 2 * np.pi, 2 * n3 * layers3), dtype=torch.float64, requires_grad=True)
+    params = torch.tensor(pvals, dtype=torch.float64, requires_grad=True)
 
     def fwd_bwd():
         params.grad = None
@@ -451,47 +557,98 @@ def bench_circuits(args):
 
     t3 = _timed(fwd_bwd, reps=1)
     t3f = _timed(lambda: f(params.detach()), reps=1)
+    grad = fwd_bwd().numpy().copy()
     # algorithmic bytes: forward = the gates + one read per distinct flip mask
     # of H; adjoint = 4S per operation (undo it on the ket and the one bra),
     # 2S per trainable parameter (the generator overlap), S (M + 1) for H|psi>
     S3 = (1 << n3) * 16
-    ops3 = template(np.zeros(2 * n3 * layers3))
+    ops3 = template(pvals)
     flips = {sum(1 << w for w, c in zip(t[2], t[1]) if c in "XY") for t in terms3}
     fwd_bytes = sum(gate_bytes(o.name, S3) for o in ops3) + S3 * len(flips)
     adj_bytes = (4 * len(ops3) + 2 * len(params) + len(flips) + 1) * S3
-    out["config3"] = {"workload": "24 qubits complex128, 8 layers RY,RZ + CZ ladder (384 params), 50-term "
-                                  "Pauli Hamiltonian, forward + adjoint backward via torch.autograd",
-                      "forward_backward_ms": round(t3 * 1e3, 1), "forward_ms": round(t3f * 1e3, 1),
-                      "algorithmic_gb": {"forward": round(fwd_bytes / 1e9, 1), "adjoint": round(adj_bytes / 1e9, 1)},
-                      "achieved_gbs": round((fwd_bytes + adj_bytes) / t3 / 1e9, 1)}
     del dev3
 
+    oops = [(o.name, o.wires, o.parameters, False, None) for o in ops3]
+    obs = [(True, [(c, [("Pauli" + ch, [w], None) for ch, w in zip(word, wires)]) for c, word, wires in terms3])]
+    final, tf = _wall(lambda: O.run(n3, oops))
+    ref, tb = _wall(lambda: O.adjoint_jacobian(final, oops, obs, list(range(len(pvals))))[0])
+    scale = sum(abs(t[0]) for t in terms3)
+    return {"workload": "24 qubits complex128, 8 layers RY,RZ + CZ ladder (384 params), 50-term "
+                        "Pauli Hamiltonian, forward + adjoint backward via torch.autograd",
+            "forward_backward_ms": round(t3 * 1e3, 1), "forward_ms": round(t3f * 1e3, 1),
+            "algorithmic_gb": {"forward": round(fwd_bytes / 1e9, 1), "adjoint": round(adj_bytes / 1e9, 1)},
+            "achieved_gbs": round((fwd_bytes + adj_bytes) / t3 / 1e9, 1),
+            "max_abs_err_vs_oracle": {"jacobian": float(np.max(np.abs(grad - ref))), "bound": 1e-10 * scale},
+            "cpu_baseline": {"kind": "port", "cores": _host_cores(), "unit": "ms", "value": round((tf + tb) * 1e3, 1),
+                             "forward_ms": round(tf * 1e3, 1), "adjoint_ms": round(tb * 1e3, 1),
+                             "sample": "forward + adjoint Jacobian, all 384 columns, once"},
+            "cpu_speedup": round((tf + tb) / t3, 1)}
+
+
+def bench_config0(O):
+    """12 qubits, 4 layers of RX, RY, RZ + CNOT ring (144 parameters), 12
+    PauliZ expectations and the adjoint Jacobian through the device, both
+    dtypes; the oracle's forward + adjoint on the host."""
+    from pennylane_lightning_gpu_gb300 import ops as Q
+    from pennylane_lightning_gpu_gb300 import workloads
+    from pennylane_lightning_gpu_gb300.lightning_gpu import LightningGPU
+
     n0, layers0 = 12, 4
-    rng = np.random.default_rng(0)
-    raw0 = workloads.layered_ansatz(n0, layers0, rng)
+    raw0 = workloads.layered_ansatz(n0, layers0, np.random.default_rng(0))
     ops0 = [Q.op(o[0], o[1], *o[2]) for o in raw0]
     tape0 = Q.QuantumTape(ops0, [Q.expval(Q.PauliZ(w)) for w in range(n0)])
-    dev0 = LightningGPU(n0)
-    t0g = _timed(lambda: dev0.adjoint_jacobian(tape0), reps=3)
     oops = [(o[0], o[1], o[2], False, None) for o in raw0]
-    final = O.run(n0, oops)
     obs = [(False, [(1.0, [("PauliZ", [w], None)])]) for w in range(n0)]
-    a = time.perf_counter()
-    O.adjoint_jacobian(final, oops, obs, list(range(len(raw0))))
-    t0c = time.perf_counter() - a
-    out["config0"] = {"workload": "12 qubits complex128, 4 layers RX,RY,RZ + CNOT ring (144 params), "
-                                  "expval PauliZ on each wire, adjoint Jacobian",
-                      "gpu_ms": round(t0g * 1e3, 2), "cpu_oracle_ms": round(t0c * 1e3, 2),
-                      "cpu_oracle_threads": os.cpu_count()}
+
+    def cpu():
+        final = O.run(n0, oops)
+        z = np.diag([1.0, -1.0])
+        vals = np.array([O.expval_matrix(final, z, [w]).real for w in range(n0)])
+        return vals, O.adjoint_jacobian(final, oops, obs, list(range(sum(1 for o in raw0 if o[2]))))
+
+    cpu()
+    reps = []
+    for _ in range(5):
+        (ref_vals, ref_jac), t = _wall(cpu)
+        reps.append(t)
+    t0c = statistics.median(reps)
+    out = {"workload": "12 qubits, 4 layers RX,RY,RZ + CNOT ring (144 params), expval PauliZ on each wire, "
+                       "adjoint Jacobian",
+           "cpu_baseline": {"kind": "port", "cores": _host_cores(), "unit": "ms", "value": round(t0c * 1e3, 2),
+                            "sample": "forward + 12 expvals + adjoint Jacobian, median of 5 (complex128)"}}
+    for dt, key in ((np.complex128, "c128"), (np.complex64, "c64")):
+        dev0 = LightningGPU(n0, c_dtype=dt)
+        t0g = _timed(lambda: (dev0.execute(tape0), dev0.adjoint_jacobian(tape0)), reps=3)
+        vals = np.asarray(dev0.execute(tape0))
+        jac = np.asarray(dev0.adjoint_jacobian(tape0))
+        out[key] = {"gpu_ms": round(t0g * 1e3, 2), "cpu_speedup": round(t0c / t0g, 1),
+                    "max_abs_err_vs_oracle": {"expvals": float(np.max(np.abs(vals - ref_vals))),
+                                              "jacobian": float(np.max(np.abs(jac - ref_jac))),
+                                              "bound": 1e-10 if key == "c128" else 1e-5}}
+        del dev0
     return out
 
 
+def bench_circuits(args):
+    """The 28-qubit circuit, the 24-qubit differentiation and the 12-qubit
+    adjoint workloads end to end through the LightningGPU device, each with
+    its CPU (oracle) baseline and the error of its results against the
+    oracle."""
+    from oracle import oracle as O
+
+    return {"config1": bench_config1(O), "config3": bench_config3(O), "config0": bench_config0(O)}
+
+
 def bench_batched(args):
-    """Config 2: 4096 circuits (n uniform 10..20, 2..6 layers of the layered
-    ansatz, observable sum_i Z_i) in one persistent graph-captured launch vs
-    the plain per-circuit loop (timed on a seeded subset, scaled)."""
+    """4096 circuits (n uniform 10..20, 2..6 layers of the layered ansatz,
+    observable sum_i Z_i) in one persistent graph-captured launch, against
+    two plain loops over the same circuits on the same GPU (one kernel per
+    gate, and the library's own fused multi-gate apply; timed on a seeded
+    subset and scaled) and against the oracle on the host (a seeded subset,
+    timed and used for the error of the results)."""
     import torch
 
+    from oracle import oracle as O
     from pennylane_lightning_gpu_gb300 import batched
 
     out = {"workload": "%d circuits, n uniform 10..20, 2..6 layers of RX/RY/RZ + CNOT ring, sum_i Z_i"
@@ -500,11 +657,29 @@ def bench_batched(args):
     rng = np.random.default_rng(0)
     sub_idx = sorted(rng.choice(len(circuits), size=min(args.batch_plain, len(circuits)), replace=False))
     sub = [circuits[i] for i in sub_idx]
+    cpu_idx = sub_idx[: args.batch_cpu]
+    scale_sub = len(circuits) / len(sub)
+
+    # the oracle: sequential loop over a seeded subset (CPU baseline + reference values)
+    ref = {}
+    t0 = time.perf_counter()
+    for i in cpu_idx:
+        n, ops, obs = circuits[i]
+        psi = O.run(n, [(o[0], o[1], o[2], o[3], None) for o in ops])
+        words, wires, coeffs = _pauli_terms_args(obs)
+        ref[i] = O.expval_pauli_words(psi, words, wires, coeffs)
+    cpu_s = (time.perf_counter() - t0) * len(circuits) / len(cpu_idx)
+    out["cpu_baseline"] = {"kind": "port", "cores": _host_cores(), "unit": "circuits/s",
+                           "value": round(len(circuits) / cpu_s, 1),
+                           "sample": "%d circuits of the batch one at a time (complex128), scaled to %d"
+                                     % (len(cpu_idx), len(circuits))}
     for dt, key in ((np.complex64, "c64"), (np.complex128, "c128")):
+        torch.cuda.synchronize()
         t0 = time.perf_counter()
         ex = batched.build_executor(circuits, dt)
         prep = time.perf_counter() - t0
-        ex.run()
+        first = ex.run()
+        first_s = time.perf_counter() - t0  # build, plan, upload, capture and the first run
         ts = []
         for _ in range(3):
             torch.cuda.synchronize()
@@ -514,40 +689,116 @@ def bench_batched(args):
         run_s = min(ts)
         a = time.perf_counter()
         plain = batched.plain_loop(sub, dt)
-        plain_s = (time.perf_counter() - a) * len(circuits) / len(sub)
-        err = float(np.max(np.abs(res[sub_idx] - plain)))
+        plain_s = (time.perf_counter() - a) * scale_sub
+        a = time.perf_counter()
+        plain_f = batched.plain_loop(sub, dt, fusion=True)
+        plain_fused_s = (time.perf_counter() - a) * scale_sub
         amp = 8 if dt == np.complex64 else 16
         alg = sum(sum(gate_bytes(o[0], (1 << n) * amp) for o in ops) + (1 << n) * amp for n, ops, _ in circuits)
+        err = max(abs(float(res[i]) - ref[i]) / circuits[i][0] for i in cpu_idx)
         out[key] = {"circuits_per_s": round(len(circuits) / run_s, 1), "run_s": round(run_s, 4),
+                    "first_run_circuits_per_s": round(len(circuits) / first_s, 1), "first_run_s": round(first_s, 3),
+                    "prepare_s": round(prep, 3),
                     "achieved_gbs": round(alg / run_s / 1e9, 1),
                     "plain_loop_circuits_per_s": round(len(circuits) / plain_s, 1),
-                    "speedup_vs_plain": round(plain_s / run_s, 2), "prepare_s": round(prep, 3),
-                    "max_abs_diff_vs_plain": err, "plain_sample": len(sub), "stats": ex.stats()}
-        del ex
+                    "plain_fused_loop_circuits_per_s": round(len(circuits) / plain_fused_s, 1),
+                    "speedup_vs_plain": round(plain_s / run_s, 2),
+                    "speedup_vs_plain_fused": round(plain_fused_s / run_s, 2),
+                    "first_run_speedup_vs_plain_fused": round(plain_fused_s / first_s, 2),
+                    "first_run_speedup_vs_plain": round(plain_s / first_s, 2),
+                    "cpu_speedup": round(cpu_s / run_s, 1),
+                    "max_abs_diff_vs_plain": float(np.max(np.abs(res[sub_idx] - plain))),
+                    "max_abs_diff_vs_plain_fused": float(np.max(np.abs(res[sub_idx] - plain_f))),
+                    "max_abs_err_vs_oracle_per_term": err, "bound_per_term": 1e-10 if key == "c128" else 1e-5,
+                    "oracle_sample": len(cpu_idx), "plain_sample": len(sub), "stats": ex.stats()}
+        del ex, first
     return out
 
 
+def _oracle_request(O, r):
+    """The oracle's answer to one serving request (complex128)."""
+    psi = O.run(r.n, [(o[0], o[1], o[2], o[3], None) for o in r.ops])
+    if r.kind == "expval":
+        words, wires, coeffs = _pauli_terms_args(r.obs)
+        return psi, O.expval_pauli_words(psi, words, wires, coeffs)
+    if r.kind == "probs":
+        return psi, O.probs(psi, list(r.wires))
+    return psi, O.sample_indices(psi, int(r.seed), int(r.shots), float_draws=True)
+
+
 def bench_serving(args):
-    """Config 4: Poisson stream of requests (n log-uniform 8..30, depth 2..10,
-    expval / probs / shots), complex64, served with continuous batching vs a
-    sequential loop over the same trace."""
+    """Poisson streams of requests (n log-uniform 8..30, depth 2..10, expval /
+    probs / shots, complex64) at several arrival rates, served with continuous
+    batching and by a sequential loop over the same trace; the error of the
+    served results against the oracle; and the oracle serving the trace on
+    the host."""
+    from oracle import oracle as O
     from pennylane_lightning_gpu_gb300 import serving
 
-    trace = serving.make_trace(args.serve_requests, rate=args.serve_rate, seed=4)
-    srv = serving.CircuitServer(np.complex64, slots=8)
-    try:
-        done, makespan = serving.replay(srv, trace)
-    finally:
-        srv.close()
-    served = serving.report(done, makespan)
-    seq, seq_makespan = serving.sequential_baseline(serving.make_trace(args.serve_requests, rate=args.serve_rate,
-                                                                       seed=4), np.complex64)
-    base = serving.report(seq, seq_makespan)
-    return {"workload": "%d requests, Poisson rate %.0f/s, n log-uniform 8..30, depth 2..10, complex64"
-                        % (args.serve_requests, args.serve_rate),
-            "served": served, "sequential": base,
+    rates = [float(x) for x in args.serve_rates.split(",")]
+    out = {"workload": "%d requests per rate, Poisson arrivals, n log-uniform 8..30, depth 2..10 of RX/RY/RZ + "
+                       "CNOT ring, expval sum_i Z_i / probs on min(n, 10) wires / 1e3..1e4 shots, complex64"
+                       % args.serve_requests, "sweep": []}
+    last = None
+    for rate in rates:
+        trace = serving.make_trace(args.serve_requests, rate=rate, seed=4)
+        srv = serving.CircuitServer(np.complex64, slots=8)
+        try:
+            done, makespan = serving.replay(srv, trace)
+            hits, batches = srv.graph_hits, srv.batches
+        finally:
+            srv.close()
+        served = serving.report(done, makespan)
+        seq, seq_makespan = serving.sequential_baseline(serving.make_trace(args.serve_requests, rate=rate, seed=4),
+                                                        np.complex64)
+        base = serving.report(seq, seq_makespan)
+        # requests of >= 24 qubits fill the GPU's bandwidth on their own: their
+        # sequential service times add up to a floor for any schedule's makespan
+        floor = sum(r.finish - r.start for r in seq if r.n >= 24)
+        out["sweep"].append({
+            "rate_per_s": rate, "served": served, "sequential": base,
             "throughput_speedup": round(served["circuits_per_s"] / base["circuits_per_s"], 2),
-            "p99_speedup": round(base["p99_ms"] / served["p99_ms"], 2)}
+            "p50_speedup": round(base["p50_ms"] / served["p50_ms"], 2),
+            "p99_speedup": round(base["p99_ms"] / served["p99_ms"], 2),
+            "micro_batches": batches, "graph_replays": hits,
+            "makespan_floor_s": round(floor, 4),
+            "max_throughput_speedup_possible": round(seq_makespan / max(floor, 1e-9), 2)})
+        last = (done, seq)
+    # error of the served results (the last rate) against the oracle, on the
+    # requests the oracle finishes quickly
+    done, seq = last
+    errs = {"expval": 0.0, "probs": 0.0, "shots_index_mismatches": 0, "requests_checked": 0}
+    for r in sorted(done, key=lambda x: x.rid):
+        if r.error is not None or r.n > 16:
+            continue
+        _, ref = _oracle_request(O, r)
+        if r.kind == "expval":
+            errs["expval"] = max(errs["expval"], abs(float(r.result) - ref) / r.n)
+        elif r.kind == "probs":
+            errs["probs"] = max(errs["probs"], float(np.max(np.abs(np.asarray(r.result) - ref))))
+        else:
+            errs["shots_index_mismatches"] += int(np.sum(np.asarray(r.result) != ref))
+        errs["requests_checked"] += 1
+    out["max_abs_err_vs_oracle"] = dict(errs, bound=1e-5, note="expval per term of sum_i Z_i; shots against the "
+                                                                "oracle's sampler on its own complex128 state")
+    # the oracle serving the trace on the host: measured for n <= 22, larger
+    # requests scaled from the measured time per amplitude-gate
+    trace = serving.make_trace(args.serve_requests, rate=rates[0], seed=4)
+    cpu_s, work_meas, work_all = 0.0, 0.0, 0.0
+    for r in trace:
+        w = float(len(r.ops) + 1) * (1 << r.n)
+        work_all += w
+        if r.n <= 22:
+            t0 = time.perf_counter()
+            _oracle_request(O, r)
+            cpu_s += time.perf_counter() - t0
+            work_meas += w
+    est = cpu_s * work_all / max(work_meas, 1.0)
+    out["cpu_baseline"] = {"kind": "port", "cores": _host_cores(), "unit": "circuits/s",
+                           "value": round(len(trace) / est, 2),
+                           "sample": "the oracle serving the trace in order (complex128): requests of <= 22 qubits "
+                                     "measured (%.2f s), larger ones scaled by gates x 2^n" % cpu_s}
+    return out
 
 
 def profile_case(name):
@@ -630,7 +881,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--qubits", type=int, default=N_QUBITS)
-    ap.add_argument("--cpu-gates", type=int, default=4)
+    ap.add_argument("--cpu-steps", type=int, default=1)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-variants", action="store_true")
     ap.add_argument("--no-circuits", action="store_true")
@@ -642,8 +893,9 @@ def main():
                     help="run one section alone (profiling runs); the default prints the full line")
     ap.add_argument("--batch-circuits", type=int, default=4096)
     ap.add_argument("--batch-plain", type=int, default=256)
+    ap.add_argument("--batch-cpu", type=int, default=24)
     ap.add_argument("--serve-requests", type=int, default=160)
-    ap.add_argument("--serve-rate", type=float, default=100.0)
+    ap.add_argument("--serve-rates", default="100,400,1600,6400")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     if args.case:

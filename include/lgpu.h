@@ -55,6 +55,7 @@ typedef enum { LGPU_H2D = 0, LGPU_D2H = 1, LGPU_D2D = 2 } lgpu_copy_kind_t;
 
 #define LGPU_MAX_QUBITS 34
 #define LGPU_MAX_DENSE_TARGETS 12
+#define LGPU_MAX_EXPVAL_TARGETS 13
 #define LGPU_MAX_CONTROLS 16
 
 typedef struct lgpu_context_s *lgpu_context_t;
@@ -220,8 +221,12 @@ lgpu_status_t lgpu_apply_fused_block(void *sv, uint32_t n, lgpu_dtype_t dt, uint
                                      const lgpu_fused_gate_t *gates, lgpu_stream_t stream);
 
 /* ---- measurements ----------------------------------------------------------- */
-/* <sv|M|sv> for a dense 2^t x 2^t host matrix on tgts, t <= 10; out = (re, im)
- * (custatevecComputeExpectation at StateVectorCudaManaged.hpp:1602-1639, 1674-1712). */
+/* <sv|M|sv> for a dense 2^t x 2^t host matrix on tgts,
+ * t <= LGPU_MAX_EXPVAL_TARGETS (13: the reference's device sends Hamiltonians
+ * on fewer than 14 wires as one dense matrix, lightning_gpu.py:856-861);
+ * out = (re, im) (custatevecComputeExpectation at
+ * StateVectorCudaManaged.hpp:1602-1639, 1674-1712).  The matrix is copied
+ * into the context's scratch (up to 1 GiB for 13 targets). */
 lgpu_status_t lgpu_expval_matrix(lgpu_context_t ctx, const void *sv, uint32_t n, lgpu_dtype_t dt,
                                  const double *matrix, uint32_t t, const int32_t *tgts,
                                  double *out, int out_on_device, lgpu_stream_t stream);
@@ -265,7 +270,10 @@ lgpu_status_t lgpu_dot(lgpu_context_t ctx, const void *a, const void *b, uint32_
  * room for a context's scratch, and a context's first use or growth allocates
  * and synchronises the whole device.  The first call on a device looks up the
  * array's address (with that device current) and belongs before any stream
- * capture.  Calls that can overlap on one device share the array and race:
+ * capture; lgpu_device_reset forgets the address, so the first call after a
+ * reset looks it up again.  `stream` must belong to the current device
+ * (LGPU_ERR_INVALID_ARG otherwise).  With a host `out` the call synchronises
+ * `stream`.  Calls that can overlap on one device share the array and race:
  * order them.  A reduction whose grid needs more scratch than the array
  * holds is rejected with LGPU_ERR_INVALID_ARG. */
 lgpu_status_t lgpu_dot_static(const void *a, const void *b, uint32_t n, lgpu_dtype_t dt,

@@ -171,6 +171,24 @@ void apply_matrix(std::vector<std::complex<P>> &sv, int n, const Mat &m,
     if (std::adjacent_find(bits.begin(), bits.end()) != bits.end())
         throw OracleError("repeated wire");
     const int64_t ngroups = int64_t(1) << (n - int(bits.size()));
+    if (t == 1) {
+        // the same arithmetic as the general loop below, without its per-group buffers
+        const uint64_t o1 = off[1];
+        const cd m00 = m[0], m01 = m[1], m10 = m[2], m11 = m[3];
+#pragma omp parallel for schedule(static)
+        for (int64_t g = 0; g < ngroups; g++) {
+            const uint64_t base = insert_zero_bits(uint64_t(g), bits) | cmask;
+            const std::complex<double> x(sv[base]), y(sv[base | o1]);
+            std::complex<double> r0 = 0, r1 = 0;
+            r0 += m00 * x;
+            r0 += m01 * y;
+            r1 += m10 * x;
+            r1 += m11 * y;
+            sv[base] = std::complex<P>(r0);
+            sv[base | o1] = std::complex<P>(r1);
+        }
+        return;
+    }
 #pragma omp parallel
     {
         std::vector<std::complex<P>> in(dim), out(dim);
@@ -215,17 +233,34 @@ void apply_pauli_rotation(std::vector<std::complex<P>> &sv, int n, double angle,
     const cd ph = iny[ny & 3];
     const double c = std::cos(angle), s = std::sin(angle);
     const int64_t N = int64_t(1) << n;
-    std::vector<std::complex<P>> out(sv);
-#pragma omp parallel for schedule(static)
-    for (int64_t i = 0; i < N; i++) {
-        if ((uint64_t(i) & cmask) != cmask) continue;
-        const uint64_t j = uint64_t(i) ^ flip;
+    // (P a)_i = ph * sign(j) * a_j with j = i ^ flip; exp(i angle P) a = c a + i s P a.
+    // Computed in place: amplitudes i and j = i ^ flip depend only on each other.
+    auto out_of = [&](uint64_t i, const cd &ai, const cd &aj) {
+        const uint64_t j = i ^ flip;
         const double sign = (__builtin_popcountll(j & sgn) & 1) ? -1.0 : 1.0;
-        // (P a)_i = ph * sign(j) * a_j ; exp(i angle P) a = c a + i s P a
-        const cd pa = ph * sign * cd(sv[j]);
-        out[i] = std::complex<P>(c * cd(sv[i]) + cd(0, s) * pa);
+        const cd pa = ph * sign * aj;
+        return std::complex<P>(c * ai + cd(0, s) * pa);
+    };
+    if (flip == 0) {
+#pragma omp parallel for schedule(static)
+        for (int64_t i = 0; i < N; i++) {
+            if ((uint64_t(i) & cmask) != cmask) continue;
+            const cd a = cd(sv[size_t(i)]);
+            sv[size_t(i)] = out_of(uint64_t(i), a, a);
+        }
+        return;
     }
-    sv.swap(out);
+    const int hb = 63 - __builtin_clzll(flip);
+    const uint64_t lo = (uint64_t(1) << hb) - 1;
+#pragma omp parallel for schedule(static)
+    for (int64_t g = 0; g < N / 2; g++) {
+        const uint64_t i = ((uint64_t(g) & ~lo) << 1) | (uint64_t(g) & lo);  // bit hb of i is 0
+        if ((i & cmask) != cmask) continue;
+        const uint64_t j = i ^ flip;
+        const cd ai = cd(sv[i]), aj = cd(sv[j]);
+        sv[i] = out_of(i, ai, aj);
+        sv[j] = out_of(j, aj, ai);
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -484,6 +519,15 @@ struct Observable {
     bool is_hamiltonian = false;
 };
 
+// dst = src with the host's threads (large states; same values as a copy).
+template <class P>
+void par_copy(std::vector<std::complex<P>> &dst, const std::vector<std::complex<P>> &src) {
+    dst.resize(src.size());
+    const int64_t N = int64_t(src.size());
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < N; i++) dst[size_t(i)] = src[size_t(i)];
+}
+
 // applyInPlace: Named -> applyOperation(name); Hermitian -> matrix;
 // TensorProd -> sequential; Hamiltonian -> sum_t c_t O_t|psi>
 // (ObservablesGPU.hpp:119-127, 168-179, 271-275, 346-362).
@@ -496,11 +540,14 @@ void apply_observable(std::vector<std::complex<P>> &sv, int n, const Observable 
         apply_term(sv, obs.terms[0]);
         return;
     }
-    std::vector<std::complex<P>> buf(sv.size(), 0.0);
+    std::vector<std::complex<P>> buf(sv.size(), 0.0), tmp(sv.size());
+    const int64_t N = int64_t(sv.size());
     for (const auto &t : obs.terms) {
-        std::vector<std::complex<P>> tmp(sv);
+        par_copy(tmp, sv);
         apply_term(tmp, t);
-        for (size_t i = 0; i < sv.size(); i++) buf[i] += std::complex<P>(t.coeff) * tmp[i];
+        const std::complex<P> c(t.coeff);
+#pragma omp parallel for schedule(static)
+        for (int64_t i = 0; i < N; i++) buf[size_t(i)] += c * tmp[size_t(i)];
     }
     sv.swap(buf);
 }
@@ -565,9 +612,14 @@ std::vector<std::vector<double>> adjoint_jacobian(const std::vector<std::complex
     size_t num_param_ops = 0;
     for (const auto &op : ops)
         if (!op.params.empty()) num_param_ops++;
-    std::vector<std::complex<P>> lambda(final_state);
-    std::vector<std::vector<std::complex<P>>> bras(K, lambda);
-    for (size_t k = 0; k < K; k++) apply_observable(bras[k], n, obs[k]);
+    std::vector<std::complex<P>> lambda, mu;
+    par_copy(lambda, final_state);
+    std::vector<std::vector<std::complex<P>>> bras(K);
+    for (size_t k = 0; k < K; k++) {
+        par_copy(bras[k], lambda);
+        apply_observable(bras[k], n, obs[k]);
+    }
+    const int64_t N = int64_t(lambda.size());
     size_t tp_number = trainable.size() - 1;
     size_t cur_param = num_param_ops - 1;
     auto tp_it = trainable.rbegin();
@@ -578,10 +630,13 @@ std::vector<std::vector<double>> adjoint_jacobian(const std::vector<std::complex
         if (op.name == "QubitStateVector" || op.name == "StatePrep" || op.name == "BasisState")
             continue;
         if (tp_it == trainable.rend()) break;
-        std::vector<std::complex<P>> mu(lambda);
+        // mu = lambda before this operation is undone (needed only for a
+        // trainable parameter: mu <- G mu)
+        const bool grad = !op.params.empty() && cur_param == *tp_it;
+        if (grad) par_copy(mu, lambda);
         apply_operation(lambda, n, op.name, op.wires, !op.inverse, op.params, op.matrix);
         if (!op.params.empty()) {
-            if (cur_param == *tp_it) {
+            if (grad) {
                 double s = 0;
                 if (!generator_scale(op.name, s))
                     throw OracleError("no generator for " + op.name);
@@ -589,8 +644,10 @@ std::vector<std::vector<double>> adjoint_jacobian(const std::vector<std::complex
                 apply_generator(mu, n, op.name, op.wires);
                 for (size_t k = 0; k < K; k++) {
                     double im = 0;
-                    for (size_t i = 0; i < mu.size(); i++)
-                        im += (std::conj(cd(bras[k][i])) * cd(mu[i])).imag();
+                    const auto &bra = bras[k];
+#pragma omp parallel for reduction(+ : im) schedule(static)
+                    for (int64_t i = 0; i < N; i++)
+                        im += (std::conj(cd(bra[size_t(i)])) * cd(mu[size_t(i)])).imag();
                     jac[k][tp_number] = -2.0 * s * im;
                 }
                 tp_number--;

@@ -38,8 +38,12 @@ class BatchedExecutor:
         self.n_circuits += 1
         return self._ex.add_circuit(int(n), names, wires, params, inv, obs)
 
-    def prepare(self):
-        self._ex.prepare()
+    def prepare(self, capture=True):
+        """Plan and upload.  capture=True also runs the batch once and
+        captures the CUDA graph that every run() replays (new parameters go
+        through the graph); capture=False enqueues the steps on every run()
+        (a batch that runs once)."""
+        self._ex.prepare(bool(capture))
         return self
 
     def run(self, params=None):

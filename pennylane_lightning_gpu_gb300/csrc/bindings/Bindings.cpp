@@ -545,8 +545,8 @@ template <class PrecisionT> void batched_bindings(py::module_ &m) {
                 return be.addCircuit(n, names, wires, params, inverses, terms);
             },
             "Add a circuit (ops as names/wires/params/inverses, observable as (coeff, word, wires) terms).")
-        .def("prepare", &BE::prepare, py::call_guard<py::gil_scoped_release>(),
-             "Plan, upload and capture the CUDA graph.")
+        .def("prepare", &BE::prepare, py::arg("capture") = true, py::call_guard<py::gil_scoped_release>(),
+             "Plan and upload; with capture=True also run once and capture the CUDA graph that run() replays.")
         .def(
             "run",
             [](BE &be, py::object params) {

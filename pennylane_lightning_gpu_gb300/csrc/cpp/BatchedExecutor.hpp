@@ -76,7 +76,11 @@ template <class Precision> class BatchedExecutor {
     // tile bits of circuits above kmax qubits (a 3-stage ring of 64 KB tiles)
     int klarge() const { return std::is_same_v<Precision, double> ? 12 : 13; }
 
-    void prepare() {
+    // capture = true: one eager run (sets kernel attributes, validates), then
+    // the graph is captured and every run() replays it.  capture = false: no
+    // run and no graph; every run() enqueues the steps directly (for a batch
+    // that runs once, e.g. one micro-batch of a server).
+    void prepare(bool capture = true) {
         PL_ABORT_IF(prepared_, "prepare() called twice");
         PL_ABORT_IF(circuits_.empty(), "no circuits");
         std::vector<lgpu_bcircuit_t> hc;
@@ -256,12 +260,13 @@ template <class Precision> class BatchedExecutor {
         args_.out = static_cast<double *>(d_out_);
         args_.threads = uint32_t(threads_);
         args_.klarge = uint32_t(klarge());
-        // one eager run (sets kernel attributes, validates), then capture
-        enqueue();
-        PL_LGPU_IS_SUCCESS(lgpu_stream_sync(stream_));
-        PL_LGPU_IS_SUCCESS(lgpu_graph_begin(stream_));
-        enqueue();
-        PL_LGPU_IS_SUCCESS(lgpu_graph_end(stream_, &graph_));
+        if (capture) {
+            enqueue();
+            PL_LGPU_IS_SUCCESS(lgpu_stream_sync(stream_));
+            PL_LGPU_IS_SUCCESS(lgpu_graph_begin(stream_));
+            enqueue();
+            PL_LGPU_IS_SUCCESS(lgpu_graph_end(stream_, &graph_));
+        }
         prepared_ = true;
     }
 
@@ -276,7 +281,10 @@ template <class Precision> class BatchedExecutor {
             PL_ABORT_IF(params->size() != params_.size(), "parameter vector has the wrong length");
             std::memcpy(h_params_, params->data(), params->size() * sizeof(double));
         }
-        PL_LGPU_IS_SUCCESS(lgpu_graph_launch(graph_, stream_));
+        if (graph_)
+            PL_LGPU_IS_SUCCESS(lgpu_graph_launch(graph_, stream_));
+        else
+            enqueue();
     }
     std::vector<double> wait() {
         PL_LGPU_IS_SUCCESS(lgpu_stream_sync(stream_));

@@ -25,6 +25,14 @@ lgpu_status_t cuda_fail(cudaError_t e, const char *what) {
     return fail(LGPU_ERR_CUDA, msg);
 }
 
+static std::atomic<unsigned> g_reset_epoch{0};
+
+unsigned reset_epoch() { return g_reset_epoch.load(std::memory_order_acquire); }
+
+// Drops the host-side caches that refer to device `dev`'s context (pooled
+// contexts, the static scratch address); defined with those caches below.
+void forget_device_state(int dev);
+
 static std::atomic<int> g_f64_mode{-1};
 
 int f64_mode() {
@@ -303,7 +311,13 @@ lgpu_status_t lgpu_device_sm_count(int device, int *sms) {
 }
 
 lgpu_status_t lgpu_device_reset(void) {
+    int dev = 0;
+    LGPU_CUDA_TRY(cudaGetDevice(&dev));
     LGPU_CUDA_TRY(cudaDeviceReset());
+    // The reset freed every allocation of the old context and unloaded its
+    // module: cached addresses and kernel attributes of this device are stale.
+    g_reset_epoch.fetch_add(1, std::memory_order_acq_rel);
+    forget_device_state(dev);
     return LGPU_OK;
 }
 
@@ -669,9 +683,17 @@ constexpr int kStaticMaxDevices = 64;
 static std::atomic<void *> g_static_ptr[kStaticMaxDevices];
 static std::mutex g_static_mu;
 
-lgpu_status_t static_scratch(void **out) {
+lgpu_status_t static_scratch(cudaStream_t stream, void **out) {
     int dev = 0;
     LGPU_CUDA_TRY(cudaGetDevice(&dev));
+    int stream_dev = dev;
+    // The legacy and per-thread default streams (handles 0, 1, 2) follow the
+    // current device.
+    if (reinterpret_cast<uintptr_t>(stream) > 2) LGPU_CUDA_TRY(cudaStreamGetDevice(stream, &stream_dev));
+    if (stream_dev != dev)
+        return fail(LGPU_ERR_INVALID_ARG, "lgpu_dot_static: the stream belongs to device " +
+                                              std::to_string(stream_dev) + " but device " + std::to_string(dev) +
+                                              " is current; make the stream's device current");
     if (dev < 0 || dev >= kStaticMaxDevices)
         return fail(LGPU_ERR_UNSUPPORTED, "lgpu_dot_static: device ordinal " + std::to_string(dev) +
                                               " is beyond the " + std::to_string(kStaticMaxDevices) +
@@ -687,6 +709,19 @@ lgpu_status_t static_scratch(void **out) {
     }
     *out = p;
     return LGPU_OK;
+}
+
+void forget_device_state(int dev) {
+    if (dev < 0 || dev >= kStaticMaxDevices) return;
+    {
+        std::lock_guard<std::mutex> lock(g_static_mu);
+        g_static_ptr[dev].store(nullptr, std::memory_order_release);
+    }
+    std::lock_guard<std::mutex> lock(g_ctx_pool_mu);
+    // The pooled contexts' scratch and pinned buffers died with the reset:
+    // drop the host records without freeing through the new context.
+    for (lgpu_context_t c : g_ctx_pool[dev]) delete c;
+    g_ctx_pool[dev].clear();
 }
 
 }  // namespace lgpu
@@ -710,7 +745,7 @@ lgpu_status_t lgpu_dot_static(const void *a, const void *b, uint32_t n, lgpu_dty
                                               std::to_string(need) + " bytes of scratch; the static scratch holds " +
                                               std::to_string(kStaticScratchBytes) + " bytes");
     void *base = nullptr;
-    LGPU_TRY(static_scratch(&base));
+    LGPU_TRY(static_scratch(s, &base));
     unsigned *counter = static_cast<unsigned *>(base);
     double2 *partials = reinterpret_cast<double2 *>(static_cast<char *>(base) + 256);
     double2 *res = partials + size_t(g);

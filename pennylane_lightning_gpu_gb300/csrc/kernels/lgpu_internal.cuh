@@ -197,22 +197,34 @@ __device__ __forceinline__ bool last_block_arrive(unsigned *counter) {
     return is_last;
 }
 
+// Number of lgpu_device_reset calls so far.  A reset destroys the device's
+// context: kernel attributes set with cudaFuncSetAttribute, module addresses
+// and allocations are gone, so every per-device cache of them is tagged with
+// the count at which it was filled and refilled when the count has moved.
+unsigned reset_epoch();
+
 // Opt `kernel` in to `smem` bytes of dynamic shared memory on the current
-// device, once per (kernel, device, size).  cudaFuncSetAttribute is not a
-// stream operation: the first launch of each size runs outside any stream
-// capture.  `cache` is the kernel's own array (a static of the caller);
-// concurrent host threads may race to set the same value, which is harmless.
+// device, once per (kernel, device, size, reset epoch).  cudaFuncSetAttribute
+// is not a stream operation: the first launch of each size runs outside any
+// stream capture.  `cache` is the kernel's own array (a static of the caller)
+// holding (epoch << 40) | bytes; concurrent host threads may race to set the
+// same value, which is harmless.
 inline lgpu_status_t ensure_smem(const void *kernel, size_t smem, std::atomic<size_t> (&cache)[64]) {
     if (smem <= 48 * 1024) return LGPU_OK;
     int dev = 0;
     LGPU_CUDA_TRY(cudaGetDevice(&dev));
     const bool cached = dev >= 0 && dev < 64;
-    if (cached && smem <= cache[dev].load(std::memory_order_acquire)) return LGPU_OK;
+    const size_t epoch = size_t(reset_epoch()) << 40, bytes_mask = (size_t(1) << 40) - 1;
+    if (cached) {
+        const size_t v = cache[dev].load(std::memory_order_acquire);
+        if ((v & ~bytes_mask) == epoch && smem <= (v & bytes_mask)) return LGPU_OK;
+    }
     const cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
     if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute");
     if (cached) {
         size_t cur = cache[dev].load(std::memory_order_relaxed);
-        while (cur < smem && !cache[dev].compare_exchange_weak(cur, smem, std::memory_order_release)) {
+        while (((cur & ~bytes_mask) != epoch || (cur & bytes_mask) < smem) &&
+               !cache[dev].compare_exchange_weak(cur, epoch | smem, std::memory_order_release)) {
         }
     }
     return LGPU_OK;

@@ -166,6 +166,126 @@ static lgpu_status_t expval_big(lgpu_context_t ctx, const cplx_t<T> *sv, uint32_
 }
 
 // ---------------------------------------------------------------------------
+// Dense matrix expectation on t = 11..13 targets (a Hamiltonian of up to 13
+// wires handed over as one dense matrix of 2^t x 2^t, up to 1 GiB).  Work
+// items are (group g, chunk of kGemvRows rows); each CTA takes a contiguous
+// range of items, copies its group's 2^t amplitudes into shared memory as
+// double2 (reloaded only when the group changes) and each warp forms, for
+// its kGemvRows / 8 rows, x_r = sum_c M_rc a_c with the lanes striding the
+// row (coalesced reads of the row-major matrix, a fixed order per lane and a
+// fixed shuffle tree), then conj(a_r) x_r.  FP64 throughout; deterministic.
+// ---------------------------------------------------------------------------
+constexpr int kGemvRows = 32;
+
+template <class T, class I>
+__global__ void __launch_bounds__(kReduceBlock)
+    expval_gemv_kernel(const cplx_t<T> *__restrict__ sv, Holes holes, uint64_t nitems, uint64_t per_cta, int t,
+                       const I *__restrict__ off, const double2 *__restrict__ mat, double2 *partials,
+                       unsigned *counter, double2 *out) {
+    extern __shared__ double2 stile[];
+    __shared__ double2 sm[kReduceBlock / 32];
+    const int D = 1 << t;
+    const int chunks_log = t - 5;  // log2(D / kGemvRows)
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    constexpr int kRowsPerWarp = kGemvRows / (kReduceBlock / 32);
+    double2 acc = make_double2(0.0, 0.0);
+    const uint64_t first = uint64_t(blockIdx.x) * per_cta;
+    const uint64_t last = first + per_cta < nitems ? first + per_cta : nitems;
+    I loaded = ~I(0);
+    for (uint64_t item = first; item < last; item++) {
+        const I g = I(item >> chunks_log);
+        const int chunk = int(item & ((uint64_t(1) << chunks_log) - 1));
+        if (g != loaded) {
+            const I base = insert_holes<I>(g, holes);
+            __syncthreads();
+            for (int c = threadIdx.x; c < D; c += kReduceBlock) {
+                const cplx_t<T> v = sv[base | off[c]];
+                stile[c] = make_double2(double(v.x), double(v.y));
+            }
+            __syncthreads();
+            loaded = g;
+        }
+#pragma unroll 1
+        for (int rr = 0; rr < kRowsPerWarp; rr++) {
+            const int r = chunk * kGemvRows + warp * kRowsPerWarp + rr;
+            const double2 *row = mat + size_t(r) * size_t(D);
+            double xr = 0.0, xi = 0.0;
+            for (int c = lane; c < D; c += 32) {
+                const double2 mv = __ldg(&row[c]), av = stile[c];
+                xr = fma(mv.x, av.x, fma(-mv.y, av.y, xr));
+                xi = fma(mv.x, av.y, fma(mv.y, av.x, xi));
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                xr += __shfl_xor_sync(0xffffffffu, xr, o);
+                xi += __shfl_xor_sync(0xffffffffu, xi, o);
+            }
+            if (lane == 0) {
+                const double2 a = stile[r];
+                acc.x = fma(a.x, xr, fma(a.y, xi, acc.x));
+                acc.y = fma(a.x, xi, fma(-a.y, xr, acc.y));
+            }
+        }
+    }
+    __syncthreads();
+    double2 v = block_reduce_d2<kReduceBlock>(acc, sm);
+    if (threadIdx.x == 0) partials[blockIdx.x] = v;
+    if (last_block_arrive(counter)) {
+        double2 s = make_double2(0.0, 0.0);
+        for (unsigned b = threadIdx.x; b < gridDim.x; b += kReduceBlock) {
+            const double2 p = __ldcg(&partials[b]);
+            s.x += p.x;
+            s.y += p.y;
+        }
+        __syncthreads();
+        s = block_reduce_d2<kReduceBlock>(s, sm);
+        if (threadIdx.x == 0) {
+            *out = s;
+            *counter = 0u;
+        }
+    }
+}
+
+template <class T, class I>
+static lgpu_status_t expval_gemv(lgpu_context_t ctx, const cplx_t<T> *sv, uint32_t n, const double *matrix,
+                                 const std::vector<int> &tg, double *out, int out_on_device, cudaStream_t s) {
+    const int t = int(tg.size());
+    const int D = 1 << t;
+    std::vector<I> off(static_cast<size_t>(D));
+    for (int r = 0; r < D; r++) {
+        uint64_t o = 0;
+        for (int k = 0; k < t; k++)
+            if ((r >> (t - 1 - k)) & 1) o |= uint64_t(1) << tg[size_t(k)];
+        off[size_t(r)] = I(o);
+    }
+    const uint64_t ngroups = uint64_t(1) << (n - t);
+    const uint64_t nitems = ngroups << (t - 5);
+    const size_t smem = size_t(D) * sizeof(double2);
+    // resident CTAs per SM at this shared-memory size (227 KB usable per SM)
+    const unsigned per_sm = unsigned(std::max<size_t>(1, std::min<size_t>(4, (size_t(227) << 10) / (smem + 2048))));
+    const unsigned g = unsigned(std::min<uint64_t>(nitems, uint64_t(sm_count()) * per_sm));
+    const uint64_t per_cta = (nitems + g - 1) / g;
+    const size_t mbytes = size_t(D) * D * sizeof(double2);
+    const size_t obytes = size_t(D) * sizeof(I);
+    void *p = nullptr;
+    const size_t head = 256 + size_t(g) * sizeof(double2) + 256;
+    LGPU_TRY(ctx_scratch(ctx, head + mbytes + obytes + 256, &p));
+    auto *counter = static_cast<unsigned *>(p);
+    auto *partials = reinterpret_cast<double2 *>(static_cast<char *>(p) + 256);
+    auto *res = partials + g;
+    auto *dmat = reinterpret_cast<double2 *>(static_cast<char *>(p) + head);
+    auto *doff = reinterpret_cast<I *>(static_cast<char *>(p) + head + mbytes);
+    LGPU_CUDA_TRY(cudaMemcpyAsync(dmat, matrix, mbytes, cudaMemcpyHostToDevice, s));
+    LGPU_CUDA_TRY(cudaMemcpyAsync(doff, off.data(), obytes, cudaMemcpyHostToDevice, s));
+    static std::atomic<size_t> attr_g[64];
+    LGPU_TRY(ensure_smem(reinterpret_cast<const void *>(expval_gemv_kernel<T, I>), smem, attr_g));
+    expval_gemv_kernel<T, I><<<g, kReduceBlock, smem, s>>>(sv, make_holes(tg), nitems, per_cta, t, doff, dmat,
+                                                          partials, counter, res);
+    LGPU_CHECK_LAUNCH();
+    return deliver(ctx, res, 1, out, out_on_device, s);
+}
+
+// ---------------------------------------------------------------------------
 // Dense matrix expectation, t <= 2, without FP64 work per amplitude:
 // <a|M|a> = sum_rc M_rc G_rc with the Gram sums G_rc = sum_g conj(a_gr) a_gc
 // (Hermitian: D real diagonal sums and D(D-1)/2 complex ones).  Each thread
@@ -404,7 +524,9 @@ static lgpu_status_t expval_dispatch(lgpu_context_t ctx, const void *sv, uint32_
     case 2: return expval_gram<T, I, 2>(ctx, p, n, matrix, tg, out, od, s);
     case 3: return expval_df<T, I, 3>(ctx, p, n, matrix, tg, out, od, s);
     case 4: return expval_small<T, I, 4>(ctx, p, n, matrix, tg, out, od, s);
-    default: return expval_big<T, I>(ctx, p, n, matrix, tg, out, od, s);
+    default:
+        if (tg.size() > 10) return expval_gemv<T, I>(ctx, p, n, matrix, tg, out, od, s);
+        return expval_big<T, I>(ctx, p, n, matrix, tg, out, od, s);
     }
 }
 
@@ -1667,7 +1789,9 @@ lgpu_status_t lgpu_expval_matrix(lgpu_context_t ctx, const void *sv, uint32_t n,
                                  int out_on_device, lgpu_stream_t stream) {
     LGPU_TRY(check_state(sv, n, dt));
     if (!matrix || !out) return fail(LGPU_ERR_INVALID_ARG, "null matrix/output");
-    if (t < 1 || t > 10 || t > n) return fail(LGPU_ERR_INVALID_ARG, "expval: number of targets must be in [1, 10]");
+    if (t < 1 || t > LGPU_MAX_EXPVAL_TARGETS || t > n)
+        return fail(LGPU_ERR_INVALID_ARG, "expval: number of targets must be in [1, " +
+                                              std::to_string(LGPU_MAX_EXPVAL_TARGETS) + "] and at most n");
     std::vector<int> tg;
     LGPU_TRY(check_bits(n, t, tgts, "target", &tg));
     std::vector<int> srt(tg);

@@ -44,7 +44,11 @@ class LightningGPU:
                   "PauliZ", "Hadamard", "S", "T", "SX", "CNOT", "SWAP", "CSWAP", "Toffoli", "CY", "CZ", "PhaseShift",
                   "ControlledPhaseShift", "RX", "RY", "RZ", "Rot", "CRX", "CRY", "CRZ", "CRot", "IsingXX", "IsingYY",
                   "IsingZZ", "MultiRZ", "SingleExcitation", "SingleExcitationMinus", "SingleExcitationPlus",
-                  "DoubleExcitation", "DoubleExcitationMinus", "DoubleExcitationPlus"}
+                  "DoubleExcitation", "DoubleExcitationMinus", "DoubleExcitationPlus", "QFT", "GroverOperator"}
+    # dense matrix operations and the widest register the device applies them
+    # to directly (reference stopping_condition, lightning_gpu.py:504-511);
+    # wider ones must be decomposed before they reach the device
+    matrix_operations = {"QFT": 9, "GroverOperator": 12}
     observables = {"PauliX", "PauliY", "PauliZ", "Hadamard", "Identity", "Hermitian", "Projector", "Hamiltonian",
                    "SparseHamiltonian"}
 
@@ -142,7 +146,21 @@ class LightningGPU:
             else:
                 method(wires, invert, o.parameters)
 
+    def supports_operation(self, op):
+        """True when the device applies `op` itself (name known; QFT below 10
+        wires, GroverOperator below 13, as the reference's stopping condition)."""
+        name = op if isinstance(op, str) else op.name
+        if name not in self.operations:
+            return False
+        limit = self.matrix_operations.get(name)
+        return limit is None or isinstance(op, str) or len(op.wires) <= limit
+
     def apply(self, operations, **kwargs):
+        for o in operations:
+            limit = self.matrix_operations.get(o.name)
+            if limit is not None and len(o.wires) > limit:
+                raise DeviceError("%s on %d wires is not applied by the device (at most %d wires): decompose it "
+                                  "first" % (o.name, len(o.wires), limit))
         if operations:
             if isinstance(operations[0], Q.StatePrep):
                 self._apply_state_vector_GPU(operations[0].state, operations[0].wires)

@@ -65,6 +65,19 @@ def _multirz(t, k):
     return np.diag(np.exp(-0.5j * t * z))
 
 
+def _qft(k):
+    """Quantum Fourier transform on k wires: (1/sqrt(N)) w^(r c), w = exp(2 pi i / N)."""
+    d = 1 << k
+    rc = np.outer(np.arange(d), np.arange(d)) % d
+    return np.exp(2j * np.pi * rc / d) / np.sqrt(d)
+
+
+def _grover(k):
+    """Grover diffusion operator on k wires: 2 |s><s| - I, |s> the uniform superposition."""
+    d = 1 << k
+    return np.full((d, d), 2.0 / d, dtype=complex) - np.eye(d)
+
+
 _MATRICES = {
     "Identity": lambda p, k: np.eye(2, dtype=complex),
     "PauliX": lambda p, k: np.array([[0, 1], [1, 0]], dtype=complex),
@@ -100,6 +113,8 @@ _MATRICES = {
     "DoubleExcitation": lambda p, k: _double_exc(p[0]),
     "DoubleExcitationMinus": lambda p, k: _double_exc(p[0], np.exp(-0.5j * p[0])),
     "DoubleExcitationPlus": lambda p, k: _double_exc(p[0], np.exp(0.5j * p[0])),
+    "QFT": lambda p, k: _qft(k),
+    "GroverOperator": lambda p, k: _grover(k),
 }
 
 _NUM_PARAMS = {"RX": 1, "RY": 1, "RZ": 1, "PhaseShift": 1, "Rot": 3, "CRX": 1, "CRY": 1, "CRZ": 1, "CRot": 3,
@@ -155,6 +170,14 @@ def op(name, wires, *params, matrix=None):
 
 def QubitUnitary(U, wires):
     return Operation("QubitUnitary", wires, (), U)
+
+
+def QFT(wires):
+    return Operation("QFT", wires)
+
+
+def GroverOperator(wires):
+    return Operation("GroverOperator", wires)
 
 
 class StatePrep(Operation):

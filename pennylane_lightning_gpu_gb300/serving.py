@@ -8,10 +8,14 @@ requests concurrently:
 * admission by HBM footprint: a request needs 2^n amplitudes; it is admitted
   when the resident bytes plus its own stay within the budget (free HBM at
   start minus a reserve, or an explicit budget) and a worker slot is free;
-* each worker slot owns a CUDA stream; the native calls release the GIL, so
-  the kernels of different requests overlap on the device;
+* a fixed pool of worker threads, one per slot, each owning a CUDA stream;
+  the native calls release the GIL, so the kernels of different requests
+  overlap on the device;
 * small expectation-value requests (n <= small_n) waiting together are
-  micro-batched into one persistent batched launch;
+  micro-batched into one persistent batched launch.  A batch whose circuits
+  have the same structure as an earlier batch (gates, wires, observables;
+  only rotation angles differ) replays that batch's captured graph with the
+  new angles; otherwise the batch is planned and run once without a graph;
 * requests that arrive while others run are admitted as soon as memory and
   slots free up (continuous batching, not a FIFO drained one at a time).
 
@@ -74,9 +78,27 @@ def run_request(m, req, dtype, stream_ptr=None):
     return out
 
 
+# Gates whose parameters the batched executor keeps in its parameter vector
+# (rebuilt on the device at every run); every other gate's parameters are part
+# of a batch's structure.
+_VECTOR_PARAMS = {"RX", "RY", "RZ", "CRX", "CRY", "CRZ", "PhaseShift", "ControlledPhaseShift", "Rot", "CRot",
+                  "IsingXX", "IsingYY", "IsingZZ"}
+
+
+def _structure(req):
+    ops = tuple((o[0], tuple(o[1]), bool(o[3]) if len(o) > 3 else False,
+                 len(o[2]) if o[0] in _VECTOR_PARAMS else tuple(float(x) for x in o[2])) for o in req.ops)
+    obs = tuple((float(c), str(w), tuple(ws)) for c, w, ws in req.obs)
+    return (req.n, ops, obs)
+
+
+def _vector_params(reqs):
+    return np.array([float(x) for r in reqs for o in r.ops if o[0] in _VECTOR_PARAMS for x in o[2]], np.float64)
+
+
 class CircuitServer:
     def __init__(self, dtype=np.complex64, slots=8, hbm_budget=None, reserve_bytes=8 << 30, small_n=12,
-                 micro_batch=True, max_batch=256):
+                 micro_batch=True, max_batch=256, graph_cache=16):
         import torch
 
         self.m = native()
@@ -91,14 +113,21 @@ class CircuitServer:
         self.streams = [torch.cuda.Stream() for _ in range(slots)]
         self._lock = threading.Condition()
         self._waiting = collections.deque()
-        self._free_slots = list(range(slots))
         self._resident = 0
         self.max_resident = 0
         self._done = []
         self._closed = False
         self._inflight = 0
-        self._dispatcher = threading.Thread(target=self._dispatch_loop, daemon=True)
-        self._dispatcher.start()
+        # captured batches by structure (least recently used first), and those in use
+        self._graphs = collections.OrderedDict()
+        self._graph_cache = int(graph_cache)
+        self._graphs_busy = set()
+        self.graph_hits = 0
+        self.batches = 0
+        self._workers = [threading.Thread(target=self._worker_loop, args=(slot,), daemon=True)
+                         for slot in range(slots)]
+        for w in self._workers:
+            w.start()
 
     # ---- client side ------------------------------------------------------
     def submit(self, req):
@@ -143,25 +172,23 @@ class CircuitServer:
         with self._lock:
             self._closed = True
             self._lock.notify_all()
-        self._dispatcher.join(timeout=10)
+        for w in self._workers:
+            w.join(timeout=10)
+        self._graphs.clear()
 
-    # ---- dispatcher ---------------------------------------------------------
-    def _dispatch_loop(self):
+    # ---- workers ------------------------------------------------------------
+    def _worker_loop(self, slot):
         while True:
             with self._lock:
-                while not self._closed and not (self._waiting and self._free_slots):
+                while True:
+                    job = self._admit_locked() if self._waiting else None
+                    if job is not None:
+                        self._inflight += 1
+                        break
+                    if self._closed and not self._waiting:
+                        return
                     self._lock.wait(timeout=0.05)
-                if self._closed and not self._waiting:
-                    return
-                if not self._free_slots:
-                    continue
-                job = self._admit_locked()
-                if job is None:
-                    self._lock.wait(timeout=0.002)
-                    continue
-                slot = self._free_slots.pop()
-                self._inflight += 1
-            threading.Thread(target=self._worker, args=(slot, job), daemon=True).start()
+            self._run_job(slot, job)
 
     def _admit_locked(self):
         """Pick the next job: a micro-batch of small expval requests or the
@@ -186,19 +213,53 @@ class CircuitServer:
                 return ("single", [r], need)
         return None
 
-    def _worker(self, slot, job):
+    def _run_batch(self, reqs):
+        """One micro-batch: replay a captured batch of the same structure with
+        the new angles, else plan and run once (and keep it for replays)."""
+        from .batched import BatchedExecutor
+
+        reqs = sorted(reqs, key=lambda r: _structure(r))
+        key = tuple(_structure(r) for r in reqs)
+        with self._lock:
+            self.batches += 1
+            ex = self._graphs.get(key)
+            if ex is not None and key not in self._graphs_busy:
+                self._graphs.move_to_end(key)
+                self._graphs_busy.add(key)
+                self.graph_hits += 1
+            else:
+                ex = None
+        if ex is not None:
+            try:
+                res = ex.run(_vector_params(reqs))
+            finally:
+                with self._lock:
+                    self._graphs_busy.discard(key)
+            return reqs, res
+        ex = BatchedExecutor(self.dtype)
+        for r in reqs:
+            ex.add(r.n, r.ops, r.obs)
+        keep = self._graph_cache > 0
+        res = ex.prepare(capture=keep).run()
+        if keep:
+            with self._lock:
+                if key not in self._graphs:
+                    self._graphs[key] = ex
+                    while len(self._graphs) > self._graph_cache:
+                        old = next(iter(self._graphs))
+                        if old in self._graphs_busy:
+                            break
+                        self._graphs.pop(old)
+        return reqs, res
+
+    def _run_job(self, slot, job):
         kind, reqs, need = job
         t0 = time.perf_counter()
         for r in reqs:
             r.start = t0
         try:
             if kind == "batch":
-                from .batched import BatchedExecutor
-
-                ex = BatchedExecutor(self.dtype)
-                for r in reqs:
-                    ex.add(r.n, r.ops, r.obs)
-                res = ex.prepare().run()
+                reqs, res = self._run_batch(reqs)
                 for r, v in zip(reqs, res):
                     r.result = float(v)
             else:
@@ -213,7 +274,6 @@ class CircuitServer:
                 r.finish = t1
                 self._done.append(r)
             self._resident -= need
-            self._free_slots.append(slot)
             self._inflight -= 1
             self._lock.notify_all()
 

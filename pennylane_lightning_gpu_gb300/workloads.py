@@ -85,3 +85,26 @@ def random_state(n, rng, dtype=np.complex128):
 def sum_z_hamiltonian_terms(n):
     """sum_i Z_i as (coeff, word, wires) terms."""
     return [(1.0, "Z", [w]) for w in range(n)]
+
+
+def circuit_28q_workload(n=28, seed=11, layers=20):
+    """The 28-qubit circuit workload at any width n: `layers` layers of 28
+    random rotations (RX/RY/RZ/Rot) and 14 random CNOT/CZ/CRY (840 operations
+    for 20 layers, whatever n is), then a 100-term random Pauli Hamiltonian
+    (1..6 wires per word, N(0, 1) coefficients).  n = 28 with seed 11 is the
+    benchmarked instance; smaller n keep the operation count for oracle
+    comparisons."""
+    rng = np.random.default_rng(seed)
+    ops = random_circuit(n, layers, rng, rot_per_layer=28, ent_per_layer=14)
+    terms = random_pauli_hamiltonian(n, 100, rng, max_wires=6)
+    return ops, terms
+
+
+def adjoint_24q_workload(n=24, layers=8, seed=13):
+    """The differentiation workload: RY, RZ on every wire plus a CZ ladder per
+    layer (2 n layers parameters: 384 at n = 24, 8 layers), a 50-term random
+    Pauli Hamiltonian and uniform angles, all from one seed."""
+    rng = np.random.default_rng(seed)
+    terms = random_pauli_hamiltonian(n, 50, rng, max_wires=6)
+    params = rng.uniform(0, TWO_PI, 2 * n * layers)
+    return terms, params

@@ -22,7 +22,8 @@ Sources:
      test_multiple_rx_gradient), with the short circuits restated and
      checked against the test source text.
 
-Usage:  python tests/golden/make_golden.py [/path/to/reference]
+Usage:  python tests/golden/make_golden.py /path/to/reference
+        (or set LGPU_REFERENCE_ROOT to the checkout of the reference)
 """
 import ast
 import json
@@ -33,7 +34,9 @@ import sys
 
 import numpy as np
 
-REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+REF = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("LGPU_REFERENCE_ROOT")
+if __name__ == "__main__" and not REF:
+    sys.exit("usage: make_golden.py /path/to/reference (or set LGPU_REFERENCE_ROOT)")
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "reference_known_answers.json")
 CPP_TESTS = "pennylane_lightning_gpu/src/tests"

@@ -96,3 +96,28 @@ def test_report_percentiles_and_errors():
     assert abs(out["p50_ms"] - 50.5) < 1e-9
     assert abs(out["p99_ms"] - 99.01) < 1e-9
     assert out["circuits_per_s"] == 50.0
+
+
+def test_batch_structure_key_ignores_angles_only():
+    """Two micro-batches replay the same captured graph exactly when their
+    circuits differ only in the angles the batched executor rebuilds on the
+    device; the new angles are gathered in circuit and gate order."""
+    from pennylane_lightning_gpu_gb300 import workloads
+    from pennylane_lightning_gpu_gb300.serving import _structure, _vector_params
+
+    def req(seed, n=6, depth=2, extra=()):
+        r = Request(seed, n, workloads.layered_ansatz(n, depth, np.random.default_rng(seed)) + list(extra), "expval")
+        r.obs = workloads.sum_z_hamiltonian_terms(n)
+        return r
+
+    a, b = req(1), req(2)
+    assert _structure(a) == _structure(b)
+    assert _structure(a) != _structure(req(1, depth=3))
+    assert _structure(a) != _structure(req(1, n=7))
+    # a gate whose angle is baked into its matrix is part of the structure
+    c, d = req(1, extra=[("MultiRZ", [0, 1], [0.3], False)]), req(2, extra=[("MultiRZ", [0, 1], [0.4], False)])
+    assert _structure(c) != _structure(d)
+    p = _vector_params([a, b])
+    assert p.size == 2 * 2 * 6 * 3
+    assert np.allclose(p[:36], [o[2][0] for o in a.ops if o[2]])
+    assert np.allclose(p[36:], [o[2][0] for o in b.ops if o[2]])

@@ -335,3 +335,32 @@ def test_mpi_rejected():
 
     with pytest.raises(DeviceError):
         _dev(2, mpi=True)
+
+
+@pytest.mark.parametrize("name,nw,n", [("QFT", 3, 5), ("QFT", 9, 11), ("GroverOperator", 4, 6),
+                                       ("GroverOperator", 12, 13)])
+def test_qft_and_grover_matrix_operations(oracle, name, nw, n):
+    """QFT (below 10 wires) and GroverOperator (below 13) are applied as dense
+    matrices, as the reference's stopping condition allows
+    (lightning_gpu.py:504-511); wider ones raise."""
+    rng = np.random.default_rng(nw)
+    wires = [int(x) for x in rng.choice(n, size=nw, replace=False)]
+    pre = [Q.op("Hadamard", w) for w in range(n)] + [Q.op("RY", w, 0.3 * (w + 1)) for w in range(n)]
+    op = getattr(Q, name)(wires)
+    dev = _dev(n)
+    assert dev.supports_operation(op)
+    dev.apply(pre + [op, op.adjoint() if name == "QFT" else Q.op("PauliX", wires[0])])
+    tail = (op.matrix().conj().T, wires) if name == "QFT" else (np.array([[0, 1], [1, 0]]), [wires[0]])
+    ref = oracle.run(n, _oracle_ops(pre) + [("QubitUnitary", wires, [], False, op.matrix()),
+                                            ("QubitUnitary", tail[1], [], False, tail[0])])
+    assert np.max(np.abs(dev.state - ref)) < 1e-10
+
+
+def test_wide_qft_and_grover_are_refused():
+    from pennylane_lightning_gpu_gb300.lightning_gpu import DeviceError
+
+    dev = _dev(14)
+    for op in (Q.QFT(list(range(10))), Q.GroverOperator(list(range(13)))):
+        assert not dev.supports_operation(op)
+        with pytest.raises(DeviceError, match="decompose"):
+            dev.apply([op])

@@ -80,13 +80,29 @@ def test_controlled_per_gate_semantics(native, oracle, dtype):
     assert np.max(np.abs(sv.GetState() - ref)) < tol(dtype)
 
 
+def _wide_unitary(t, rng):
+    """A dense 2^t x 2^t unitary without a 2^t-sized QR: random phases times
+    the Kronecker product of random unitaries on at most 3 wires each, with
+    its rows permuted (every entry is generally non-zero)."""
+    u = np.ones((1, 1), complex)
+    left = t
+    while left:
+        k = min(3, left)
+        u = np.kron(u, random_unitary(1 << k, rng))
+        left -= k
+    d = 1 << t
+    return (np.exp(2j * np.pi * rng.random(d))[:, None] * u)[rng.permutation(d)]
+
+
 @pytest.mark.parametrize("dtype", DTYPES)
-@pytest.mark.parametrize("t", [1, 2, 3, 4, 5, 6, 7])
+@pytest.mark.parametrize("t", [1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12])
 def test_dense_matrix(native, oracle, dtype, t):
+    """Dense QubitUnitary on t = 1..12 targets (12 is the reference's widest
+    dense matrix gate: GroverOperator below 13 wires)."""
     rng = np.random.default_rng(100 + t)
     n = max(t + 2, 6)
     for adj in (False, True):
-        u = random_unitary(1 << t, rng)
+        u = random_unitary(1 << t, rng) if t <= 7 else _wide_unitary(t, rng)
         wires = [int(x) for x in rng.choice(n, size=t, replace=False)]
         _check(native, oracle, dtype, n, [("QubitUnitary", wires, [], adj, u)], rng)
 
@@ -125,13 +141,17 @@ def test_fused_random_circuit(native, oracle, dtype, n, layers):
 
 
 @pytest.mark.parametrize("dtype", DTYPES)
-@pytest.mark.parametrize("k", [1, 2, 3, 4, 5, 6, 7])
+@pytest.mark.parametrize("k", [1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12, 13])
 def test_expval_matrix(native, oracle, dtype, k):
+    """<psi|H|psi> for a dense Hermitian H on k = 1..13 wires (13: the widest
+    Hamiltonian the reference's device hands over as one dense matrix)."""
     rng = np.random.default_rng(200 + k)
-    n = k + 3
+    n = k + 3 if k <= 7 else k + 1
     psi = random_state(n, rng)
     sv = make_sv(native, dtype, psi)
     h = random_hermitian(1 << k, rng)
+    if k > 7:
+        h /= np.sqrt(1 << k)  # spectral norm O(1)
     wires = [int(x) for x in rng.choice(n, size=k, replace=False)]
     got = sv.ExpectationValue(wires, h.ravel())
     ref = oracle.expval_matrix(psi, h, wires).real

@@ -1,10 +1,16 @@
 """Allocation-free inner product ``lgpu_dot_static`` against ``lgpu_dot``,
 both called through the C ABI of liblgpu_gb300.so.
 
-The file name keeps it last in collection, so it runs both after every other
-GPU test and, on its own, in a fresh process.
+The file name keeps it last in collection, so a run of the whole suite
+reaches it after every other GPU test; it also passes when run on its own.
+The device-reset case runs in a child process of its own, because a reset
+ends every allocation of the process's CUDA context.
 """
 import ctypes
+import os
+import subprocess
+import sys
+import textwrap
 
 import numpy as np
 import pytest
@@ -100,3 +106,71 @@ def test_dot_static_rejects_bad_arguments():
     out = (ctypes.c_double * 2)()
     assert lib.lgpu_dot_static(None, None, 4, C128, out, 0, None) == LGPU_ERR_INVALID_ARG
     assert b"null" in lib.lgpu_last_error_string()
+
+
+def test_dot_static_rejects_null_output():
+    import torch
+
+    lib = _lib()
+    a = torch.ones(1 << 4, dtype=torch.complex128, device="cuda")
+    stream = torch.cuda.current_stream().cuda_stream
+    assert lib.lgpu_dot_static(a.data_ptr(), a.data_ptr(), 4, C128, None, 0, stream) == LGPU_ERR_INVALID_ARG
+    assert b"null" in lib.lgpu_last_error_string()
+
+
+_RESET_SCRIPT = textwrap.dedent("""
+    import ctypes, sys
+    import numpy as np
+    lib = ctypes.CDLL(sys.argv[1])
+    vp, u32, i32, dp = ctypes.c_void_p, ctypes.c_uint32, ctypes.c_int, ctypes.POINTER(ctypes.c_double)
+    lib.lgpu_malloc.argtypes = [ctypes.POINTER(vp), ctypes.c_size_t]
+    lib.lgpu_free.argtypes = [vp]
+    lib.lgpu_memcpy.argtypes = [vp, vp, ctypes.c_size_t, i32, i32, vp]
+    lib.lgpu_context_create.argtypes = [i32, ctypes.POINTER(vp)]
+    lib.lgpu_context_destroy.argtypes = [vp]
+    lib.lgpu_dot.argtypes = [vp, vp, vp, u32, i32, dp, i32, vp]
+    lib.lgpu_dot_static.argtypes = [vp, vp, u32, i32, dp, i32, vp]
+    lib.lgpu_last_error_string.restype = ctypes.c_char_p
+    n = 14
+    rng = np.random.default_rng(3)
+    host = rng.normal(size=(2, 1 << n)) + 1j * rng.normal(size=(2, 1 << n))
+    host = np.ascontiguousarray(host / np.linalg.norm(host, axis=1, keepdims=True))
+
+    def one_round():
+        ptrs = []
+        for v in host:
+            p = vp()
+            assert lib.lgpu_malloc(ctypes.byref(p), v.nbytes) == 0, lib.lgpu_last_error_string()
+            assert lib.lgpu_memcpy(p, v.ctypes.data, v.nbytes, 0, 0, None) == 0, lib.lgpu_last_error_string()
+            ptrs.append(p)
+        ctx = vp()
+        assert lib.lgpu_context_create(0, ctypes.byref(ctx)) == 0
+        ref = (ctypes.c_double * 2)()
+        assert lib.lgpu_dot(ctx, ptrs[0], ptrs[1], n, 1, ref, 0, None) == 0, lib.lgpu_last_error_string()
+        for _ in range(2):
+            got = (ctypes.c_double * 2)()
+            rc = lib.lgpu_dot_static(ptrs[0], ptrs[1], n, 1, got, 0, None)
+            assert rc == 0, lib.lgpu_last_error_string()
+            assert abs(complex(got[0], got[1]) - complex(ref[0], ref[1])) < 1e-12, (got[0], ref[0])
+        assert abs(complex(ref[0], ref[1]) - np.vdot(host[0], host[1])) < 1e-12
+        lib.lgpu_context_destroy(ctx)
+        for p in ptrs:
+            assert lib.lgpu_free(p) == 0
+
+    one_round()
+    assert lib.lgpu_device_reset() == 0, lib.lgpu_last_error_string()
+    one_round()  # the scratch address is looked up again in the new context
+    print("reset ok")
+""")
+
+
+def test_dot_static_after_device_reset():
+    """lgpu_dot_static, lgpu_device_reset, lgpu_dot_static again, each against
+    lgpu_dot, in a child process that owns its own CUDA context."""
+    import pennylane_lightning_gpu_gb300 as pkg
+
+    pkg.build()
+    r = subprocess.run([sys.executable, "-c", _RESET_SCRIPT, pkg.library_path()], capture_output=True, text=True,
+                       timeout=300, env=dict(os.environ))
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "reset ok" in r.stdout
