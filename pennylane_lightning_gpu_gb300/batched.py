@@ -38,6 +38,28 @@ class BatchedExecutor:
         self.n_circuits += 1
         return self._ex.add_circuit(int(n), names, wires, params, inv, obs)
 
+    def add_template(self, n, ops, observable):
+        """A circuit structure shared by many parameter sets, lowered and fused
+        once; returns its id.  The parameters of the parametric gates in `ops`
+        are placeholders (template_num_params(tid) of them, in op order)."""
+        names = [o[0] for o in ops]
+        wires = [list(o[1]) for o in ops]
+        params = [[float(x) for x in o[2]] for o in ops]
+        inv = [bool(o[3]) if len(o) > 3 else False for o in ops]
+        obs = [(float(c), str(w), list(ws)) for c, w, ws in observable]
+        return self._ex.add_template(int(n), names, wires, params, inv, obs)
+
+    def template_num_params(self, tid):
+        return self._ex.template_num_params(int(tid))
+
+    def add_instances(self, tid, params):
+        """One circuit per row of `params` (count x template_num_params)."""
+        params = np.ascontiguousarray(params, np.float64)
+        if params.ndim == 1:
+            params = params.reshape(1, -1)
+        self.n_circuits += params.shape[0]
+        return self._ex.add_instances(int(tid), params)
+
     def prepare(self, capture=True):
         """Plan and upload.  capture=True also runs the batch once and
         captures the CUDA graph that every run() replays (new parameters go
@@ -63,6 +85,16 @@ def build_executor(circuits, dtype=np.complex128, kmax=0, threads=512, grid=0):
     for n, ops, obs in circuits:
         ex.add(n, ops, obs)
     return ex.prepare()
+
+
+def build_executor_from_templates(templates, dtype=np.complex128, kmax=0, threads=512, grid=0, capture=True):
+    """`templates` is a list of ((n, ops, observable), params[count, P]);
+    circuits are numbered template by template, row by row."""
+    ex = BatchedExecutor(dtype, kmax, threads, grid)
+    for (n, ops, obs), params in templates:
+        tid = ex.add_template(n, ops, obs)
+        ex.add_instances(tid, params)
+    return ex.prepare(capture)
 
 
 def plain_loop(circuits, dtype=np.complex128, fusion=False):
@@ -148,6 +180,34 @@ def autotune(circuits, dtype=np.complex128, sample=256, repeats=3, candidates=No
         except OSError:  # pragma: no cover - read-only home
             pass
     return k, t, record
+
+
+def config2_templates(count=4096, nmin=10, nmax=20, lmin=2, lmax=6, seed=2):
+    """The batched workload of config2_circuits as templates and parameter
+    rows: returns (templates, order) where templates is a list of
+    ((n, ops, observable), params[k, P]) for each (n, layers) that occurs and
+    order[j] = (template index, row) of circuit j.  The angles are drawn from
+    the same seeded stream in the same order, so circuit j is exactly
+    config2_circuits(...)[j]."""
+    from . import workloads
+
+    rng = np.random.default_rng(seed)
+    shapes, rows, order = {}, {}, []
+    for _ in range(count):
+        n = int(rng.integers(nmin, nmax + 1))
+        layers = int(rng.integers(lmin, lmax + 1))
+        p = rng.uniform(0, 2 * np.pi, 3 * n * layers)
+        key = (n, layers)
+        if key not in shapes:
+            ops = workloads.layered_ansatz(n, layers, np.random.default_rng(0))
+            shapes[key] = (len(shapes), (n, ops, workloads.sum_z_hamiltonian_terms(n)))
+            rows[key] = []
+        order.append((shapes[key][0], len(rows[key])))
+        rows[key].append(p)
+    templates = [None] * len(shapes)
+    for key, (ti, circ) in shapes.items():
+        templates[ti] = (circ, np.array(rows[key]))
+    return templates, order
 
 
 def config2_circuits(count=4096, nmin=10, nmax=20, lmin=2, lmax=6, seed=2):

@@ -545,6 +545,26 @@ template <class PrecisionT> void batched_bindings(py::module_ &m) {
                 return be.addCircuit(n, names, wires, params, inverses, terms);
             },
             "Add a circuit (ops as names/wires/params/inverses, observable as (coeff, word, wires) terms).")
+        .def(
+            "add_template",
+            [](BE &be, size_t n, const std::vector<std::string> &names, const std::vector<std::vector<size_t>> &wires,
+               const std::vector<std::vector<double>> &params, const std::vector<bool> &inverses,
+               const std::vector<std::tuple<double, std::string, std::vector<size_t>>> &obs) {
+                std::vector<typename BE::PTerm> terms;
+                for (const auto &t : obs) terms.push_back({std::get<0>(t), std::get<1>(t), std::get<2>(t)});
+                return be.addTemplate(n, names, wires, params, inverses, terms);
+            },
+            "Add a circuit structure shared by many parameter sets; returns its id.")
+        .def("template_num_params", &BE::templateNumParams)
+        .def(
+            "add_instances",
+            [](BE &be, size_t tid, const py::array_t<double, py::array::c_style | py::array::forcecast> &params) {
+                const size_t P = be.templateNumParams(tid);
+                PL_ABORT_IF(params.ndim() != 2 || size_t(params.shape(1)) != P,
+                            "instance parameters must have shape (count, template_num_params)");
+                return be.addInstances(tid, params.data(), size_t(params.shape(0)));
+            },
+            "Add one circuit per row of `params` (shape (count, template_num_params)); returns the first index.")
         .def("prepare", &BE::prepare, py::arg("capture") = true, py::call_guard<py::gil_scoped_release>(),
              "Plan and upload; with capture=True also run once and capture the CUDA graph that run() replays.")
         .def(

@@ -45,28 +45,51 @@ template <class Precision> class BatchedExecutor {
     BatchedExecutor(const BatchedExecutor &) = delete;
     BatchedExecutor &operator=(const BatchedExecutor &) = delete;
 
-    // Add a circuit; returns its index.  params[i] are the op's parameters,
-    // `trainable` parameters are appended to the executor's parameter vector
-    // in op order (their indices are returned by paramOffset()).
+    // Add a circuit; returns its index.  params[i] are the op's parameters;
+    // those of the parametric gates (RX, RY, RZ, their controlled forms,
+    // PhaseShift, ControlledPhaseShift, Rot, CRot, IsingXX/YY/ZZ) are appended
+    // to the executor's parameter vector in op order (the circuit's first one
+    // is at paramOffset()); the others are built into fixed matrices.
     size_t addCircuit(size_t n, const std::vector<std::string> &names, const std::vector<std::vector<size_t>> &wires,
                       const std::vector<std::vector<double>> &params, const std::vector<bool> &inverses,
                       const std::vector<PTerm> &observable) {
         PL_ABORT_IF(prepared_, "addCircuit after prepare()");
-        PL_ABORT_IF(n < 1 || n > 30, "batched circuits must have 1..30 qubits");
-        PL_ABORT_IF(names.size() != wires.size() || names.size() != params.size() || names.size() != inverses.size(),
-                    "names, wires, params and inverses must have the same length");
-        Circuit c;
-        c.n = n;
-        c.param_off = params_.size();
-        cur_param_base_ = c.param_off;
-        for (size_t i = 0; i < names.size(); i++) c.ops.push_back(lowerOp(n, names[i], wires[i], params[i], inverses[i]));
-        for (const auto &t : observable) {
-            PL_ABORT_IF(t.word.size() != t.wires.size(), "Pauli word and wires differ in length");
-            for (size_t w : t.wires) PL_ABORT_IF(w >= n, "observable wire out of range");
-            c.obs.push_back(t);
-        }
-        circuits_.push_back(std::move(c));
+        auto shape = makeShape(n, names, wires, params, inverses, observable, params_);
+        const size_t off = params_.size() - shape->nparams;
+        circuits_.push_back(Circuit{std::move(shape), off});
         return circuits_.size() - 1;
+    }
+
+    // A circuit structure shared by many parameter sets (a template): it is
+    // lowered and fused once.  `params` gives the operations' parameters; those
+    // of the parametric gates are placeholders that every instance replaces
+    // (templateNumParams() of them, in op order), the others are fixed.
+    size_t addTemplate(size_t n, const std::vector<std::string> &names, const std::vector<std::vector<size_t>> &wires,
+                       const std::vector<std::vector<double>> &params, const std::vector<bool> &inverses,
+                       const std::vector<PTerm> &observable) {
+        PL_ABORT_IF(prepared_, "addTemplate after prepare()");
+        std::vector<double> placeholders;
+        templates_.push_back(makeShape(n, names, wires, params, inverses, observable, placeholders));
+        return templates_.size() - 1;
+    }
+    size_t templateNumParams(size_t tid) const { return templates_.at(tid)->nparams; }
+
+    // `count` circuits of template `tid`, instance i taking the parameters
+    // params[i * P .. (i + 1) * P) with P = templateNumParams(tid); returns the
+    // index of the first new circuit.
+    size_t addInstances(size_t tid, const double *params, size_t count) {
+        PL_ABORT_IF(prepared_, "addInstances after prepare()");
+        PL_ABORT_IF(tid >= templates_.size(), "unknown template");
+        const auto &shape = templates_[tid];
+        const size_t P = shape->nparams;
+        const size_t first = circuits_.size();
+        params_.reserve(params_.size() + count * P);
+        circuits_.reserve(circuits_.size() + count);
+        for (size_t i = 0; i < count; i++) {
+            circuits_.push_back(Circuit{shape, params_.size()});
+            params_.insert(params_.end(), params + i * P, params + (i + 1) * P);
+        }
+        return first;
     }
 
     size_t paramOffset(size_t circuit) const { return circuits_.at(circuit).param_off; }
@@ -91,54 +114,15 @@ template <class Precision> class BatchedExecutor {
         std::vector<double> cost(circuits_.size());
         size_t max_big = 0;
         for (size_t ci = 0; ci < circuits_.size(); ci++) {
-            const Circuit &c = circuits_[ci];
+            const Shape &c = *circuits_[ci].shape;
+            const size_t param_off = circuits_[ci].param_off;
             lgpu_bcircuit_t rec{};
             rec.n = uint32_t(c.n);
             rec.block_off = uint32_t(hb.size());
             rec.out = uint32_t(ci);
-            // blocks: [(tile bits, gate indices)]
-            std::vector<std::pair<std::vector<int>, std::vector<size_t>>> blocks;
-            if (int(c.n) <= kmax_) {
-                std::vector<int> all(c.n);
-                std::iota(all.begin(), all.end(), 0);
-                std::vector<size_t> idx(c.ops.size());
-                std::iota(idx.begin(), idx.end(), 0);
-                blocks.push_back({all, idx});
-            } else {
-                max_big = std::max(max_big, c.n);
-                std::vector<Engine::GateDesc> descs;
-                for (const auto &o : c.ops) {
-                    Engine::GateDesc d;
-                    d.kind = Engine::GateDesc::MATRIX;
-                    d.tgts = o.tgts;
-                    d.ctrls = o.ctrls;
-                    descs.push_back(d);
-                }
-                const auto plan = Engine::plan_fusion(descs, c.n, klarge(), 5, 1);
-                for (const auto &b : plan) {
-                    PL_ABORT_IF(b.tile_bits.empty(), "batched execution: an operation does not fit a fused tile");
-                    blocks.push_back({b.tile_bits, b.gates});
-                }
-                // the observable is evaluated on the last block's tiles
-                uint64_t flips = 0;
-                for (const auto &t : c.obs)
-                    for (size_t k = 0; k < t.word.size(); k++)
-                        if (t.word[k] == 'X' || t.word[k] == 'Y') flips |= uint64_t(1) << Engine::bit_of(c.n, t.wires[k]);
-                auto covers = [&](const std::vector<int> &tb) {
-                    uint64_t m = 0;
-                    for (int b : tb) m |= uint64_t(1) << b;
-                    return (flips & ~m) == 0;
-                };
-                if (blocks.empty() || !covers(blocks.back().first)) {
-                    std::vector<int> fb;
-                    for (int b = 0; b < int(c.n); b++)
-                        if ((flips >> b) & 1) fb.push_back(b);
-                    std::vector<int> tile;
-                    PL_ABORT_IF_NOT(Engine::tile_for(fb, klarge(), 5, c.n, tile),
-                                    "batched execution: observable flip bits do not fit one tile");
-                    blocks.push_back({tile, {}});
-                }
-            }
+            if (int(c.n) > kmax_) max_big = std::max(max_big, c.n);
+            // blocks: [(tile bits, gate indices)], planned once per shape
+            const auto &blocks = planBlocks(*circuits_[ci].shape);
             double work = 0;
             for (const auto &blk : blocks) {
                 lgpu_bblock_t b{};
@@ -176,12 +160,12 @@ template <class Precision> class BatchedExecutor {
                         pool.resize(pool.size() + 16, 0.0);
                         hg.push_back(head);
                         for (size_t t = i; t < j; t++) {
-                            lgpu_bgate_t g = record(c.ops[gl[t]], pos, c.param_off, pool);
+                            lgpu_bgate_t g = record(c.ops[gl[t]], pos, param_off, pool);
                             g.kind = 7;  // folded into the head
                             hg.push_back(g);
                         }
                     } else {
-                        hg.push_back(record(c.ops[gl[i]], pos, c.param_off, pool));
+                        hg.push_back(record(c.ops[gl[i]], pos, param_off, pool));
                     }
                     i = j;
                 }
@@ -312,15 +296,98 @@ template <class Precision> class BatchedExecutor {
         int32_t param = -1;              // relative to the circuit's parameter offset
         std::vector<cd> matrix;          // fixed gates (already adjointed)
     };
-    struct Circuit {
+    using Blocks = std::vector<std::pair<std::vector<int>, std::vector<size_t>>>;
+    // A lowered circuit structure: its operations (parameter indices relative
+    // to the circuit's first parameter), observable and fused blocks.
+    struct Shape {
         size_t n = 0;
-        size_t param_off = 0;
+        size_t nparams = 0;
         std::vector<Op> ops;
         std::vector<PTerm> obs;
+        bool planned = false;
+        Blocks blocks;
+    };
+    struct Circuit {
+        std::shared_ptr<Shape> shape;
+        size_t param_off = 0;
     };
 
+    // Lower a circuit; its parametric gates' parameters are appended to `pvec`.
+    std::shared_ptr<Shape> makeShape(size_t n, const std::vector<std::string> &names,
+                                     const std::vector<std::vector<size_t>> &wires,
+                                     const std::vector<std::vector<double>> &params, const std::vector<bool> &inverses,
+                                     const std::vector<PTerm> &observable, std::vector<double> &pvec) {
+        PL_ABORT_IF(n < 1 || n > 30, "batched circuits must have 1..30 qubits");
+        PL_ABORT_IF(names.size() != wires.size() || names.size() != params.size() || names.size() != inverses.size(),
+                    "names, wires, params and inverses must have the same length");
+        auto sh = std::make_shared<Shape>();
+        sh->n = n;
+        const size_t base = pvec.size();
+        sh->ops.reserve(names.size());
+        for (size_t i = 0; i < names.size(); i++)
+            sh->ops.push_back(lowerOp(n, names[i], wires[i], params[i], inverses[i], pvec, base));
+        for (const auto &t : observable) {
+            PL_ABORT_IF(t.word.size() != t.wires.size(), "Pauli word and wires differ in length");
+            for (size_t w : t.wires) PL_ABORT_IF(w >= n, "observable wire out of range");
+            sh->obs.push_back(t);
+        }
+        sh->nparams = pvec.size() - base;
+        return sh;
+    }
+
+    // Fused blocks of a shape (computed on first use): one block holding the
+    // whole state when n <= kmax; otherwise tiles of klarge() bits, with a last
+    // block whose tiles cover the observable's flip bits.
+    const Blocks &planBlocks(Shape &c) {
+        if (c.planned) return c.blocks;
+        Blocks &blocks = c.blocks;
+        if (int(c.n) <= kmax_) {
+            std::vector<int> all(c.n);
+            std::iota(all.begin(), all.end(), 0);
+            std::vector<size_t> idx(c.ops.size());
+            std::iota(idx.begin(), idx.end(), 0);
+            blocks.push_back({all, idx});
+        } else {
+            std::vector<Engine::GateDesc> descs;
+            descs.reserve(c.ops.size());
+            for (const auto &o : c.ops) {
+                Engine::GateDesc d;
+                d.kind = Engine::GateDesc::MATRIX;
+                d.tgts = o.tgts;
+                d.ctrls = o.ctrls;
+                descs.push_back(d);
+            }
+            const auto plan = Engine::plan_fusion(descs, c.n, klarge(), 5, 1);
+            for (const auto &b : plan) {
+                PL_ABORT_IF(b.tile_bits.empty(), "batched execution: an operation does not fit a fused tile");
+                blocks.push_back({b.tile_bits, b.gates});
+            }
+            // the observable is evaluated on the last block's tiles
+            uint64_t flips = 0;
+            for (const auto &t : c.obs)
+                for (size_t k = 0; k < t.word.size(); k++)
+                    if (t.word[k] == 'X' || t.word[k] == 'Y') flips |= uint64_t(1) << Engine::bit_of(c.n, t.wires[k]);
+            auto covers = [&](const std::vector<int> &tb) {
+                uint64_t m = 0;
+                for (int b : tb) m |= uint64_t(1) << b;
+                return (flips & ~m) == 0;
+            };
+            if (blocks.empty() || !covers(blocks.back().first)) {
+                std::vector<int> fb;
+                for (int b = 0; b < int(c.n); b++)
+                    if ((flips >> b) & 1) fb.push_back(b);
+                std::vector<int> tile;
+                PL_ABORT_IF_NOT(Engine::tile_for(fb, klarge(), 5, c.n, tile),
+                                "batched execution: observable flip bits do not fit one tile");
+                blocks.push_back({tile, {}});
+            }
+        }
+        c.planned = true;
+        return blocks;
+    }
+
     Op lowerOp(size_t n, const std::string &name, const std::vector<size_t> &wires, const std::vector<double> &params,
-               bool adjoint) {
+               bool adjoint, std::vector<double> &pvec, size_t pbase) {
         Engine::GateDesc d = Engine::lower_operation(n, name, wires, adjoint, params, {});
         Op o;
         o.tgts = d.tgts;
@@ -330,10 +397,11 @@ template <class Precision> class BatchedExecutor {
         PL_ABORT_IF(d.tgts.size() > 2, ("batched execution supports 1- and 2-target gates, not " + name).c_str());
         PL_ABORT_IF(d.ctrls.size() > 2, "batched execution supports at most 2 controls");
         auto par = [&](uint8_t pk, size_t count) {
+            PL_ABORT_IF(params.size() < count, ("missing parameter for " + name).c_str());
             o.pkind = pk;
             o.adjoint = adjoint;
-            o.param = int32_t(params_.size() - circuits_param_base());
-            for (size_t k = 0; k < count; k++) params_.push_back(params[k]);
+            o.param = int32_t(pvec.size() - pbase);
+            for (size_t k = 0; k < count; k++) pvec.push_back(params[k]);
         };
         const std::string base = name;
         if (base == "RX" || base == "CRX") { o.kind = 4; par(1, 1); return o; }
@@ -371,7 +439,6 @@ template <class Precision> class BatchedExecutor {
         }
         return o;
     }
-    size_t circuits_param_base() const { return cur_param_base_; }
 
     lgpu_bgate_t record(const Op &o, const std::vector<int> &pos, size_t param_off, std::vector<double> &pool) {
         lgpu_bgate_t g{};
@@ -446,8 +513,8 @@ template <class Precision> class BatchedExecutor {
     lgpu_graph_t graph_ = nullptr;
     bool prepared_ = false;
     std::vector<Circuit> circuits_;
+    std::vector<std::shared_ptr<Shape>> templates_;
     std::vector<double> params_;
-    size_t cur_param_base_ = 0;
     size_t ngates_ = 0, nblocks_ = 0, scratch_amps_ = 0;
     std::vector<void *> owned_;
     void *d_circ_ = nullptr, *d_order_ = nullptr, *d_blocks_ = nullptr, *d_gates_ = nullptr, *d_terms_ = nullptr,

@@ -618,7 +618,20 @@ __global__ void __launch_bounds__(512, 1) batch_kernel(lgpu_batch_args_t a) {
                         }
                     }
                     if (__syncthreads_or(timed_out)) {
-                        if (threadIdx.x == 0) atomicOr(&g_batch_error, 1u);
+                        if (threadIdx.x == 0) {
+                            atomicOr(&g_batch_error, 1u);
+                            // the loads issued so far (tiles j .. kRing - 1 at j = 0,
+                            // else j .. j + kRing - 2; one per stage) may still be
+                            // landing in this CTA's shared memory: wait for them,
+                            // bounded again, before the CTA leaves
+                            const uint64_t last = j == 0 ? uint64_t(kRing - 1) : j + uint64_t(kRing) - 2;
+                            for (uint64_t jj = j; jj <= last && jj < ntiles; jj++) {
+                                const int s2 = int((u0 + jj) % kRing);
+                                const uint32_t par2 = (phase_bits >> s2) & 1u;
+                                for (uint32_t sp = 0; !b_try_wait(&full_bar[s2], par2) && sp <= kBatchWaitLimit; sp++) {
+                                }
+                            }
+                        }
                         failed = true;
                         break;
                     }

@@ -215,7 +215,8 @@ __global__ void __launch_bounds__(kBulkThreads, 1)
         }
     }
     bool failed = false;
-    for (uint64_t j = 0;; j++) {
+    uint64_t j = 0;
+    for (;; j++) {
         const uint64_t tile = blockIdx.x + j * G;
         if (tile >= p.ntiles) break;
         const int s = int(j % kBulkStages);
@@ -264,6 +265,18 @@ __global__ void __launch_bounds__(kBulkThreads, 1)
                     bulk_wait_read1();
                     issue_load(next, int(jp % kBulkStages));
                 }
+            }
+        }
+    }
+    if (failed && threadIdx.x == 0) {
+        // Loads issued before the time-out may still be landing in this CTA's
+        // shared memory: wait (bounded again) for each of them before leaving.
+        // At iteration j the loads of iterations j .. max(2, j + 1) are out.
+        const uint64_t last = j + 1 > uint64_t(kBulkStages - 1) ? j + 1 : uint64_t(kBulkStages - 1);
+        for (uint64_t jj = j; jj <= last && blockIdx.x + jj * G < p.ntiles; jj++) {
+            const int s = int(jj % kBulkStages);
+            const uint32_t parity = uint32_t((jj / kBulkStages) & 1);
+            for (uint32_t spins = 0; !mbar_try_wait(&full_bar[s], parity) && spins <= kWaitLimit; spins++) {
             }
         }
     }

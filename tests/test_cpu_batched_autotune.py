@@ -83,3 +83,23 @@ def test_config2_workload_shape():
         per_layer = 3 * n + n  # RX, RY, RZ on every wire + CNOT ring
         assert len(ops) % per_layer == 0 and 2 <= len(ops) // per_layer <= 6
         assert len(obs) == n
+
+
+def test_config2_templates_reproduce_the_circuits():
+    """The template form of the 4096-circuit batch (one structure per
+    (n, layers), one parameter row per circuit) holds exactly the circuits of
+    config2_circuits, angles included."""
+    import numpy as np
+
+    from pennylane_lightning_gpu_gb300 import batched
+
+    circuits = batched.config2_circuits(count=300, seed=2)
+    templates, order = batched.config2_templates(count=300, seed=2)
+    assert len(order) == 300
+    assert sum(p.shape[0] for _, p in templates) == 300
+    for j, (ti, row) in enumerate(order):
+        (n, ops, obs), params = templates[ti]
+        n0, ops0, obs0 = circuits[j]
+        assert n == n0 and obs == obs0
+        assert [(o[0], o[1], o[3]) for o in ops] == [(o[0], o[1], o[3]) for o in ops0]
+        assert np.array_equal(params[row], [o[2][0] for o in ops0 if o[2]])

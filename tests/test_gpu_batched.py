@@ -74,3 +74,17 @@ def test_autotune_cache(tmp_path, monkeypatch):
     assert (k, t) in [(12, 256), (14, 256)]
     k2, t2, rec2 = batched.autotune(circuits, np.complex64, sample=16, repeats=1)
     assert (k2, t2) == (k, t)
+
+
+@pytest.mark.parametrize("dtype", [np.complex128, np.complex64])
+def test_templates_match_per_circuit_adds(dtype):
+    """The same batch added as templates plus parameter rows and as one
+    circuit at a time gives the same bits per circuit."""
+    templates, order = batched.config2_templates(count=200, nmin=10, nmax=18, seed=7)
+    circuits = batched.config2_circuits(count=200, nmin=10, nmax=18, seed=7)
+    a = batched.build_executor(circuits, dtype).run()
+    ex = batched.build_executor_from_templates(templates, dtype, capture=False)
+    b = ex.run()
+    base = np.cumsum([0] + [p.shape[0] for _, p in templates])
+    got = np.array([b[base[ti] + row] for ti, row in order])
+    assert np.array_equal(got, a)
