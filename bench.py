@@ -369,6 +369,7 @@ def run_ours(args):
         line["lightning_qubit"] = lightning_qubit_probe()
     if single and not args.no_circuits:
         line["circuits"] = bench_circuits(args)
+        line["tensor_core"] = bench_tensor_core()
     if single and not args.no_batched:
         line["batched"] = bench_batched(args)
     if single and not args.no_serving:
@@ -629,6 +630,80 @@ def bench_config0(O):
                                               "bound": 1e-10 if key == "c128" else 1e-5}}
         del dev0
     return out
+
+
+def _rot_matrix(phi, theta, omega):
+    c, s = np.cos(theta / 2), np.sin(theta / 2)
+    return np.array([[np.exp(-0.5j * (phi + omega)) * c, -np.exp(0.5j * (phi - omega)) * s],
+                     [np.exp(-0.5j * (phi - omega)) * s, np.exp(0.5j * (phi + omega)) * c]])
+
+
+def bench_tensor_core(n=28, reps=5):
+    """Dense 6-target complex64 gates on the six lowest state bits: the
+    tensor-core kernel (tcgen05, three TF32 products) against the FP32
+    shared-memory kernel on the same matrix, and against the fused FP32 path
+    applying the six 1-qubit gates that the matrix folds (Rot on each of the six
+    lowest wires), on a 28-qubit complex64 state."""
+    import torch
+
+    import pennylane_lightning_gpu_gb300 as pkg
+
+    m = pkg.native()
+    rng = np.random.default_rng(8)
+    S = (1 << n) * 8
+    wires = list(range(n - 6, n))
+    angles = rng.uniform(0, 2 * np.pi, (6, 3))
+    u = np.array([[1.0]])
+    for a in angles:  # wires n-6 .. n-1: the first is the most significant matrix bit
+        u = np.kron(u, _rot_matrix(*a))
+    sv = m.LightningGPU_C64(n, m.DevTag(0, 0))
+    sv.Hadamard([0], False, [])
+
+    def timed(fn):
+        fn()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        for _ in range(reps):
+            fn()
+        b.record()
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / reps
+
+    mode = m.get_tensor_mode()
+    try:
+        m.set_tensor_mode(1)
+        t_tc = timed(lambda: sv.apply("QubitUnitary", wires, False, [], u.ravel()))
+        m.set_tensor_mode(0)
+        t_simt = timed(lambda: sv.apply("QubitUnitary", wires, False, [], u.ravel()))
+    finally:
+        m.set_tensor_mode(mode)
+    names, ws, inv, ps = ["Rot"] * 6, [[w] for w in wires], [False] * 6, [list(a) for a in angles]
+    t_fused = timed(lambda: sv.apply(names, ws, inv, ps))
+    # agreement of the three paths on a 20-qubit state
+    k = 20
+    psi = np.random.default_rng(9).normal(size=(2, 1 << k))
+    psi = (psi[0] + 1j * psi[1]) / np.linalg.norm(psi)
+    outs = {}
+    for tag in ("tc", "simt", "fused"):
+        s2 = m.LightningGPU_C64(psi.astype(np.complex64))
+        m.set_tensor_mode(1 if tag == "tc" else 0)
+        if tag == "fused":
+            s2.apply(names, [[w + k - n] for w in wires], inv, ps)
+        else:
+            s2.apply("QubitUnitary", [w + k - n for w in wires], False, [], u.ravel())
+        outs[tag] = s2.GetState().astype(np.complex128)
+    m.set_tensor_mode(mode)
+    peak, _ = _peaks()
+    return {"workload": "dense 64x64 complex64 matrix on the six lowest state bits of a %d-qubit state (%.0f GiB), "
+                        "the Kronecker product of six Rot gates" % (n, S / 2**30),
+            "tensor_core_ms": round(t_tc, 4), "fp32_shared_memory_ms": round(t_simt, 4),
+            "fused_six_rot_gates_ms": round(t_fused, 4),
+            "tensor_core_gbs": round(2 * S / (t_tc / 1e3) / 1e9, 1),
+            "tensor_core_frac_of_hbm": round(2 * S / (t_tc / 1e3) / 1e9 / peak, 3),
+            "speedup_vs_fp32_kernel": round(t_simt / t_tc, 2), "speedup_vs_fused_gates": round(t_fused / t_tc, 2),
+            "max_abs_diff_20q": {"tc_vs_fp32_kernel": float(np.max(np.abs(outs["tc"] - outs["simt"]))),
+                                 "tc_vs_fused": float(np.max(np.abs(outs["tc"] - outs["fused"])))}}
 
 
 def bench_circuits(args):
@@ -900,6 +975,16 @@ def profile_case(name):
         terms += workloads.sum_z_hamiltonian_terms(n)
         sv.ExpectationValue([t[1] for t in terms], [list(t[2]) for t in terms],
                             np.array([t[0] for t in terms], np.complex64))
+    elif name == "dense6":
+        n = 25
+        sv = m.LightningGPU_C64(n)
+        sv.apply(["Hadamard"] * n, [[w] for w in range(n)], [False] * n, [[]] * n)
+        u = np.linalg.qr(np.random.default_rng(4).normal(size=(64, 64)) + 0j)[0]
+        for mode in (1, 0):  # tensor cores, then the FP32 shared-memory kernel
+            m.set_tensor_mode(mode)
+            sv.apply("QubitUnitary", list(range(n - 6, n)), False, [], u.ravel())
+        m.set_tensor_mode(1)
+        sv.synchronize()
     elif name == "adjoint":
         n = 12
         raw = workloads.layered_ansatz(n, 4, np.random.default_rng(0))
@@ -938,9 +1023,10 @@ def main():
     ap.add_argument("--no-circuits", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-serving", action="store_true")
-    ap.add_argument("--case", choices=["fused", "fused128", "gram", "batch", "pauli", "adjoint", "adjblock"], default=None,
+    ap.add_argument("--case", choices=["fused", "fused128", "gram", "batch", "pauli", "adjoint", "adjblock", "dense6"],
+                    default=None,
                     help="run one small secondary-kernel case (profiling) and exit")
-    ap.add_argument("--only", choices=["batched", "serving", "circuits"], default=None,
+    ap.add_argument("--only", choices=["batched", "serving", "circuits", "tensor_core"], default=None,
                     help="run one section alone (profiling runs); the default prints the full line")
     ap.add_argument("--batch-circuits", type=int, default=4096)
     ap.add_argument("--batch-plain", type=int, default=256)
@@ -957,6 +1043,9 @@ def main():
         return
     if args.only == "serving":
         print(json.dumps({"serving": bench_serving(args)}))
+        return
+    if args.only == "tensor_core":
+        print(json.dumps({"tensor_core": bench_tensor_core()}))
         return
     if args.only == "circuits":
         print(json.dumps({"circuits": bench_circuits(args)}))

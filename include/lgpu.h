@@ -85,6 +85,16 @@ int lgpu_get_f64_mode(void);
 lgpu_status_t lgpu_set_stream_mode(int mode);
 int lgpu_get_stream_mode(void);
 
+/* Kernel family for dense 6-target complex64 matrices on the six lowest state
+ * bits (any target order, no controls, n >= 12) (process-wide): 1 (default) =
+ * tensor cores (tcgen05.mma kind::tf32, three TF32 products per FP32 value,
+ * FP32 accumulation in tensor memory); 0 = the shared-memory FP32 kernel used
+ * for every other dense matrix of 6..12 targets.  LGPU_TC=0 selects 0 at
+ * start-up.  No counterpart in the reference (custatevecApplyMatrix chooses
+ * its kernels internally). */
+lgpu_status_t lgpu_set_tensor_mode(int mode);
+int lgpu_get_tensor_mode(void);
+
 /* Device-side error flag of the engine's bounded waits (1 = a kernel gave up
  * waiting for a bulk copy and left its tile unprocessed).  reset != 0 clears
  * it.  The C++ layer checks it at every synchronisation point.  No

@@ -636,6 +636,10 @@ PYBIND11_MODULE(lightning_gpu_qubit_ops, m) {
         "set_stream_mode", [](int mode) { PL_LGPU_IS_SUCCESS(lgpu_set_stream_mode(mode)); },
         "1-target gate kernels: 1 bulk-copy pipelined tiles, 0 grid-stride");
     m.def("get_stream_mode", &lgpu_get_stream_mode);
+    m.def(
+        "set_tensor_mode", [](int mode) { PL_LGPU_IS_SUCCESS(lgpu_set_tensor_mode(mode)); },
+        "1: dense 6-target complex64 gates on the lowest six bits on the tensor cores; 0: FP32 shared-memory kernel.");
+    m.def("get_tensor_mode", &lgpu_get_tensor_mode);
 
     py::class_<DevPool>(m, "DevPool")
         .def(py::init<>())

@@ -69,6 +69,18 @@ int fused_df_enabled() {
     return m;
 }
 
+static std::atomic<int> g_tc_mode{-1};
+
+int tc_enabled() {
+    int m = g_tc_mode.load(std::memory_order_relaxed);
+    if (m < 0) {
+        const char *e = std::getenv("LGPU_TC");
+        m = (e && e[0] == '0') ? 0 : 1;
+        g_tc_mode.store(m, std::memory_order_relaxed);
+    }
+    return m;
+}
+
 int current_device() {
     int d = 0;
     cudaGetDevice(&d);
@@ -272,6 +284,14 @@ lgpu_status_t lgpu_set_stream_mode(int mode) {
 }
 
 int lgpu_get_stream_mode(void) { return bulk_enabled(); }
+
+lgpu_status_t lgpu_set_tensor_mode(int mode) {
+    if (mode != 0 && mode != 1) return fail(LGPU_ERR_INVALID_ARG, "tensor mode must be 0 or 1");
+    g_tc_mode.store(mode, std::memory_order_relaxed);
+    return LGPU_OK;
+}
+
+int lgpu_get_tensor_mode(void) { return tc_enabled(); }
 
 const char *lgpu_last_error_string(void) { return g_last_error.c_str(); }
 

@@ -283,6 +283,12 @@ __global__ void __launch_bounds__(kBulkThreads, 1)
     if (threadIdx.x == 0) bulk_wait_all();
 }
 
+}  // namespace lgpu
+
+#include "lgpu_tc.cuh"
+
+namespace lgpu {
+
 template <class T, class I> struct PhaseParams {
     Holes holes;
     I set;  // bits forced to 1
@@ -1013,6 +1019,50 @@ static lgpu_status_t run_gatebig(cplx_t<T> *sv, uint32_t n, const std::vector<Cm
     return LGPU_OK;
 }
 
+// Dense 6-target complex64 gate on the six lowest state bits (targets in any
+// order, no controls) on the tensor cores: U is reordered so that row and
+// column indices are the state's own low six bits.
+static bool dense6_tc_applies(uint32_t n, uint32_t t, const GateGeometry &g) {
+    if (t != 6 || n < 12 || !g.ctrls.empty() || !tc_enabled()) return false;
+    uint32_t seen = 0;
+    for (int b : g.tgts) {
+        if (b < 0 || b > 5) return false;
+        seen |= 1u << b;
+    }
+    return seen == 0x3Fu;
+}
+
+static lgpu_status_t run_dense6_tc(float2 *sv, uint32_t n, const std::vector<Cm> &m, const GateGeometry &g,
+                                   cudaStream_t s) {
+    int rowof[64];
+    for (int x = 0; x < 64; x++) {
+        int r = 0;
+        for (int k = 0; k < 6; k++)
+            if ((x >> g.tgts[size_t(k)]) & 1) r |= 1 << (5 - k);
+        rowof[x] = r;
+    }
+    std::vector<float2> u(64 * 64);
+    for (int x = 0; x < 64; x++)
+        for (int y = 0; y < 64; y++) {
+            const Cm v = m[size_t(rowof[x] * 64 + rowof[y])];
+            u[size_t(x * 64 + y)] = make_float2(float(v.re), float(v.im));
+        }
+    void *dbuf = nullptr;
+    const size_t bytes = u.size() * sizeof(float2);
+    LGPU_CUDA_TRY(cudaMallocAsync(&dbuf, bytes, s));
+    LGPU_CUDA_TRY(cudaMemcpyAsync(dbuf, u.data(), bytes, cudaMemcpyHostToDevice, s));
+    TcDense6Params p{};
+    p.u = static_cast<const float2 *>(dbuf);
+    p.ntiles = (uint64_t(1) << n) / uint64_t(kTcCols * 64);
+    static std::atomic<size_t> attr[64];
+    LGPU_TRY(ensure_smem(reinterpret_cast<const void *>(dense6_tc_kernel), kTcSmemBytes, attr));
+    const unsigned grid = unsigned(std::min<uint64_t>(p.ntiles, uint64_t(sm_count())));
+    dense6_tc_kernel<<<grid, kTcThreads, kTcSmemBytes, s>>>(sv, p);
+    LGPU_CHECK_LAUNCH();
+    LGPU_CUDA_TRY(cudaFreeAsync(dbuf, s));
+    return LGPU_OK;
+}
+
 template <class T, class I>
 static lgpu_status_t apply_matrix_t(cplx_t<T> *sv, unsigned nstates, cplx_t<T> *const *svs, uint32_t n,
                                     const double *matrix, uint32_t t, const GateGeometry &g,
@@ -1032,6 +1082,8 @@ static lgpu_status_t apply_matrix_t(cplx_t<T> *sv, unsigned nstates, cplx_t<T> *
     case 5: return run_gatek<T, I, 5>(sv, nstates, svs, n, m, g, s);
     default:
         // t > 5: multi-state calls are split per state by the caller
+        if constexpr (sizeof(T) == 4)
+            if (dense6_tc_applies(n, t, g)) return run_dense6_tc(sv, n, m, g, s);
         return run_gatebig<T, I>(sv, n, m, g, s);
     }
 }

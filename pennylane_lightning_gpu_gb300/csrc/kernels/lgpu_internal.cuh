@@ -56,6 +56,10 @@ int fused_df_enabled();
 // Uncontrolled 1-target gates use the bulk-copy pipelined kernel when 1
 // (default); the grid-stride kernel when 0.  See lgpu_set_stream_mode().
 int bulk_enabled();
+// Dense 6-target complex64 gates on the six lowest state bits run on the
+// tensor cores (tcgen05) when 1 (default); the shared-memory FP32 kernel when
+// 0 (environment LGPU_TC=0).  See lgpu_set_tensor_mode().
+int tc_enabled();
 // device error flag of the batched kernel's bounded waits (lgpu_batch.cu)
 lgpu_status_t batch_error_fetch(unsigned *v, bool reset);
 
