@@ -101,6 +101,15 @@ int lgpu_get_tensor_mode(void);
  * counterpart in the reference. */
 lgpu_status_t lgpu_device_error(int *code, int reset);
 
+/* The same per stream: 1 when a kernel launched on `stream` gave up waiting
+ * since the last reset of this stream's word; reset != 0 clears it.  The
+ * call synchronises `stream`.  The default streams share one word; other
+ * streams get their own (beyond 255 distinct streams, words are shared
+ * round-robin).  The C++ layer checks its own stream's word at every
+ * synchronisation, so a time-out on one stream is not raised at another's.
+ * No counterpart in the reference. */
+lgpu_status_t lgpu_stream_error(lgpu_stream_t stream, int *code, int reset);
+
 /* Diagnostic of the bounded waits: one CTA waits on an mbarrier that expects
  * bytes no copy will deliver, with the streaming kernels' give-up logic and a
  * limit of `spin_limit` polls (at most 2^24); the call synchronises `stream`

@@ -273,7 +273,7 @@ template <class Precision> class BatchedExecutor {
     std::vector<double> wait() {
         PL_LGPU_IS_SUCCESS(lgpu_stream_sync(stream_));
         int code = 0;
-        PL_LGPU_IS_SUCCESS(lgpu_device_error(&code, 1));
+        PL_LGPU_IS_SUCCESS(lgpu_stream_error(stream_, &code, 1));
         PL_ABORT_IF(code != 0, "A batched kernel timed out waiting for a bulk copy; results are invalid");
         std::vector<double> out(circuits_.size());
         std::memcpy(out.data(), h_out_, out.size() * sizeof(double));

@@ -591,7 +591,7 @@ class StateVectorCudaManaged : public StateVectorCudaBase<Precision, StateVector
     void sync() const {
         PL_LGPU_IS_SUCCESS(lgpu_stream_sync(BaseType::lstream()));
         int code = 0;
-        PL_LGPU_IS_SUCCESS(lgpu_device_error(&code, 1));
+        PL_LGPU_IS_SUCCESS(lgpu_stream_error(BaseType::lstream(), &code, 1));
         PL_ABORT_IF(code != 0, "A GPU kernel timed out waiting for a bulk copy; the state is invalid");
     }
     lgpu_context_t ctx() const { return ctx_->get(); }

@@ -493,7 +493,7 @@ __device__ __forceinline__ void b_fence() { asm volatile("fence.proxy.async.shar
 // DFM (complex128): gates run in float-float on a float-float tile; the tile
 // is converted in place after a load and before a store or the observable.
 template <class T, bool EMU, bool DFM = false>
-__global__ void __launch_bounds__(512, 1) batch_kernel(lgpu_batch_args_t a) {
+__global__ void __launch_bounds__(512, 1) batch_kernel(lgpu_batch_args_t a, unsigned *err) {
     using C = cplx_t<T>;
     extern __shared__ __align__(128) unsigned char smem_raw[];
     C *ring = reinterpret_cast<C *>(smem_raw);
@@ -620,6 +620,7 @@ __global__ void __launch_bounds__(512, 1) batch_kernel(lgpu_batch_args_t a) {
                     if (__syncthreads_or(timed_out)) {
                         if (threadIdx.x == 0) {
                             atomicOr(&g_batch_error, 1u);
+                            atomicOr(err, 1u);
                             // the loads issued so far (tiles j .. kRing - 1 at j = 0,
                             // else j .. j + kRing - 2; one per stage) may still be
                             // landing in this CTA's shared memory: wait for them,
@@ -706,7 +707,9 @@ static lgpu_status_t launch_batch(const lgpu_batch_args_t &args, unsigned grid, 
     // runs the batch eagerly once before capturing it).
     static std::atomic<size_t> attr[64];
     LGPU_TRY(ensure_smem(reinterpret_cast<const void *>(batch_kernel<T, EMU, DFM>), smem, attr));
-    batch_kernel<T, EMU, DFM><<<grid, args.threads, smem, s>>>(args);
+    unsigned *err = nullptr;
+    LGPU_TRY(stream_error_ptr(s, &err));
+    batch_kernel<T, EMU, DFM><<<grid, args.threads, smem, s>>>(args, err);
     LGPU_CHECK_LAUNCH();
     return LGPU_OK;
 }

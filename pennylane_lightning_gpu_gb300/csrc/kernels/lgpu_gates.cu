@@ -15,6 +15,8 @@
 //  * fused_kernel     a block of 1/2-target gates applied to shared-memory
 //                     tiles of 2^k amplitudes: one HBM pass for many gates.
 #include <cstring>
+#include <mutex>
+#include <unordered_map>
 
 #include "lgpu_bodies.cuh"
 #include "lgpu_df64.cuh"
@@ -80,6 +82,15 @@ __global__ void __launch_bounds__(kGateBlock)
 // g_lgpu_device_error and leaves.
 // ---------------------------------------------------------------------------
 __device__ unsigned int g_lgpu_device_error = 0;
+// One error word per stream (slot); kernels with bounded waits receive the
+// address of their launch stream's word and set it besides the device-wide flag.
+__device__ unsigned int g_lgpu_stream_error[kErrSlots];
+
+// Mark a timed-out wait: the launch stream's word and the device-wide flag.
+__device__ __forceinline__ void report_timeout(unsigned *err) {
+    if (err) atomicOr(err, 1u);
+    atomicOr(&g_lgpu_device_error, 1u);
+}
 
 constexpr int kBulkThreads = 512;
 constexpr int kBulkStages = 3;
@@ -110,7 +121,7 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
 // count that no copy will deliver (a flag nothing sets) and waits with the
 // streaming kernels' bounded spin; it gives up after `spin_limit` polls and
 // records the time-out in g_lgpu_device_error, as they do.
-__global__ void wait_selftest_kernel(uint32_t spin_limit) {
+__global__ void wait_selftest_kernel(uint32_t spin_limit, unsigned *err) {
     __shared__ __align__(8) uint64_t bar;
     if (threadIdx.x == 0) {
         mbar_init(&bar, 1);
@@ -127,7 +138,7 @@ __global__ void wait_selftest_kernel(uint32_t spin_limit) {
             break;
         }
     }
-    if (__syncthreads_or(timed_out) && threadIdx.x == 0) atomicOr(&g_lgpu_device_error, 1u);
+    if (__syncthreads_or(timed_out) && threadIdx.x == 0) report_timeout(err);
 }
 
 __device__ __forceinline__ void bulk_load(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
@@ -147,6 +158,7 @@ __device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wa
 __device__ __forceinline__ void fence_async_shared() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 
 template <class T> struct BulkParams {
+    unsigned *err;   // the launch stream's error word
     uint64_t ntiles;
     int t;           // target bit
     int ch_log2;     // log2(CH)
@@ -232,7 +244,7 @@ __global__ void __launch_bounds__(kBulkThreads, 1)
         // Every thread leaves its bounded wait; the CTA then decides together.
         failed = __syncthreads_or(timed_out) != 0;
         if (failed) {
-            if (threadIdx.x == 0) atomicOr(&g_lgpu_device_error, 1u);
+            if (threadIdx.x == 0) report_timeout(p.err);
             break;
         }
         C *buf = ring + size_t(s) * 2 * CH;
@@ -377,31 +389,61 @@ template <class T, class I> struct GbigParams {
     I cset;
     I ngroups;
     int t;
+    int batch;             // groups per CTA iteration: batch * 2^t = 4096 (or all groups)
     const I *off;          // D offsets (device)
-    const cplx_t<T> *mat;  // D x D row-major (device)
+    const cplx_t<T> *matT; // D x D, transposed: matT[c * D + r] = M[r][c] (device)
 };
 
+// Dense gates on 6..12 targets: each CTA iteration stages `batch` groups
+// (4096 amplitudes) in shared memory; thread j computes rows r = j mod RB
+// (+ RB, ...) of groups j / RB (+ GB, ...), RB = min(D, 256), GB = 256 / RB:
+// 16 outputs per thread, each matrix element read once (coalesced, from the
+// transposed copy) and used for all of the thread's groups.  State-precision
+// arithmetic (FP32 for complex64, FP64 for complex128).
+constexpr int kGbigThreads = 256;
+constexpr int kGbigOut = 16;  // outputs per thread per iteration
+
 template <class T, class I>
-__global__ void __launch_bounds__(256) gatebig_kernel(cplx_t<T> *__restrict__ sv, const GbigParams<T, I> p) {
+__global__ void __launch_bounds__(kGbigThreads) gatebig_kernel(cplx_t<T> *__restrict__ sv, const GbigParams<T, I> p) {
     using C = cplx_t<T>;
     extern __shared__ unsigned char smem_raw[];
-    C *tile = reinterpret_cast<C *>(smem_raw);
+    C *tile = reinterpret_cast<C *>(smem_raw);  // [batch][D]
     const int D = 1 << p.t;
-    for (I g = blockIdx.x; g < p.ngroups; g += gridDim.x) {
-        const I base = insert_holes<I>(g, p.holes) | p.cset;
+    const int RB = D < kGbigThreads ? D : kGbigThreads, GB = kGbigThreads / RB;
+    const int r0 = threadIdx.x % RB, gl = threadIdx.x / RB;
+    const int rows = D / RB, grp = (p.batch + GB - 1) / GB;  // rows * grp <= kGbigOut
+    const I nbatches = (p.ngroups + I(p.batch) - 1) / I(p.batch);
+    for (I bt = blockIdx.x; bt < nbatches; bt += gridDim.x) {
+        const I g0 = bt * I(p.batch);
         __syncthreads();
-        for (int c = threadIdx.x; c < D; c += blockDim.x) tile[c] = sv[base | p.off[c]];
+        for (int e = threadIdx.x; e < p.batch * D; e += kGbigThreads) {
+            const int b = e / D, c = e % D;
+            const I g = g0 + I(b);
+            if (g < p.ngroups) tile[e] = sv[(insert_holes<I>(g, p.holes) | p.cset) | p.off[c]];
+        }
         __syncthreads();
-        for (int r = threadIdx.x; r < D; r += blockDim.x) {
-            double xr = 0, xi = 0;
-            const C *row = p.mat + size_t(r) * D;
+        for (int ri = 0; ri < rows; ri++) {
+            const int r = r0 + ri * RB;
+            C acc[kGbigOut];
+#pragma unroll
+            for (int q = 0; q < kGbigOut; q++) acc[q] = mk<T>(T(0), T(0));
             for (int c = 0; c < D; c++) {
-                const C mv = row[c];
-                const C av = tile[c];
-                xr = fma(double(mv.x), double(av.x), fma(-double(mv.y), double(av.y), xr));
-                xi = fma(double(mv.x), double(av.y), fma(double(mv.y), double(av.x), xi));
+                const C mv = p.matT[size_t(c) * D + r];
+#pragma unroll
+                for (int q = 0; q < kGbigOut; q++) {
+                    if (q < grp && gl + q * GB < p.batch) {
+                        const C av = tile[(gl + q * GB) * D + c];
+                        acc[q] = cfma<T>(mv, av, acc[q]);
+                    }
+                }
             }
-            sv[base | p.off[r]] = mk<T>(T(xr), T(xi));
+#pragma unroll
+            for (int q = 0; q < kGbigOut; q++) {
+                if (q < grp && gl + q * GB < p.batch) {
+                    const I g = g0 + I(gl + q * GB);
+                    if (g < p.ngroups) sv[(insert_holes<I>(g, p.holes) | p.cset) | p.off[r]] = acc[q];
+                }
+            }
         }
     }
 }
@@ -924,6 +966,7 @@ static lgpu_status_t run_gate1(cplx_t<T> *sv, unsigned nstates, cplx_t<T> *const
         const int ch_log2 = sizeof(T) == 8 ? 11 : 12;  // 32 KB halves, 64 KB tiles
         if (int(n) >= ch_log2 + 2) {
             BulkParams<T> bp{};
+            LGPU_TRY(stream_error_ptr(s, &bp.err));
             bp.ntiles = (uint64_t(1) << n) >> (ch_log2 + 1);
             bp.t = tb;
             bp.ch_log2 = ch_log2;
@@ -990,8 +1033,12 @@ static lgpu_status_t run_gatebig(cplx_t<T> *sv, uint32_t n, const std::vector<Cm
             if ((r >> (t - 1 - k)) & 1) o |= uint64_t(1) << g.tgts[size_t(k)];
         off[size_t(r)] = I(o);
     }
-    std::vector<cplx_t<T>> mh(size_t(D) * D);
-    for (size_t e = 0; e < mh.size(); e++) mh[e] = mk<T>(T(m[e].re), T(m[e].im));
+    std::vector<cplx_t<T>> mh(size_t(D) * D);  // transposed
+    for (int r = 0; r < D; r++)
+        for (int c = 0; c < D; c++) {
+            const Cm v = m[size_t(r) * D + c];
+            mh[size_t(c) * D + r] = mk<T>(T(v.re), T(v.im));
+        }
     // Stream-ordered pool allocation for the device copy of the matrix.
     void *dbuf = nullptr;
     const size_t mbytes = mh.size() * sizeof(cplx_t<T>), obytes = off.size() * sizeof(I);
@@ -1007,13 +1054,17 @@ static lgpu_status_t run_gatebig(cplx_t<T> *sv, uint32_t n, const std::vector<Cm
     p.cset = I(g.cset);
     p.ngroups = I(uint64_t(1) << (n - holes.size()));
     p.t = t;
+    p.batch = int(std::min<uint64_t>(uint64_t(4096 / D), uint64_t(p.ngroups)));
+    if (p.batch < 1) p.batch = 1;
     p.off = doff;
-    p.mat = dmat;
-    const size_t smem = size_t(D) * sizeof(cplx_t<T>);
+    p.matT = dmat;
+    const size_t smem = size_t(p.batch) * D * sizeof(cplx_t<T>);
     static std::atomic<size_t> attr[64];
     LGPU_TRY(ensure_smem(reinterpret_cast<const void *>(gatebig_kernel<T, I>), smem, attr));
-    const unsigned grid = unsigned(std::min<uint64_t>(uint64_t(p.ngroups), uint64_t(sm_count()) * 4));
-    gatebig_kernel<T, I><<<grid, 256, smem, s>>>(sv, p);
+    const uint64_t nbatches = (uint64_t(p.ngroups) + p.batch - 1) / p.batch;
+    const unsigned per_sm = sizeof(T) == 8 ? 3 : 6;
+    const unsigned grid = unsigned(std::min<uint64_t>(nbatches, uint64_t(sm_count()) * per_sm));
+    gatebig_kernel<T, I><<<grid, kGbigThreads, smem, s>>>(sv, p);
     LGPU_CHECK_LAUNCH();
     LGPU_CUDA_TRY(cudaFreeAsync(dbuf, s));
     return LGPU_OK;
@@ -1052,8 +1103,9 @@ static lgpu_status_t run_dense6_tc(float2 *sv, uint32_t n, const std::vector<Cm>
     LGPU_CUDA_TRY(cudaMallocAsync(&dbuf, bytes, s));
     LGPU_CUDA_TRY(cudaMemcpyAsync(dbuf, u.data(), bytes, cudaMemcpyHostToDevice, s));
     TcDense6Params p{};
+    LGPU_TRY(stream_error_ptr(s, &p.err));
     p.u = static_cast<const float2 *>(dbuf);
-    p.ntiles = (uint64_t(1) << n) / uint64_t(kTcCols * 64);
+    p.ntiles = (uint64_t(1) << n) / uint64_t(kTcTileAmps);
     static std::atomic<size_t> attr[64];
     LGPU_TRY(ensure_smem(reinterpret_cast<const void *>(dense6_tc_kernel), kTcSmemBytes, attr));
     const unsigned grid = unsigned(std::min<uint64_t>(p.ntiles, uint64_t(sm_count())));
@@ -1348,6 +1400,47 @@ static lgpu_status_t fused_t(cplx_t<T> *sv, uint32_t n, const std::vector<int> &
 
 }  // namespace lgpu
 
+namespace lgpu {
+
+// Stream -> error slot: the legacy and per-thread default streams (handles
+// 0, 1, 2) use slot 0; other streams get slots 1 .. kErrSlots - 1 in order of
+// first use, and share them round-robin beyond that.
+static std::mutex g_err_mu;
+static std::unordered_map<uintptr_t, int> g_err_slot;
+static int g_err_next = 0;
+static std::atomic<unsigned *> g_err_base[64];
+static std::atomic<unsigned> g_err_epoch[64];
+
+lgpu_status_t stream_error_ptr(cudaStream_t s, unsigned **out) {
+    int dev = 0;
+    LGPU_CUDA_TRY(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) return fail(LGPU_ERR_UNSUPPORTED, "device ordinal beyond 63");
+    const uintptr_t h = reinterpret_cast<uintptr_t>(s);
+    std::lock_guard<std::mutex> lock(g_err_mu);
+    int slot = 0;
+    if (h > 2) {
+        auto it = g_err_slot.find(h);
+        if (it == g_err_slot.end()) {
+            slot = 1 + (g_err_next++ % (kErrSlots - 1));
+            g_err_slot.emplace(h, slot);
+        } else {
+            slot = it->second;
+        }
+    }
+    unsigned *base = g_err_base[dev].load(std::memory_order_acquire);
+    if (!base || g_err_epoch[dev].load(std::memory_order_acquire) != reset_epoch()) {
+        void *p = nullptr;
+        LGPU_CUDA_TRY(cudaGetSymbolAddress(&p, g_lgpu_stream_error));
+        base = static_cast<unsigned *>(p);
+        g_err_base[dev].store(base, std::memory_order_release);
+        g_err_epoch[dev].store(reset_epoch(), std::memory_order_release);
+    }
+    *out = base + slot;
+    return LGPU_OK;
+}
+
+}  // namespace lgpu
+
 using namespace lgpu;
 
 extern "C" {
@@ -1355,7 +1448,9 @@ extern "C" {
 lgpu_status_t lgpu_selftest_bounded_wait(uint32_t spin_limit, lgpu_stream_t stream) {
     if (spin_limit == 0 || spin_limit > kWaitLimit) return fail(LGPU_ERR_INVALID_ARG, "spin limit out of range");
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
-    wait_selftest_kernel<<<1, 64, 0, s>>>(spin_limit);
+    unsigned *err = nullptr;
+    LGPU_TRY(stream_error_ptr(s, &err));
+    wait_selftest_kernel<<<1, 64, 0, s>>>(spin_limit, err);
     LGPU_CHECK_LAUNCH();
     LGPU_CUDA_TRY(cudaStreamSynchronize(s));
     return LGPU_OK;
@@ -1370,6 +1465,22 @@ lgpu_status_t lgpu_device_error(int *code, int reset) {
     if (reset && v) {
         unsigned z = 0;
         LGPU_CUDA_TRY(cudaMemcpyToSymbol(g_lgpu_device_error, &z, sizeof(z)));
+    }
+    return LGPU_OK;
+}
+
+lgpu_status_t lgpu_stream_error(lgpu_stream_t stream, int *code, int reset) {
+    if (!code) return fail(LGPU_ERR_INVALID_ARG, "code is null");
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    unsigned *err = nullptr;
+    LGPU_TRY(stream_error_ptr(s, &err));
+    unsigned v = 0;
+    LGPU_CUDA_TRY(cudaMemcpyAsync(&v, err, sizeof(v), cudaMemcpyDeviceToHost, s));
+    LGPU_CUDA_TRY(cudaStreamSynchronize(s));
+    *code = int(v);
+    if (reset && v) {
+        LGPU_CUDA_TRY(cudaMemsetAsync(err, 0, sizeof(unsigned), s));
+        LGPU_CUDA_TRY(cudaStreamSynchronize(s));
     }
     return LGPU_OK;
 }

@@ -62,6 +62,11 @@ int bulk_enabled();
 int tc_enabled();
 // device error flag of the batched kernel's bounded waits (lgpu_batch.cu)
 lgpu_status_t batch_error_fetch(unsigned *v, bool reset);
+// Per-stream error words of the bounded waits: kernels launched on stream s
+// receive *out (a device address on the current device) and set it on a
+// time-out; lgpu_stream_error reads it.
+constexpr int kErrSlots = 256;
+lgpu_status_t stream_error_ptr(cudaStream_t s, unsigned **out);
 
 // ---------------------------------------------------------------------------
 // Scratch context

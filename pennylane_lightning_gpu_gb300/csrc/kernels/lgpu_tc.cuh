@@ -13,34 +13,42 @@
 // lo = TF32 rounding of the remainder (Rlo.Xlo, about 2^-22 relative, is
 // dropped).  The error per output is a few FP32 ulps of the column's size.
 //
-// One persistent CTA per SM (128 threads, 224 KB of shared memory):
+// One persistent CTA per SM (256 threads, 224 KB of shared memory), tiles of
+// 64 columns (4096 amplitudes, 32 KB):
 //   R hi / lo      : 2 x 64 KB, built once from U (A operands, K-major)
-//   X hi / lo      : 2 x 32 KB, rebuilt per tile (B operands, K-major)
+//   X hi / lo      : 2 x 32 KB, rebuilt per tile (B operands, K-major, N = 64)
 //   staging        : 32 KB, the next tile lands here by one cp.async.bulk
+//   D              : two slots of 64 TMEM columns
+// While the tensor core multiplies tile j into D slot j & 1, the CTA reads out
+// and stores tile j - 1 from the other slot; the load of tile j + 1 is issued
+// with the MMAs of tile j.  The operand descriptors are built once; a K step
+// adds 256 bytes (16 in the address field) to them.
 // Operands use the no-swizzle canonical layout: core matrices of 8 rows x 16
 // bytes (128 contiguous bytes), 32 of them along K per group of 8 rows
 // (LBO = 128 B between K-neighbours, SBO = 4096 B between row groups).
-// D lives in 64 TMEM columns; warp w reads lanes 32w..32w+31 (output reals
-// 32w..32w+31) of all 64 columns and stores them: for each column the warp
-// writes 128 contiguous bytes.
+// Warp w reads TMEM lanes 32 (w % 4) .. + 31 (output reals) of 32 of the 64
+// columns and stores them: for each column the warp writes 128 contiguous
+// bytes.
 //
-// Every wait (the tile's bulk copy, the MMA commit) is bounded; a CTA that
-// gives up records it in g_lgpu_device_error, waits (bounded again) for the
-// copy it issued, frees its tensor memory and leaves.
+// Every wait (a tile's bulk copy, an MMA commit) is bounded; a CTA that gives
+// up records it in its stream's error word and the device-wide flag, waits
+// (bounded again) for the copies and MMAs it issued, frees its tensor memory
+// and leaves.
 #pragma once
 
 namespace lgpu {
 
-constexpr int kTcThreads = 128;
+constexpr int kTcThreads = 256;
 constexpr int kTcCols = 64;   // state columns per tile (N)
 constexpr int kTcK = 128;     // real inputs per column (K)
 constexpr int kTcM = 128;     // real outputs per column (M)
-constexpr uint32_t kTcTmemCols = 64;
+constexpr uint32_t kTcTmemCols = 128;  // two D slots of kTcCols columns
 constexpr uint32_t kTcGroupBytes = (kTcK / 4) * 128;  // one group of 8 rows: 32 core matrices
 constexpr uint32_t kTcRBytes = (kTcM / 8) * kTcGroupBytes;     // 64 KB
 constexpr uint32_t kTcXBytes = (kTcCols / 8) * kTcGroupBytes;  // 32 KB
 constexpr uint32_t kTcTileBytes = kTcCols * 64 * 8;            // 32 KB of complex64 amplitudes
-constexpr size_t kTcSmemBytes = 2 * size_t(kTcRBytes) + 2 * size_t(kTcXBytes) + kTcTileBytes;  // 224 KB
+constexpr uint32_t kTcTileAmps = kTcCols * 64;
+constexpr size_t kTcSmemBytes = 2 * size_t(kTcRBytes) + 2 * size_t(kTcXBytes) + size_t(kTcTileBytes);  // 224 KB
 
 // Byte offset of element (row, k) in a K-major no-swizzle operand.
 __host__ __device__ __forceinline__ uint32_t tc_off(uint32_t row, uint32_t k) {
@@ -107,13 +115,14 @@ __device__ __forceinline__ bool tc_wait(uint64_t *bar, uint32_t parity) {
 }
 
 struct TcDense6Params {
+    unsigned *err;      // the launch stream's error word
     const float2 *u;    // 64 x 64 row-major, rows / columns in state-bit order (bit 0 = LSB)
     uint64_t ntiles;    // 2^n / 4096
 };
 
 __global__ void __launch_bounds__(kTcThreads, 1) dense6_tc_kernel(float2 *__restrict__ sv, const TcDense6Params p) {
     extern __shared__ __align__(1024) unsigned char tc_smem[];
-    __shared__ __align__(8) uint64_t bar_load, bar_mma;
+    __shared__ __align__(8) uint64_t bar_load, bar_mma[2];
     __shared__ uint32_t tmem_slot;
     unsigned char *r_hi = tc_smem;
     unsigned char *r_lo = tc_smem + kTcRBytes;
@@ -122,10 +131,12 @@ __global__ void __launch_bounds__(kTcThreads, 1) dense6_tc_kernel(float2 *__rest
     float4 *stage = reinterpret_cast<float4 *>(x_lo + kTcXBytes);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const uint64_t G = gridDim.x;
+    const uint64_t J = p.ntiles > blockIdx.x ? (p.ntiles - blockIdx.x + G - 1) / G : 0;  // tiles of this CTA
 
     if (tid == 0) {
         mbar_init(&bar_load, 1);
-        mbar_init(&bar_mma, 1);
+        mbar_init(&bar_mma[0], 1);
+        mbar_init(&bar_mma[1], 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (warp == 0) {
@@ -148,94 +159,115 @@ __global__ void __launch_bounds__(kTcThreads, 1) dense6_tc_kernel(float2 *__rest
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = tmem_slot;
+    const uint64_t d_rh = tc_desc(smem_u32(r_hi)), d_rl = tc_desc(smem_u32(r_lo));
+    const uint64_t d_xh = tc_desc(smem_u32(x_hi)), d_xl = tc_desc(smem_u32(x_lo));
 
-    const uint64_t first = blockIdx.x;
-    // thread 0's record of work in flight: the parity of an issued load not
-    // yet waited for (-1: none), and whether a committed MMA batch is pending
-    int load_parity = -1;
-    bool mma_pending = false;
-    if (tid == 0 && first < p.ntiles) {
+    auto tile_ptr = [&](uint64_t j) { return sv + (blockIdx.x + j * G) * uint64_t(kTcTileAmps); };
+    auto issue_load = [&](uint64_t j) {
         mbar_expect_tx(&bar_load, kTcTileBytes);
-        bulk_load(stage, sv + first * uint64_t(kTcCols * 64), kTcTileBytes, &bar_load);
-        load_parity = 0;
-    }
+        bulk_load(stage, tile_ptr(j), kTcTileBytes, &bar_load);
+    };
+    // Read out D of tile j (slot j & 1) and store it: warp w takes lanes
+    // 32 (w % 4) .. + 31 and columns 32 (w / 4) .. + 31.
+    auto store_tile = [&](uint64_t j) {
+        const int q = int(j & 1);
+        float *dst = reinterpret_cast<float *>(tile_ptr(j));
+        const uint32_t row = uint32_t((warp & 3) * 32 + lane);
+        const uint32_t taddr = tmem + (uint32_t((warp & 3) * 32) << 16) + uint32_t(q * kTcCols);
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            const int c0 = (warp >> 2) * 32 + h * 16;
+            float v[16];
+            tc_ld16(taddr + uint32_t(c0), v);
+            tc_wait_ld();
+#pragma unroll
+            for (int i = 0; i < 16; i++) __stcs(dst + size_t(c0 + i) * kTcK + row, v[i]);
+        }
+    };
+    // issue / wait bookkeeping (thread 0 issues; everyone waits): the load of
+    // tile j completes phase j & 1 of bar_load; the MMA batch of tile j
+    // completes phase (j >> 1) & 1 of bar_mma[j & 1]
+    uint64_t loads_issued = 0, loads_done = 0, mmas_issued = 0, mmas_done = 0;
+    if (tid == 0 && J > 0) issue_load(0);
+    loads_issued = J > 0 ? 1 : 0;
+
     bool failed = false;
-    uint32_t it = 0;
-    for (uint64_t tile = first; tile < p.ntiles; tile += G, it++) {
-        const bool landed = tc_wait(&bar_load, it & 1u);
-        if (__syncthreads_or(!landed)) {
+    for (uint64_t j = 0; j < J; j++) {
+        if (j >= 1) {  // X is reused: the MMAs of tile j - 1 must be done
+            const uint64_t jp = j - 1;
+            if (__syncthreads_or(!tc_wait(&bar_mma[jp & 1], uint32_t((jp >> 1) & 1))))  {
+                failed = true;
+                break;
+            }
+            mmas_done = j;
+        }
+        if (__syncthreads_or(!tc_wait(&bar_load, uint32_t(j & 1)))) {
             failed = true;
             break;
         }
-        if (tid == 0) load_parity = -1;
-        // staging -> X hi / lo.  Lane L takes column 8g + (L & 7) and the
-        // 16-byte chunks (4 s + (L >> 3) + (L & 7)) mod 32: conflict-free reads
-        // (8 distinct chunk slots per phase) and writes (8 rows of one core matrix).
-#pragma unroll 4
-        for (int s = 0; s < 16; s++) {
-            const int grp = warp * 2 + (s >> 3);                              // 8 column groups
-            const int col = grp * 8 + (lane & 7);
-            const int chunk = (4 * (s & 7) + (lane >> 3) + (lane & 7)) & 31;  // 4 reals
-            const float4 x = stage[col * 32 + chunk];
-            float4 h, l;
-            h.x = tc_tf32(x.x);
-            l.x = tc_tf32(x.x - h.x);
-            h.y = tc_tf32(x.y);
-            l.y = tc_tf32(x.y - h.y);
-            h.z = tc_tf32(x.z);
-            l.z = tc_tf32(x.z - h.z);
-            h.w = tc_tf32(x.w);
-            l.w = tc_tf32(x.w - h.w);
-            const uint32_t o = tc_off(uint32_t(col), uint32_t(chunk * 4));
-            *reinterpret_cast<float4 *>(x_hi + o) = h;
-            *reinterpret_cast<float4 *>(x_lo + o) = l;
+        loads_done = j + 1;
+        // staging -> X hi / lo.  Lane L takes column 8 (w % 8) + (L & 7) and
+        // the 16-byte chunks (4 t + (L >> 3) + (L & 7)) mod 32, t = 0..7:
+        // conflict-free reads (8 distinct chunk slots per phase) and writes
+        // (8 rows of one core matrix).
+        {
+            const int col = warp * 8 + (lane & 7);
+#pragma unroll
+            for (int t = 0; t < 8; t++) {
+                const int chunk = (4 * t + (lane >> 3) + (lane & 7)) & 31;  // 4 reals
+                const float4 x = stage[col * 32 + chunk];
+                float4 h, l;
+                h.x = tc_tf32(x.x);
+                l.x = tc_tf32(x.x - h.x);
+                h.y = tc_tf32(x.y);
+                l.y = tc_tf32(x.y - h.y);
+                h.z = tc_tf32(x.z);
+                l.z = tc_tf32(x.z - h.z);
+                h.w = tc_tf32(x.w);
+                l.w = tc_tf32(x.w - h.w);
+                const uint32_t o = tc_off(uint32_t(col), uint32_t(chunk * 4));
+                *reinterpret_cast<float4 *>(x_hi + o) = h;
+                *reinterpret_cast<float4 *>(x_lo + o) = l;
+            }
         }
         fence_async_shared();  // the operands are read by the tensor core (async proxy)
         __syncthreads();
         if (tid == 0) {
-            const uint64_t next = tile + G;
-            if (next < p.ntiles) {  // the staging buffer is free: every thread has read it
-                mbar_expect_tx(&bar_load, kTcTileBytes);
-                bulk_load(stage, sv + next * uint64_t(kTcCols * 64), kTcTileBytes, &bar_load);
-                load_parity = int((it + 1) & 1u);
-            }
+            if (j + 1 < J) issue_load(j + 1);  // the staging buffer is free: every thread has read it
             tc_fence_after();
-            const uint32_t rh = smem_u32(r_hi), rl = smem_u32(r_lo), xh = smem_u32(x_hi), xl = smem_u32(x_lo);
+            const uint32_t d = tmem + uint32_t(int(j & 1) * kTcCols);
 #pragma unroll 1
             for (uint32_t ks = 0; ks < kTcK / 8; ks++) {  // 8 reals = 32 bytes = two core matrices along K
-                const uint32_t o = ks * 256u;
-                tc_mma(tmem, tc_desc(rh + o), tc_desc(xh + o), ks > 0);
-                tc_mma(tmem, tc_desc(rh + o), tc_desc(xl + o), 1u);
-                tc_mma(tmem, tc_desc(rl + o), tc_desc(xh + o), 1u);
+                const uint64_t o = uint64_t(ks) * 16u;    // 256 bytes in the address field (16-byte units)
+                tc_mma(d, d_rh + o, d_xh + o, ks > 0);
+                tc_mma(d, d_rh + o, d_xl + o, 1u);
+                tc_mma(d, d_rl + o, d_xh + o, 1u);
             }
-            tc_commit(&bar_mma);
-            mma_pending = true;
+            tc_commit(&bar_mma[j & 1]);
         }
-        const bool done = tc_wait(&bar_mma, it & 1u);
-        if (__syncthreads_or(!done)) {
-            failed = true;
-            break;
-        }
-        if (tid == 0) mma_pending = false;
-        tc_fence_after();
-        // D rows 32 warp .. 32 warp + 31 (output reals), all 64 columns
-        float *dst = reinterpret_cast<float *>(sv + tile * uint64_t(kTcCols * 64));
-        const uint32_t row = uint32_t(warp * 32 + lane);
-#pragma unroll
-        for (int c0 = 0; c0 < kTcCols; c0 += 16) {
-            float v[16];
-            tc_ld16(tmem + (uint32_t(warp * 32) << 16) + uint32_t(c0), v);
-            tc_wait_ld();
-#pragma unroll
-            for (int j = 0; j < 16; j++) __stcs(dst + size_t(c0 + j) * kTcK + row, v[j]);
+        loads_issued = j + 1 < J ? j + 2 : J;
+        mmas_issued = j + 1;
+        if (j >= 1) {  // tile j - 1 (its MMAs are done) while the tensor core works on tile j
+            tc_fence_after();
+            store_tile(j - 1);
         }
         tc_fence_before();
-        __syncthreads();  // D and the X operands are reused by the next tile
+        __syncthreads();  // D slot (j - 1) & 1 is free for tile j + 1
+    }
+    if (!failed && J > 0) {
+        const uint64_t jl = J - 1;
+        if (__syncthreads_or(!tc_wait(&bar_mma[jl & 1], uint32_t((jl >> 1) & 1)))) {
+            failed = true;
+        } else {
+            mmas_done = J;
+            tc_fence_after();
+            store_tile(jl);
+        }
     }
     if (failed && tid == 0) {
-        atomicOr(&g_lgpu_device_error, 1u);
-        if (load_parity >= 0) tc_wait(&bar_load, uint32_t(load_parity));  // a copy into the staging buffer
-        if (mma_pending) tc_wait(&bar_mma, it & 1u);                        // an MMA batch still running
+        report_timeout(p.err);
+        for (uint64_t j = loads_done; j < loads_issued; j++) tc_wait(&bar_load, uint32_t(j & 1));
+        for (uint64_t j = mmas_done; j < mmas_issued; j++) tc_wait(&bar_mma[j & 1], uint32_t((j >> 1) & 1));
     }
     tc_fence_before();
     __syncthreads();

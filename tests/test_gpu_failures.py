@@ -19,6 +19,7 @@ def _lib():
     lib = ctypes.CDLL(pkg.library_path())
     lib.lgpu_selftest_bounded_wait.argtypes = [ctypes.c_uint32, ctypes.c_void_p]
     lib.lgpu_device_error.argtypes = [ctypes.POINTER(ctypes.c_int), ctypes.c_int]
+    lib.lgpu_stream_error.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int), ctypes.c_int]
     lib.lgpu_last_error_string.restype = ctypes.c_char_p
     return lib
 
@@ -37,7 +38,31 @@ def test_bounded_wait_gives_up_and_is_reported(native):
     sv.Hadamard([0], False, [])
     st = np.asarray(sv.GetState())
     assert abs(st[0] - 2 ** -0.5) < 1e-12 and abs(st[4] - 2 ** -0.5) < 1e-12
+    assert lib.lgpu_stream_error(None, ctypes.byref(code), 0) == 0 and code.value == 0
+    # the device-wide flag keeps the record until it is reset
+    assert lib.lgpu_device_error(ctypes.byref(code), 1) == 0 and code.value == 1
     assert lib.lgpu_device_error(ctypes.byref(code), 0) == 0 and code.value == 0
+
+
+def test_time_out_is_reported_on_its_own_stream_only(native):
+    """A bounded wait that gives up on stream A is raised at A's
+    synchronisation and not at a state's on stream B."""
+    torch = pytest.importorskip("torch")
+    lib = _lib()
+    code = ctypes.c_int(0)
+    a, b = torch.cuda.Stream(), torch.cuda.Stream()
+    for st in (a, b):
+        assert lib.lgpu_stream_error(st.cuda_stream, ctypes.byref(code), 1) == 0
+    assert lib.lgpu_selftest_bounded_wait(4096, a.cuda_stream) == 0, lib.lgpu_last_error_string()
+    assert lib.lgpu_stream_error(b.cuda_stream, ctypes.byref(code), 0) == 0 and code.value == 0
+    sv_b = native.LightningGPU_C128(3, native.DevTag(0, b.cuda_stream))
+    sv_b.Hadamard([0], False, [])
+    sv_b.synchronize()  # nothing timed out on B
+    sv_a = native.LightningGPU_C128(3, native.DevTag(0, a.cuda_stream))
+    with pytest.raises(native.PLException, match="timed out"):
+        sv_a.synchronize()
+    sv_a.synchronize()  # A's word was cleared
+    assert lib.lgpu_device_error(ctypes.byref(code), 1) == 0 and code.value == 1
 
 
 def test_selftest_rejects_bad_limit():

@@ -57,3 +57,26 @@ def test_tensor_mode_rejects_bad_values(native):
     with pytest.raises(native.PLException):
         native.set_tensor_mode(2)
     assert native.get_tensor_mode() == 1
+
+
+def test_dense6_long_pipeline_matches_fp32_kernel(native):
+    """24 qubits: each CTA runs dozens of units through the two-slot pipeline;
+    the result equals the FP32 shared-memory kernel's (itself checked against
+    the oracle by test_dense_matrix) within the complex64 tolerance."""
+    rng = np.random.default_rng(24)
+    n = 24
+    psi = random_state(n, rng).astype(np.complex64)
+    u = random_unitary(64, rng)
+    wires = list(range(n - 1, n - 7, -1))
+    sv = make_sv(native, "c64", psi)
+    sv.apply("QubitUnitary", wires, False, [], u.ravel())
+    got = sv.GetState()
+    native.set_tensor_mode(0)
+    try:
+        sv2 = make_sv(native, "c64", psi)
+        sv2.apply("QubitUnitary", wires, False, [], u.ravel())
+        ref = sv2.GetState()
+    finally:
+        native.set_tensor_mode(1)
+    assert np.max(np.abs(got - ref)) < 1e-5
+    assert abs(np.linalg.norm(got.astype(np.complex128)) - np.linalg.norm(psi.astype(np.complex128))) < 1e-5
