@@ -9,6 +9,8 @@
 //  * sampling: FP64 chunk sums -> single-CTA exclusive scan -> one warp per
 //    draw searches its chunk with a warp prefix sum
 //  * sum_t c_t P_t |psi> (Hamiltonian apply) and CSR sparse products
+#include <type_traits>
+
 #include "lgpu_bodies.cuh"
 #include "lgpu_df64.cuh"
 #include "lgpu_internal.cuh"
@@ -804,12 +806,39 @@ template <> struct TileAcc<double> {
     DF v{0.0f, 0.0f};
     __device__ __forceinline__ void add(DF x) { v = df_sum<2>({v, x}); }
     __device__ __forceinline__ void warp_reduce() {
+        v = df_sum<1>({v});  // the loop's pair is unnormalised: rebuild it first
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1)
             v = df_sum<2>({v, DF{__shfl_xor_sync(0xffffffffu, v.hi, o), __shfl_xor_sync(0xffffffffu, v.lo, o)}});
     }
     __device__ __forceinline__ double value() const { return df_to_double(v); }
 };
+
+// acc += sign * (a b + c d) for float-float a, b, c, d, sign = +-1 given as
+// the bit pattern 0 or 0x80000000: the two leading products are split exactly
+// (FMA), their errors and the cross terms gather in one float, the leading
+// parts enter the running sum through TwoSum; the pair stays unnormalised
+// (its low part collects the error terms) and is rebuilt once at the end.
+__device__ __forceinline__ void df_acc_dot2(DF &acc, uint32_t sbit, DF a, DF b, DF c, DF d) {
+    float p1 = df_mul_rn(a.hi, b.hi), p2 = df_mul_rn(c.hi, d.hi);
+    float e = df_fma(a.hi, b.hi, -p1);
+    e = df_add_rn(e, df_fma(c.hi, d.hi, -p2));
+    e = df_fma(a.hi, b.lo, e);
+    e = df_fma(a.lo, b.hi, e);
+    e = df_fma(c.hi, d.lo, e);
+    e = df_fma(c.lo, d.hi, e);
+    p1 = __uint_as_float(__float_as_uint(p1) ^ sbit);
+    p2 = __uint_as_float(__float_as_uint(p2) ^ sbit);
+    e = __uint_as_float(__float_as_uint(e) ^ sbit);
+    float s = df_add_rn(acc.hi, p1);
+    float bb = df_sub_rn(s, acc.hi);
+    const float err1 = df_add_rn(df_sub_rn(acc.hi, df_sub_rn(s, bb)), df_sub_rn(p1, bb));
+    const float s2 = df_add_rn(s, p2);
+    bb = df_sub_rn(s2, s);
+    const float err2 = df_add_rn(df_sub_rn(s, df_sub_rn(s2, bb)), df_sub_rn(p2, bb));
+    acc.lo = df_add_rn(acc.lo, df_add_rn(df_add_rn(err1, err2), e));
+    acc.hi = s2;
+}
 
 __device__ __forceinline__ void pt_cp_async16(void *smem_dst, const void *gsrc) {
     asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(static_cast<uint32_t>(__cvta_generic_to_shared(smem_dst))),
@@ -868,38 +897,46 @@ __global__ void __launch_bounds__(kPauliTileThreads, 3) pauli_tile_kernel(const 
             const bool im = (p.use_im >> t) & 1u;
             if (f == 0) {
                 for (int e = threadIdx.x; e < E; e += kPauliTileThreads) {
-                    const bool neg = ((__popc(uint32_t(e) & sg) & 1) ^ neg0) != 0;
+                    const uint32_t par = (__popc(uint32_t(e) & sg) & 1) ^ neg0;
                     if constexpr (sizeof(T) == 4) {
                         const C a = cur[swz<T>(e)];
                         const float q = fmaf(a.x, a.x, a.y * a.y);
-                        acc[t].add(neg ? -q : q);
+                        acc[t].add(par ? -q : q);
                     } else {
                         const float4 a = reinterpret_cast<const float4 *>(cur)[swz<T>(e)];
                         const DF r{a.x, a.y}, i{a.z, a.w};
-                        DF q = df_sum<2>({df_mul(r, r), df_mul(i, i)});
-                        acc[t].add(neg ? df_neg(q) : q);
+                        df_acc_dot2(acc[t].v, par << 31, r, r, i, i);
                     }
                 }
             } else {
                 const uint32_t low = f & (0u - f);  // lowest flip bit: pairs from its clear half
-                PairWalk w(low, threadIdx.x, kPauliTileThreads);
-                for (int c = threadIdx.x; c < (E >> 1); c += kPauliTileThreads) {
-                    const int e0 = int(w.x), e1 = int(w.x ^ f);
-                    w.step();
-                    const bool neg = ((__popc(uint32_t(e0) & sg) & 1) ^ neg0) != 0;
-                    if constexpr (sizeof(T) == 4) {
-                        const C a = cur[swz<T>(e0)], b = cur[swz<T>(e1)];
-                        const float q = im ? fmaf(a.x, b.y, -a.y * b.x) : fmaf(a.x, b.x, a.y * b.y);
-                        acc[t].add(neg ? -q : q);
-                    } else {
-                        const float4 a4 = reinterpret_cast<const float4 *>(cur)[swz<T>(e0)];
-                        const float4 b4 = reinterpret_cast<const float4 *>(cur)[swz<T>(e1)];
-                        const DF ar{a4.x, a4.y}, ai{a4.z, a4.w}, br{b4.x, b4.y}, bi{b4.z, b4.w};
-                        const DF q = im ? df_sum<2>({df_mul(ar, bi), df_neg(df_mul(ai, br))})
-                                        : df_sum<2>({df_mul(ar, br), df_mul(ai, bi)});
-                        acc[t].add(neg ? df_neg(q) : q);
+                // the real or the imaginary part of conj(a) b, chosen once per word
+                auto pairs = [&](auto imc) {
+                    constexpr bool IM = decltype(imc)::value;
+                    PairWalk w(low, threadIdx.x, kPauliTileThreads);
+                    for (int c = threadIdx.x; c < (E >> 1); c += kPauliTileThreads) {
+                        const int e0 = int(w.x), e1 = int(w.x ^ f);
+                        w.step();
+                        const uint32_t par = (__popc(uint32_t(e0) & sg) & 1) ^ neg0;
+                        if constexpr (sizeof(T) == 4) {
+                            const C a = cur[swz<T>(e0)], b = cur[swz<T>(e1)];
+                            const float q = IM ? fmaf(a.x, b.y, -a.y * b.x) : fmaf(a.x, b.x, a.y * b.y);
+                            acc[t].add(par ? -q : q);
+                        } else {
+                            const float4 a4 = reinterpret_cast<const float4 *>(cur)[swz<T>(e0)];
+                            const float4 b4 = reinterpret_cast<const float4 *>(cur)[swz<T>(e1)];
+                            const DF ar{a4.x, a4.y}, ai{a4.z, a4.w}, br{b4.x, b4.y}, bi{b4.z, b4.w};
+                            if constexpr (IM)  // ar bi - ai br
+                                df_acc_dot2(acc[t].v, par << 31, ar, bi, df_neg(ai), br);
+                            else  // ar br + ai bi
+                                df_acc_dot2(acc[t].v, par << 31, ar, br, ai, bi);
+                        }
                     }
-                }
+                };
+                if (im)
+                    pairs(std::true_type{});
+                else
+                    pairs(std::false_type{});
             }
         }
         __syncthreads();  // `cur` is the target of a load issued next iteration

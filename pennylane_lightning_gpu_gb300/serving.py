@@ -35,7 +35,7 @@ from ._native import native
 
 class Request:
     __slots__ = ("rid", "n", "ops", "kind", "obs", "wires", "shots", "seed", "arrival", "start", "finish",
-                 "result", "error")
+                 "result", "error", "device_s")
 
     def __init__(self, rid, n, ops, kind, obs=None, wires=None, shots=0, seed=0, arrival=0.0):
         self.rid, self.n, self.ops, self.kind = rid, n, ops, kind
@@ -44,6 +44,7 @@ class Request:
         self.start = self.finish = None
         self.result = None
         self.error = None
+        self.device_s = None  # GPU time of the request when served alone (sequential_baseline)
 
     def footprint(self, amp_bytes):
         return (1 << self.n) * amp_bytes
@@ -326,6 +327,8 @@ def replay(server, trace, time_scale=1.0):
 def sequential_baseline(trace, dtype=np.complex64, time_scale=1.0):
     """One request at a time in arrival order on the default stream; a
     request starts at max(its arrival, the previous completion)."""
+    import torch
+
     m = native()
     t0 = time.perf_counter()
     for r in trace:
@@ -334,9 +337,14 @@ def sequential_baseline(trace, dtype=np.complex64, time_scale=1.0):
         if due > now:
             time.sleep(due - now)
         arrival = t0 + r.arrival * time_scale
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         r.start = time.perf_counter()
+        ev0.record()
         r.result = run_request(m, r, dtype)
+        ev1.record()
         r.finish = time.perf_counter()
+        ev1.synchronize()
+        r.device_s = ev0.elapsed_time(ev1) / 1e3
         r.arrival = arrival
     return trace, time.perf_counter() - t0
 
