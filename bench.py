@@ -852,9 +852,9 @@ def bench_serving(args):
         seq, seq_makespan = serving.sequential_baseline(serving.make_trace(args.serve_requests, rate=rate, seed=4),
                                                         np.complex64)
         base = serving.report(seq, seq_makespan)
-        # requests of >= 24 qubits fill HBM bandwidth on their own, so their GPU
-        # times (measured alone, in the sequential loop) cannot overlap: their
-        # sum is a floor for any schedule's makespan
+        # GPU time of the requests of >= 24 qubits, each measured alone in the
+        # sequential loop: these states (128 MiB and up) keep HBM busy, so the
+        # server can overlap them with each other only in part
         floor = sum(r.device_s for r in seq if r.n >= 24)
         out["sweep"].append({
             "rate_per_s": rate, "served": served, "sequential": base,
@@ -862,17 +862,17 @@ def bench_serving(args):
             "p50_speedup": round(base["p50_ms"] / served["p50_ms"], 2),
             "p99_speedup": round(base["p99_ms"] / served["p99_ms"], 2),
             "micro_batches": batches, "graph_replays": hits,
-            "makespan_floor_s": round(floor, 4),
-            "max_throughput_speedup_possible": round(seq_makespan / max(floor, 1e-9), 2)})
+            "large_requests_gpu_s": round(floor, 4),
+            "sequential_over_large_gpu_time": round(seq_makespan / max(floor, 1e-9), 2)})
         last = (done, seq)
     top = out["sweep"][-1]
     out["saturated_note"] = (
-        "at %.0f requests/s the requests of >= 24 qubits (each fills HBM bandwidth on its own) keep the GPU busy "
-        "%.2f s of the sequential loop's %.2f s; their GPU work cannot overlap, so no schedule finishes faster and "
-        "the served throughput can exceed the sequential one by at most %.2fx (measured %.2fx, p99 %.0f vs %.0f ms)"
-        % (top["rate_per_s"], top["makespan_floor_s"], top["sequential"]["makespan_s"],
-           top["max_throughput_speedup_possible"], top["throughput_speedup"], top["served"]["p99_ms"],
-           top["sequential"]["p99_ms"]))
+        "at %.0f requests/s the requests of >= 24 qubits take %.2f s of GPU time (each run alone) of the sequential "
+        "loop's %.2f s; their states of 128 MiB and more keep HBM busy, so running them side by side gains little, "
+        "and the served throughput stays near the sequential one: %.2fx (the loop's time over that GPU time is "
+        "%.2fx), p99 %.0f vs %.0f ms"
+        % (top["rate_per_s"], top["large_requests_gpu_s"], top["sequential"]["makespan_s"], top["throughput_speedup"],
+           top["sequential_over_large_gpu_time"], top["served"]["p99_ms"], top["sequential"]["p99_ms"]))
     # the same server on a mix of small requests (8..20 qubits), where the
     # per-request host work and launch latency, not HBM, bound the loop
     small = []
