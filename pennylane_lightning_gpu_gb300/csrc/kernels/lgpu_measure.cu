@@ -914,23 +914,37 @@ __global__ void __launch_bounds__(kPauliTileThreads, 3) pauli_tile_kernel(const 
                 auto pairs = [&](auto imc) {
                     constexpr bool IM = decltype(imc)::value;
                     PairWalk w(low, threadIdx.x, kPauliTileThreads);
-                    for (int c = threadIdx.x; c < (E >> 1); c += kPauliTileThreads) {
-                        const int e0 = int(w.x), e1 = int(w.x ^ f);
-                        w.step();
-                        const uint32_t par = (__popc(uint32_t(e0) & sg) & 1) ^ neg0;
-                        if constexpr (sizeof(T) == 4) {
+                    if constexpr (sizeof(T) == 4) {
+                        for (int c = threadIdx.x; c < (E >> 1); c += kPauliTileThreads) {
+                            const int e0 = int(w.x), e1 = int(w.x ^ f);
+                            w.step();
+                            const uint32_t par = (__popc(uint32_t(e0) & sg) & 1) ^ neg0;
                             const C a = cur[swz<T>(e0)], b = cur[swz<T>(e1)];
                             const float q = IM ? fmaf(a.x, b.y, -a.y * b.x) : fmaf(a.x, b.x, a.y * b.y);
                             acc[t].add(par ? -q : q);
-                        } else {
-                            const float4 a4 = reinterpret_cast<const float4 *>(cur)[swz<T>(e0)];
-                            const float4 b4 = reinterpret_cast<const float4 *>(cur)[swz<T>(e1)];
-                            const DF ar{a4.x, a4.y}, ai{a4.z, a4.w}, br{b4.x, b4.y}, bi{b4.z, b4.w};
-                            if constexpr (IM)  // ar bi - ai br
-                                df_acc_dot2(acc[t].v, par << 31, ar, bi, df_neg(ai), br);
-                            else  // ar br + ai bi
-                                df_acc_dot2(acc[t].v, par << 31, ar, br, ai, bi);
                         }
+                    } else {
+                        // two independent running sums (pairs c and c + threads), so
+                        // the TwoSum chains of neighbouring pairs overlap
+                        DF s2{0.0f, 0.0f};
+                        for (int c = threadIdx.x; c < (E >> 1); c += 2 * kPauliTileThreads) {
+#pragma unroll
+                            for (int u = 0; u < 2; u++) {
+                                if (u == 1 && c + kPauliTileThreads >= (E >> 1)) break;
+                                const int e0 = int(w.x), e1 = int(w.x ^ f);
+                                w.step();
+                                const uint32_t par = (__popc(uint32_t(e0) & sg) & 1) ^ neg0;
+                                const float4 a4 = reinterpret_cast<const float4 *>(cur)[swz<T>(e0)];
+                                const float4 b4 = reinterpret_cast<const float4 *>(cur)[swz<T>(e1)];
+                                const DF ar{a4.x, a4.y}, ai{a4.z, a4.w}, br{b4.x, b4.y}, bi{b4.z, b4.w};
+                                DF &dst = u == 0 ? acc[t].v : s2;
+                                if constexpr (IM)  // ar bi - ai br
+                                    df_acc_dot2(dst, par << 31, ar, bi, df_neg(ai), br);
+                                else  // ar br + ai bi
+                                    df_acc_dot2(dst, par << 31, ar, br, ai, bi);
+                            }
+                        }
+                        acc[t].v = df_sum<2>({acc[t].v, s2});
                     }
                 };
                 if (im)

@@ -73,10 +73,12 @@ __device__ __forceinline__ uint64_t tc_desc(uint32_t saddr) {
 constexpr uint32_t kTcIdesc = (1u << 4) | (2u << 7) | (2u << 10) | (uint32_t(kTcCols >> 3) << 17) |
                               (uint32_t(kTcM >> 4) << 24);
 
+// TF32 rounding (nearest, ties away from zero) of a finite float with two
+// integer operations: add half a TF32 ulp to the magnitude bits, clear the 13
+// low mantissa bits (a carry into the exponent is the correct rounding up).
+// The same bits as cvt.rna.tf32.f32, which runs on a slower conversion pipe.
 __device__ __forceinline__ float tc_tf32(float x) {
-    uint32_t r;
-    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
-    return __uint_as_float(r);
+    return __uint_as_float((__float_as_uint(x) + 0x1000u) & 0xFFFFE000u);
 }
 
 // D (TMEM) (+)= A (TMEM, row m in lane m, K along columns) . B (shared memory)
