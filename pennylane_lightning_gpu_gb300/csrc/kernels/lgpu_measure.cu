@@ -1,14 +1,17 @@
 // liblgpu_gb300: measurements.
 //
 //  * expval of a dense matrix on t bits (FP64 accumulation, deterministic)
-//  * Pauli-word expectations grouped by flip mask: one streaming pass per
-//    distinct flip mask evaluates up to 16 words through an 8-point
-//    Walsh-Hadamard transform of each thread's elements
+//  * Pauli-word expectations: on large states, tile passes that serve up to
+//    8 words with different flip masks per read of the state; otherwise one
+//    streaming pass per distinct flip mask evaluates up to 16 words through
+//    an 8-point Walsh-Hadamard transform of each thread's elements
 //  * marginal probabilities: shared-memory histogram per CTA with register
 //    run-length accumulation, then a fixed-order cross-CTA sum
 //  * sampling: FP64 chunk sums -> single-CTA exclusive scan -> one warp per
 //    draw searches its chunk with a warp prefix sum
 //  * sum_t c_t P_t |psi> (Hamiltonian apply) and CSR sparse products
+#include <cstring>
+#include <memory>
 #include <type_traits>
 
 #include "lgpu_bodies.cuh"
@@ -764,38 +767,68 @@ static lgpu_status_t wht_dispatch(const PauliWhtParams<T, I> &b, unsigned g, dou
 }
 
 // ---------------------------------------------------------------------------
-// Tiled Pauli-word passes: words with different flip masks in one pass.
-// A tile is 2^k amplitudes (the low run 0..m-1 of state bits plus up to 6
-// high bits, as the fused gate blocks); every word of the pass flips only
-// tile bits, so each pair (x, x ^ flip) lies in one tile.  A CTA streams
-// tiles through two shared-memory buffers (cp.async); per word each thread
-// sums (-1)^popc(x & sign) * (|a_x|^2, or Re / Im of conj(a_x) a_{x^flip} over
-// the x with the lowest flip bit clear) in registers over all of its CTA's
-// tiles: complex64 in float (each thread's share is small), complex128 in
-// float-float on the tile converted once after the load (no FP64 instruction
-// per pair).  At the end warp sums go to per-warp double slots; a CTA writes
-// its totals and a second kernel sums the CTAs in a fixed order.  The raw
-// sums equal those of the Walsh-Hadamard pass.
+// Tiled Pauli-word passes: words with different flip masks in one read.
+// A tile is 2^K amplitudes (K = 12 for complex64, 11 for complex128: 32 KB):
+// the low run 0..m-1 of state bits (runs of at least 128 bytes) plus up to
+// kTileHiMax higher bits.  Every word of a pass flips only tile bits, so each
+// pair (x, x ^ flip) lies in one tile.  A CTA streams tiles through two
+// shared-memory buffers (cp.async); complex128 tiles are converted after the
+// load to float-float, (re.hi, im.hi, re.lo, im.lo) per amplitude.
+//
+// The work of a thread has a fixed shape.  Tile element e = tid + 256 j (tid
+// the thread, j = 0 .. E/256 - 1): the sign (-1)^popc(e & sign) of a diagonal
+// word splits into a per-thread bit and a per-word constant bit for j, and
+// |a_e|^2 is formed once per element for all diagonal words of the pass.  For
+// a word with flips, pair c = tid + 256 j has its first element x = c with a
+// zero inserted at the lowest flip position b0, so x = X | J_j with X from the
+// thread and J_j from j on disjoint bits; its partner x ^ flip =
+// (X ^ (flip off the J bits)) | (J_j ^ (flip on the J bits)), again disjoint.
+// Both addresses are a per-thread base plus a per-word constant, and the sign
+// a per-thread bit XOR a per-word constant bit: no index walk and no
+// population count per pair.
+//
+// Sums: complex64 in float per thread (each thread's share is small);
+// complex128 in float-float, products split exactly by FMA and two running
+// sums per word (even and odd j), so the TwoSum chains of neighbouring pairs
+// overlap.  At the end warp sums go to per-warp double slots; a CTA writes its
+// totals and a second kernel sums the CTAs in a fixed order.  The raw sums
+// equal those of the Walsh-Hadamard pass.
 // ---------------------------------------------------------------------------
 constexpr int kPauliTileThreads = 256;
 
+template <class T> struct PtGeom {
+    static constexpr int K = sizeof(T) == 4 ? 12 : 11;   // tile bits (32 KB tiles)
+    static constexpr int E = 1 << K;                     // elements per tile
+    static constexpr int NA = E / kPauliTileThreads;     // elements per thread
+    static constexpr int NP = NA / 2;                    // pairs per thread and word
+    static constexpr int LEB = sizeof(T) == 4 ? 3 : 4;   // log2 of the bytes per tile element
+    static constexpr int MMIN = sizeof(T) == 4 ? 4 : 3;  // runs of at least 128 bytes
+};
+constexpr int kPtMaxNA = 16;
+static_assert(PtGeom<float>::NA <= kPtMaxNA && PtGeom<double>::NA <= kPtMaxNA, "per-thread element count");
+static_assert((kPauliTileThreads & (kPauliTileThreads - 1)) == 0 && kPauliTileThreads == 256,
+              "the j part of a tile index starts at bit 8");
+
 template <class I> struct PauliTileParams {
     const void *sv;
-    Holes holes;
+    Holes holes;  // tile bit positions
     I ntiles;
-    int k, m, nw;
-    I hi_off[64];
-    uint32_t tflip[kTileWords];  // flip mask in tile positions (0: diagonal word)
-    uint32_t tsign[kTileWords];  // sign mask in tile positions
-    uint64_t osign[kTileWords];  // sign mask outside the tile (state bits)
-    uint32_t use_im;             // bit t: word t sums Im(conj(a_x) a_{x^flip})
-    double *partials;            // [gridDim.x][nw]
+    int m, nw, nd;                          // low run; words; the first nd are diagonal
+    uint32_t use_im;                        // bit t: word t sums Im(conj(a_x) a_{x^flip})
+    I hi_off[1 << kTileHiMax];              // state offset of each run of 2^m amplitudes
+    uint32_t tsign[kTileWords];             // sign mask in tile positions
+    uint64_t osign[kTileWords];             // sign mask outside the tile (state bits)
+    uint32_t b0[kTileWords];                // words with flips: lowest flip position
+    uint32_t fxb[kTileWords];               // flip bits off the J bits, times the element bytes
+    uint32_t ja[kTileWords][kPtMaxNA / 2];  // J_j times the element bytes
+    uint32_t jb[kTileWords][kPtMaxNA / 2];  // (J_j ^ flip bits on the J bits) times the element bytes
+    uint32_t cs[kTileWords][kPtMaxNA];      // bit 31: parity of (the j part & the sign mask)
+    double *partials;                       // [gridDim.x][nw]
 };
 
 template <class T> struct TileAcc;
 template <> struct TileAcc<float> {
     float v = 0.0f;
-    __device__ __forceinline__ void add(float x) { v += x; }
     __device__ __forceinline__ void warp_reduce() {
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -803,41 +836,51 @@ template <> struct TileAcc<float> {
     __device__ __forceinline__ double value() const { return double(v); }
 };
 template <> struct TileAcc<double> {
-    DF v{0.0f, 0.0f};
-    __device__ __forceinline__ void add(DF x) { v = df_sum<2>({v, x}); }
+    DF v[2] = {DF{0.0f, 0.0f}, DF{0.0f, 0.0f}};  // two running sums, unnormalised
     __device__ __forceinline__ void warp_reduce() {
-        v = df_sum<1>({v});  // the loop's pair is unnormalised: rebuild it first
+        DF s = df_sum<2>({v[0], v[1]});  // renormalised
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1)
-            v = df_sum<2>({v, DF{__shfl_xor_sync(0xffffffffu, v.hi, o), __shfl_xor_sync(0xffffffffu, v.lo, o)}});
+            s = df_sum<2>({s, DF{__shfl_xor_sync(0xffffffffu, s.hi, o), __shfl_xor_sync(0xffffffffu, s.lo, o)}});
+        v[0] = s;
     }
-    __device__ __forceinline__ double value() const { return df_to_double(v); }
+    __device__ __forceinline__ double value() const { return df_to_double(v[0]); }
 };
 
-// acc += sign * (a b + c d) for float-float a, b, c, d, sign = +-1 given as
-// the bit pattern 0 or 0x80000000: the two leading products are split exactly
-// (FMA), their errors and the cross terms gather in one float, the leading
-// parts enter the running sum through TwoSum; the pair stays unnormalised
-// (its low part collects the error terms) and is rebuilt once at the end.
-__device__ __forceinline__ void df_acc_dot2(DF &acc, uint32_t sbit, DF a, DF b, DF c, DF d) {
-    float p1 = df_mul_rn(a.hi, b.hi), p2 = df_mul_rn(c.hi, d.hi);
-    float e = df_fma(a.hi, b.hi, -p1);
-    e = df_add_rn(e, df_fma(c.hi, d.hi, -p2));
-    e = df_fma(a.hi, b.lo, e);
-    e = df_fma(a.lo, b.hi, e);
-    e = df_fma(c.hi, d.lo, e);
-    e = df_fma(c.lo, d.hi, e);
-    p1 = __uint_as_float(__float_as_uint(p1) ^ sbit);
-    p2 = __uint_as_float(__float_as_uint(p2) ^ sbit);
-    e = __uint_as_float(__float_as_uint(e) ^ sbit);
-    float s = df_add_rn(acc.hi, p1);
-    float bb = df_sub_rn(s, acc.hi);
-    const float err1 = df_add_rn(df_sub_rn(acc.hi, df_sub_rn(s, bb)), df_sub_rn(p1, bb));
-    const float s2 = df_add_rn(s, p2);
-    bb = df_sub_rn(s2, s);
-    const float err2 = df_add_rn(df_sub_rn(s, df_sub_rn(s2, bb)), df_sub_rn(p2, bb));
-    acc.lo = df_add_rn(acc.lo, df_add_rn(df_add_rn(err1, err2), e));
-    acc.hi = s2;
+__device__ __forceinline__ float pt_flip_sign(float x, uint32_t sbit) { return __uint_as_float(__float_as_uint(x) ^ sbit); }
+
+// acc += sign * (a b + c d) for float-float a, b, c, d, sign = +-1 given as the
+// bit pattern 0 or 0x80000000.  The leading products are split exactly by
+// FMA, their sum exactly by TwoSum, and that sum's leading part enters the
+// running sum through a second TwoSum; the error terms and the cross products
+// gather in acc.lo, which stays unnormalised until the end.
+__device__ __forceinline__ void df_acc_dot2(DF &acc, uint32_t sbit, float ah, float al, float bh, float bl, float ch,
+                                            float cl, float dh, float dl) {
+    const float p1 = df_mul_rn(ah, bh), p2 = df_mul_rn(ch, dh);
+    float e = df_add_rn(df_fma(ah, bh, -p1), df_fma(ch, dh, -p2));
+    e = df_fma(ah, bl, e);
+    e = df_fma(al, bh, e);
+    e = df_fma(ch, dl, e);
+    e = df_fma(cl, dh, e);
+    float s = df_add_rn(p1, p2);
+    float bb = df_sub_rn(s, p1);
+    e = df_add_rn(e, df_add_rn(df_sub_rn(p1, df_sub_rn(s, bb)), df_sub_rn(p2, bb)));
+    s = pt_flip_sign(s, sbit);
+    e = pt_flip_sign(e, sbit);
+    const float h = df_add_rn(acc.hi, s);
+    bb = df_sub_rn(h, acc.hi);
+    acc.lo = df_add_rn(acc.lo, df_add_rn(df_add_rn(df_sub_rn(acc.hi, df_sub_rn(h, bb)), df_sub_rn(s, bb)), e));
+    acc.hi = h;
+}
+
+// acc += sign * (qh + ql), the pair unnormalised.
+__device__ __forceinline__ void df_acc_signed(DF &acc, uint32_t sbit, float qh, float ql) {
+    qh = pt_flip_sign(qh, sbit);
+    ql = pt_flip_sign(ql, sbit);
+    const float h = df_add_rn(acc.hi, qh);
+    const float bb = df_sub_rn(h, acc.hi);
+    acc.lo = df_add_rn(acc.lo, df_add_rn(df_add_rn(df_sub_rn(acc.hi, df_sub_rn(h, bb)), df_sub_rn(qh, bb)), ql));
+    acc.hi = h;
 }
 
 __device__ __forceinline__ void pt_cp_async16(void *smem_dst, const void *gsrc) {
@@ -846,111 +889,148 @@ __device__ __forceinline__ void pt_cp_async16(void *smem_dst, const void *gsrc) 
                  : "memory");
 }
 
-template <class T, class I>
+__device__ __forceinline__ uint32_t pt_insert_zero(uint32_t v, uint32_t b) {
+    const uint32_t low = (1u << b) - 1u;
+    return ((v & ~low) << 1) | (v & low);
+}
+
+// A float-float copy of a complex128 state, (re.hi, im.hi, re.lo, im.lo) per
+// amplitude: tile passes over it skip the per-tile conversion.
+__global__ void __launch_bounds__(256) df_state_copy_kernel(const double2 *__restrict__ src, float4 *__restrict__ dst,
+                                                             uint64_t count) {
+    const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
+    for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < count; i += stride) {
+        const double2 v = src[i];
+        const DF r = df_from_double(v.x), im = df_from_double(v.y);
+        dst[i] = make_float4(r.hi, im.hi, r.lo, im.lo);
+    }
+}
+
+// DFSRC: the complex128 source is already in float-float form.
+template <class T, class I, bool DFSRC>
 __global__ void __launch_bounds__(kPauliTileThreads, 3) pauli_tile_kernel(const PauliTileParams<I> p) {
-    using C = cplx_t<T>;
-    extern __shared__ __align__(128) unsigned char pt_smem[];
-    const int E = 1 << p.k;
-    C *buf[2] = {reinterpret_cast<C *>(pt_smem), reinterpret_cast<C *>(pt_smem) + E};
+    using Gm = PtGeom<T>;
+    constexpr int E = Gm::E, NA = Gm::NA, NP = Gm::NP, EB = 1 << Gm::LEB;
     constexpr int W = kPauliTileThreads / 32;
-    double *slot = reinterpret_cast<double *>(reinterpret_cast<C *>(pt_smem) + 2 * E);  // [nw][W]
-    for (int i = threadIdx.x; i < p.nw * W; i += kPauliTileThreads) slot[i] = 0.0;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int lowmask = (1 << p.m) - 1;
-    const C *sv = static_cast<const C *>(p.sv);
-    constexpr int EPC = sizeof(C) == 8 ? 2 : 1;  // amplitudes per 16-byte chunk (m >= 1)
-    auto load = [&](I tau, C *dst) {
+    extern __shared__ __align__(128) unsigned char pt_smem[];
+    double *slot = reinterpret_cast<double *>(pt_smem + 2 * E * EB);  // [nw][W], after the two tile buffers
+    const int tid = threadIdx.x;
+    for (int i = tid; i < p.nw * W; i += kPauliTileThreads) slot[i] = 0.0;
+    const int lane = tid & 31, warp = tid >> 5;
+    const uint32_t lowmask = (1u << p.m) - 1u;
+    // 16-byte chunks: two complex64 or one complex128 amplitude each
+    constexpr int EPC = sizeof(T) == 4 ? 2 : 1;
+    constexpr int GEB = sizeof(T) == 4 ? 8 : 16;  // bytes per amplitude in the state
+    const unsigned char *src = static_cast<const unsigned char *>(p.sv);
+    auto load = [&](I tau, unsigned char *dst) {
         const I base = insert_holes<I>(tau, p.holes);
-        for (int c = threadIdx.x; c < E / EPC; c += kPauliTileThreads) {
-            const int e = c * EPC;
-            pt_cp_async16(&dst[swz<T>(e)], &sv[base + p.hi_off[e >> p.m] + I(e & lowmask)]);
+        for (int c = tid; c < E / EPC; c += kPauliTileThreads) {
+            const uint32_t e = uint32_t(c * EPC);
+            const I gi = base + p.hi_off[e >> p.m] + I(e & lowmask);
+            pt_cp_async16(dst + size_t(e) * EB, src + size_t(gi) * GEB);
         }
         asm volatile("cp.async.commit_group;" ::: "memory");
     };
     TileAcc<T> acc[kTileWords];  // per-thread sums over all tiles of this CTA
     const I G = I(gridDim.x);
     I tau = blockIdx.x;
-    if (tau < p.ntiles) load(tau, buf[0]);
+    if (tau < p.ntiles) load(tau, pt_smem);
     else asm volatile("cp.async.commit_group;" ::: "memory");
     __syncthreads();
     for (int it = 0; tau < p.ntiles; tau += G, it++) {
-        C *cur = buf[it & 1];
-        if (tau + G < p.ntiles) load(tau + G, buf[(it + 1) & 1]);
+        unsigned char *cur = pt_smem + (it & 1) * (E * EB);
+        if (tau + G < p.ntiles) load(tau + G, pt_smem + ((it + 1) & 1) * (E * EB));
         else asm volatile("cp.async.commit_group;" ::: "memory");
         asm volatile("cp.async.wait_group 1;" ::: "memory");
         __syncthreads();
-        if constexpr (sizeof(T) == 8) {  // complex128 -> float-float in place
-            for (int e = threadIdx.x; e < E; e += kPauliTileThreads) {
+        if constexpr (sizeof(T) == 8 && !DFSRC) {  // complex128 -> float-float in place
+#pragma unroll 4
+            for (int j = 0; j < NA; j++) {
+                const int e = tid + j * kPauliTileThreads;
                 const double2 v = reinterpret_cast<const double2 *>(cur)[e];
                 const DF r = df_from_double(v.x), im = df_from_double(v.y);
-                reinterpret_cast<float4 *>(cur)[e] = make_float4(r.hi, r.lo, im.hi, im.lo);
+                reinterpret_cast<float4 *>(cur)[e] = make_float4(r.hi, im.hi, r.lo, im.lo);
             }
             __syncthreads();
         }
         const I base = insert_holes<I>(tau, p.holes);
-        // compile-time word index: acc[t] stays a register
+        // diagonal words: |a_e|^2 once per element
+        if (p.nd > 0) {
+            uint32_t pd[kTileWords];
+#pragma unroll
+            for (int t = 0; t < kTileWords; t++)
+                pd[t] = uint32_t(__popc(uint32_t(tid) & p.tsign[t]) + __popcll(uint64_t(base) & p.osign[t])) << 31;
+#pragma unroll
+            for (int j = 0; j < NA; j++) {
+                const int e = tid + j * kPauliTileThreads;
+                if constexpr (sizeof(T) == 4) {
+                    const float2 a = reinterpret_cast<const float2 *>(cur)[e];
+                    const float q = fmaf(a.x, a.x, a.y * a.y);
+#pragma unroll
+                    for (int t = 0; t < kTileWords; t++) {
+                        if (t >= p.nd) break;
+                        acc[t].v += pt_flip_sign(q, pd[t] ^ p.cs[t][j]);
+                    }
+                } else {
+                    const float4 a = reinterpret_cast<const float4 *>(cur)[e];  // (rh, ih, rl, il)
+                    const float p1 = df_mul_rn(a.x, a.x), p2 = df_mul_rn(a.y, a.y);
+                    float ql = df_add_rn(df_fma(a.x, a.x, -p1), df_fma(a.y, a.y, -p2));
+                    ql = df_fma(df_add_rn(a.x, a.x), a.z, ql);
+                    ql = df_fma(df_add_rn(a.y, a.y), a.w, ql);
+                    const float qh = df_add_rn(p1, p2);
+                    const float bb = df_sub_rn(qh, p1);
+                    ql = df_add_rn(ql, df_add_rn(df_sub_rn(p1, df_sub_rn(qh, bb)), df_sub_rn(p2, bb)));
+#pragma unroll
+                    for (int t = 0; t < kTileWords; t++) {
+                        if (t >= p.nd) break;
+                        df_acc_signed(acc[t].v[j & 1], pd[t] ^ p.cs[t][j], qh, ql);
+                    }
+                }
+            }
+        }
+        // words with flips
 #pragma unroll
         for (int t = 0; t < kTileWords; t++) {
             if (t >= p.nw) break;
-            const uint32_t f = p.tflip[t], sg = p.tsign[t];
-            const uint32_t neg0 = uint32_t(__popcll(uint64_t(base) & p.osign[t]) & 1);
+            if (t < p.nd) continue;
+            const uint32_t X = pt_insert_zero(uint32_t(tid), p.b0[t]);
+            const uint32_t P =
+                uint32_t(__popc(X & p.tsign[t]) + __popcll(uint64_t(base) & p.osign[t])) << 31;
+            const unsigned char *pa = cur + (X << Gm::LEB);
+            const unsigned char *pb = cur + ((X << Gm::LEB) ^ p.fxb[t]);
             const bool im = (p.use_im >> t) & 1u;
-            if (f == 0) {
-                for (int e = threadIdx.x; e < E; e += kPauliTileThreads) {
-                    const uint32_t par = (__popc(uint32_t(e) & sg) & 1) ^ neg0;
-                    if constexpr (sizeof(T) == 4) {
-                        const C a = cur[swz<T>(e)];
-                        const float q = fmaf(a.x, a.x, a.y * a.y);
-                        acc[t].add(par ? -q : q);
-                    } else {
-                        const float4 a = reinterpret_cast<const float4 *>(cur)[swz<T>(e)];
-                        const DF r{a.x, a.y}, i{a.z, a.w};
-                        df_acc_dot2(acc[t].v, par << 31, r, r, i, i);
+            if constexpr (sizeof(T) == 4) {
+                if (im) {
+#pragma unroll
+                    for (int j = 0; j < NP; j++) {
+                        const float2 a = *reinterpret_cast<const float2 *>(pa + p.ja[t][j]);
+                        const float2 b = *reinterpret_cast<const float2 *>(pb + p.jb[t][j]);
+                        acc[t].v += pt_flip_sign(fmaf(a.x, b.y, -a.y * b.x), P ^ p.cs[t][j]);
+                    }
+                } else {
+#pragma unroll
+                    for (int j = 0; j < NP; j++) {
+                        const float2 a = *reinterpret_cast<const float2 *>(pa + p.ja[t][j]);
+                        const float2 b = *reinterpret_cast<const float2 *>(pb + p.jb[t][j]);
+                        acc[t].v += pt_flip_sign(fmaf(a.x, b.x, a.y * b.y), P ^ p.cs[t][j]);
                     }
                 }
             } else {
-                const uint32_t low = f & (0u - f);  // lowest flip bit: pairs from its clear half
-                // the real or the imaginary part of conj(a) b, chosen once per word
-                auto pairs = [&](auto imc) {
-                    constexpr bool IM = decltype(imc)::value;
-                    PairWalk w(low, threadIdx.x, kPauliTileThreads);
-                    if constexpr (sizeof(T) == 4) {
-                        for (int c = threadIdx.x; c < (E >> 1); c += kPauliTileThreads) {
-                            const int e0 = int(w.x), e1 = int(w.x ^ f);
-                            w.step();
-                            const uint32_t par = (__popc(uint32_t(e0) & sg) & 1) ^ neg0;
-                            const C a = cur[swz<T>(e0)], b = cur[swz<T>(e1)];
-                            const float q = IM ? fmaf(a.x, b.y, -a.y * b.x) : fmaf(a.x, b.x, a.y * b.y);
-                            acc[t].add(par ? -q : q);
-                        }
-                    } else {
-                        // two independent running sums (pairs c and c + threads), so
-                        // the TwoSum chains of neighbouring pairs overlap
-                        DF s2{0.0f, 0.0f};
-                        for (int c = threadIdx.x; c < (E >> 1); c += 2 * kPauliTileThreads) {
+                if (im) {  // ar bi - ai br
 #pragma unroll
-                            for (int u = 0; u < 2; u++) {
-                                if (u == 1 && c + kPauliTileThreads >= (E >> 1)) break;
-                                const int e0 = int(w.x), e1 = int(w.x ^ f);
-                                w.step();
-                                const uint32_t par = (__popc(uint32_t(e0) & sg) & 1) ^ neg0;
-                                const float4 a4 = reinterpret_cast<const float4 *>(cur)[swz<T>(e0)];
-                                const float4 b4 = reinterpret_cast<const float4 *>(cur)[swz<T>(e1)];
-                                const DF ar{a4.x, a4.y}, ai{a4.z, a4.w}, br{b4.x, b4.y}, bi{b4.z, b4.w};
-                                DF &dst = u == 0 ? acc[t].v : s2;
-                                if constexpr (IM)  // ar bi - ai br
-                                    df_acc_dot2(dst, par << 31, ar, bi, df_neg(ai), br);
-                                else  // ar br + ai bi
-                                    df_acc_dot2(dst, par << 31, ar, br, ai, bi);
-                            }
-                        }
-                        acc[t].v = df_sum<2>({acc[t].v, s2});
+                    for (int j = 0; j < NP; j++) {
+                        const float4 a = *reinterpret_cast<const float4 *>(pa + p.ja[t][j]);
+                        const float4 b = *reinterpret_cast<const float4 *>(pb + p.jb[t][j]);
+                        df_acc_dot2(acc[t].v[j & 1], P ^ p.cs[t][j], a.x, a.z, b.y, b.w, -a.y, -a.w, b.x, b.z);
                     }
-                };
-                if (im)
-                    pairs(std::true_type{});
-                else
-                    pairs(std::false_type{});
+                } else {  // ar br + ai bi
+#pragma unroll
+                    for (int j = 0; j < NP; j++) {
+                        const float4 a = *reinterpret_cast<const float4 *>(pa + p.ja[t][j]);
+                        const float4 b = *reinterpret_cast<const float4 *>(pb + p.jb[t][j]);
+                        df_acc_dot2(acc[t].v[j & 1], P ^ p.cs[t][j], a.x, a.z, b.x, b.z, a.y, a.w, b.y, b.w);
+                    }
+                }
             }
         }
         __syncthreads();  // `cur` is the target of a load issued next iteration
@@ -963,7 +1043,7 @@ __global__ void __launch_bounds__(kPauliTileThreads, 3) pauli_tile_kernel(const 
         if (lane == 0) slot[t * W + warp] = acc[t].value();
     }
     __syncthreads();
-    for (int t = threadIdx.x; t < p.nw; t += kPauliTileThreads) {
+    for (int t = tid; t < p.nw; t += kPauliTileThreads) {
         double v = 0.0;
         for (int w = 0; w < W; w++) v += slot[t * W + w];
         p.partials[size_t(blockIdx.x) * p.nw + t] = v;
@@ -985,14 +1065,13 @@ template <class T, class I>
 static lgpu_status_t pauli_tile_raw(lgpu_context_t ctx, const void *sv, uint32_t n, uint32_t nwords,
                                     const uint64_t *flip, const uint64_t *sign, std::vector<double> &raw,
                                     std::vector<char> &done, cudaStream_t s) {
+    using Gm = PtGeom<T>;
     done.assign(nwords, 0);
     raw.assign(nwords, 0.0);
-    const int kmax = sizeof(T) == 4 ? 12 : 11;  // 32 KB tiles, two per CTA, three CTAs per SM
-    const auto passes = plan_tile_passes(n, nwords, flip, kmax);
+    if (n < uint32_t(Gm::K)) return LGPU_OK;
+    const auto passes = plan_tile_passes(n, nwords, flip, Gm::K, Gm::MMIN);
     if (passes.empty()) return LGPU_OK;
     const unsigned sms = unsigned(sm_count());
-    size_t maxk = 0;
-    for (const auto &tp : passes) maxk = std::max(maxk, tp.tile.size());
     const unsigned grid_cap = sms * 3;
     void *scr = nullptr;
     const size_t pbytes = sizeof(double) * size_t(grid_cap) * kTileWords;
@@ -1000,29 +1079,65 @@ static lgpu_status_t pauli_tile_raw(lgpu_context_t ctx, const void *sv, uint32_t
     LGPU_TRY(ctx_scratch(ctx, 256 + pbytes + rbytes, &scr));
     double *partials = reinterpret_cast<double *>(static_cast<char *>(scr) + 256);
     double *results = reinterpret_cast<double *>(static_cast<char *>(scr) + 256 + pbytes);
-    static std::atomic<size_t> attr[64];
+    static std::atomic<size_t> attr[64], attr_df[64];
+    // complex128 over three or more passes: convert the state to float-float
+    // once (one read and one write of the state) instead of in every pass,
+    // when a copy of the state's size takes at most a quarter of the free memory
+    void *dfcopy = nullptr;
+    const size_t svbytes = (size_t(1) << n) * sizeof(cplx_t<T>);
+    if (sizeof(T) == 8 && passes.size() >= 3) {
+        size_t freeb = 0, totalb = 0;
+        if (cudaMemGetInfo(&freeb, &totalb) == cudaSuccess && svbytes <= freeb / 4) {
+            if (cudaMallocAsync(&dfcopy, svbytes, s) != cudaSuccess) {
+                cudaGetLastError();
+                dfcopy = nullptr;
+            }
+        } else {
+            cudaGetLastError();
+        }
+    }
+    struct FreeOnExit {
+        void *p;
+        cudaStream_t s;
+        ~FreeOnExit() {
+            if (p) cudaFreeAsync(p, s);
+        }
+    } df_guard{dfcopy, s};
+    if (dfcopy) {
+        const uint64_t count = uint64_t(1) << n;
+        const unsigned g = grid_for(count, 256, 8, 8);
+        df_state_copy_kernel<<<g, 256, 0, s>>>(static_cast<const double2 *>(sv), static_cast<float4 *>(dfcopy), count);
+        LGPU_CHECK_LAUNCH();
+    }
+    std::vector<std::vector<uint32_t>> order(passes.size());  // word of each result slot
     for (size_t pi = 0; pi < passes.size(); pi++) {
         const TilePass &tp = passes[pi];
         const int k = int(tp.tile.size());
-        std::vector<int> pos(n, -1);
-        for (int q = 0; q < k; q++) pos[size_t(tp.tile[size_t(q)])] = q;
+        if (k != Gm::K) return fail(LGPU_ERR_UNSUPPORTED, "Pauli tile pass of unexpected size");
         int m = 0;
         while (m < k && tp.tile[size_t(m)] == m) m++;
-        PauliTileParams<I> b{};
-        b.sv = sv;
-        b.holes = make_holes(tp.tile);
-        b.ntiles = I(uint64_t(1) << (n - uint32_t(k)));
-        b.k = k;
-        b.m = m;
-        b.nw = int(tp.words.size());
+        auto b = std::make_unique<PauliTileParams<I>>();
+        std::memset(b.get(), 0, sizeof(PauliTileParams<I>));
+        b->sv = sv;
+        b->holes = make_holes(tp.tile);
+        b->ntiles = I(uint64_t(1) << (n - uint32_t(k)));
+        b->m = m;
         for (int h = 0; h < (1 << (k - m)); h++) {
             uint64_t o = 0;
             for (int q = m; q < k; q++)
                 if ((h >> (q - m)) & 1) o |= uint64_t(1) << tp.tile[size_t(q)];
-            b.hi_off[h] = I(o);
+            b->hi_off[h] = I(o);
         }
-        for (int t = 0; t < b.nw; t++) {
-            const uint32_t w = tp.words[size_t(t)];
+        // diagonal words first
+        auto &ord = order[pi];
+        for (uint32_t w : tp.words)
+            if (flip[w] == 0) ord.push_back(w);
+        b->nd = int(ord.size());
+        for (uint32_t w : tp.words)
+            if (flip[w] != 0) ord.push_back(w);
+        b->nw = int(ord.size());
+        for (int t = 0; t < b->nw; t++) {
+            const uint32_t w = ord[size_t(t)];
             uint32_t tf = 0, ts = 0;
             uint64_t os = sign[w];
             for (int q = 0; q < k; q++) {
@@ -1033,18 +1148,44 @@ static lgpu_status_t pauli_tile_raw(lgpu_context_t ctx, const void *sv, uint32_t
                     os &= ~(uint64_t(1) << bit);
                 }
             }
-            b.tflip[t] = tf;
-            b.tsign[t] = ts;
-            b.osign[t] = os;
-            if (flip[w] && (__builtin_popcountll(flip[w] & sign[w]) & 1)) b.use_im |= 1u << t;
+            b->tsign[t] = ts;
+            b->osign[t] = os;
+            if (flip[w] && (__builtin_popcountll(flip[w] & sign[w]) & 1)) b->use_im |= 1u << t;
+            if (tf == 0) {
+                for (int j = 0; j < Gm::NA; j++)
+                    b->cs[t][j] = uint32_t(__builtin_popcount((uint32_t(j) << 8) & ts) & 1) << 31;
+                continue;
+            }
+            const uint32_t b0 = uint32_t(__builtin_ctz(tf));
+            auto ins = [&](uint32_t v) { return ((v & ~((1u << b0) - 1u)) << 1) | (v & ((1u << b0) - 1u)); };
+            const uint32_t jm = ins(uint32_t(Gm::NP - 1) << 8);
+            b->b0[t] = b0;
+            b->fxb[t] = (tf & ~jm) << Gm::LEB;
+            for (int j = 0; j < Gm::NP; j++) {
+                const uint32_t J = ins(uint32_t(j) << 8);
+                b->ja[t][j] = J << Gm::LEB;
+                b->jb[t][j] = (J ^ (tf & jm)) << Gm::LEB;
+                b->cs[t][j] = uint32_t(__builtin_popcount(J & ts) & 1) << 31;
+            }
         }
-        const size_t smem = 2 * (size_t(1) << k) * sizeof(cplx_t<T>) + sizeof(double) * size_t(b.nw) * 8;
-        const unsigned grid = unsigned(std::min<uint64_t>(uint64_t(b.ntiles), grid_cap));
-        b.partials = partials;
-        LGPU_TRY(ensure_smem(reinterpret_cast<const void *>(pauli_tile_kernel<T, I>), smem, attr));
-        pauli_tile_kernel<T, I><<<grid, kPauliTileThreads, smem, s>>>(b);
+        const size_t smem = 2 * size_t(Gm::E) * (size_t(1) << Gm::LEB) + sizeof(double) * size_t(b->nw) * 8;
+        const unsigned grid = unsigned(std::min<uint64_t>(uint64_t(b->ntiles), grid_cap));
+        b->partials = partials;
+        bool launched = false;
+        if constexpr (sizeof(T) == 8) {
+            if (dfcopy) {
+                b->sv = dfcopy;
+                LGPU_TRY(ensure_smem(reinterpret_cast<const void *>(pauli_tile_kernel<T, I, true>), smem, attr_df));
+                pauli_tile_kernel<T, I, true><<<grid, kPauliTileThreads, smem, s>>>(*b);
+                launched = true;
+            }
+        }
+        if (!launched) {
+            LGPU_TRY(ensure_smem(reinterpret_cast<const void *>(pauli_tile_kernel<T, I, false>), smem, attr));
+            pauli_tile_kernel<T, I, false><<<grid, kPauliTileThreads, smem, s>>>(*b);
+        }
         LGPU_CHECK_LAUNCH();
-        pauli_tile_reduce<<<1, kTileWords, 0, s>>>(partials, int(grid), b.nw, results + pi * kTileWords);
+        pauli_tile_reduce<<<1, kTileWords, 0, s>>>(partials, int(grid), b->nw, results + pi * kTileWords);
         LGPU_CHECK_LAUNCH();
     }
     std::vector<double> host(passes.size() * kTileWords);
@@ -1054,9 +1195,9 @@ static lgpu_status_t pauli_tile_raw(lgpu_context_t ctx, const void *sv, uint32_t
     LGPU_CUDA_TRY(cudaStreamSynchronize(s));
     std::memcpy(host.data(), pin, rbytes);
     for (size_t pi = 0; pi < passes.size(); pi++)
-        for (size_t t = 0; t < passes[pi].words.size(); t++) {
-            raw[passes[pi].words[t]] = host[pi * kTileWords + t];
-            done[passes[pi].words[t]] = 1;
+        for (size_t t = 0; t < order[pi].size(); t++) {
+            raw[order[pi][t]] = host[pi * kTileWords + t];
+            done[order[pi][t]] = 1;
         }
     return LGPU_OK;
 }

@@ -245,6 +245,34 @@ def test_pauli_words(native, oracle, dtype, n):
 
 
 @pytest.mark.parametrize("dtype", DTYPES)
+@pytest.mark.parametrize("nwords", [3, 12, 30])
+def test_pauli_tile_pass_counts(native, oracle, dtype, nwords):
+    """Tile passes on an 18-qubit state with one, a few and many passes
+    (complex128 converts each tile in the pass itself below three passes and
+    reads a float-float copy of the state from three on): every word against
+    the oracle.  The words mix diagonal ones, real and imaginary pair sums,
+    flips on bit 0, on the bits of a tile's per-thread index part (8..10) and
+    on the highest state bits."""
+    n = 18
+    rng = np.random.default_rng(77 + nwords)
+    psi = random_state(n, rng)
+    sv = make_sv(native, dtype, psi)
+    fixed = [("Z", [0]), ("ZZZ", [3, 9, 17]), ("X", [n - 1]), ("XY", [n - 1, n - 2]), ("YX", [n - 9, n - 10]),
+             ("XZY", [n - 1, n - 5, n - 11]), ("XXYYX", [0, 4, 8, 12, 16]), ("Y", [n - 3])]
+    words = [w for w, _ in fixed][:nwords]
+    wires = [ws for _, ws in fixed][:nwords]
+    while len(words) < nwords:
+        k = int(rng.integers(1, 7))
+        ws = [int(x) for x in rng.choice(n, size=k, replace=False)]
+        words.append("".join(rng.choice(list("XYZ"), size=k)))
+        wires.append(ws)
+    per = sv.PauliWordExpectations(words, wires)
+    for j in range(nwords):
+        rj = oracle.expval_pauli_words(psi, [words[j]], [wires[j]], np.array([1.0]))
+        assert abs(per[j] - rj) < tol(dtype), (words[j], wires[j], per[j], rj)
+
+
+@pytest.mark.parametrize("dtype", DTYPES)
 @pytest.mark.parametrize("n", [3, 8, 14])
 def test_probabilities(native, oracle, dtype, n):
     rng = np.random.default_rng(400 + n)
