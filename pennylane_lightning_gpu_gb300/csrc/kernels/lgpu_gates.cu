@@ -19,6 +19,7 @@
 #include <unordered_map>
 
 #include "lgpu_bodies.cuh"
+#include "lgpu_df2.cuh"
 #include "lgpu_df64.cuh"
 #include "lgpu_f64emu.cuh"
 #include "lgpu_fused_plan.h"
@@ -535,27 +536,40 @@ __device__ __forceinline__ void tile_pairs(cplx_t<T> *tile, int E, int q, uint32
 }
 
 // complex128 gates on a tile held in float-float form: each amplitude is a
-// float4 (re.hi, re.lo, im.hi, im.lo) in the slot of its double2, so the
-// layout and the swizzle are those of the complex128 tile.
+// float4 (re.hi, im.hi, re.lo, im.lo) in the slot of its double2, so the
+// layout and the swizzle are those of the complex128 tile.  The bodies run as
+// paired float-float lanes (re, im) (lgpu_df2.cuh): the same operations as
+// the scalar bodies in half the FP32 instructions.
 template <int BODY, int NT>
 __device__ __forceinline__ void tile_pairs_df(float4 *tile, int E, int q, uint32_t in_mask, uint32_t in_val,
                                               const DF *m) {
     const uint32_t holes = in_mask | (1u << q);
     const int nfree = E >> __popc(holes);
-    DF mr[8];
-#pragma unroll
-    for (int i = 0; i < 8; i++) mr[i] = m[i];
+    DF2 c[8];
+    if constexpr (BODY != kDfSignDiag && BODY != 2) df2_coeffs(m, c);
+    const float s0 = m[0].hi, s1 = m[6].hi;  // diag(+-1, +-1): exact sign flips
     PairWalk w(holes, threadIdx.x, NT);
 #pragma unroll 2
     for (int f = threadIdx.x; f < nfree; f += NT) {
         const int e0 = int(w.x | in_val);
         const int e1 = e0 | (1 << q);
         w.step();
-        const float4 a = tile[swz<double>(e0)], b = tile[swz<double>(e1)];
-        DF xr{a.x, a.y}, xi{a.z, a.w}, yr{b.x, b.y}, yi{b.z, b.w};
-        body1_dfv<BODY>(mr, xr, xi, yr, yi);
-        tile[swz<double>(e0)] = make_float4(xr.hi, xr.lo, xi.hi, xi.lo);
-        tile[swz<double>(e1)] = make_float4(yr.hi, yr.lo, yi.hi, yi.lo);
+        float4 a = tile[swz<double>(e0)], b = tile[swz<double>(e1)];
+        if constexpr (BODY == kDfSignDiag) {
+            a = make_float4(a.x * s0, a.y * s0, a.z * s0, a.w * s0);
+            b = make_float4(b.x * s1, b.y * s1, b.z * s1, b.w * s1);
+        } else if constexpr (BODY == 2) {
+            const float4 t = a;
+            a = b;
+            b = t;
+        } else {
+            DF2 x{f2_pack(a.x, a.y), f2_pack(a.z, a.w)}, y{f2_pack(b.x, b.y), f2_pack(b.z, b.w)};
+            body1_df2<BODY>(c, x, y);
+            a = make_float4(f2_x(x.hi), f2_y(x.hi), f2_x(x.lo), f2_y(x.lo));
+            b = make_float4(f2_x(y.hi), f2_y(y.hi), f2_x(y.lo), f2_y(y.lo));
+        }
+        tile[swz<double>(e0)] = a;
+        tile[swz<double>(e1)] = b;
     }
 }
 
@@ -578,9 +592,9 @@ __device__ __forceinline__ void tile_quads_df(float4 *tile, int E, int qa, int q
         DF ar[4], ai[4];
 #pragma unroll
         for (int c = 0; c < 4; c++) {
-            const float4 v = tile[idx[c]];
-            ar[c] = DF{v.x, v.y};
-            ai[c] = DF{v.z, v.w};
+            const float4 v = tile[idx[c]];  // (re.hi, im.hi, re.lo, im.lo)
+            ar[c] = DF{v.x, v.z};
+            ai[c] = DF{v.y, v.w};
         }
 #pragma unroll
         for (int r = 0; r < 4; r++) {
@@ -594,7 +608,7 @@ __device__ __forceinline__ void tile_quads_df(float4 *tile, int E, int qa, int q
                 ti[2 * c + 1] = df_mul(mim, ar[c]);
             }
             const DF xr = df_sum<8>(tr), xi = df_sum<8>(ti);
-            tile[idx[r]] = make_float4(xr.hi, xr.lo, xi.hi, xi.lo);
+            tile[idx[r]] = make_float4(xr.hi, xi.hi, xr.lo, xi.lo);
         }
     }
 }
@@ -787,7 +801,7 @@ __global__ void __launch_bounds__(NT, MINB)
             for (int e = threadIdx.x; e < E; e += NT) {
                 const double2 v = reinterpret_cast<const double2 *>(cur)[e];
                 const DF r = df_from_double(v.x), i = df_from_double(v.y);
-                reinterpret_cast<float4 *>(cur)[e] = make_float4(r.hi, r.lo, i.hi, i.lo);
+                reinterpret_cast<float4 *>(cur)[e] = make_float4(r.hi, i.hi, r.lo, i.lo);
             }
             __syncthreads();
         }
@@ -802,7 +816,7 @@ __global__ void __launch_bounds__(NT, MINB)
                 } else if constexpr (DFM && sizeof(T) == 8) {
                     const float4 v = reinterpret_cast<const float4 *>(cur)[swz<T>(e)];
                     __stcs(reinterpret_cast<double2 *>(dst),
-                           make_double2(df_to_double(DF{v.x, v.y}), df_to_double(DF{v.z, v.w})));
+                           make_double2(df_to_double(DF{v.x, v.z}), df_to_double(DF{v.y, v.w})));
                 } else {
                     __stcs(dst, cur[swz<T>(e)]);
                 }
