@@ -15,6 +15,7 @@
 //                   tiles of the last block and reduced inside the CTA, so each
 //                   result is written by exactly one CTA in a fixed order.
 #include "lgpu_bodies.cuh"
+#include "lgpu_df2.cuh"
 #include "lgpu_df64.cuh"
 #include "lgpu_f64emu.cuh"
 #include "lgpu_internal.cuh"
@@ -214,14 +215,14 @@ __device__ __forceinline__ void batch_pairs(cplx_t<T> *tile, int E, int q, uint3
     }
 }
 
-// complex128 in float-float (lgpu_df64.cuh): the tile holds float4
-// (re.hi, re.lo, im.hi, im.lo) per amplitude, in the slot of its double2.
+// complex128 in float-float: the tile holds float4 (re.hi, im.hi, re.lo,
+// im.lo) per amplitude, in the slot of its double2; the bodies run as paired
+// float-float lanes (re, im) (lgpu_df2.cuh).
 template <int BODY>
 __device__ __forceinline__ void batch_pairs_df(float4 *tile, int E, int q, uint32_t cmask, uint32_t cval,
                                                const DF *mp) {
-    DF m[8];
-#pragma unroll
-    for (int i = 0; i < 8; i++) m[i] = mp[i];
+    DF2 c[8];
+    if constexpr (BODY != B_PERM) df2_coeffs(mp, c);
     const uint32_t holes = cmask | (1u << q);
     const int nfree = E >> __popc(holes);
     PairWalk w(holes, threadIdx.x, blockDim.x);
@@ -230,11 +231,16 @@ __device__ __forceinline__ void batch_pairs_df(float4 *tile, int E, int q, uint3
         const int e0 = int(w.x | cval);
         const int e1 = e0 | (1 << q);
         w.step();
-        const float4 a = tile[e0], b = tile[e1];
-        DF xr{a.x, a.y}, xi{a.z, a.w}, yr{b.x, b.y}, yi{b.z, b.w};
-        body1_dfv<BODY>(m, xr, xi, yr, yi);
-        tile[e0] = make_float4(xr.hi, xr.lo, xi.hi, xi.lo);
-        tile[e1] = make_float4(yr.hi, yr.lo, yi.hi, yi.lo);
+        float4 a = tile[e0], b = tile[e1];
+        if constexpr (BODY == B_PERM) {
+            tile[e0] = b;
+            tile[e1] = a;
+        } else {
+            DF2 x{f2_pack(a.x, a.y), f2_pack(a.z, a.w)}, y{f2_pack(b.x, b.y), f2_pack(b.z, b.w)};
+            body1_df2<BODY>(c, x, y);
+            tile[e0] = make_float4(f2_x(x.hi), f2_y(x.hi), f2_x(x.lo), f2_y(x.lo));
+            tile[e1] = make_float4(f2_x(y.hi), f2_y(y.hi), f2_x(y.lo), f2_y(y.lo));
+        }
     }
 }
 
@@ -269,9 +275,9 @@ __device__ __forceinline__ void tile_gate_df(float4 *tile, int E, const lgpu_bga
         DF ar[4], ai[4];
 #pragma unroll
         for (int c = 0; c < 4; c++) {
-            const float4 v = tile[idx[c]];
-            ar[c] = DF{v.x, v.y};
-            ai[c] = DF{v.z, v.w};
+            const float4 v = tile[idx[c]];  // (re.hi, im.hi, re.lo, im.lo)
+            ar[c] = DF{v.x, v.z};
+            ai[c] = DF{v.y, v.w};
         }
 #pragma unroll
         for (int row = 0; row < 4; row++) {
@@ -285,7 +291,7 @@ __device__ __forceinline__ void tile_gate_df(float4 *tile, int E, const lgpu_bga
                 ti[2 * c + 1] = df_mul(mim, ar[c]);
             }
             const DF xr = df_sum<8>(tr), xi = df_sum<8>(ti);
-            tile[idx[row]] = make_float4(xr.hi, xr.lo, xi.hi, xi.lo);
+            tile[idx[row]] = make_float4(xr.hi, xi.hi, xr.lo, xi.lo);
         }
     }
 }
@@ -296,13 +302,13 @@ __device__ __forceinline__ void tile_to_df(void *tile, int E) {
     for (int e = threadIdx.x; e < E; e += blockDim.x) {
         const double2 v = reinterpret_cast<const double2 *>(tile)[e];
         const DF r = df_from_double(v.x), i = df_from_double(v.y);
-        reinterpret_cast<float4 *>(tile)[e] = make_float4(r.hi, r.lo, i.hi, i.lo);
+        reinterpret_cast<float4 *>(tile)[e] = make_float4(r.hi, i.hi, r.lo, i.lo);
     }
 }
 __device__ __forceinline__ void tile_from_df(void *tile, int E) {
     for (int e = threadIdx.x; e < E; e += blockDim.x) {
         const float4 v = reinterpret_cast<const float4 *>(tile)[e];
-        reinterpret_cast<double2 *>(tile)[e] = make_double2(df_to_double(DF{v.x, v.y}), df_to_double(DF{v.z, v.w}));
+        reinterpret_cast<double2 *>(tile)[e] = make_double2(df_to_double(DF{v.x, v.z}), df_to_double(DF{v.y, v.w}));
     }
 }
 

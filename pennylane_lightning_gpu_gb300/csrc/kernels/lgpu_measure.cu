@@ -15,6 +15,7 @@
 #include <type_traits>
 
 #include "lgpu_bodies.cuh"
+#include "lgpu_df2.cuh"
 #include "lgpu_df64.cuh"
 #include "lgpu_internal.cuh"
 #include "lgpu_pauli_plan.h"
@@ -836,52 +837,55 @@ template <> struct TileAcc<float> {
     __device__ __forceinline__ double value() const { return double(v); }
 };
 template <> struct TileAcc<double> {
-    DF v[2] = {DF{0.0f, 0.0f}, DF{0.0f, 0.0f}};  // two running sums, unnormalised
+    DF2 v{F2{0ull}, F2{0ull}};  // two running sums in the lanes, unnormalised
+    DF r{0.0f, 0.0f};
     __device__ __forceinline__ void warp_reduce() {
-        DF s = df_sum<2>({v[0], v[1]});  // renormalised
+        DF s = df_sum<2>({DF{f2_x(v.hi), f2_x(v.lo)}, DF{f2_y(v.hi), f2_y(v.lo)}});  // renormalised
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1)
             s = df_sum<2>({s, DF{__shfl_xor_sync(0xffffffffu, s.hi, o), __shfl_xor_sync(0xffffffffu, s.lo, o)}});
-        v[0] = s;
+        r = s;
     }
-    __device__ __forceinline__ double value() const { return df_to_double(v[0]); }
+    __device__ __forceinline__ double value() const { return df_to_double(r); }
 };
 
+// a with the sign bits sx, sy XOR-ed into its lanes.
+__device__ __forceinline__ F2 f2_flip(F2 a, uint32_t sx, uint32_t sy) {
+    return f2_pack(__uint_as_float(__float_as_uint(f2_x(a)) ^ sx), __uint_as_float(__float_as_uint(f2_y(a)) ^ sy));
+}
+
+// acc += (sx a_x b_x, sy a_y b_y) lane by lane for float-float lanes a, b and
+// signs given as the bit patterns 0 / 0x80000000.  The leading products are
+// split exactly (a scalar FMA per lane for the error, which negates an
+// operand for free), the sums by TwoSum; the error terms and the cross
+// products gather in acc.lo, which stays unnormalised until the end.
+__device__ __forceinline__ void df2_acc_mul(DF2 &acc, uint32_t sx, uint32_t sy, const DF2 &a, const DF2 &b) {
+    F2 p = f2_mul(a.hi, b.hi);
+    const float ex = __fmaf_rn(f2_x(a.hi), f2_x(b.hi), -f2_x(p));
+    const float ey = __fmaf_rn(f2_y(a.hi), f2_y(b.hi), -f2_y(p));
+    F2 e = f2_fma(a.hi, b.lo, f2_pack(ex, ey));
+    e = f2_fma(a.lo, b.hi, e);
+    p = f2_flip(p, sx, sy);
+    e = f2_flip(e, sx, sy);
+    const F2 h = f2_add(acc.hi, p);
+    const F2 bb = f2_sub(h, acc.hi);
+    const F2 err = f2_add(f2_sub(acc.hi, f2_sub(h, bb)), f2_sub(p, bb));
+    acc.lo = f2_add(acc.lo, f2_add(err, e));
+    acc.hi = h;
+}
+
+// acc += (sx q_x, sy q_y) lane by lane for unnormalised float-float lanes q.
+__device__ __forceinline__ void df2_acc_signed(DF2 &acc, uint32_t sx, uint32_t sy, F2 qh, F2 ql) {
+    qh = f2_flip(qh, sx, sy);
+    ql = f2_flip(ql, sx, sy);
+    const F2 h = f2_add(acc.hi, qh);
+    const F2 bb = f2_sub(h, acc.hi);
+    const F2 err = f2_add(f2_sub(acc.hi, f2_sub(h, bb)), f2_sub(qh, bb));
+    acc.lo = f2_add(acc.lo, f2_add(err, ql));
+    acc.hi = h;
+}
+
 __device__ __forceinline__ float pt_flip_sign(float x, uint32_t sbit) { return __uint_as_float(__float_as_uint(x) ^ sbit); }
-
-// acc += sign * (a b + c d) for float-float a, b, c, d, sign = +-1 given as the
-// bit pattern 0 or 0x80000000.  The leading products are split exactly by
-// FMA, their sum exactly by TwoSum, and that sum's leading part enters the
-// running sum through a second TwoSum; the error terms and the cross products
-// gather in acc.lo, which stays unnormalised until the end.
-__device__ __forceinline__ void df_acc_dot2(DF &acc, uint32_t sbit, float ah, float al, float bh, float bl, float ch,
-                                            float cl, float dh, float dl) {
-    const float p1 = df_mul_rn(ah, bh), p2 = df_mul_rn(ch, dh);
-    float e = df_add_rn(df_fma(ah, bh, -p1), df_fma(ch, dh, -p2));
-    e = df_fma(ah, bl, e);
-    e = df_fma(al, bh, e);
-    e = df_fma(ch, dl, e);
-    e = df_fma(cl, dh, e);
-    float s = df_add_rn(p1, p2);
-    float bb = df_sub_rn(s, p1);
-    e = df_add_rn(e, df_add_rn(df_sub_rn(p1, df_sub_rn(s, bb)), df_sub_rn(p2, bb)));
-    s = pt_flip_sign(s, sbit);
-    e = pt_flip_sign(e, sbit);
-    const float h = df_add_rn(acc.hi, s);
-    bb = df_sub_rn(h, acc.hi);
-    acc.lo = df_add_rn(acc.lo, df_add_rn(df_add_rn(df_sub_rn(acc.hi, df_sub_rn(h, bb)), df_sub_rn(s, bb)), e));
-    acc.hi = h;
-}
-
-// acc += sign * (qh + ql), the pair unnormalised.
-__device__ __forceinline__ void df_acc_signed(DF &acc, uint32_t sbit, float qh, float ql) {
-    qh = pt_flip_sign(qh, sbit);
-    ql = pt_flip_sign(ql, sbit);
-    const float h = df_add_rn(acc.hi, qh);
-    const float bb = df_sub_rn(h, acc.hi);
-    acc.lo = df_add_rn(acc.lo, df_add_rn(df_add_rn(df_sub_rn(acc.hi, df_sub_rn(h, bb)), df_sub_rn(qh, bb)), ql));
-    acc.hi = h;
-}
 
 __device__ __forceinline__ void pt_cp_async16(void *smem_dst, const void *gsrc) {
     asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(static_cast<uint32_t>(__cvta_generic_to_shared(smem_dst))),
@@ -960,30 +964,40 @@ __global__ void __launch_bounds__(kPauliTileThreads, 3) pauli_tile_kernel(const 
 #pragma unroll
             for (int t = 0; t < kTileWords; t++)
                 pd[t] = uint32_t(__popc(uint32_t(tid) & p.tsign[t]) + __popcll(uint64_t(base) & p.osign[t])) << 31;
+            if constexpr (sizeof(T) == 4) {
 #pragma unroll
-            for (int j = 0; j < NA; j++) {
-                const int e = tid + j * kPauliTileThreads;
-                if constexpr (sizeof(T) == 4) {
-                    const float2 a = reinterpret_cast<const float2 *>(cur)[e];
+                for (int j = 0; j < NA; j++) {
+                    const float2 a = reinterpret_cast<const float2 *>(cur)[tid + j * kPauliTileThreads];
                     const float q = fmaf(a.x, a.x, a.y * a.y);
 #pragma unroll
                     for (int t = 0; t < kTileWords; t++) {
                         if (t >= p.nd) break;
                         acc[t].v += pt_flip_sign(q, pd[t] ^ p.cs[t][j]);
                     }
-                } else {
-                    const float4 a = reinterpret_cast<const float4 *>(cur)[e];  // (rh, ih, rl, il)
-                    const float p1 = df_mul_rn(a.x, a.x), p2 = df_mul_rn(a.y, a.y);
-                    float ql = df_add_rn(df_fma(a.x, a.x, -p1), df_fma(a.y, a.y, -p2));
-                    ql = df_fma(df_add_rn(a.x, a.x), a.z, ql);
-                    ql = df_fma(df_add_rn(a.y, a.y), a.w, ql);
-                    const float qh = df_add_rn(p1, p2);
-                    const float bb = df_sub_rn(qh, p1);
-                    ql = df_add_rn(ql, df_add_rn(df_sub_rn(p1, df_sub_rn(qh, bb)), df_sub_rn(p2, bb)));
+                }
+            } else {
+                // elements j and j + 1 in the two lanes
+#pragma unroll
+                for (int j = 0; j < NA; j += 2) {
+                    float qh[2], ql[2];
+#pragma unroll
+                    for (int u = 0; u < 2; u++) {
+                        const float4 a =
+                            reinterpret_cast<const float4 *>(cur)[tid + (j + u) * kPauliTileThreads];  // (rh, ih, rl, il)
+                        const float p1 = df_mul_rn(a.x, a.x), p2 = df_mul_rn(a.y, a.y);
+                        float l = df_add_rn(df_fma(a.x, a.x, -p1), df_fma(a.y, a.y, -p2));
+                        l = df_fma(df_add_rn(a.x, a.x), a.z, l);
+                        l = df_fma(df_add_rn(a.y, a.y), a.w, l);
+                        const float h = df_add_rn(p1, p2);
+                        const float bb = df_sub_rn(h, p1);
+                        ql[u] = df_add_rn(l, df_add_rn(df_sub_rn(p1, df_sub_rn(h, bb)), df_sub_rn(p2, bb)));
+                        qh[u] = h;
+                    }
+                    const F2 qh2 = f2_pack(qh[0], qh[1]), ql2 = f2_pack(ql[0], ql[1]);
 #pragma unroll
                     for (int t = 0; t < kTileWords; t++) {
                         if (t >= p.nd) break;
-                        df_acc_signed(acc[t].v[j & 1], pd[t] ^ p.cs[t][j], qh, ql);
+                        df2_acc_signed(acc[t].v, pd[t] ^ p.cs[t][j], pd[t] ^ p.cs[t][j + 1], qh2, ql2);
                     }
                 }
             }
@@ -1016,19 +1030,24 @@ __global__ void __launch_bounds__(kPauliTileThreads, 3) pauli_tile_kernel(const 
                     }
                 }
             } else {
-                if (im) {  // ar bi - ai br
+                // lanes: the two products of Re or Im of conj(a) b
+                if (im) {  // (ar bi, -ai br)
 #pragma unroll
                     for (int j = 0; j < NP; j++) {
                         const float4 a = *reinterpret_cast<const float4 *>(pa + p.ja[t][j]);
                         const float4 b = *reinterpret_cast<const float4 *>(pb + p.jb[t][j]);
-                        df_acc_dot2(acc[t].v[j & 1], P ^ p.cs[t][j], a.x, a.z, b.y, b.w, -a.y, -a.w, b.x, b.z);
+                        const uint32_t sb = P ^ p.cs[t][j];
+                        df2_acc_mul(acc[t].v, sb, sb ^ 0x80000000u, DF2{f2_pack(a.x, a.y), f2_pack(a.z, a.w)},
+                                    DF2{f2_pack(b.y, b.x), f2_pack(b.w, b.z)});
                     }
-                } else {  // ar br + ai bi
+                } else {  // (ar br, ai bi)
 #pragma unroll
                     for (int j = 0; j < NP; j++) {
                         const float4 a = *reinterpret_cast<const float4 *>(pa + p.ja[t][j]);
                         const float4 b = *reinterpret_cast<const float4 *>(pb + p.jb[t][j]);
-                        df_acc_dot2(acc[t].v[j & 1], P ^ p.cs[t][j], a.x, a.z, b.x, b.z, a.y, a.w, b.y, b.w);
+                        const uint32_t sb = P ^ p.cs[t][j];
+                        df2_acc_mul(acc[t].v, sb, sb, DF2{f2_pack(a.x, a.y), f2_pack(a.z, a.w)},
+                                    DF2{f2_pack(b.x, b.y), f2_pack(b.z, b.w)});
                     }
                 }
             }
