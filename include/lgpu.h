@@ -395,6 +395,23 @@ lgpu_status_t lgpu_adjoint_block(lgpu_context_t ctx, void *ket, void *const *bra
                                  const lgpu_adj_block_step_t *steps, uint32_t nsteps, double *jac_dev,
                                  uint32_t jac_stride, lgpu_stream_t stream);
 
+/* Float-float form of a complex128 state: each amplitude's 16 bytes hold the
+ * floats (re.hi, im.hi, re.lo, im.lo), re = re.hi + re.lo to about 2^-47
+ * relative.  A reverse sweep made of consecutive blocks keeps lambda and the
+ * bras in this form between blocks, so each block skips the conversion of
+ * its tiles: LGPU_FF_IN = the states arrive in float-float form, LGPU_FF_OUT
+ * = leave them in it (complex128 only; 0 = lgpu_adjoint_block).  No other
+ * call accepts a state in this form: lgpu_state_ff(sv, n, 0, stream) turns it
+ * back into complex128, lgpu_state_ff(sv, n, 1, stream) converts the other
+ * way; both in place, stream-ordered. */
+#define LGPU_FF_IN 1u
+#define LGPU_FF_OUT 2u
+lgpu_status_t lgpu_adjoint_block_ff(lgpu_context_t ctx, void *ket, void *const *bras, uint32_t nbras, uint32_t n,
+                                    lgpu_dtype_t dt, uint32_t k, const int32_t *tile_bits,
+                                    const lgpu_adj_block_step_t *steps, uint32_t nsteps, double *jac_dev,
+                                    uint32_t jac_stride, uint32_t ff_flags, lgpu_stream_t stream);
+lgpu_status_t lgpu_state_ff(void *sv, uint32_t n, int to_ff, lgpu_stream_t stream);
+
 /* ---- CUDA graphs (stream capture) ------------------------------------------
  * Capture everything issued on `stream` between begin and end into an
  * executable graph; launch replays it on any stream.  No counterpart in the

@@ -175,6 +175,18 @@ template <class T = double> class AdjointJacobianGPU {
 
         const bool blocks = num_observables >= 1 && blocks_enabled();
         std::unique_ptr<SV> lam0;  // lambda before a block, when the bras run in pairs
+        // complex128: between consecutive blocks lambda and the bras stay in
+        // float-float form (lgpu_state_ff); any other operation gets them back
+        // as complex128 first
+        const bool ff_ok = SV::dt() == LGPU_C128;
+        bool in_ff = false;
+        auto leave_ff = [&]() {
+            if (!in_ff) return;
+            PL_LGPU_IS_SUCCESS(lgpu_state_ff(lambda.getData(), n, 0, lambda.lstream()));
+            for (size_t k = 0; k < num_observables; k++)
+                PL_LGPU_IS_SUCCESS(lgpu_state_ff(bra_ptrs[k], n, 0, lambda.lstream()));
+            in_ff = false;
+        };
         for (int op_idx = static_cast<int>(ops_name.size() - 1); op_idx >= 0; op_idx--) {
             PL_ABORT_IF(ops.getOpsParams()[size_t(op_idx)].size() > 1,
                         "The operation is not supported using the adjoint differentiation method");
@@ -225,14 +237,17 @@ template <class T = double> class AdjointJacobianGPU {
                         if (!lam0) lam0 = std::make_unique<SV>(lambda.getNumQubits(), dt_local, true);
                         lam0->updateData(lambda);
                     }
+                    const uint32_t ff = ff_ok ? ((in_ff ? LGPU_FF_IN : 0u) | LGPU_FF_OUT) : 0u;
                     for (size_t b0 = 0; b0 < num_observables; b0 += 2) {
                         if (b0 > 0) lambda.updateData(*lam0);
                         const uint32_t nb = uint32_t(std::min<size_t>(2, num_observables - b0));
-                        PL_LGPU_IS_SUCCESS(lgpu_adjoint_block(lambda.ctx(), lambda.getData(), bra_ptrs.data() + b0, nb,
-                                                              n, SV::dt(), uint32_t(tb.size()), tb.data(), steps.data(),
-                                                              uint32_t(steps.size()), jac_dev.getData() + b0,
-                                                              uint32_t(K), lambda.lstream()));
+                        PL_LGPU_IS_SUCCESS(lgpu_adjoint_block_ff(lambda.ctx(), lambda.getData(), bra_ptrs.data() + b0,
+                                                                 nb, n, SV::dt(), uint32_t(tb.size()), tb.data(),
+                                                                 steps.data(), uint32_t(steps.size()),
+                                                                 jac_dev.getData() + b0, uint32_t(K), ff,
+                                                                 lambda.lstream()));
                     }
+                    in_ff = ff_ok;
                     for (const auto &cs : scales) col_scale[cs.first] = cs.second;
                     current_param_idx = cpi;
                     trainableParamNumber = tpn;
@@ -242,6 +257,7 @@ template <class T = double> class AdjointJacobianGPU {
                 }
             }
 
+            leave_ff();
             const bool inv = ops.getOpsInverses()[size_t(op_idx)];
             const auto &wires = ops.getOpsWires()[size_t(op_idx)];
             Engine::GateDesc udag = lower(lambda, ops, size_t(op_idx), !inv);
@@ -306,6 +322,7 @@ template <class T = double> class AdjointJacobianGPU {
             }
             if (ops.hasParams(size_t(op_idx))) current_param_idx--;
         }
+        leave_ff();  // lambda and the bras leave the sweep as complex128
         // One device-to-host copy of all columns.
         std::vector<double> host(tp_size * K);
         jac_dev.CopyGpuDataToHost(host.data(), host.size(), false);

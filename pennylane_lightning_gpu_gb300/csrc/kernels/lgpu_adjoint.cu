@@ -11,6 +11,7 @@
 #include <memory>
 
 #include "lgpu_bodies.cuh"
+#include "lgpu_df2.cuh"
 #include "lgpu_df64.cuh"
 #include "lgpu_internal.cuh"
 #include "lgpu_reduce.cuh"
@@ -668,6 +669,7 @@ template <class I> struct AdjBlockParams {
     double2 *ket;
     double2 *bras[kAdjBlockBras];
     double *partials;  // [gridDim.x][nslots][nb]
+    int in_ff, out_ff;  // complex128: the states are read / left in float-float form
     AStep steps[kAdjBlockSteps];
 };
 
@@ -704,7 +706,26 @@ __device__ __forceinline__ DF df_shfl_xor(DF v, int o) {
 }
 
 // One step on the tile: the pairs (e0, e0 | 1 << q) with the in-tile controls
-// set.  BODY / GK at compile time (G_NONE: U^dag only).
+// set.  BODY / GK at compile time (G_NONE: U^dag only).  Amplitudes are float4
+// (re.hi, im.hi, re.lo, im.lo); U^dag runs as paired float-float lanes
+// (re, im) (lgpu_df2.cuh), the overlap in scalar float-float.
+template <int BODY>
+__device__ __forceinline__ void adj_udag_pair(const DF2 (&c)[8], float s0, float s1, float4 &a, float4 &b) {
+    if constexpr (BODY == kDfSignDiag) {  // diag(+-1, +-1): exact sign flips
+        a = make_float4(a.x * s0, a.y * s0, a.z * s0, a.w * s0);
+        b = make_float4(b.x * s1, b.y * s1, b.z * s1, b.w * s1);
+    } else if constexpr (BODY == B_PERM) {
+        const float4 t = a;
+        a = b;
+        b = t;
+    } else {
+        DF2 x{f2_pack(a.x, a.y), f2_pack(a.z, a.w)}, y{f2_pack(b.x, b.y), f2_pack(b.z, b.w)};
+        body1_df2<BODY>(c, x, y);
+        a = make_float4(f2_x(x.hi), f2_y(x.hi), f2_x(x.lo), f2_y(x.lo));
+        b = make_float4(f2_x(y.hi), f2_y(y.hi), f2_x(y.lo), f2_y(y.lo));
+    }
+}
+
 template <int BODY, int GK, int NB>
 __device__ __forceinline__ void adj_block_step(float4 *kt, float4 *const (&bt)[kAdjBlockBras], int E, const AStep &st,
                                                DF (&acc)[kAdjBlockBras]) {
@@ -715,6 +736,9 @@ __device__ __forceinline__ void adj_block_step(float4 *kt, float4 *const (&bt)[k
 #pragma unroll
         for (int i = 0; i < 8; i++) g[i] = st.g[i];
     }
+    DF2 c[8];
+    if constexpr (BODY != kDfSignDiag && BODY != B_PERM) df2_coeffs(u, c);
+    const float s0 = u[0].hi, s1 = u[6].hi;
     const uint32_t holes = st.in_mask | (1u << st.q);
     const int nfree = E >> __popc(holes);
     PairWalk w(holes, threadIdx.x, kAdjBlockThreads);
@@ -722,21 +746,23 @@ __device__ __forceinline__ void adj_block_step(float4 *kt, float4 *const (&bt)[k
         const int e0 = int(w.x | st.in_val);
         const int e1 = e0 | (1 << st.q);
         w.step();
-        const int s0 = swz<double>(e0), s1 = swz<double>(e1);
-        const float4 ka = kt[s0], kb = kt[s1];
-        DF kv[4] = {DF{ka.x, ka.y}, DF{ka.z, ka.w}, DF{kb.x, kb.y}, DF{kb.z, kb.w}};
+        const int s0i = swz<double>(e0), s1i = swz<double>(e1);
+        float4 ka = kt[s0i], kb = kt[s1i];
+        const DF kv[4] = {DF{ka.x, ka.z}, DF{ka.y, ka.w}, DF{kb.x, kb.z}, DF{kb.y, kb.w}};
 #pragma unroll
         for (int b = 0; b < NB; b++) {
-            const float4 ba = bt[b][s0], bb = bt[b][s1];
-            DF bv[4] = {DF{ba.x, ba.y}, DF{ba.z, ba.w}, DF{bb.x, bb.y}, DF{bb.z, bb.w}};
-            if constexpr (GK != G_NONE) acc[b] = df_sum<2>({acc[b], gexp_df<GK>(g, bv, kv)});
-            body1_dfv<BODY>(u, bv[0], bv[1], bv[2], bv[3]);
-            bt[b][s0] = make_float4(bv[0].hi, bv[0].lo, bv[1].hi, bv[1].lo);
-            bt[b][s1] = make_float4(bv[2].hi, bv[2].lo, bv[3].hi, bv[3].lo);
+            float4 ba = bt[b][s0i], bb = bt[b][s1i];
+            if constexpr (GK != G_NONE) {
+                const DF bv[4] = {DF{ba.x, ba.z}, DF{ba.y, ba.w}, DF{bb.x, bb.z}, DF{bb.y, bb.w}};
+                acc[b] = df_sum<2>({acc[b], gexp_df<GK>(g, bv, kv)});
+            }
+            adj_udag_pair<BODY>(c, s0, s1, ba, bb);
+            bt[b][s0i] = ba;
+            bt[b][s1i] = bb;
         }
-        body1_dfv<BODY>(u, kv[0], kv[1], kv[2], kv[3]);
-        kt[s0] = make_float4(kv[0].hi, kv[0].lo, kv[1].hi, kv[1].lo);
-        kt[s1] = make_float4(kv[2].hi, kv[2].lo, kv[3].hi, kv[3].lo);
+        adj_udag_pair<BODY>(c, s0, s1, ka, kb);
+        kt[s0i] = ka;
+        kt[s1i] = kb;
     }
 }
 
@@ -800,13 +826,14 @@ __global__ void __launch_bounds__(kAdjBlockThreads, 3) adjoint_block_kernel(cons
         asm volatile("cp.async.commit_group;" ::: "memory");
         asm volatile("cp.async.wait_group 0;" ::: "memory");
         __syncthreads();
-        // complex128 -> float-float in place (same 16 bytes per amplitude)
-        for (int e = threadIdx.x; e < E * (NB + 1); e += kAdjBlockThreads) {
-            const double2 v = reinterpret_cast<const double2 *>(kt)[e];
-            const DF r = df_from_double(v.x), i = df_from_double(v.y);
-            kt[e] = make_float4(r.hi, r.lo, i.hi, i.lo);
+        if (!p.in_ff) {  // complex128 -> float-float in place (same 16 bytes per amplitude)
+            for (int e = threadIdx.x; e < E * (NB + 1); e += kAdjBlockThreads) {
+                const double2 v = reinterpret_cast<const double2 *>(kt)[e];
+                const DF r = df_from_double(v.x), i = df_from_double(v.y);
+                kt[e] = make_float4(r.hi, i.hi, r.lo, i.lo);
+            }
+            __syncthreads();
         }
-        __syncthreads();
         for (int si = 0; si < p.nsteps; si++) {
             const AStep &st = p.steps[si];
             if ((uint64_t(base) & st.out_mask) != st.out_val) continue;  // tile-uniform
@@ -828,15 +855,21 @@ __global__ void __launch_bounds__(kAdjBlockThreads, 3) adjoint_block_kernel(cons
             }
             __syncthreads();
         }
-        // float-float -> complex128, streamed out
+        // streamed out: float-float as it is, or converted to complex128
         for (int e = threadIdx.x; e < E; e += kAdjBlockThreads) {
             const I gi = base + p.hi_off[e >> p.m] + I(e & lowmask);
             const float4 v = kt[swz<double>(e)];
-            __stcs(&p.ket[gi], make_double2(df_to_double(DF{v.x, v.y}), df_to_double(DF{v.z, v.w})));
+            if (p.out_ff) {
+                __stcs(reinterpret_cast<float4 *>(&p.ket[gi]), v);
 #pragma unroll
-            for (int b = 0; b < NB; b++) {
-                const float4 x = bt[b][swz<double>(e)];
-                __stcs(&p.bras[b][gi], make_double2(df_to_double(DF{x.x, x.y}), df_to_double(DF{x.z, x.w})));
+                for (int b = 0; b < NB; b++) __stcs(reinterpret_cast<float4 *>(&p.bras[b][gi]), bt[b][swz<double>(e)]);
+            } else {
+                __stcs(&p.ket[gi], make_double2(df_to_double(DF{v.x, v.z}), df_to_double(DF{v.y, v.w})));
+#pragma unroll
+                for (int b = 0; b < NB; b++) {
+                    const float4 x = bt[b][swz<double>(e)];
+                    __stcs(&p.bras[b][gi], make_double2(df_to_double(DF{x.x, x.z}), df_to_double(DF{x.y, x.w})));
+                }
             }
         }
         __syncthreads();
@@ -1195,10 +1228,29 @@ __global__ void __launch_bounds__(kSweepThreads, 1)
     }
 }
 
+// A complex128 state converted in place between complex128 and float-float
+// (re.hi, im.hi, re.lo, im.lo) per amplitude.
+__global__ void __launch_bounds__(256) state_to_ff_kernel(double2 *sv, uint64_t count) {
+    const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
+    for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < count; i += stride) {
+        const double2 v = sv[i];
+        const DF r = df_from_double(v.x), im = df_from_double(v.y);
+        reinterpret_cast<float4 *>(sv)[i] = make_float4(r.hi, im.hi, r.lo, im.lo);
+    }
+}
+__global__ void __launch_bounds__(256) state_from_ff_kernel(double2 *sv, uint64_t count) {
+    const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
+    for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < count; i += stride) {
+        const float4 v = reinterpret_cast<const float4 *>(sv)[i];
+        sv[i] = make_double2(df_to_double(DF{v.x, v.z}), df_to_double(DF{v.y, v.w}));
+    }
+}
+
 template <class I>
 static lgpu_status_t adjoint_block_t(lgpu_context_t ctx, void *ket, void *const *bras, uint32_t nbras, uint32_t n,
                                      const std::vector<int> &tile_bits, const lgpu_adj_block_step_t *steps,
-                                     uint32_t nsteps, double *jac, uint32_t stride, bool c64, cudaStream_t s) {
+                                     uint32_t nsteps, double *jac, uint32_t stride, bool c64, uint32_t ff_flags,
+                                     cudaStream_t s) {
     const int k = int(tile_bits.size());
     std::vector<int> pos(n, -1);
     for (int q = 0; q < k; q++) pos[size_t(tile_bits[size_t(q)])] = q;
@@ -1212,6 +1264,8 @@ static lgpu_status_t adjoint_block_t(lgpu_context_t ctx, void *ket, void *const 
     p->k = k;
     p->m = m;
     p->nb = int(nbras);
+    p->in_ff = (ff_flags & LGPU_FF_IN) ? 1 : 0;
+    p->out_ff = (ff_flags & LGPU_FF_OUT) ? 1 : 0;
     for (int h = 0; h < (1 << (k - m)); h++) {
         uint64_t o = 0;
         for (int q = m; q < k; q++)
@@ -1331,15 +1385,28 @@ lgpu_status_t lgpu_adjoint_step(lgpu_context_t ctx, void *ket, void *const *bras
 }
 
 
-lgpu_status_t lgpu_adjoint_block(lgpu_context_t ctx, void *ket, void *const *bras, uint32_t nbras, uint32_t n,
-                                 lgpu_dtype_t dt, uint32_t k, const int32_t *tile_bits,
-                                 const lgpu_adj_block_step_t *steps, uint32_t nsteps, double *jac_dev,
-                                 uint32_t jac_stride, lgpu_stream_t stream) {
+lgpu_status_t lgpu_adjoint_block_ff(lgpu_context_t ctx, void *ket, void *const *bras, uint32_t nbras, uint32_t n,
+                                    lgpu_dtype_t dt, uint32_t k, const int32_t *tile_bits,
+                                    const lgpu_adj_block_step_t *steps, uint32_t nsteps, double *jac_dev,
+                                    uint32_t jac_stride, uint32_t ff_flags, lgpu_stream_t stream) {
     LGPU_TRY(check_state(ket, n, dt));
     if (nbras < 1 || nbras > uint32_t(kAdjBlockBras) || !bras)
         return fail(LGPU_ERR_INVALID_ARG, "adjoint block: 1 or 2 bras");
     for (uint32_t b = 0; b < nbras; b++) LGPU_TRY(check_state(bras[b], n, dt));
-    if (nsteps == 0) return LGPU_OK;
+    if (ff_flags & ~uint32_t(LGPU_FF_IN | LGPU_FF_OUT)) return fail(LGPU_ERR_INVALID_ARG, "adjoint block: unknown flags");
+    if (ff_flags && dt != LGPU_C128)
+        return fail(LGPU_ERR_INVALID_ARG, "adjoint block: float-float states are complex128 only");
+    if (nsteps == 0) {
+        // nothing to apply; the states still take the requested form
+        if ((ff_flags & LGPU_FF_IN) != 0 && (ff_flags & LGPU_FF_OUT) == 0) {
+            LGPU_TRY(lgpu_state_ff(ket, n, 0, stream));
+            for (uint32_t b = 0; b < nbras; b++) LGPU_TRY(lgpu_state_ff(bras[b], n, 0, stream));
+        } else if ((ff_flags & LGPU_FF_IN) == 0 && (ff_flags & LGPU_FF_OUT) != 0) {
+            LGPU_TRY(lgpu_state_ff(ket, n, 1, stream));
+            for (uint32_t b = 0; b < nbras; b++) LGPU_TRY(lgpu_state_ff(bras[b], n, 1, stream));
+        }
+        return LGPU_OK;
+    }
     if (!steps || nsteps > uint32_t(kAdjBlockSteps)) return fail(LGPU_ERR_INVALID_ARG, "adjoint block: 1 to 48 steps");
     if (k < 1 || k > 11 || k > n) return fail(LGPU_ERR_INVALID_ARG, "adjoint block: tile of 1 to 11 bits");
     if (!jac_dev || jac_stride < nbras) return fail(LGPU_ERR_INVALID_ARG, "adjoint block: Jacobian output");
@@ -1350,8 +1417,31 @@ lgpu_status_t lgpu_adjoint_block(lgpu_context_t ctx, void *ket, void *const *bra
         return fail(LGPU_ERR_INVALID_ARG, "tile bits must be distinct");
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
     const bool c64 = dt == LGPU_C64;
-    return n <= 32 ? adjoint_block_t<uint32_t>(ctx, ket, bras, nbras, n, tb, steps, nsteps, jac_dev, jac_stride, c64, s)
-                   : adjoint_block_t<uint64_t>(ctx, ket, bras, nbras, n, tb, steps, nsteps, jac_dev, jac_stride, c64, s);
+    return n <= 32 ? adjoint_block_t<uint32_t>(ctx, ket, bras, nbras, n, tb, steps, nsteps, jac_dev, jac_stride, c64,
+                                               ff_flags, s)
+                   : adjoint_block_t<uint64_t>(ctx, ket, bras, nbras, n, tb, steps, nsteps, jac_dev, jac_stride, c64,
+                                               ff_flags, s);
+}
+
+lgpu_status_t lgpu_adjoint_block(lgpu_context_t ctx, void *ket, void *const *bras, uint32_t nbras, uint32_t n,
+                                 lgpu_dtype_t dt, uint32_t k, const int32_t *tile_bits,
+                                 const lgpu_adj_block_step_t *steps, uint32_t nsteps, double *jac_dev,
+                                 uint32_t jac_stride, lgpu_stream_t stream) {
+    return lgpu_adjoint_block_ff(ctx, ket, bras, nbras, n, dt, k, tile_bits, steps, nsteps, jac_dev, jac_stride, 0,
+                                 stream);
+}
+
+lgpu_status_t lgpu_state_ff(void *sv, uint32_t n, int to_ff, lgpu_stream_t stream) {
+    LGPU_TRY(check_state(sv, n, LGPU_C128));
+    const uint64_t count = uint64_t(1) << n;
+    const unsigned g = grid_for(count, 256, 8, 8);
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    if (to_ff)
+        state_to_ff_kernel<<<g, 256, 0, s>>>(static_cast<double2 *>(sv), count);
+    else
+        state_from_ff_kernel<<<g, 256, 0, s>>>(static_cast<double2 *>(sv), count);
+    LGPU_CHECK_LAUNCH();
+    return LGPU_OK;
 }
 
 uint32_t lgpu_adjoint_sweep_max_qubits(lgpu_dtype_t dt) { return dt == LGPU_C128 ? 12u : 13u; }

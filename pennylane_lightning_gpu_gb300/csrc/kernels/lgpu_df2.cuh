@@ -28,11 +28,13 @@ __device__ __forceinline__ F2 f2_pack(float a, float b) {
 __device__ __forceinline__ float f2_x(F2 a) {
     float x, y;
     asm("mov.b64 {%0, %1}, %2;" : "=f"(x), "=f"(y) : "l"(a.v));
+    (void)y;
     return x;
 }
 __device__ __forceinline__ float f2_y(F2 a) {
     float x, y;
     asm("mov.b64 {%0, %1}, %2;" : "=f"(x), "=f"(y) : "l"(a.v));
+    (void)x;
     return y;
 }
 __device__ __forceinline__ F2 f2_mul(F2 a, F2 b) {

@@ -1,0 +1,163 @@
+"""Float-float form of complex128 states through the C ABI: the in-place
+conversion lgpu_state_ff, and adjoint blocks that read and leave lambda and
+the bras in that form (lgpu_adjoint_block_ff) against the same blocks on
+complex128 states (lgpu_adjoint_block).
+
+Tolerances: the float-float split keeps 48 of the 53 significand bits, so a
+round trip changes an amplitude by at most 2^-47 of its magnitude; the two
+block paths apply the same float-float arithmetic to the same values and
+agree to 1e-13 (states and Jacobian entries).
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+LGPU_OK, LGPU_ERR_INVALID_ARG = 0, 1
+C64, C128 = 0, 1
+FF_IN, FF_OUT = 1, 2
+
+
+class Step(ctypes.Structure):
+    _fields_ = [("tgt", ctypes.c_int32), ("nctrl", ctypes.c_int32), ("ctrl", ctypes.c_int32 * 2),
+                ("ctrl_val", ctypes.c_int32 * 2), ("gen_kind", ctypes.c_int32), ("col", ctypes.c_int32),
+                ("u", ctypes.c_double * 8), ("g", ctypes.c_double * 8)]
+
+
+def _lib():
+    import pennylane_lightning_gpu_gb300 as pkg
+
+    pkg.build()
+    lib = ctypes.CDLL(pkg.library_path())
+    vp, u32, i32 = ctypes.c_void_p, ctypes.c_uint32, ctypes.c_int
+    lib.lgpu_context_create.argtypes = [i32, ctypes.POINTER(vp)]
+    lib.lgpu_context_destroy.argtypes = [vp]
+    lib.lgpu_state_ff.argtypes = [vp, u32, i32, vp]
+    block = [vp, vp, ctypes.POINTER(vp), u32, u32, i32, u32, ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(Step),
+             u32, vp, u32]
+    lib.lgpu_adjoint_block.argtypes = block + [vp]
+    lib.lgpu_adjoint_block_ff.argtypes = block + [u32, vp]
+    return lib
+
+
+def _state(n, seed):
+    rng = np.random.default_rng(seed)
+    v = rng.normal(size=1 << n) + 1j * rng.normal(size=1 << n)
+    return v / np.linalg.norm(v)
+
+
+def _mat(m):
+    out = (ctypes.c_double * 8)()
+    for i, z in enumerate(np.asarray(m, np.complex128).ravel()):
+        out[2 * i], out[2 * i + 1] = z.real, z.imag
+    return out
+
+
+def _steps(rng, n):
+    """A run of 1-target steps on tile bits 0..10: RY and RX with generators
+    (Jacobian columns 0, 1, 2), a CZ as a controlled sign flip, a general
+    dense U^dag with a dense generator, and an RZ."""
+    def ry(t):
+        c, s = np.cos(t / 2), np.sin(t / 2)
+        return np.array([[c, s], [-s, c]])
+
+    def rx(t):
+        c, s = np.cos(t / 2), np.sin(t / 2)
+        return np.array([[c, 1j * s], [1j * s, c]])
+
+    y = np.array([[0, -1j], [1j, 0]])
+    x = np.array([[0, 1], [1, 0]])
+    q, _ = np.linalg.qr(rng.normal(size=(2, 2)) + 1j * rng.normal(size=(2, 2)))
+    h = rng.normal(size=(2, 2)) + 1j * rng.normal(size=(2, 2))
+    h = h + h.conj().T
+    spec = [(0, [], ry(0.7), y, 0), (3, [], rx(1.9), x, 1), (2, [(1, 1)], np.diag([1, -1]), None, -1),
+            (7, [(n - 1, 0)], q, h, 2), (10, [], np.diag([np.exp(-0.4j), np.exp(0.4j)]), None, -1)]
+    steps = (Step * len(spec))()
+    for s, (tgt, ctrls, u, g, col) in zip(steps, spec):
+        s.tgt = tgt
+        s.nctrl = len(ctrls)
+        for i, (c, v) in enumerate(ctrls):
+            s.ctrl[i], s.ctrl_val[i] = c, v
+        s.u = _mat(u)
+        s.gen_kind = 0 if g is not None else -1
+        s.col = col if g is not None else 0
+        if g is not None:
+            s.g = _mat(g)
+    return steps
+
+
+@pytest.mark.parametrize("n", [12, 20])
+def test_state_ff_round_trip(n):
+    import torch
+
+    lib = _lib()
+    psi = _state(n, 5 + n)
+    psi[3] = 0.0  # zero amplitudes stay zero
+    d = torch.from_numpy(psi.copy()).cuda()
+    stream = torch.cuda.current_stream().cuda_stream
+    assert lib.lgpu_state_ff(d.data_ptr(), n, 1, stream) == LGPU_OK
+    f = d.view(torch.float32).reshape(-1, 4).cpu().numpy().astype(np.float64)  # (re.hi, im.hi, re.lo, im.lo)
+    re, im = f[:, 0] + f[:, 2], f[:, 1] + f[:, 3]
+    assert np.all(np.abs(re - psi.real) <= 2.0 ** -47 * np.abs(psi.real) + 1e-300)
+    assert np.all(np.abs(im - psi.imag) <= 2.0 ** -47 * np.abs(psi.imag) + 1e-300)
+    assert lib.lgpu_state_ff(d.data_ptr(), n, 0, stream) == LGPU_OK
+    back = d.cpu().numpy()
+    assert np.max(np.abs(back - psi)) <= 2.0 ** -46 * np.max(np.abs(psi))
+    assert back[3] == 0.0
+
+
+@pytest.mark.parametrize("nbras", [1, 2])
+def test_adjoint_block_ff_matches_complex128_blocks(nbras):
+    """Two consecutive blocks: complex128 in and out of each, against
+    float-float out of the first, in and out of the second, converted back."""
+    import torch
+
+    lib = _lib()
+    n = 18
+    rng = np.random.default_rng(40 + nbras)
+    steps = _steps(rng, n)
+    tile = (ctypes.c_int32 * 11)(*range(11))
+    stream = torch.cuda.current_stream().cuda_stream
+    ket0 = _state(n, 1)
+    bras0 = [_state(n, 2 + b) for b in range(nbras)]
+    ctx = ctypes.c_void_p()
+    assert lib.lgpu_context_create(0, ctypes.byref(ctx)) == LGPU_OK
+    try:
+        results = []
+        for ff in (False, True):
+            ket = torch.from_numpy(ket0.copy()).cuda()
+            bras = [torch.from_numpy(b.copy()).cuda() for b in bras0]
+            bptr = (ctypes.c_void_p * nbras)(*[b.data_ptr() for b in bras])
+            jac = torch.zeros(2 * 3 * nbras, dtype=torch.float64, device="cuda")
+            for blk in range(2):
+                out = jac.data_ptr() + blk * 3 * nbras * 8
+                if ff:
+                    flags = (FF_IN if blk else 0) | FF_OUT
+                    st = lib.lgpu_adjoint_block_ff(ctx, ket.data_ptr(), bptr, nbras, n, C128, 11, tile, steps,
+                                                   len(steps), out, nbras, flags, stream)
+                else:
+                    st = lib.lgpu_adjoint_block(ctx, ket.data_ptr(), bptr, nbras, n, C128, 11, tile, steps,
+                                                len(steps), out, nbras, stream)
+                assert st == LGPU_OK
+            if ff:
+                assert lib.lgpu_state_ff(ket.data_ptr(), n, 0, stream) == LGPU_OK
+                for b in bras:
+                    assert lib.lgpu_state_ff(b.data_ptr(), n, 0, stream) == LGPU_OK
+            torch.cuda.synchronize()
+            results.append((ket.cpu().numpy(), [b.cpu().numpy() for b in bras], jac.cpu().numpy()))
+        (k0, b0, j0), (k1, b1, j1) = results
+        assert np.max(np.abs(k0 - k1)) < 1e-13
+        for x, y in zip(b0, b1):
+            assert np.max(np.abs(x - y)) < 1e-13
+        assert np.max(np.abs(j0 - j1)) < 1e-13
+        assert np.max(np.abs(j0)) > 1e-3  # the generators' overlaps are not all zero
+        # complex64 states have no float-float form
+        d = torch.zeros(1 << 10, dtype=torch.complex64, device="cuda")
+        dp = (ctypes.c_void_p * 1)(d.data_ptr())
+        assert lib.lgpu_adjoint_block_ff(ctx, d.data_ptr(), dp, 1, 10, C64, 10,
+                                         (ctypes.c_int32 * 10)(*range(10)), steps, len(steps),
+                                         jac.data_ptr(), 1, FF_OUT, stream) == LGPU_ERR_INVALID_ARG
+    finally:
+        lib.lgpu_context_destroy(ctx)
