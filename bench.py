@@ -938,7 +938,8 @@ def profile_case(name):
     sum_i Z_i on a 25-qubit complex128 state), adjoint (12-qubit
     complex128, 4 layers, 12 PauliZ observables), adjblock (24-qubit
     complex128, 2 layers of RY, RZ + CZ ladder, one PauliZ observable: the
-    fused adjoint blocks)."""
+    fused adjoint blocks), adjoint24 (the 24-qubit, 384-parameter forward +
+    adjoint backward through torch.autograd, once: for a launch list)."""
     import pennylane_lightning_gpu_gb300 as pkg
     from pennylane_lightning_gpu_gb300 import batched, workloads
 
@@ -998,6 +999,17 @@ def profile_case(name):
                                    [np.zeros(0, np.complex128) for o in raw])
         obs = [m.NamedObsGPU_C128("PauliZ", [w]) for w in range(n)]
         adj.adjoint_jacobian(sv, obs, opsd, list(range(3 * n * 4)))
+    elif name == "adjoint24":
+        import torch
+
+        from pennylane_lightning_gpu_gb300 import torch_adjoint as TA
+        from pennylane_lightning_gpu_gb300.lightning_gpu import LightningGPU
+
+        terms, pvals = workloads.adjoint_24q_workload(24, 8)
+        f = TA.expval_function(TA.ry_rz_cz_template(24, 8), [TA.pauli_hamiltonian(terms)], LightningGPU(24))
+        params = torch.tensor(pvals, dtype=torch.float64, requires_grad=True)
+        f(params).sum().backward()
+        torch.cuda.synchronize()
     elif name == "adjblock":
         n, layers = 24, 2
         raw = workloads.ry_rz_cz_ansatz(n, layers, np.random.default_rng(3))
@@ -1026,7 +1038,7 @@ def main():
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-serving", action="store_true")
     ap.add_argument("--case", choices=["fused", "fused128", "gram", "batch", "pauli", "pauli128", "adjoint", "adjblock",
-                                       "dense6"],
+                                       "adjoint24", "dense6"],
                     default=None,
                     help="run one small secondary-kernel case (profiling) and exit")
     ap.add_argument("--only", choices=["batched", "serving", "circuits", "tensor_core"], default=None,
