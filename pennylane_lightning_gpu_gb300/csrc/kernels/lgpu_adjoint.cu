@@ -1032,13 +1032,18 @@ __global__ void __launch_bounds__(kAdjBlockThreads, 3) adjoint_block_f32_kernel(
 }
 
 // jac[col[s] * stride + b] = sum over CTAs (in CTA order) of the partials.
+// One warp per (slot, bra): lane l sums the CTAs l, l + 32, ... in order, then
+// a fixed shuffle tree adds the lanes (the same order every run).
 __global__ void adjoint_block_reduce(const double *__restrict__ partials, int nctas, int nslots, int nb,
                                      const int *__restrict__ cols, double *__restrict__ jac, int stride) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= nslots * nb) return;
+    const int i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    const int lane = threadIdx.x & 31;
+    if (i >= nslots * nb) return;  // whole warps leave together
     double t = 0.0;
-    for (int c = 0; c < nctas; c++) t += partials[size_t(c) * nslots * nb + i];
-    jac[size_t(cols[i / nb]) * stride + (i % nb)] = t;
+    for (int c = lane; c < nctas; c += 32) t += partials[size_t(c) * nslots * nb + i];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    if (lane == 0) jac[size_t(cols[i / nb]) * stride + (i % nb)] = t;
 }
 
 // ---------------------------------------------------------------------------
@@ -1348,8 +1353,8 @@ static lgpu_status_t adjoint_block_t(lgpu_context_t ctx, void *ket, void *const 
     LGPU_CHECK_LAUNCH();
     if (!cols.empty()) {
         const int total = p->nslots * int(nbras);
-        adjoint_block_reduce<<<(total + 127) / 128, 128, 0, s>>>(p->partials, int(grid), p->nslots, int(nbras), dcols,
-                                                                 jac, int(stride));
+        adjoint_block_reduce<<<(total + 3) / 4, 128, 0, s>>>(p->partials, int(grid), p->nslots, int(nbras), dcols, jac,
+                                                             int(stride));
         LGPU_CHECK_LAUNCH();
     }
     return LGPU_OK;

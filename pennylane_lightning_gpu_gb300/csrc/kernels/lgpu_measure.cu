@@ -1069,13 +1069,16 @@ __global__ void __launch_bounds__(kPauliTileThreads, 3) pauli_tile_kernel(const 
     }
 }
 
-// out[t] = sum over CTAs (in CTA order) of the partials.
+// out[t] = the sum over CTAs of the partials: one warp per word, lane l sums
+// the CTAs l, l + 32, ... in order, then a fixed shuffle tree adds the lanes.
 __global__ void pauli_tile_reduce(const double *__restrict__ partials, int nctas, int nw, double *__restrict__ out) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= nw) return;
+    const int t = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (t >= nw) return;  // whole warps leave together
     double v = 0.0;
-    for (int c = 0; c < nctas; c++) v += partials[size_t(c) * nw + t];
-    out[t] = v;
+    for (int c = lane; c < nctas; c += 32) v += partials[size_t(c) * nw + t];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) out[t] = v;
 }
 
 // Raw sums of the words (as the Walsh-Hadamard pass defines them) by tile
@@ -1204,7 +1207,7 @@ static lgpu_status_t pauli_tile_raw(lgpu_context_t ctx, const void *sv, uint32_t
             pauli_tile_kernel<T, I, false><<<grid, kPauliTileThreads, smem, s>>>(*b);
         }
         LGPU_CHECK_LAUNCH();
-        pauli_tile_reduce<<<1, kTileWords, 0, s>>>(partials, int(grid), b->nw, results + pi * kTileWords);
+        pauli_tile_reduce<<<1, 32 * kTileWords, 0, s>>>(partials, int(grid), b->nw, results + pi * kTileWords);
         LGPU_CHECK_LAUNCH();
     }
     std::vector<double> host(passes.size() * kTileWords);
@@ -1904,6 +1907,230 @@ __global__ void __launch_bounds__(256)
     }
 }
 
+// ---------------------------------------------------------------------------
+// Pauli sum apply by tile passes (from 16 qubits): the words of a pass (as the
+// expectation tile passes group them) flip only tile bits, so
+// (sum_t c_t P_t in)_e = sum_t c_t sigma_t(e ^ flip_t) in_{e ^ flip_t} needs
+// only the tile of `in`.  A CTA streams tiles of `in` through two shared-memory
+// buffers; each thread forms its output elements e = tid + 256 j in registers
+// over the pass's words (the source index e ^ flip = (tid ^ flip's low 8 bits)
+// | ((j << 8) ^ flip's high bits), so the address is a per-thread base plus a
+// per-word constant, and the sign a per-thread bit XOR a per-word constant
+// bit) and adds them to `out`.  complex128 works in float-float: the tile is
+// converted after its load, the products and sums run as paired lanes
+// (re, im), and `out` holds float-float values (re.hi, im.hi, re.lo, im.lo)
+// from the first pass to the last, then is converted back once.  complex64
+// works in FP32.  Replaces one FP64-bound pass per distinct flip mask.
+// ---------------------------------------------------------------------------
+template <class I> struct PauliApplyParams {
+    const void *in;
+    void *out;
+    Holes holes;
+    I ntiles;
+    int m, nw, accumulate;
+    I hi_off[1 << kTileHiMax];
+    uint32_t xlo[kTileWords];               // flip bits below bit 8 (tile positions)
+    uint32_t tsign[kTileWords];             // sign mask in tile positions
+    uint64_t osign[kTileWords];             // sign mask outside the tile (state bits)
+    uint32_t ja[kTileWords][kPtMaxNA];      // ((j << 8) ^ flip bits from bit 8) times the element bytes
+    uint32_t cs[kTileWords][kPtMaxNA];      // bit 31: parity of (((j << 8) ^ flip bits from bit 8) & sign mask)
+    float c[kTileWords][4];                 // c_t i^ny_t: (re.hi, im.hi, re.lo, im.lo); complex64 (re, im, -, -)
+};
+
+template <class T, class I>
+__global__ void __launch_bounds__(kPauliTileThreads, 3) pauli_apply_tile_kernel(const PauliApplyParams<I> p) {
+    using Gm = PtGeom<T>;
+    constexpr int E = Gm::E, NA = Gm::NA, EB = 1 << Gm::LEB;
+    extern __shared__ __align__(128) unsigned char pa_smem[];
+    const int tid = threadIdx.x;
+    const uint32_t lowmask = (1u << p.m) - 1u;
+    constexpr int EPC = sizeof(T) == 4 ? 2 : 1;   // amplitudes per 16-byte chunk
+    constexpr int GEB = sizeof(T) == 4 ? 8 : 16;  // bytes per amplitude in the state
+    const unsigned char *src = static_cast<const unsigned char *>(p.in);
+    auto load = [&](I tau, unsigned char *dst) {
+        const I base = insert_holes<I>(tau, p.holes);
+        for (int c = tid; c < E / EPC; c += kPauliTileThreads) {
+            const uint32_t e = uint32_t(c * EPC);
+            const I gi = base + p.hi_off[e >> p.m] + I(e & lowmask);
+            pt_cp_async16(dst + size_t(e) * EB, src + size_t(gi) * GEB);
+        }
+        asm volatile("cp.async.commit_group;" ::: "memory");
+    };
+    const I G = I(gridDim.x);
+    I tau = blockIdx.x;
+    if (tau < p.ntiles) load(tau, pa_smem);
+    else asm volatile("cp.async.commit_group;" ::: "memory");
+    for (int it = 0; tau < p.ntiles; tau += G, it++) {
+        unsigned char *cur = pa_smem + (it & 1) * (E * EB);
+        if (tau + G < p.ntiles) load(tau + G, pa_smem + ((it + 1) & 1) * (E * EB));
+        else asm volatile("cp.async.commit_group;" ::: "memory");
+        asm volatile("cp.async.wait_group 1;" ::: "memory");
+        __syncthreads();
+        if constexpr (sizeof(T) == 8) {  // complex128 -> float-float in place
+#pragma unroll 4
+            for (int j = 0; j < NA; j++) {
+                const int e = tid + j * kPauliTileThreads;
+                const double2 v = reinterpret_cast<const double2 *>(cur)[e];
+                const DF r = df_from_double(v.x), im = df_from_double(v.y);
+                reinterpret_cast<float4 *>(cur)[e] = make_float4(r.hi, im.hi, r.lo, im.lo);
+            }
+            __syncthreads();
+        }
+        const I base = insert_holes<I>(tau, p.holes);
+        // per word: this thread's source base and sign bit for the tile
+        uint32_t xb[kTileWords], ps[kTileWords];
+#pragma unroll
+        for (int t = 0; t < kTileWords; t++) {
+            const uint32_t x = uint32_t(tid) ^ p.xlo[t];
+            xb[t] = x << Gm::LEB;
+            ps[t] = uint32_t(__popc(x & p.tsign[t]) + __popcll(uint64_t(base) & p.osign[t])) << 31;
+        }
+#pragma unroll 2
+        for (int j = 0; j < NA; j++) {
+            const int e = tid + j * kPauliTileThreads;
+            const I gi = base + p.hi_off[uint32_t(e) >> p.m] + I(uint32_t(e) & lowmask);
+            if constexpr (sizeof(T) == 4) {
+                float ar = 0.0f, ai = 0.0f;
+#pragma unroll
+                for (int t = 0; t < kTileWords; t++) {
+                    if (t >= p.nw) break;
+                    const float2 x = *reinterpret_cast<const float2 *>(cur + xb[t] + p.ja[t][j]);
+                    const uint32_t sb = ps[t] ^ p.cs[t][j];
+                    const float xr = pt_flip_sign(x.x, sb), xi = pt_flip_sign(x.y, sb);
+                    const float cr = p.c[t][0], ci = p.c[t][1];
+                    ar = fmaf(cr, xr, fmaf(-ci, xi, ar));
+                    ai = fmaf(cr, xi, fmaf(ci, xr, ai));
+                }
+                float2 *o = static_cast<float2 *>(p.out) + gi;
+                if (p.accumulate) {
+                    const float2 v = *o;
+                    ar += v.x;
+                    ai += v.y;
+                }
+                *o = make_float2(ar, ai);
+            } else {
+                DF2 acc{F2{0ull}, F2{0ull}};
+#pragma unroll
+                for (int t = 0; t < kTileWords; t++) {
+                    if (t >= p.nw) break;
+                    const float4 x = *reinterpret_cast<const float4 *>(cur + xb[t] + p.ja[t][j]);
+                    const uint32_t sb = ps[t] ^ p.cs[t][j];
+                    const float xr = pt_flip_sign(x.x, sb), xi = pt_flip_sign(x.y, sb);
+                    const float xrl = pt_flip_sign(x.z, sb), xil = pt_flip_sign(x.w, sb);
+                    const DF2 X{f2_pack(xr, xi), f2_pack(xrl, xil)}, Xs{f2_pack(xi, xr), f2_pack(xil, xrl)};
+                    // (cr, cr) (xr, xi) + (-ci, ci) (xi, xr) = c x in the lanes (re, im)
+                    const DF2 C1{f2_pack(p.c[t][0], p.c[t][0]), f2_pack(p.c[t][2], p.c[t][2])};
+                    const DF2 C2{f2_pack(-p.c[t][1], p.c[t][1]), f2_pack(-p.c[t][3], p.c[t][3])};
+                    acc = df2_sum<3>({acc, df2_mul(C1, X), df2_mul(C2, Xs)});
+                }
+                float4 *o = static_cast<float4 *>(p.out) + gi;
+                if (p.accumulate) {
+                    const float4 v = *o;
+                    acc = df2_sum<2>({acc, DF2{f2_pack(v.x, v.y), f2_pack(v.z, v.w)}});
+                }
+                *o = make_float4(f2_x(acc.hi), f2_y(acc.hi), f2_x(acc.lo), f2_y(acc.lo));
+            }
+        }
+        __syncthreads();  // `cur` is the target of a load issued next iteration
+    }
+    asm volatile("cp.async.wait_group 0;" ::: "memory");
+}
+
+// out (float-float, (re.hi, im.hi, re.lo, im.lo) per amplitude) -> complex128, in place.
+__global__ void __launch_bounds__(256) ff_to_c128_kernel(double2 *sv, uint64_t count) {
+    const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
+    for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < count; i += stride) {
+        const float4 v = reinterpret_cast<const float4 *>(sv)[i];
+        sv[i] = make_double2(df_to_double(DF{v.x, v.z}), df_to_double(DF{v.y, v.w}));
+    }
+}
+
+// The terms whose flips fit a tile, by tile passes; done[w] = 1 for those.
+// `out` ends as complex128 (the first pass overwrites it).
+template <class T, class I>
+static lgpu_status_t pauli_apply_tiles(const void *in, void *out, uint32_t n, uint32_t nterms, const double *coeffs,
+                                       const uint64_t *flip, const uint64_t *sign, const uint8_t *ny,
+                                       std::vector<char> &done, cudaStream_t s) {
+    using Gm = PtGeom<T>;
+    done.assign(nterms, 0);
+    if (n < uint32_t(Gm::K)) return LGPU_OK;
+    const auto passes = plan_tile_passes(n, nterms, flip, Gm::K, Gm::MMIN);
+    if (passes.empty()) return LGPU_OK;
+    const unsigned grid_cap = unsigned(sm_count()) * 3;
+    static std::atomic<size_t> attr[64];
+    const size_t smem = 2 * size_t(Gm::E) * (size_t(1) << Gm::LEB);
+    LGPU_TRY(ensure_smem(reinterpret_cast<const void *>(pauli_apply_tile_kernel<T, I>), smem, attr));
+    for (size_t pi = 0; pi < passes.size(); pi++) {
+        const TilePass &tp = passes[pi];
+        const int k = int(tp.tile.size());
+        if (k != Gm::K) return fail(LGPU_ERR_UNSUPPORTED, "Pauli tile pass of unexpected size");
+        int m = 0;
+        while (m < k && tp.tile[size_t(m)] == m) m++;
+        auto b = std::make_unique<PauliApplyParams<I>>();
+        std::memset(b.get(), 0, sizeof(PauliApplyParams<I>));
+        b->in = in;
+        b->out = out;
+        b->holes = make_holes(tp.tile);
+        b->ntiles = I(uint64_t(1) << (n - uint32_t(k)));
+        b->m = m;
+        b->nw = int(tp.words.size());
+        b->accumulate = pi > 0 ? 1 : 0;
+        for (int h = 0; h < (1 << (k - m)); h++) {
+            uint64_t o = 0;
+            for (int q = m; q < k; q++)
+                if ((h >> (q - m)) & 1) o |= uint64_t(1) << tp.tile[size_t(q)];
+            b->hi_off[h] = I(o);
+        }
+        for (int t = 0; t < b->nw; t++) {
+            const uint32_t w = tp.words[size_t(t)];
+            uint32_t tf = 0, ts = 0;
+            uint64_t os = sign[w];
+            for (int q = 0; q < k; q++) {
+                const int bit = tp.tile[size_t(q)];
+                if ((flip[w] >> bit) & 1u) tf |= 1u << q;
+                if ((sign[w] >> bit) & 1u) {
+                    ts |= 1u << q;
+                    os &= ~(uint64_t(1) << bit);
+                }
+            }
+            b->xlo[t] = tf & 0xFFu;
+            b->tsign[t] = ts;
+            b->osign[t] = os;
+            for (int j = 0; j < Gm::NA; j++) {
+                const uint32_t J = (uint32_t(j) << 8) ^ (tf & ~0xFFu);
+                b->ja[t][j] = J << Gm::LEB;
+                b->cs[t][j] = uint32_t(__builtin_popcount(J & ts) & 1) << 31;
+            }
+            double cr = coeffs[2 * w], ci = coeffs[2 * w + 1];
+            for (int q = 0; q < (ny[w] & 3); q++) {  // multiply by i
+                const double tr = -ci;
+                ci = cr;
+                cr = tr;
+            }
+            if (sizeof(T) == 8) {
+                const DF r = df_split_host(cr), i = df_split_host(ci);
+                b->c[t][0] = r.hi;
+                b->c[t][1] = i.hi;
+                b->c[t][2] = r.lo;
+                b->c[t][3] = i.lo;
+            } else {
+                b->c[t][0] = float(cr);
+                b->c[t][1] = float(ci);
+            }
+            done[w] = 1;
+        }
+        const unsigned grid = unsigned(std::min<uint64_t>(uint64_t(b->ntiles), grid_cap));
+        pauli_apply_tile_kernel<T, I><<<grid, kPauliTileThreads, smem, s>>>(*b);
+        LGPU_CHECK_LAUNCH();
+    }
+    if (sizeof(T) == 8) {
+        const uint64_t count = uint64_t(1) << n;
+        ff_to_c128_kernel<<<grid_for(count, 256, 8, 8), 256, 0, s>>>(static_cast<double2 *>(out), count);
+        LGPU_CHECK_LAUNCH();
+    }
+    return LGPU_OK;
+}
+
 template <class T>
 static lgpu_status_t pauli_sum_t(const void *in, void *out, uint32_t n, uint32_t nterms, const double *coeffs,
                                  const uint64_t *flip, const uint64_t *sign, const uint8_t *ny, cudaStream_t s) {
@@ -1925,7 +2152,23 @@ static lgpu_status_t pauli_sum_t(const void *in, void *out, uint32_t n, uint32_t
         LGPU_CUDA_TRY(cudaMemsetAsync(out, 0, N * sizeof(cplx_t<T>), s));
         return LGPU_OK;
     }
+    // from 16 qubits the terms whose flips fit a tile go through tile passes
+    // (float-float / FP32); the rest add to `out` one pass per flip mask
+    std::vector<char> done(nterms, 0);
+    if (n >= 16) {
+        const lgpu_status_t st = n <= 32
+                                     ? pauli_apply_tiles<T, uint32_t>(in, out, n, nterms, coeffs, flip, sign, ny, done, s)
+                                     : pauli_apply_tiles<T, uint64_t>(in, out, n, nterms, coeffs, flip, sign, ny, done, s);
+        LGPU_TRY(st);
+        for (uint32_t w = 0; w < nterms; w++)
+            if (done[w]) {
+                first = false;
+                break;
+            }
+    }
     for (size_t gi = 0; gi < keys.size(); gi++) {
+        auto &gw = groups[gi];
+        gw.erase(std::remove_if(gw.begin(), gw.end(), [&](uint32_t w) { return done[w] != 0; }), gw.end());
         for (size_t o = 0; o < groups[gi].size(); o += kSumTerms) {
             PSumParams<T> p{};
             p.flip = keys[gi];

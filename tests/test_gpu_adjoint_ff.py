@@ -1,7 +1,9 @@
 """Float-float form of complex128 states through the C ABI: the in-place
 conversion lgpu_state_ff, and adjoint blocks that read and leave lambda and
 the bras in that form (lgpu_adjoint_block_ff) against the same blocks on
-complex128 states (lgpu_adjoint_block).
+complex128 states (lgpu_adjoint_block).  Also the Pauli-sum apply that builds
+the adjoint's bras from a Hamiltonian (lgpu_apply_pauli_sum: tile passes in
+float-float from 16 qubits) against the formula on the host.
 
 Tolerances: the float-float split keeps 48 of the 53 significand bits, so a
 round trip changes an amplitude by at most 2^-47 of its magnitude; the two
@@ -161,3 +163,70 @@ def test_adjoint_block_ff_matches_complex128_blocks(nbras):
                                          jac.data_ptr(), 1, FF_OUT, stream) == LGPU_ERR_INVALID_ARG
     finally:
         lib.lgpu_context_destroy(ctx)
+
+
+def _pauli_masks(n, words, wires):
+    flip, sign, ny = [], [], []
+    for word, ws in zip(words, wires):
+        f = s = y = 0
+        for ch, w in zip(word, ws):
+            b = 1 << (n - 1 - w)
+            if ch in "XY":
+                f |= b
+            if ch in "YZ":
+                s |= b
+            if ch == "Y":
+                y += 1
+        flip.append(f)
+        sign.append(s)
+        ny.append(y)
+    return flip, sign, ny
+
+
+@pytest.mark.parametrize("dt,dtype,tol", [(C128, np.complex128, 1e-13), (C64, np.complex64, 2e-5)])
+@pytest.mark.parametrize("n", [16, 19])
+def test_apply_pauli_sum_tiles_and_wide_words(n, dt, dtype, tol):
+    """out = sum_t c_t P_t |in> through lgpu_apply_pauli_sum from 16 qubits:
+    words that fit a tile go through the tile passes (float-float for
+    complex128), the 9- and 10-flip words through the per-flip-mask passes
+    added afterwards; against the formula on the host.  Tolerance: absolute,
+    relative to sum_t |c_t| (complex128 1e-13, complex64 2e-5)."""
+    import torch
+
+    lib = _lib()
+    vp, u32, i32 = ctypes.c_void_p, ctypes.c_uint32, ctypes.c_int
+    lib.lgpu_apply_pauli_sum.argtypes = [vp, vp, u32, i32, u32, ctypes.POINTER(ctypes.c_double),
+                                         ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64),
+                                         ctypes.POINTER(ctypes.c_uint8), vp]
+    rng = np.random.default_rng(90 + n)
+    words, wires = ["Z", "ZZ", "XY", "YX", "X", "Y"], [[0], [2, n - 1], [n - 1, n - 2], [0, 1], [n - 9], [3]]
+    while len(words) < 40:
+        k = int(rng.integers(1, 7))
+        wires.append([int(x) for x in rng.choice(n, size=k, replace=False)])
+        words.append("".join(rng.choice(list("XYZ"), size=k)))
+    words += ["XXXXXXXXX", "YXYXYXYXYX"]
+    wires += [list(range(9)), list(range(n - 10, n))]
+    coeffs = rng.normal(size=len(words)) + 1j * rng.normal(size=len(words))
+    flip, sign, ny = _pauli_masks(n, words, wires)
+    psi = _state(n, 7).astype(dtype)
+    din = torch.from_numpy(psi.copy()).cuda()
+    dout = torch.full_like(din, 3.0)  # overwritten by the first pass
+    c = np.ascontiguousarray(np.stack([coeffs.real, coeffs.imag], axis=1).ravel())
+    st = lib.lgpu_apply_pauli_sum(din.data_ptr(), dout.data_ptr(), n, dt, len(words),
+                                  c.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                  (ctypes.c_uint64 * len(words))(*flip), (ctypes.c_uint64 * len(words))(*sign),
+                                  (ctypes.c_uint8 * len(words))(*ny), torch.cuda.current_stream().cuda_stream)
+    assert st == LGPU_OK
+    got = dout.cpu().numpy().astype(np.complex128)
+    ref = np.zeros(1 << n, np.complex128)
+    idx = np.arange(1 << n, dtype=np.int64)
+    p64 = psi.astype(np.complex128)
+    for f, s, y, cf in zip(flip, sign, ny, coeffs):
+        j = idx ^ f
+        par = np.zeros(1 << n, np.int64)
+        m = j & s
+        while np.any(m):
+            par ^= m & 1
+            m >>= 1
+        ref += cf * (1j ** y) * (1 - 2 * par) * p64[j]
+    assert np.max(np.abs(got - ref)) < tol * np.sum(np.abs(coeffs))
