@@ -25,18 +25,8 @@ __device__ __forceinline__ F2 f2_pack(float a, float b) {
     asm("mov.b64 %0, {%1, %2};" : "=l"(r.v) : "f"(a), "f"(b));
     return r;
 }
-__device__ __forceinline__ float f2_x(F2 a) {
-    float x, y;
-    asm("mov.b64 {%0, %1}, %2;" : "=f"(x), "=f"(y) : "l"(a.v));
-    (void)y;
-    return x;
-}
-__device__ __forceinline__ float f2_y(F2 a) {
-    float x, y;
-    asm("mov.b64 {%0, %1}, %2;" : "=f"(x), "=f"(y) : "l"(a.v));
-    (void)x;
-    return y;
-}
+__device__ __forceinline__ float f2_x(F2 a) { return __uint_as_float(static_cast<unsigned>(a.v)); }
+__device__ __forceinline__ float f2_y(F2 a) { return __uint_as_float(static_cast<unsigned>(a.v >> 32)); }
 __device__ __forceinline__ F2 f2_mul(F2 a, F2 b) {
     F2 r;
     asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r.v) : "l"(a.v), "l"(b.v));
