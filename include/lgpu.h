@@ -411,6 +411,13 @@ lgpu_status_t lgpu_adjoint_block_ff(lgpu_context_t ctx, void *ket, void *const *
                                     const lgpu_adj_block_step_t *steps, uint32_t nsteps, double *jac_dev,
                                     uint32_t jac_stride, uint32_t ff_flags, lgpu_stream_t stream);
 lgpu_status_t lgpu_state_ff(void *sv, uint32_t n, int to_ff, lgpu_stream_t stream);
+/* lgpu_apply_fused_block with the same float-float flags (complex128 only): a
+ * run of consecutive blocks keeps the state in float-float form from one
+ * block to the next, so only the first block converts its tiles on load and
+ * only the last converts them back on store. */
+lgpu_status_t lgpu_apply_fused_block_ff(void *sv, uint32_t n, lgpu_dtype_t dt, uint32_t k,
+                                        const int32_t *tile_bits, uint32_t ngates,
+                                        const lgpu_fused_gate_t *gates, uint32_t ff_flags, lgpu_stream_t stream);
 
 /* ---- CUDA graphs (stream capture) ------------------------------------------
  * Capture everything issued on `stream` between begin and end into an

@@ -558,7 +558,13 @@ class StateVectorCudaManaged : public StateVectorCudaBase<Precision, StateVector
         const int kmax = std::min<int>(fusionTileBits(), int(nq()));
         const auto plan = Engine::plan_fusion(descs, nq(), kmax, std::min<int>(fusionMinLowBits(), kmax), 2,
                                               size_t(kFusionMaxHighBits));
-        for (const auto &blk : plan) {
+        // complex128: consecutive fused blocks pass the state on in float-float
+        // form (lgpu_apply_fused_block_ff); the last block of such a run
+        // converts it back
+        const bool ff_ok = dt() == LGPU_C128;
+        bool in_ff = false;
+        for (size_t bi = 0; bi < plan.size(); bi++) {
+            const auto &blk = plan[bi];
             if (blk.tile_bits.empty()) {
                 for (size_t gi : blk.gates) applyDesc(descs[gi]);
                 continue;
@@ -582,8 +588,12 @@ class StateVectorCudaManaged : public StateVectorCudaBase<Precision, StateVector
                 fg.push_back(g);
             }
             std::vector<int32_t> tb(blk.tile_bits.begin(), blk.tile_bits.end());
-            PL_LGPU_IS_SUCCESS(lgpu_apply_fused_block(BaseType::getData(), nq(), dt(), uint32_t(tb.size()), tb.data(),
-                                                      uint32_t(fg.size()), fg.data(), BaseType::lstream()));
+            const bool next_fused = bi + 1 < plan.size() && !plan[bi + 1].tile_bits.empty();
+            const uint32_t ff = ff_ok ? ((in_ff ? LGPU_FF_IN : 0u) | (next_fused ? LGPU_FF_OUT : 0u)) : 0u;
+            PL_LGPU_IS_SUCCESS(lgpu_apply_fused_block_ff(BaseType::getData(), nq(), dt(), uint32_t(tb.size()),
+                                                         tb.data(), uint32_t(fg.size()), fg.data(), ff,
+                                                         BaseType::lstream()));
+            in_ff = ff_ok && next_fused;
         }
     }
 

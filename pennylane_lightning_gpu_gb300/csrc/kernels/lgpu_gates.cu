@@ -15,6 +15,7 @@
 //  * fused_kernel     a block of 1/2-target gates applied to shared-memory
 //                     tiles of 2^k amplitudes: one HBM pass for many gates.
 #include <cstring>
+#include <memory>
 #include <mutex>
 #include <unordered_map>
 
@@ -503,6 +504,7 @@ template <class T, class I> struct FusedParams {
     FGroup groups[kFusedMaxGates];
     T mats[kFusedMatPool];
     KConst kc[kFusedMaxGates][4];  // integer-pipe multipliers (complex128 structured bodies)
+    int in_ff, out_ff;             // float-float path: the state arrives / is left in float-float form
 };
 
 // Amplitudes per thread in a register group: 16 (complex64).  complex128
@@ -797,13 +799,14 @@ __global__ void __launch_bounds__(NT, MINB)
         }
         __syncthreads();  // ... and everyone's
         if constexpr (DFM && sizeof(T) == 8) {
-            // complex128 -> float-float in place (same 16 bytes per amplitude)
-            for (int e = threadIdx.x; e < E; e += NT) {
-                const double2 v = reinterpret_cast<const double2 *>(cur)[e];
-                const DF r = df_from_double(v.x), i = df_from_double(v.y);
-                reinterpret_cast<float4 *>(cur)[e] = make_float4(r.hi, i.hi, r.lo, i.lo);
+            if (!p.in_ff) {  // complex128 -> float-float in place (same 16 bytes per amplitude)
+                for (int e = threadIdx.x; e < E; e += NT) {
+                    const double2 v = reinterpret_cast<const double2 *>(cur)[e];
+                    const DF r = df_from_double(v.x), i = df_from_double(v.y);
+                    reinterpret_cast<float4 *>(cur)[e] = make_float4(r.hi, i.hi, r.lo, i.lo);
+                }
+                __syncthreads();
             }
-            __syncthreads();
         }
         const I base = insert_holes<I>(tau, p.holes);
         fused_tile<T, I, EMU, NT, DFM>(cur, E, base, p);
@@ -815,8 +818,11 @@ __global__ void __launch_bounds__(NT, MINB)
                     __stcs(reinterpret_cast<float4 *>(dst), *reinterpret_cast<const float4 *>(&cur[swz<T>(e)]));
                 } else if constexpr (DFM && sizeof(T) == 8) {
                     const float4 v = reinterpret_cast<const float4 *>(cur)[swz<T>(e)];
-                    __stcs(reinterpret_cast<double2 *>(dst),
-                           make_double2(df_to_double(DF{v.x, v.z}), df_to_double(DF{v.y, v.w})));
+                    if (p.out_ff)
+                        __stcs(reinterpret_cast<float4 *>(dst), v);
+                    else
+                        __stcs(reinterpret_cast<double2 *>(dst),
+                               make_double2(df_to_double(DF{v.x, v.z}), df_to_double(DF{v.y, v.w})));
                 } else {
                     __stcs(dst, cur[swz<T>(e)]);
                 }
@@ -1320,7 +1326,7 @@ static lgpu_status_t launch_fused_df(double2 *sv, const FusedParams<double, I> &
 
 template <class T, class I>
 static lgpu_status_t fused_t(cplx_t<T> *sv, uint32_t n, const std::vector<int> &tile_bits,
-                             uint32_t ngates, const lgpu_fused_gate_t *gates, cudaStream_t s) {
+                             uint32_t ngates, const lgpu_fused_gate_t *gates, uint32_t ff_flags, cudaStream_t s) {
     static_assert(sizeof(FusedParams<T, I>) <= 32000, "fused kernel parameters exceed the 32 KB limit");
     const int k = int(tile_bits.size());
     // Tile position of each state bit
@@ -1342,6 +1348,9 @@ static lgpu_status_t fused_t(cplx_t<T> *sv, uint32_t n, const std::vector<int> &
     }
     const bool emu = sizeof(T) == 8 && f64_mode() == 1;
     const bool dfm = sizeof(T) == 8 && f64_mode() == 1 && fused_df_enabled();
+    std::unique_ptr<FusedParams<T, I>> guard(p);
+    if (!dfm && (ff_flags & LGPU_FF_IN))  // the complex128 kernels need complex128 amplitudes
+        LGPU_TRY(lgpu_state_ff(sv, n, 0, reinterpret_cast<lgpu_stream_t>(s)));
     uint32_t done = 0;
     lgpu_status_t st = LGPU_OK;
     while (done < ngates && st == LGPU_OK) {
@@ -1400,6 +1409,10 @@ static lgpu_status_t fused_t(cplx_t<T> *sv, uint32_t n, const std::vector<int> &
         if (st != LGPU_OK) break;
         p->ngates = cnt;
         p->ngroups = group_fused_gates(p->gates, p->kc, cnt, sizeof(T) == 4 ? k : 0, fused_reg_bits<T>(), p->groups);
+        // float-float path: the first launch reads the state as it arrives, the
+        // last leaves it as asked, launches in between keep float-float
+        p->in_ff = dfm && (done > 0 || (ff_flags & LGPU_FF_IN)) ? 1 : 0;
+        p->out_ff = dfm && (done + uint32_t(cnt) < ngates || (ff_flags & LGPU_FF_OUT)) ? 1 : 0;
         const size_t smem = (size_t(1) << k) * sizeof(cplx_t<T>);
         if constexpr (sizeof(T) == 8)
             st = dfm ? launch_fused_df<I>(sv, *p, smem, s)
@@ -1408,7 +1421,8 @@ static lgpu_status_t fused_t(cplx_t<T> *sv, uint32_t n, const std::vector<int> &
             st = launch_fused<T, I, false>(sv, *p, smem, s);
         done += uint32_t(cnt);
     }
-    delete p;
+    if (st == LGPU_OK && !dfm && (ff_flags & LGPU_FF_OUT))
+        st = lgpu_state_ff(sv, n, 1, reinterpret_cast<lgpu_stream_t>(s));
     return st;
 }
 
@@ -1584,8 +1598,21 @@ lgpu_status_t lgpu_apply_pauli_rotation_multi(void *const *svs, uint32_t nstates
 lgpu_status_t lgpu_apply_fused_block(void *sv, uint32_t n, lgpu_dtype_t dt, uint32_t k,
                                      const int32_t *tile_bits, uint32_t ngates,
                                      const lgpu_fused_gate_t *gates, lgpu_stream_t stream) {
+    return lgpu_apply_fused_block_ff(sv, n, dt, k, tile_bits, ngates, gates, 0, stream);
+}
+
+lgpu_status_t lgpu_apply_fused_block_ff(void *sv, uint32_t n, lgpu_dtype_t dt, uint32_t k,
+                                        const int32_t *tile_bits, uint32_t ngates,
+                                        const lgpu_fused_gate_t *gates, uint32_t ff_flags, lgpu_stream_t stream) {
     LGPU_TRY(check_state(sv, n, dt));
-    if (ngates == 0) return LGPU_OK;
+    if (ff_flags & ~uint32_t(LGPU_FF_IN | LGPU_FF_OUT)) return fail(LGPU_ERR_INVALID_ARG, "fused block: unknown flags");
+    if (ff_flags && dt != LGPU_C128)
+        return fail(LGPU_ERR_INVALID_ARG, "fused block: float-float states are complex128 only");
+    if (ngates == 0) {  // nothing to apply; the state still takes the requested form
+        const bool in = (ff_flags & LGPU_FF_IN) != 0, out = (ff_flags & LGPU_FF_OUT) != 0;
+        if (in != out) return lgpu_state_ff(sv, n, out ? 1 : 0, stream);
+        return LGPU_OK;
+    }
     if (!gates) return fail(LGPU_ERR_INVALID_ARG, "gates is null");
     const uint32_t kmax = dt == LGPU_C128 ? 12u : 13u;
     if (k < 1 || k > kmax || k > n)
@@ -1597,10 +1624,10 @@ lgpu_status_t lgpu_apply_fused_block(void *sv, uint32_t n, lgpu_dtype_t dt, uint
         return fail(LGPU_ERR_INVALID_ARG, "tile bits must be distinct");
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
     if (dt == LGPU_C128)
-        return n <= 32 ? fused_t<double, uint32_t>(static_cast<double2 *>(sv), n, tb, ngates, gates, s)
-                       : fused_t<double, uint64_t>(static_cast<double2 *>(sv), n, tb, ngates, gates, s);
-    return n <= 32 ? fused_t<float, uint32_t>(static_cast<float2 *>(sv), n, tb, ngates, gates, s)
-                   : fused_t<float, uint64_t>(static_cast<float2 *>(sv), n, tb, ngates, gates, s);
+        return n <= 32 ? fused_t<double, uint32_t>(static_cast<double2 *>(sv), n, tb, ngates, gates, ff_flags, s)
+                       : fused_t<double, uint64_t>(static_cast<double2 *>(sv), n, tb, ngates, gates, ff_flags, s);
+    return n <= 32 ? fused_t<float, uint32_t>(static_cast<float2 *>(sv), n, tb, ngates, gates, 0, s)
+                   : fused_t<float, uint64_t>(static_cast<float2 *>(sv), n, tb, ngates, gates, 0, s);
 }
 
 }  // extern "C"

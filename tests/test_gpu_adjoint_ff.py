@@ -1,7 +1,8 @@
 """Float-float form of complex128 states through the C ABI: the in-place
 conversion lgpu_state_ff, and adjoint blocks that read and leave lambda and
 the bras in that form (lgpu_adjoint_block_ff) against the same blocks on
-complex128 states (lgpu_adjoint_block).  Also the Pauli-sum apply that builds
+complex128 states (lgpu_adjoint_block); fused gate blocks that pass the
+state on in that form (lgpu_apply_fused_block_ff).  Also the Pauli-sum apply that builds
 the adjoint's bras from a Hamiltonian (lgpu_apply_pauli_sum: tile passes in
 float-float from 16 qubits) against the formula on the host.
 
@@ -230,3 +231,64 @@ def test_apply_pauli_sum_tiles_and_wide_words(n, dt, dtype, tol):
             m >>= 1
         ref += cf * (1j ** y) * (1 - 2 * par) * p64[j]
     assert np.max(np.abs(got - ref)) < tol * np.sum(np.abs(coeffs))
+
+
+class FusedGate(ctypes.Structure):
+    _fields_ = [("ntgt", ctypes.c_int32), ("tgt", ctypes.c_int32 * 2), ("nctrl", ctypes.c_int32),
+                ("ctrl", ctypes.c_int32 * 4), ("ctrl_val", ctypes.c_int32 * 4), ("m", ctypes.c_double * 32)]
+
+
+def _fused_block(rng, tile, n, count):
+    gates = (FusedGate * count)()
+    for g in gates:
+        two = rng.random() < 0.25
+        t = [int(x) for x in rng.choice(tile, size=2 if two else 1, replace=False)]
+        g.ntgt = len(t)
+        for i, b in enumerate(t):
+            g.tgt[i] = b
+        d = 1 << len(t)
+        u, _ = np.linalg.qr(rng.normal(size=(d, d)) + 1j * rng.normal(size=(d, d)))
+        if rng.random() < 0.3:  # a controlled gate, the control anywhere but on the targets
+            c = int(rng.choice([b for b in range(n) if b not in t]))
+            g.nctrl, g.ctrl[0], g.ctrl_val[0] = 1, c, int(rng.integers(0, 2))
+        for i, z in enumerate(u.ravel()):
+            g.m[2 * i], g.m[2 * i + 1] = z.real, z.imag
+    return gates
+
+
+def test_fused_blocks_ff_match_complex128_blocks():
+    """Three consecutive fused blocks on different tiles: complex128 in and
+    out of each, against float-float out of the first, in and out of the
+    second, in of the third (the state ends as complex128)."""
+    import torch
+
+    lib = _lib()
+    vp, u32, i32 = ctypes.c_void_p, ctypes.c_uint32, ctypes.c_int
+    blk = [vp, u32, i32, u32, ctypes.POINTER(ctypes.c_int32), u32, ctypes.POINTER(FusedGate)]
+    lib.lgpu_apply_fused_block.argtypes = blk + [vp]
+    lib.lgpu_apply_fused_block_ff.argtypes = blk + [u32, vp]
+    n = 19
+    rng = np.random.default_rng(17)
+    tiles = [list(range(12)), list(range(5)) + list(range(12, 19)), list(range(3)) + [5, 8, 11, 13, 15, 16, 17, 18]]
+    blocks = [(t, _fused_block(rng, t, n, 30)) for t in tiles]
+    psi = _state(n, 23)
+    stream = torch.cuda.current_stream().cuda_stream
+    out = []
+    for ff in (False, True):
+        d = torch.from_numpy(psi.copy()).cuda()
+        for i, (t, g) in enumerate(blocks):
+            tb = (ctypes.c_int32 * len(t))(*t)
+            if ff:
+                flags = (FF_IN if i > 0 else 0) | (FF_OUT if i + 1 < len(blocks) else 0)
+                st = lib.lgpu_apply_fused_block_ff(d.data_ptr(), n, C128, len(t), tb, len(g), g, flags, stream)
+            else:
+                st = lib.lgpu_apply_fused_block(d.data_ptr(), n, C128, len(t), tb, len(g), g, stream)
+            assert st == LGPU_OK
+        out.append(d.cpu().numpy())
+    assert np.max(np.abs(out[0] - out[1])) < 1e-13
+    assert abs(np.linalg.norm(out[1]) - 1.0) < 1e-12
+    # complex64 states have no float-float form
+    d64 = torch.zeros(1 << 12, dtype=torch.complex64, device="cuda")
+    tb = (ctypes.c_int32 * 12)(*range(12))
+    assert lib.lgpu_apply_fused_block_ff(d64.data_ptr(), 12, C64, 12, tb, 1, blocks[0][1], FF_OUT,
+                                         stream) == LGPU_ERR_INVALID_ARG
