@@ -296,15 +296,8 @@ __device__ __forceinline__ void tile_gate_df(float4 *tile, int E, const lgpu_bga
     }
 }
 
-// complex128 tile <-> float-float tile, in place (all threads; the caller
+// float-float tile -> complex128, in place (all threads; the caller
 // synchronises afterwards).
-__device__ __forceinline__ void tile_to_df(void *tile, int E) {
-    for (int e = threadIdx.x; e < E; e += blockDim.x) {
-        const double2 v = reinterpret_cast<const double2 *>(tile)[e];
-        const DF r = df_from_double(v.x), i = df_from_double(v.y);
-        reinterpret_cast<float4 *>(tile)[e] = make_float4(r.hi, i.hi, r.lo, i.lo);
-    }
-}
 __device__ __forceinline__ void tile_from_df(void *tile, int E) {
     for (int e = threadIdx.x; e < E; e += blockDim.x) {
         const float4 v = reinterpret_cast<const float4 *>(tile)[e];
@@ -561,10 +554,11 @@ __global__ void __launch_bounds__(512, 1) batch_kernel(lgpu_batch_args_t a, unsi
             if (k == int(cir.n)) {
                 // ---- whole state in shared memory ----
                 C *tile = ring;
-                for (int e = threadIdx.x; e < E; e += blockDim.x) tile[e] = mk<T>(T(e == 0 ? 1 : 0), T(0));
-                if constexpr (DFM) {  // (1, 0) and 0 are exact float-float values
-                    __syncthreads();
-                    tile_to_df(tile, E);
+                if constexpr (DFM) {  // |0...0> in float-float form: (1, 0, 0, 0) and zeros
+                    for (int e = threadIdx.x; e < E; e += blockDim.x)
+                        reinterpret_cast<float4 *>(tile)[e] = make_float4(e == 0 ? 1.0f : 0.0f, 0.0f, 0.0f, 0.0f);
+                } else {
+                    for (int e = threadIdx.x; e < E; e += blockDim.x) tile[e] = mk<T>(T(e == 0 ? 1 : 0), T(0));
                 }
                 __syncthreads();
                 for (uint32_t gi = 0; gi < blk.gate_cnt; gi++) {
@@ -608,9 +602,14 @@ __global__ void __launch_bounds__(512, 1) batch_kernel(lgpu_batch_args_t a, unsi
                     // |0...0> needs no load: wait until the stage's previous store has read it
                     if (threadIdx.x == 0) b_wait_read_2();
                     __syncthreads();
-                    for (int e = threadIdx.x; e < E; e += blockDim.x) tile[e] = mk<T>(T(0), T(0));
+                    for (int e = threadIdx.x; e < E; e += blockDim.x) tile[e] = mk<T>(T(0), T(0));  // zero in either form
                     __syncthreads();
-                    if (threadIdx.x == 0 && base == 0) tile[0] = mk<T>(T(1), T(0));
+                    if (threadIdx.x == 0 && base == 0) {
+                        if constexpr (DFM)
+                            reinterpret_cast<float4 *>(tile)[0] = make_float4(1.0f, 0.0f, 0.0f, 0.0f);
+                        else
+                            tile[0] = mk<T>(T(1), T(0));
+                    }
                     __syncthreads();
                 } else {
                     const int st = int(use % kRing);
@@ -644,10 +643,8 @@ __global__ void __launch_bounds__(512, 1) batch_kernel(lgpu_batch_args_t a, unsi
                     }
                     phase_bits ^= 1u << st;
                 }
-                if constexpr (DFM) {
-                    tile_to_df(tile, E);
-                    __syncthreads();
-                }
+                // float-float (DFM): the circuit's state stays in float-float form in
+                // the scratch from block to block; only the last block converts back
                 for (uint32_t gi = 0; gi < blk.gate_cnt; gi++) {
                     const lgpu_bgate_t g = a.gates[blk.gate_off + gi];
                     if (g.kind == BK_CHAINED || (base & g.omask) != g.oval) continue;  // tile-uniform
@@ -658,8 +655,10 @@ __global__ void __launch_bounds__(512, 1) batch_kernel(lgpu_batch_args_t a, unsi
                     __syncthreads();
                 }
                 if constexpr (DFM) {
-                    tile_from_df(tile, E);
-                    __syncthreads();
+                    if (last) {
+                        tile_from_df(tile, E);
+                        __syncthreads();
+                    }
                 }
                 if (last) {
                     acc += wht ? tile_obs<T>(tile, k, a.terms + cir.obs_off, cir.obs_cnt, base, s_lm, s_c)
