@@ -256,10 +256,13 @@ def _fused_block(rng, tile, n, count):
     return gates
 
 
-def test_fused_blocks_ff_match_complex128_blocks():
+@pytest.mark.parametrize("f64_mode", [1, 0])
+def test_fused_blocks_ff_match_complex128_blocks(f64_mode):
     """Three consecutive fused blocks on different tiles: complex128 in and
     out of each, against float-float out of the first, in and out of the
-    second, in of the third (the state ends as complex128)."""
+    second, in of the third (the state ends as complex128).  f64_mode 0
+    selects the native-FP64 fused kernels, which take complex128 amplitudes:
+    the float-float flags then convert the state around the block."""
     import torch
 
     lib = _lib()
@@ -267,6 +270,15 @@ def test_fused_blocks_ff_match_complex128_blocks():
     blk = [vp, u32, i32, u32, ctypes.POINTER(ctypes.c_int32), u32, ctypes.POINTER(FusedGate)]
     lib.lgpu_apply_fused_block.argtypes = blk + [vp]
     lib.lgpu_apply_fused_block_ff.argtypes = blk + [u32, vp]
+    lib.lgpu_set_f64_mode.argtypes = [i32]
+    assert lib.lgpu_set_f64_mode(f64_mode) == LGPU_OK
+    try:
+        _fused_ff_case(lib, torch)
+    finally:
+        lib.lgpu_set_f64_mode(1)
+
+
+def _fused_ff_case(lib, torch):
     n = 19
     rng = np.random.default_rng(17)
     tiles = [list(range(12)), list(range(5)) + list(range(12, 19)), list(range(3)) + [5, 8, 11, 13, 15, 16, 17, 18]]
