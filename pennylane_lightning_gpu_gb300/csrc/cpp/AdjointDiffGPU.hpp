@@ -8,7 +8,12 @@
 // Per operation the engine issues ONE fused launch (lgpu_adjoint_step) that
 // reads lambda and the K bras once, forms the generator expectations, and
 // applies U^dag to all of them; mu is never materialised and the Jacobian
-// column stays on the device until one copy at the end.
+// column stays on the device until one copy at the end.  Runs of 1-target
+// operations whose targets fit a shared-memory tile take one pass for the
+// whole run (lgpu_adjoint_block_ff); a run may take an operation ahead of
+// operations it leaves behind when they share no wire (the operations and
+// their generators then commute), so each operation's Jacobian column is
+// fixed up front instead of by the walk's counters.
 #pragma once
 
 #include <cstdlib>
@@ -73,9 +78,6 @@ template <class T = double> class AdjointJacobianGPU {
         PL_ABORT_IF(jac.size() < num_observables, "Jacobian has too few rows");
         for (auto &row : jac) PL_ABORT_IF(row.size() < tp_size, "Jacobian has too few columns");
 
-        size_t trainableParamNumber = tp_size - 1;
-        size_t current_param_idx = num_param_ops - 1;
-        auto tp_it = trainableParams.rbegin();
         const auto tp_rend = trainableParams.rend();
 
         CUDA::DevTag<int> dt_local(std::move(dev_tag));
@@ -187,47 +189,96 @@ template <class T = double> class AdjointJacobianGPU {
                 PL_LGPU_IS_SUCCESS(lgpu_state_ff(bra_ptrs[k], n, 0, lambda.lstream()));
             in_ff = false;
         };
-        for (int op_idx = static_cast<int>(ops_name.size() - 1); op_idx >= 0; op_idx--) {
+        // The Jacobian column of every operation (-1: no trainable parameter),
+        // as the reference's reverse counters assign them.
+        const size_t nops = ops_name.size();
+        std::vector<int> col(nops, -1);
+        size_t cols_left = 0;
+        {
+            size_t pi = 0, t = 0;
+            for (size_t j = 0; j < nops; j++) {
+                if (!ops.hasParams(j)) continue;
+                while (t < tp_size && trainableParams[t] < pi) t++;
+                if (t < tp_size && trainableParams[t] == pi) {
+                    col[j] = int(t);
+                    cols_left++;
+                }
+                pi++;
+            }
+        }
+        auto is_prep = [&](size_t j) {
+            const std::string &nm = ops_name[j];
+            return nm == "QubitStateVector" || nm == "StatePrep" || nm == "BasisState";
+        };
+        auto wire_bits = [&](size_t j) {
+            uint64_t b = 0;
+            for (size_t w : ops.getOpsWires()[j]) b |= uint64_t(1) << Engine::bit_of(n, w);
+            return b;
+        };
+        std::vector<char> done(nops, 0);
+        int op_idx = static_cast<int>(nops) - 1;
+        while (op_idx >= 0) {
+            if (done[size_t(op_idx)]) {
+                op_idx--;
+                continue;
+            }
             PL_ABORT_IF(ops.getOpsParams()[size_t(op_idx)].size() > 1,
                         "The operation is not supported using the adjoint differentiation method");
             const std::string &name = ops_name[size_t(op_idx)];
-            if ((name == "QubitStateVector") || (name == "StatePrep") || (name == "BasisState")) continue;
-            if (tp_it == tp_rend) break;  // All done
+            if (is_prep(size_t(op_idx))) {
+                op_idx--;
+                continue;
+            }
+            if (cols_left == 0) break;  // All done
 
             // A run of 1-target operations (with controls) whose targets fit
             // one tile: one pass over lambda and the bras for the whole run.
+            // The run takes operations in reverse order; an operation that
+            // cannot join (not a 1-target step, target outside the tile) is
+            // left for later and blocks its wires, and a later operation joins
+            // only if it shares no wire with any operation left behind (so it
+            // commutes with them and with their generators).
             if (blocks) {
                 std::vector<lgpu_adj_block_step_t> steps;
                 std::vector<int> tbits, tile;
                 std::vector<std::pair<size_t, double>> scales;
-                size_t cpi = current_param_idx, tpn = trainableParamNumber;
-                auto it = tp_it;
-                int j = op_idx;
-                for (; j >= 0 && steps.size() < 48; j--) {
+                std::vector<size_t> taken;
+                uint64_t blocked = 0;
+                const uint64_t all_bits = n >= 64 ? ~uint64_t(0) : (uint64_t(1) << n) - 1;
+                int scanned = 0;
+                for (int j = op_idx; j >= 0 && steps.size() < 48 && scanned < 512 && blocked != all_bits; j--) {
+                    if (done[size_t(j)] || is_prep(size_t(j))) continue;
+                    if (ops.getOpsParams()[size_t(j)].size() > 1) break;  // aborts when the sweep reaches it
+                    scanned++;
+                    const uint64_t wb = wire_bits(size_t(j));
+                    if (wb & blocked) {
+                        blocked |= wb;
+                        continue;
+                    }
                     const std::string &nj = ops_name[size_t(j)];
-                    if ((nj == "QubitStateVector") || (nj == "StatePrep") || (nj == "BasisState")) continue;
-                    if (it == tp_rend || ops.getOpsParams()[size_t(j)].size() > 1) break;
                     const bool invj = ops.getOpsInverses()[size_t(j)];
-                    const bool grad = ops.hasParams(size_t(j)) && cpi == *it;
+                    const bool grad = col[size_t(j)] >= 0;
                     lgpu_adj_block_step_t st{};
                     double scale = 0;
-                    if (!block_step(lower(lambda, ops, size_t(j), !invj), nj, ops.getOpsWires()[size_t(j)], n, grad,
-                                    st, scale))
-                        break;
-                    std::vector<int> trial(tbits);
-                    trial.push_back(st.tgt);
-                    std::vector<int> t2;
-                    if (!Engine::tile_for(trial, 11, 5, n, t2, 6)) break;
+                    std::vector<int> trial(tbits), t2;
+                    bool ok = block_step(lower(lambda, ops, size_t(j), !invj), nj, ops.getOpsWires()[size_t(j)], n,
+                                         grad, st, scale);
+                    if (ok) {
+                        trial.push_back(st.tgt);
+                        ok = Engine::tile_for(trial, 11, 5, n, t2, 6);
+                    }
+                    if (!ok) {
+                        blocked |= wb;
+                        continue;
+                    }
                     tbits = trial;
                     tile = t2;
                     if (grad) {
-                        st.col = int32_t(tpn);
-                        scales.emplace_back(tpn, scale * (invj ? -1.0 : 1.0));
-                        tpn--;
-                        ++it;
+                        st.col = int32_t(col[size_t(j)]);
+                        scales.emplace_back(size_t(col[size_t(j)]), scale * (invj ? -1.0 : 1.0));
                     }
-                    if (ops.hasParams(size_t(j))) cpi--;
                     steps.push_back(st);
+                    taken.push_back(size_t(j));
                 }
                 if (steps.size() >= 2) {
                     std::vector<int32_t> tb(tile.begin(), tile.end());
@@ -249,11 +300,9 @@ template <class T = double> class AdjointJacobianGPU {
                     }
                     in_ff = ff_ok;
                     for (const auto &cs : scales) col_scale[cs.first] = cs.second;
-                    current_param_idx = cpi;
-                    trainableParamNumber = tpn;
-                    tp_it = it;
-                    op_idx = j + 1;  // the loop continues with operation j
-                    continue;
+                    for (size_t j : taken) done[j] = 1;
+                    cols_left -= scales.size();
+                    continue;  // op_idx again: it may have been left behind
                 }
             }
 
@@ -265,11 +314,8 @@ template <class T = double> class AdjointJacobianGPU {
             std::vector<cd> umat;
             const bool fusable = Engine::dense_on_bits(udag, ubits, umat, 4);
 
-            bool want_grad = false;
-            if (ops.hasParams(size_t(op_idx))) {
-                if (current_param_idx == *tp_it) want_grad = true;
-            }
-            if (want_grad) {
+            const int opcol = col[size_t(op_idx)];
+            if (opcol >= 0) {
                 std::vector<cd> g;
                 double scale = 0;
                 std::vector<int> gbits;
@@ -278,8 +324,8 @@ template <class T = double> class AdjointJacobianGPU {
                 PL_ABORT_IF_NOT(has_gen, ("The operation " + name +
                                           " is not supported using the adjoint differentiation method")
                                              .c_str());
-                col_scale[trainableParamNumber] = scale * (inv ? -1.0 : 1.0);
-                double *out = jac_dev.getData() + trainableParamNumber * K;
+                col_scale[size_t(opcol)] = scale * (inv ? -1.0 : 1.0);
+                double *out = jac_dev.getData() + size_t(opcol) * K;
                 if (fusable && gbits == ubits) {
                     std::vector<int32_t> b32(ubits.begin(), ubits.end());
                     PL_LGPU_IS_SUCCESS(lgpu_adjoint_step(lambda.ctx(), lambda.getData(), bra_ptrs.data(),
@@ -302,8 +348,7 @@ template <class T = double> class AdjointJacobianGPU {
                     lambda.applyDesc(udag);
                     for (auto &b : H_lambda) b.applyDesc(udag);
                 }
-                trainableParamNumber--;
-                ++tp_it;
+                cols_left--;
             } else {
                 if (fusable && ubits.size() == 1) {
                     std::vector<int32_t> b32(ubits.begin(), ubits.end());
@@ -320,7 +365,8 @@ template <class T = double> class AdjointJacobianGPU {
                     lambda.applyDescMulti(udag, all);
                 }
             }
-            if (ops.hasParams(size_t(op_idx))) current_param_idx--;
+            done[size_t(op_idx)] = 1;
+            op_idx--;
         }
         leave_ff();  // lambda and the bras leave the sweep as complex128
         // One device-to-host copy of all columns.
