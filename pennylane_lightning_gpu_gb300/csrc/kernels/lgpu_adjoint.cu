@@ -8,6 +8,7 @@
 // which replaces the reference's per-op sequence of a D2D copy of lambda,
 // U^dag on lambda, G on mu, K cuBLAS dot products and U^dag on K bras
 // (AdjointDiffGPU.hpp:560-595).
+#include <cstddef>
 #include <memory>
 
 #include "lgpu_bodies.cuh"
@@ -1059,8 +1060,8 @@ struct SweepDF {
     int sign_diag;  // U^dag = diag(+-1, +-1) on one bit
 };
 
-template <int BODY>
-__device__ __forceinline__ void sweep_pairs_df(float4 *lam, float4 *bra, int E, const SweepOp &o, const DF *mp) {
+template <int BODY, class OP>
+__device__ __forceinline__ void sweep_pairs_df(float4 *lam, float4 *bra, int E, const OP &o, const DF *mp) {
     DF m[8];
 #pragma unroll
     for (int i = 0; i < 8; i++) m[i] = mp[i];
@@ -1082,7 +1083,8 @@ __device__ __forceinline__ void sweep_pairs_df(float4 *lam, float4 *bra, int E, 
     }
 }
 
-__device__ __forceinline__ void sweep_udag_df(float4 *lam, float4 *bra, int E, const SweepOp &o, const SweepDF &d) {
+template <class OP>
+__device__ __forceinline__ void sweep_udag_df(float4 *lam, float4 *bra, int E, const OP &o, const SweepDF &d) {
     if (o.ukind == U_ONE) {
         switch (d.sign_diag ? kDfSignDiag : o.ubody) {
         case kDfSignDiag: sweep_pairs_df<kDfSignDiag>(lam, bra, E, o, d.u); break;
@@ -1130,8 +1132,8 @@ __device__ __forceinline__ void sweep_udag_df(float4 *lam, float4 *bra, int E, c
     }
 }
 
-template <int GK>
-__device__ __forceinline__ DF sweep_gen1_df(const float4 *lam, const float4 *bra, int E, const SweepOp &o,
+template <int GK, class OP>
+__device__ __forceinline__ DF sweep_gen1_df(const float4 *lam, const float4 *bra, int E, const OP &o,
                                             const DF *g) {
     DF acc{0.0f, 0.0f};
     const uint32_t holes = o.gcm | (1u << o.gt);
@@ -1148,7 +1150,8 @@ __device__ __forceinline__ DF sweep_gen1_df(const float4 *lam, const float4 *bra
     return acc;
 }
 
-__device__ __forceinline__ DF sweep_gen_df(const float4 *lam, const float4 *bra, int E, const SweepOp &o,
+template <class OP>
+__device__ __forceinline__ DF sweep_gen_df(const float4 *lam, const float4 *bra, int E, const OP &o,
                                            const SweepDF &d) {
     if (o.gkind == G_DENSE4) {
         DF acc{0.0f, 0.0f};
@@ -1193,17 +1196,39 @@ __device__ __forceinline__ DF sweep_gen_df(const float4 *lam, const float4 *bra,
     }
 }
 
+// The part of a SweepOp the float-float sweep reads (its first 48 bytes).
+struct SweepHdr {
+    int ukind, ubody, ut, uq2;
+    uint32_t ucm, ucv;
+    int gkind, gt, gq2;
+    uint32_t gcm, gcv;
+    int col;
+};
+static_assert(offsetof(SweepOp, col) + sizeof(int) == sizeof(SweepHdr) && offsetof(SweepOp, ukind) == 0,
+              "SweepHdr is the head of SweepOp");
+constexpr int kHdrWords = int(sizeof(SweepHdr) / 4), kDfWords = int(sizeof(SweepDF) / 4);
+constexpr int kDescWords = kHdrWords + kDfWords;
+static_assert(sizeof(SweepDF) % 4 == 0 && kDescWords <= kSweepThreads, "one descriptor word per thread");
+
 __global__ void __launch_bounds__(kSweepThreads, 1)
     adjoint_sweep_df_kernel(const double2 *__restrict__ ket, double2 *const *__restrict__ bras, int n,
                             const SweepOp *__restrict__ ops, const SweepDF *__restrict__ dops, int nops,
                             double *__restrict__ jac, int K) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     __shared__ DF red[kSweepThreads / 32];
+    // the operations' descriptors pass through shared memory: operation i + 1's
+    // is loaded while operation i runs (one word per thread)
+    __shared__ __align__(16) uint32_t desc[2][kDescWords];
+    auto desc_word = [&](int i, int w) -> uint32_t {
+        return w < kHdrWords ? reinterpret_cast<const uint32_t *>(ops + i)[w]
+                             : reinterpret_cast<const uint32_t *>(dops + i)[w - kHdrWords];
+    };
     const int E = 1 << n;
     float4 *lam = reinterpret_cast<float4 *>(smem_raw);
     float4 *bra = lam + E;
     const int k = blockIdx.x;
     const double2 *src = bras[k];
+    if (nops > 0 && threadIdx.x < kDescWords) desc[0][threadIdx.x] = desc_word(0, threadIdx.x);
     for (int e = threadIdx.x; e < E; e += kSweepThreads) {
         const double2 a = ket[e], b = src[e];
         const DF ar = df_from_double(a.x), ai = df_from_double(a.y), br = df_from_double(b.x), bi = df_from_double(b.y);
@@ -1213,8 +1238,10 @@ __global__ void __launch_bounds__(kSweepThreads, 1)
     __syncthreads();
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (int i = 0; i < nops; i++) {
-        const SweepOp &o = ops[i];
-        const SweepDF &d = dops[i];
+        const bool pf = i + 1 < nops && threadIdx.x < kDescWords;
+        const uint32_t next = pf ? desc_word(i + 1, threadIdx.x) : 0u;
+        const SweepHdr &o = *reinterpret_cast<const SweepHdr *>(desc[i & 1]);
+        const SweepDF &d = *reinterpret_cast<const SweepDF *>(desc[i & 1] + kHdrWords);
         if (o.col >= 0 && o.gkind != G_NONE) {
             DF v = sweep_gen_df(lam, bra, E, o, d);
 #pragma unroll
@@ -1229,6 +1256,7 @@ __global__ void __launch_bounds__(kSweepThreads, 1)
             __syncthreads();
         }
         sweep_udag_df(lam, bra, E, o, d);
+        if (pf) desc[(i + 1) & 1][threadIdx.x] = next;
         __syncthreads();
     }
 }
