@@ -489,8 +489,11 @@ __device__ __forceinline__ void b_wait_read_1() { asm volatile("cp.async.bulk.wa
 __device__ __forceinline__ void b_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
 __device__ __forceinline__ void b_fence() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 
-// DFM (complex128): gates run in float-float on a float-float tile; the tile
-// is converted in place after a load and before a store or the observable.
+// DFM (complex128): gates run in float-float on a float-float tile.  A
+// circuit's state is float-float from its first block (|0...0> is built in
+// that form) to its last, in shared memory or in the CTA's scratch between
+// blocks; only the last block converts its tiles to complex128, for the
+// observable.
 template <class T, bool EMU, bool DFM = false>
 __global__ void __launch_bounds__(512, 1) batch_kernel(lgpu_batch_args_t a, unsigned *err) {
     using C = cplx_t<T>;
