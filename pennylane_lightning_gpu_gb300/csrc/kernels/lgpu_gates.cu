@@ -617,9 +617,10 @@ __device__ __forceinline__ void tile_quads_df(float4 *tile, int E, int qa, int q
 
 // All gates of a launch on one tile held in shared memory (all threads; the
 // caller synchronises before and after).  DFM (complex128): the tile holds
-// float-float amplitudes (converted once after the load and once at the
-// store) and every gate runs in float-float arithmetic, its coefficients
-// stored as (hi, lo) float pairs in the double slots of the matrix pool.
+// float-float amplitudes (converted after the load and at the store, unless
+// the state already arrives / stays in float-float form: in_ff / out_ff) and
+// every gate runs in float-float arithmetic, its coefficients stored as
+// (hi, lo) float pairs in the double slots of the matrix pool.
 template <class T, class I, bool EMU, int NT, bool DFM = false>
 __device__ __forceinline__ void fused_tile(cplx_t<T> *tile, int E, I base, const FusedParams<T, I> &p) {
     using C = cplx_t<T>;
