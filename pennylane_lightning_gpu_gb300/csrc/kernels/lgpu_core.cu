@@ -69,6 +69,18 @@ int fused_df_enabled() {
     return m;
 }
 
+static std::atomic<int> g_diag_fold_mode{-1};
+
+int fused_diag_fold_enabled() {
+    int m = g_diag_fold_mode.load(std::memory_order_relaxed);
+    if (m < 0) {
+        const char *e = std::getenv("LGPU_DIAG_FOLD");
+        m = (e && e[0] == '0') ? 0 : 1;
+        g_diag_fold_mode.store(m, std::memory_order_relaxed);
+    }
+    return m;
+}
+
 static std::atomic<int> g_tc_mode{-1};
 
 int tc_enabled() {

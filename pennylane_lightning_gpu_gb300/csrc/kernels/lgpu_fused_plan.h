@@ -3,13 +3,19 @@
 // C++ (no CUDA types), so the grouping can be unit-tested on the host.
 #pragma once
 
+#include <algorithm>
+#include <complex>
 #include <cstdint>
 #include <cstring>
 #include <vector>
 
+#include "lgpu.h"
+
 namespace lgpu {
 
 constexpr int kFusedMaxGates = 96;
+constexpr int kDiagTableBits = 4;  // phase tables of folded diagonal gates: at most 4 tile positions
+constexpr int kDiagTableMark = 3;  // gate record ntgt of a folded phase table
 constexpr int kFusedMatPool = 2304;  // matrix elements, in the state's precision
 
 struct FGate {
@@ -133,6 +139,113 @@ inline int group_fused_gates(FGate *gates, KC *kc, int cnt, int k, int R, FGroup
         }
     }
     return ng;
+}
+
+// Diagonal gates of a float-float block folded into phase tables.  A 1-target
+// gate whose 2x2 is diagonal (other than diag(+-1, +-1), which stays a sign
+// flip), with its controls (if any) on tile bits, is a diagonal on its
+// support (target and controls).  Such gates join a group
+// whose product is one table of 2^k phases over the union of the supports
+// (k <= kDiagTableBits), applied where the group's first gate stood.  A later
+// gate may join only if no gate between them targets a bit of its support
+// (diagonal gates commute with each other and with controls), so moving it
+// back changes nothing.  A group of one gate stays that gate.  A folded group
+// is returned as a record with ntgt = kDiagTableMark, its support bits in
+// ctrl[0..k-1] in ascending tile position (table index bit b = ctrl[b]) and the
+// table in m (entry i = m[2i] + i m[2i+1]); internal[i] marks those records.
+inline std::vector<lgpu_fused_gate_t> fold_diagonal_gates(const lgpu_fused_gate_t *gates, uint32_t ngates,
+                                                          const std::vector<int> &pos, std::vector<char> &internal) {
+    using cd = std::complex<double>;
+    const int n = int(pos.size());
+    auto foldable = [&](const lgpu_fused_gate_t &g, uint64_t *support) {
+        if (g.ntgt != 1 || g.nctrl < 0 || g.nctrl > kDiagTableBits - 1) return false;
+        for (int e = 2; e < 6; e++)
+            if (g.m[e] != 0.0) return false;  // off-diagonal entries
+        // diag(+-1, +-1) (Z, CZ) stays a sign flip, cheaper than a table entry
+        auto pm1 = [](double v) { return v == 1.0 || v == -1.0; };
+        if (pm1(g.m[0]) && g.m[1] == 0.0 && pm1(g.m[6]) && g.m[7] == 0.0) return false;
+        uint64_t sb = 0;
+        auto add = [&](int b) {
+            if (b < 0 || b >= n || pos[size_t(b)] < 0 || ((sb >> b) & 1u)) return false;
+            sb |= uint64_t(1) << b;
+            return true;
+        };
+        if (!add(g.tgt[0])) return false;
+        for (int c = 0; c < g.nctrl; c++)
+            if (!add(g.ctrl[c])) return false;
+        *support = sb;
+        return true;
+    };
+    struct Group {
+        size_t slot;  // index in out
+        uint64_t support;
+        std::vector<uint32_t> members;
+    };
+    std::vector<lgpu_fused_gate_t> out;
+    std::vector<Group> groups;
+    internal.clear();
+    int open = -1;         // the group later diagonal gates may join
+    uint64_t blocked = 0;  // bits targeted by other gates since the open group's first gate
+    for (uint32_t i = 0; i < ngates; i++) {
+        const lgpu_fused_gate_t &g = gates[i];
+        uint64_t sb = 0;
+        if (foldable(g, &sb)) {
+            if (open >= 0 && (sb & blocked) == 0 &&
+                __builtin_popcountll(groups[size_t(open)].support | sb) <= kDiagTableBits) {
+                groups[size_t(open)].support |= sb;
+                groups[size_t(open)].members.push_back(i);
+                continue;
+            }
+            open = int(groups.size());
+            groups.push_back(Group{out.size(), sb, {i}});
+            out.push_back(g);  // replaced below if the group takes more gates
+            internal.push_back(0);
+            blocked = 0;
+            continue;
+        }
+        out.push_back(g);
+        internal.push_back(0);
+        // a gate whose matrix is not diagonal blocks its targets
+        const bool diag1 = g.ntgt == 1 && g.m[2] == 0.0 && g.m[3] == 0.0 && g.m[4] == 0.0 && g.m[5] == 0.0;
+        if (!diag1)
+            for (int t = 0; t < g.ntgt && t < 2; t++)
+                if (g.tgt[t] >= 0 && g.tgt[t] < 64) blocked |= uint64_t(1) << g.tgt[t];
+    }
+    for (const Group &G : groups) {
+        if (G.members.size() < 2) continue;
+        std::vector<int> bits;  // support bits in ascending tile position
+        for (int b = 0; b < n; b++)
+            if ((G.support >> b) & 1u) bits.push_back(b);
+        std::sort(bits.begin(), bits.end(), [&](int a, int b) { return pos[size_t(a)] < pos[size_t(b)]; });
+        const int k = int(bits.size());
+        lgpu_fused_gate_t r{};
+        r.ntgt = kDiagTableMark;
+        r.nctrl = k;
+        for (int b = 0; b < k; b++) r.ctrl[b] = bits[size_t(b)];
+        for (int idx = 0; idx < (1 << kDiagTableBits); idx++) {
+            cd t = idx < (1 << k) ? cd(1.0, 0.0) : cd(0.0, 0.0);
+            if (idx < (1 << k)) {
+                auto bit = [&](int state_bit) {
+                    for (int b = 0; b < k; b++)
+                        if (bits[size_t(b)] == state_bit) return (idx >> b) & 1;
+                    return 0;
+                };
+                for (uint32_t mi : G.members) {
+                    const lgpu_fused_gate_t &g = gates[mi];
+                    bool on = true;
+                    for (int c = 0; c < g.nctrl; c++)
+                        if (bit(g.ctrl[c]) != (g.ctrl_val[c] ? 1 : 0)) on = false;
+                    if (!on) continue;
+                    t *= bit(g.tgt[0]) ? cd(g.m[6], g.m[7]) : cd(g.m[0], g.m[1]);
+                }
+            }
+            r.m[2 * idx] = t.real();
+            r.m[2 * idx + 1] = t.imag();
+        }
+        out[G.slot] = r;
+        internal[G.slot] = 1;
+    }
+    return out;
 }
 
 }  // namespace lgpu

@@ -14,6 +14,8 @@
 //  * pauli_rot_kernel exp(i angle P) for Pauli words, pairwise (i, i^flip).
 //  * fused_kernel     a block of 1/2-target gates applied to shared-memory
 //                     tiles of 2^k amplitudes: one HBM pass for many gates.
+#include <algorithm>
+#include <complex>
 #include <cstring>
 #include <memory>
 #include <mutex>
@@ -507,6 +509,10 @@ template <class T, class I> struct FusedParams {
     int in_ff, out_ff;             // float-float path: the state arrives / is left in float-float form
 };
 
+// Folded diagonal gates of float-float blocks (fold_diagonal_gates in
+// lgpu_fused_plan.h): the table is staged in shared memory after the tile.
+constexpr size_t kDiagTableBytes = size_t(16) << kDiagTableBits;
+
 // Amplitudes per thread in a register group: 16 (complex64).  complex128
 // blocks run gate by gate: they are bound by the FP64 pipe, and the register
 // footprint of a group would halve the resident CTAs.
@@ -572,6 +578,24 @@ __device__ __forceinline__ void tile_pairs_df(float4 *tile, int E, int q, uint32
         }
         tile[swz<double>(e0)] = a;
         tile[swz<double>(e1)] = b;
+    }
+}
+
+// A folded diagonal (fold_diagonal_gates): every amplitude e times the phase
+// table[pext(e, mask)], the table (16 float-float complex entries, staged in
+// shared memory by the caller) indexed by the tile positions in `mask` in
+// ascending order.
+template <int NT>
+__device__ __forceinline__ void tile_diag_table_df(float4 *tile, int E, uint32_t mask, const float4 *tab) {
+    for (int e = threadIdx.x; e < E; e += NT) {
+        int idx = 0, b = 0;
+        for (uint32_t mm = mask; mm; mm &= mm - 1u, b++) idx |= ((e >> (__ffs(int(mm)) - 1)) & 1) << b;
+        const float4 t = tab[idx];  // (re.hi, re.lo, im.hi, im.lo)
+        float4 &a = tile[swz<double>(e)];
+        const DF2 x{f2_pack(a.x, a.y), f2_pack(a.z, a.w)}, xs{f2_pack(a.y, a.x), f2_pack(a.w, a.z)};
+        const DF2 c1{f2_pack(t.x, t.x), f2_pack(t.y, t.y)}, c2{f2_pack(-t.z, t.z), f2_pack(-t.w, t.w)};
+        const DF2 y = df2_sum<2>({df2_mul(c1, x), df2_mul(c2, xs)});
+        a = make_float4(f2_x(y.hi), f2_y(y.hi), f2_x(y.lo), f2_y(y.lo));
     }
 }
 
@@ -671,7 +695,14 @@ __device__ __forceinline__ void fused_tile(cplx_t<T> *tile, int E, I base, const
         if constexpr (DFM && sizeof(T) == 8) {
             float4 *t4 = reinterpret_cast<float4 *>(tile);
             const DF *md = reinterpret_cast<const DF *>(mm);
-            if (g.ntgt == 1) {
+            if (g.ntgt == kDiagTableMark) {
+                // stage the table after the tile (float-float launches are single-buffered)
+                float4 *tab = reinterpret_cast<float4 *>(t4 + E);
+                if (threadIdx.x < (1 << kDiagTableBits))
+                    tab[threadIdx.x] = reinterpret_cast<const float4 *>(md)[threadIdx.x];
+                __syncthreads();
+                tile_diag_table_df<NT>(t4, E, g.in_mask, tab);
+            } else if (g.ntgt == 1) {
                 switch (g.pad == 1 ? kDfSignDiag : int(g.body)) {
                 case kDfSignDiag: tile_pairs_df<kDfSignDiag, NT>(t4, E, g.q0, g.in_mask, g.in_val, md); break;
                 case B_DIAG: tile_pairs_df<B_DIAG, NT>(t4, E, g.q0, g.in_mask, g.in_val, md); break;
@@ -754,6 +785,7 @@ template <int N> __device__ __forceinline__ void cp_async_wait_n() {
 template <class T, class I, bool EMU, int NT, int STAGES, int MINB, bool DFM = false>
 __global__ void __launch_bounds__(NT, MINB)
     fused_kernel(cplx_t<T> *__restrict__ sv, const FusedParams<T, I> p) {
+    static_assert(!DFM || STAGES == 1, "float-float blocks are single-buffered: the phase table follows the tile");
     using C = cplx_t<T>;
     extern __shared__ __align__(128) unsigned char smem_raw[];
     const int E = 1 << p.k;
@@ -1321,8 +1353,9 @@ static lgpu_status_t launch_fused(cplx_t<T> *sv, const FusedParams<T, I> &p, siz
 template <class I>
 static lgpu_status_t launch_fused_df(double2 *sv, const FusedParams<double, I> &p, size_t tile_bytes,
                                      cudaStream_t s) {
-    return tile_bytes > 64 * 1024 ? launch_fused_nt<double, I, false, 512, 1, 1, true>(sv, p, tile_bytes, s)
-                                  : launch_fused_nt<double, I, false, 256, 1, 3, true>(sv, p, tile_bytes, s);
+    const size_t smem = tile_bytes + kDiagTableBytes;  // the phase-table area after the tile
+    return tile_bytes > 64 * 1024 ? launch_fused_nt<double, I, false, 512, 1, 1, true>(sv, p, smem, s)
+                                  : launch_fused_nt<double, I, false, 256, 1, 3, true>(sv, p, smem, s);
 }
 
 template <class T, class I>
@@ -1352,6 +1385,14 @@ static lgpu_status_t fused_t(cplx_t<T> *sv, uint32_t n, const std::vector<int> &
     std::unique_ptr<FusedParams<T, I>> guard(p);
     if (!dfm && (ff_flags & LGPU_FF_IN))  // the complex128 kernels need complex128 amplitudes
         LGPU_TRY(lgpu_state_ff(sv, n, 0, reinterpret_cast<lgpu_stream_t>(s)));
+    // float-float blocks: diagonal gates folded into phase tables
+    std::vector<char> internal;
+    std::vector<lgpu_fused_gate_t> folded;
+    if (dfm && fused_diag_fold_enabled()) {
+        folded = fold_diagonal_gates(gates, ngates, pos, internal);
+        gates = folded.data();
+        ngates = uint32_t(folded.size());
+    }
     uint32_t done = 0;
     lgpu_status_t st = LGPU_OK;
     while (done < ngates && st == LGPU_OK) {
@@ -1364,6 +1405,18 @@ static lgpu_status_t fused_t(cplx_t<T> *sv, uint32_t n, const std::vector<int> &
             FGate &dst = p->gates[cnt];
             dst = FGate{};
             dst.ntgt = uint8_t(src.ntgt);
+            if (!internal.empty() && internal[done + cnt]) {  // a folded phase table (see fold_diagonal_gates)
+                for (int b = 0; b < src.nctrl; b++) dst.in_mask |= 1u << pos[size_t(src.ctrl[b])];
+                dst.mat_off = pool;
+                for (uint32_t e = 0; e < need; e++) {
+                    const DF d = df_split_host(src.m[e]);
+                    std::memcpy(&p->mats[pool + e], &d, sizeof(DF));
+                }
+                dst.body = uint8_t(B_DENSE);
+                pool += need;
+                cnt++;
+                continue;
+            }
             if (src.ntgt != 1 && src.ntgt != 2) { st = fail(LGPU_ERR_INVALID_ARG, "fused gate: 1 or 2 targets"); break; }
             for (int j = 0; j < src.ntgt; j++) {
                 if (src.tgt[j] < 0 || uint32_t(src.tgt[j]) >= n || pos[size_t(src.tgt[j])] < 0) {

@@ -53,6 +53,9 @@ int f64_mode();
 // (default, with f64_mode() == 1); the integer-pipe bodies when 0
 // (environment LGPU_FUSED_DF=0).
 int fused_df_enabled();
+// Folding of diagonal gates into phase tables in float-float fused blocks
+// (LGPU_DIAG_FOLD=0 turns it off).
+int fused_diag_fold_enabled();
 // Uncontrolled 1-target gates use the bulk-copy pipelined kernel when 1
 // (default); the grid-stride kernel when 0.  See lgpu_set_stream_mode().
 int bulk_enabled();

@@ -1,5 +1,6 @@
 """Host unit tests of the gate lowering and the shared-memory fusion planner
 (GateLowering.hpp), of the register-group split of a fused block
+(lgpu_fused_plan.h), of the folding of diagonal gates into phase tables
 (lgpu_fused_plan.h) and of the Pauli-word tile pass plan
 (lgpu_pauli_plan.h): invariants, and state equivalence of the reordered
 gates, on random inputs (compiled with the host compiler; no GPU needed)."""
@@ -45,6 +46,7 @@ def test_register_groups_keep_the_state():
         exe = os.path.join(d, "test_fused_groups")
         subprocess.run(["g++", "-O2", "-std=c++17",
                         "-I" + os.path.join(ROOT, "pennylane_lightning_gpu_gb300", "csrc", "kernels"),
+                        "-I" + os.path.join(ROOT, "include"),
                         os.path.join(ROOT, "tests", "native", "test_fused_groups.cpp"), "-o", exe], check=True)
         r = subprocess.run([exe], capture_output=True, text=True)
         assert r.returncode == 0, r.stdout + r.stderr
@@ -75,3 +77,19 @@ def test_lowering_matches_the_oracle():
         r = subprocess.run([exe], capture_output=True, text=True)
         assert r.returncode == 0, r.stdout + r.stderr
         assert "bad 0" in r.stdout
+
+
+def test_diagonal_folding_keeps_the_state():
+    """Diagonal gates of float-float fused blocks folded into phase tables
+    (lgpu_fused_plan.h::fold_diagonal_gates): 400 random blocks transform
+    random states exactly as the unfolded gate lists do."""
+    with tempfile.TemporaryDirectory() as d:
+        exe = os.path.join(d, "test_diag_fold")
+        subprocess.run(["g++", "-O2", "-std=c++17",
+                        "-I" + os.path.join(ROOT, "pennylane_lightning_gpu_gb300", "csrc", "kernels"),
+                        "-I" + os.path.join(ROOT, "include"),
+                        os.path.join(ROOT, "tests", "native", "test_diag_fold.cpp"), "-o", exe], check=True)
+        r = subprocess.run([exe], capture_output=True, text=True)
+        assert r.returncode == 0, r.stdout + r.stderr
+        assert "bad 0" in r.stdout
+
