@@ -75,7 +75,7 @@ int fused_diag_fold_enabled() {
     int m = g_diag_fold_mode.load(std::memory_order_relaxed);
     if (m < 0) {
         const char *e = std::getenv("LGPU_DIAG_FOLD");
-        m = (e && e[0] == '0') ? 0 : 1;
+        m = (e && (e[0] == '0' || e[0] == '1')) ? e[0] - '0' : 2;
         g_diag_fold_mode.store(m, std::memory_order_relaxed);
     }
     return m;

@@ -141,20 +141,76 @@ inline int group_fused_gates(FGate *gates, KC *kc, int cnt, int k, int R, FGroup
     return ng;
 }
 
+// A dense unitary 1-target gate U (all four entries non-zero, some entry not
+// real, not of the RX form [[a, -ib], [-ib, a]]) as D_L R D_R, applied D_R
+// first: R = [[c, -s], [s, c]] real, D_R = diag(1, e^{i r}), D_L =
+// diag(e^{i l0}, e^{i l1}) with c = |U00|, s = |U10|, l0 = arg U00, l1 =
+// arg U10, r = arg(-U01) - l0.  The product matches U00, U01 and U10 by
+// construction and U11 through unitarity (U11 = det U conj(U00)); the split
+// is taken only when the product reproduces U within 1e-13.  Controls carry
+// over (a controlled product is the product of the controlled factors).  R
+// takes the real body, about half the float-float operations of the dense
+// body, and the diagonals can fold into phase tables.
+inline bool split_dense_1q(const lgpu_fused_gate_t &g, lgpu_fused_gate_t f[3]) {
+    using cd = std::complex<double>;
+    if (g.ntgt != 1) return false;
+    const cd a(g.m[0], g.m[1]), b(g.m[2], g.m[3]), c(g.m[4], g.m[5]), d(g.m[6], g.m[7]);
+    if (a == 0.0 || b == 0.0 || c == 0.0 || d == 0.0) return false;
+    if (a.imag() == 0 && b.imag() == 0 && c.imag() == 0 && d.imag() == 0) return false;  // real body already
+    if (a.imag() == 0 && d.imag() == 0 && a.real() == d.real() && b.real() == 0 && c.real() == 0) return false;
+    const double cc = std::abs(a), ss = std::abs(c);
+    const double l0 = std::arg(a), l1 = std::arg(c), r = std::arg(-b) - l0;
+    const cd eL0 = std::polar(1.0, l0), eL1 = std::polar(1.0, l1), eR = std::polar(1.0, r);
+    const cd q[4] = {eL0 * cc, -eL0 * ss * eR, eL1 * ss, eL1 * cc * eR};
+    const cd u[4] = {a, b, c, d};
+    for (int e = 0; e < 4; e++)
+        if (std::abs(q[e] - u[e]) > 1e-13) return false;
+    for (int k = 0; k < 3; k++) {
+        f[k] = g;
+        for (double &x : f[k].m) x = 0.0;
+    }
+    f[0].m[0] = 1.0;
+    f[0].m[6] = eR.real();
+    f[0].m[7] = eR.imag();
+    f[1].m[0] = cc;
+    f[1].m[2] = -ss;
+    f[1].m[4] = ss;
+    f[1].m[6] = cc;
+    f[2].m[0] = eL0.real();
+    f[2].m[1] = eL0.imag();
+    f[2].m[6] = eL1.real();
+    f[2].m[7] = eL1.imag();
+    return true;
+}
+
 // Diagonal gates of a float-float block folded into phase tables.  A 1-target
 // gate whose 2x2 is diagonal (other than diag(+-1, +-1), which stays a sign
 // flip), with its controls (if any) on tile bits, is a diagonal on its
-// support (target and controls).  Such gates join a group
-// whose product is one table of 2^k phases over the union of the supports
-// (k <= kDiagTableBits), applied where the group's first gate stood.  A later
-// gate may join only if no gate between them targets a bit of its support
-// (diagonal gates commute with each other and with controls), so moving it
-// back changes nothing.  A group of one gate stays that gate.  A folded group
-// is returned as a record with ntgt = kDiagTableMark, its support bits in
-// ctrl[0..k-1] in ascending tile position (table index bit b = ctrl[b]) and the
-// table in m (entry i = m[2i] + i m[2i+1]); internal[i] marks those records.
+// support (target and controls).  It commutes with every diagonal gate and
+// with every gate that targets none of its support bits (controls are
+// diagonal), so it may run at any point between the nearest such blocking
+// gates before and after it.  Folding places groups of these gates at common
+// points (interval stabbing: the unplaced gate whose interval ends first
+// fixes the point, at that end, and every unplaced gate whose interval holds
+// the point joins while the union of the supports stays within
+// kDiagTableBits); a group is one table of 2^k phases over the union of its
+// supports.  A group of one gate stays that gate, in place.
+//
+// With split_dense, dense 1-target unitaries are first split by
+// split_dense_1q so that their diagonals can join the tables.  A split is
+// kept only while its estimated cost (a real body plus its diagonals, each a
+// table share or a diagonal body of its own) stays below the dense body's,
+// and only if the splits add no launch (kFusedMaxGates records per launch).
+// Cost units are float-float instructions per amplitude pair, shared-memory
+// pass included: dense body 110, real body 54, diagonal body 56, table 66.
+//
+// A folded group is returned as a record with ntgt = kDiagTableMark, its
+// support bits in ctrl[0..k-1] in ascending tile position (table index bit b
+// = ctrl[b]) and the table in m (entry i = m[2i] + i m[2i+1]); internal[i]
+// marks those records.
 inline std::vector<lgpu_fused_gate_t> fold_diagonal_gates(const lgpu_fused_gate_t *gates, uint32_t ngates,
-                                                          const std::vector<int> &pos, std::vector<char> &internal) {
+                                                          const std::vector<int> &pos, std::vector<char> &internal,
+                                                          bool split_dense = false) {
     using cd = std::complex<double>;
     const int n = int(pos.size());
     auto foldable = [&](const lgpu_fused_gate_t &g, uint64_t *support) {
@@ -176,46 +232,138 @@ inline std::vector<lgpu_fused_gate_t> fold_diagonal_gates(const lgpu_fused_gate_
         *support = sb;
         return true;
     };
-    struct Group {
-        size_t slot;  // index in out
-        uint64_t support;
-        std::vector<uint32_t> members;
-    };
-    std::vector<lgpu_fused_gate_t> out;
-    std::vector<Group> groups;
-    internal.clear();
-    int open = -1;         // the group later diagonal gates may join
-    uint64_t blocked = 0;  // bits targeted by other gates since the open group's first gate
-    for (uint32_t i = 0; i < ngates; i++) {
-        const lgpu_fused_gate_t &g = gates[i];
-        uint64_t sb = 0;
-        if (foldable(g, &sb)) {
-            if (open >= 0 && (sb & blocked) == 0 &&
-                __builtin_popcountll(groups[size_t(open)].support | sb) <= kDiagTableBits) {
-                groups[size_t(open)].support |= sb;
-                groups[size_t(open)].members.push_back(i);
-                continue;
-            }
-            open = int(groups.size());
-            groups.push_back(Group{out.size(), sb, {i}});
-            out.push_back(g);  // replaced below if the group takes more gates
-            internal.push_back(0);
-            blocked = 0;
-            continue;
+    // bits a gate acts on non-diagonally (all bits when unknown); 0 for a diagonal 2x2
+    auto blocks = [](const lgpu_fused_gate_t &g) -> uint64_t {
+        if (g.ntgt == 1 && g.m[2] == 0.0 && g.m[3] == 0.0 && g.m[4] == 0.0 && g.m[5] == 0.0) return 0;
+        if (g.ntgt < 1 || g.ntgt > 2) return ~uint64_t(0);
+        uint64_t t = 0;
+        for (int j = 0; j < g.ntgt; j++) {
+            if (g.tgt[j] < 0 || g.tgt[j] >= 64) return ~uint64_t(0);
+            t |= uint64_t(1) << g.tgt[j];
         }
-        out.push_back(g);
-        internal.push_back(0);
-        // a gate whose matrix is not diagonal blocks its targets
-        const bool diag1 = g.ntgt == 1 && g.m[2] == 0.0 && g.m[3] == 0.0 && g.m[4] == 0.0 && g.m[5] == 0.0;
-        if (!diag1)
-            for (int t = 0; t < g.ntgt && t < 2; t++)
-                if (g.tgt[t] >= 0 && g.tgt[t] < 64) blocked |= uint64_t(1) << g.tgt[t];
+        return t;
+    };
+    struct Item {
+        lgpu_fused_gate_t g;
+        int origin;  // index of the split source gate (-1: an input gate)
+        int part;    // 0 = D_R, 1 = R, 2 = D_L of a split
+    };
+    struct Fold {
+        std::vector<Item> list;
+        std::vector<int> group;     // per item: its group, or -1
+        std::vector<int> slot;      // per group: placed before item slot (list size: at the end)
+        std::vector<uint64_t> sup;  // per group: support bits
+        std::vector<std::vector<int>> members;
+        size_t records = 0;
+    };
+    auto run = [&](const std::vector<char> &split) {
+        Fold F;
+        for (uint32_t i = 0; i < ngates; i++) {
+            lgpu_fused_gate_t parts[3];
+            if (split[i] && split_dense_1q(gates[i], parts)) {
+                for (int k = 0; k < 3; k++) F.list.push_back(Item{parts[k], int(i), k});
+            } else {
+                F.list.push_back(Item{gates[i], -1, 0});
+            }
+        }
+        const int N = int(F.list.size());
+        std::vector<uint64_t> S(size_t(N), 0), B(size_t(N), 0);
+        std::vector<char> fold(size_t(N), 0);
+        for (int i = 0; i < N; i++) {
+            fold[size_t(i)] = foldable(F.list[size_t(i)].g, &S[size_t(i)]) ? 1 : 0;
+            B[size_t(i)] = blocks(F.list[size_t(i)].g);
+        }
+        std::vector<int> lo(size_t(N), 0), hi(size_t(N), N), cand;
+        for (int i = 0; i < N; i++) {
+            if (!fold[size_t(i)]) continue;
+            for (int j = i - 1; j >= 0; j--)
+                if (B[size_t(j)] & S[size_t(i)]) {
+                    lo[size_t(i)] = j + 1;
+                    break;
+                }
+            for (int j = i + 1; j < N; j++)
+                if (B[size_t(j)] & S[size_t(i)]) {
+                    hi[size_t(i)] = j;
+                    break;
+                }
+            cand.push_back(i);
+        }
+        std::stable_sort(cand.begin(), cand.end(), [&](int a, int b) { return hi[size_t(a)] < hi[size_t(b)]; });
+        F.group.assign(size_t(N), -1);
+        for (size_t ci = 0; ci < cand.size(); ci++) {
+            const int d = cand[ci];
+            if (F.group[size_t(d)] >= 0) continue;
+            const int gid = int(F.slot.size());
+            const int p = hi[size_t(d)];
+            uint64_t sup = S[size_t(d)];
+            std::vector<int> mem{d};
+            F.group[size_t(d)] = gid;
+            for (size_t cj = ci + 1; cj < cand.size(); cj++) {
+                const int e = cand[cj];
+                if (F.group[size_t(e)] >= 0 || lo[size_t(e)] > p) continue;
+                if (__builtin_popcountll(sup | S[size_t(e)]) > kDiagTableBits) continue;
+                sup |= S[size_t(e)];
+                mem.push_back(e);
+                F.group[size_t(e)] = gid;
+            }
+            F.slot.push_back(p);
+            F.sup.push_back(sup);
+            F.members.push_back(mem);
+        }
+        size_t tables = 0;
+        for (const auto &m : F.members) tables += m.size() >= 2;
+        size_t folded_away = 0;
+        for (const auto &m : F.members)
+            if (m.size() >= 2) folded_away += m.size();
+        F.records = size_t(N) - folded_away + tables;
+        return F;
+    };
+    // estimated cost of a split (see above) against the dense body's 110
+    auto split_cost = [&](const Fold &F, int origin) {
+        double c = 54.0;
+        for (size_t i = 0; i < F.list.size(); i++) {
+            if (F.list[i].origin != origin || F.list[i].part == 1) continue;
+            const int gid = F.group[i];
+            const size_t k = gid >= 0 ? F.members[size_t(gid)].size() : 1;
+            c += k >= 2 ? 66.0 / double(k) : 56.0;
+        }
+        return c;
+    };
+    std::vector<char> split(ngates, 0);
+    Fold F = run(split);
+    if (split_dense) {
+        bool any = false;
+        for (uint32_t i = 0; i < ngates; i++) {
+            lgpu_fused_gate_t parts[3];
+            split[i] = split_dense_1q(gates[i], parts) ? 1 : 0;
+            any = any || split[i];
+        }
+        if (any) {
+            const size_t launches0 = (F.records + kFusedMaxGates - 1) / kFusedMaxGates;
+            Fold S = run(split);
+            for (int it = 0; it < 64; it++) {  // drop the splits that do not pay, then refold
+                bool changed = false;
+                for (uint32_t i = 0; i < ngates; i++)
+                    if (split[i] && split_cost(S, int(i)) >= 110.0) {
+                        split[i] = 0;
+                        changed = true;
+                    }
+                if (!changed) break;
+                S = run(split);
+            }
+            bool kept = false;
+            for (uint32_t i = 0; i < ngates; i++) kept = kept || split[i];
+            if (kept && (S.records + kFusedMaxGates - 1) / kFusedMaxGates <= launches0) F = std::move(S);
+        }
     }
-    for (const Group &G : groups) {
-        if (G.members.size() < 2) continue;
+    // emit: the tables placed before item p, then item p unless it was folded
+    const int N = int(F.list.size());
+    std::vector<lgpu_fused_gate_t> out;
+    internal.clear();
+    auto emit_table = [&](size_t gid) {
         std::vector<int> bits;  // support bits in ascending tile position
         for (int b = 0; b < n; b++)
-            if ((G.support >> b) & 1u) bits.push_back(b);
+            if ((F.sup[gid] >> b) & 1u) bits.push_back(b);
         std::sort(bits.begin(), bits.end(), [&](int a, int b) { return pos[size_t(a)] < pos[size_t(b)]; });
         const int k = int(bits.size());
         lgpu_fused_gate_t r{};
@@ -230,8 +378,8 @@ inline std::vector<lgpu_fused_gate_t> fold_diagonal_gates(const lgpu_fused_gate_
                         if (bits[size_t(b)] == state_bit) return (idx >> b) & 1;
                     return 0;
                 };
-                for (uint32_t mi : G.members) {
-                    const lgpu_fused_gate_t &g = gates[mi];
+                for (int mi : F.members[gid]) {
+                    const lgpu_fused_gate_t &g = F.list[size_t(mi)].g;
                     bool on = true;
                     for (int c = 0; c < g.nctrl; c++)
                         if (bit(g.ctrl[c]) != (g.ctrl_val[c] ? 1 : 0)) on = false;
@@ -242,8 +390,19 @@ inline std::vector<lgpu_fused_gate_t> fold_diagonal_gates(const lgpu_fused_gate_
             r.m[2 * idx] = t.real();
             r.m[2 * idx + 1] = t.imag();
         }
-        out[G.slot] = r;
-        internal[G.slot] = 1;
+        out.push_back(r);
+        internal.push_back(1);
+    };
+    std::vector<std::vector<size_t>> at(size_t(N) + 1);
+    for (size_t gid = 0; gid < F.members.size(); gid++)
+        if (F.members[gid].size() >= 2) at[size_t(F.slot[gid])].push_back(gid);
+    for (int p = 0; p <= N; p++) {
+        for (size_t gid : at[size_t(p)]) emit_table(gid);
+        if (p == N) break;
+        const int gid = F.group[size_t(p)];
+        if (gid >= 0 && F.members[size_t(gid)].size() >= 2) continue;
+        out.push_back(F.list[size_t(p)].g);
+        internal.push_back(0);
     }
     return out;
 }

@@ -587,9 +587,21 @@ __device__ __forceinline__ void tile_pairs_df(float4 *tile, int E, int q, uint32
 // ascending order.
 template <int NT>
 __device__ __forceinline__ void tile_diag_table_df(float4 *tile, int E, uint32_t mask, const float4 *tab) {
+    // index bit b = tile bit q_b (ascending): (e >> (q_b - b)) & (1 << b); a
+    // missing bit shifts by 31 - b >= 28, past every bit of a tile index
+    int sh[kDiagTableBits];
+    {
+        uint32_t mm = mask;
+#pragma unroll
+        for (int b = 0; b < kDiagTableBits; b++) {
+            sh[b] = mm ? (__ffs(int(mm)) - 1 - b) : (31 - b);
+            mm &= mm - 1u;
+        }
+    }
     for (int e = threadIdx.x; e < E; e += NT) {
-        int idx = 0, b = 0;
-        for (uint32_t mm = mask; mm; mm &= mm - 1u, b++) idx |= ((e >> (__ffs(int(mm)) - 1)) & 1) << b;
+        int idx = 0;
+#pragma unroll
+        for (int b = 0; b < kDiagTableBits; b++) idx |= (e >> sh[b]) & (1 << b);
         const float4 t = tab[idx];  // (re.hi, re.lo, im.hi, im.lo)
         float4 &a = tile[swz<double>(e)];
         const DF2 x{f2_pack(a.x, a.y), f2_pack(a.z, a.w)}, xs{f2_pack(a.y, a.x), f2_pack(a.w, a.z)};
@@ -1389,7 +1401,7 @@ static lgpu_status_t fused_t(cplx_t<T> *sv, uint32_t n, const std::vector<int> &
     std::vector<char> internal;
     std::vector<lgpu_fused_gate_t> folded;
     if (dfm && fused_diag_fold_enabled()) {
-        folded = fold_diagonal_gates(gates, ngates, pos, internal);
+        folded = fold_diagonal_gates(gates, ngates, pos, internal, fused_diag_fold_enabled() == 2);
         gates = folded.data();
         ngates = uint32_t(folded.size());
     }

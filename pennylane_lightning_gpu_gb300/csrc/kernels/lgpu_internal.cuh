@@ -53,8 +53,10 @@ int f64_mode();
 // (default, with f64_mode() == 1); the integer-pipe bodies when 0
 // (environment LGPU_FUSED_DF=0).
 int fused_df_enabled();
-// Folding of diagonal gates into phase tables in float-float fused blocks
-// (LGPU_DIAG_FOLD=0 turns it off).
+// Folding of diagonal gates into phase tables in float-float fused blocks:
+// 2 (default) = fold, with dense 1-target gates split into diagonals and a
+// real rotation where that pays; 1 = fold without splits; 0 = off
+// (environment LGPU_DIAG_FOLD).
 int fused_diag_fold_enabled();
 // Uncontrolled 1-target gates use the bulk-copy pipelined kernel when 1
 // (default); the grid-stride kernel when 0.  See lgpu_set_stream_mode().

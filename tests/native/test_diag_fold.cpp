@@ -1,11 +1,14 @@
 // Host test of the folding of diagonal gates into phase tables
 // (lgpu_fused_plan.h::fold_diagonal_gates), which the float-float fused blocks
-// apply instead of the gates: on random blocks (1-target gates, diagonal or
-// not, with controls inside or outside the tile, and 2-target gates) the
-// folded list must transform random states exactly as the original list
-// does, every table must cover at most kDiagTableBits tile positions, the
-// records must be flagged as folded exactly when they are tables, and
-// diag(+-1, +-1) gates must stay as they are.
+// apply instead of the gates, without and with the split of dense 1-target
+// unitaries (split_dense_1q): on random blocks (1-target gates, diagonal,
+// dense unitary or general, with controls inside or outside the tile, and
+// 2-target gates) the folded list must transform random states as the
+// original list does (within 1e-12), every table must cover at most
+// kDiagTableBits tile positions, the records must be flagged as folded
+// exactly when they are tables, diag(+-1, +-1) gates must stay as they are,
+// and the splits must add no launch of kFusedMaxGates records.  Layer-shaped
+// blocks (dense unitaries on every tile bit, then CNOTs) must keep splits.
 #include <complex>
 #include <cstdio>
 #include <random>
@@ -62,17 +65,57 @@ static void apply(std::vector<cd> &v, const lgpu_fused_gate_t &g, bool table) {
     }
 }
 
+// e^{i a} RZ(b) RY(c) RZ(d) as a 2x2 (re/im interleaved, row-major)
+static void random_unitary(std::mt19937_64 &gen, double *m) {
+    std::uniform_real_distribution<double> ang(-3.1, 3.1);
+    const double a = ang(gen), b = ang(gen), c = ang(gen), d = ang(gen);
+    const cd u[4] = {std::polar(std::cos(c / 2), a - b / 2 - d / 2), -std::polar(std::sin(c / 2), a - b / 2 + d / 2),
+                     std::polar(std::sin(c / 2), a + b / 2 - d / 2), std::polar(std::cos(c / 2), a + b / 2 + d / 2)};
+    for (int e = 0; e < 4; e++) {
+        m[2 * e] = u[e].real();
+        m[2 * e + 1] = u[e].imag();
+    }
+}
+
+static size_t launches(size_t records) { return (records + lgpu::kFusedMaxGates - 1) / lgpu::kFusedMaxGates; }
+
+static size_t real_records(const std::vector<lgpu_fused_gate_t> &f, const std::vector<char> &internal) {
+    size_t r = 0;
+    for (size_t i = 0; i < f.size(); i++)
+        r += !internal[i] && f[i].ntgt == 1 && f[i].m[1] == 0 && f[i].m[3] == 0 && f[i].m[5] == 0 && f[i].m[7] == 0 &&
+             f[i].m[0] != 0 && f[i].m[2] != 0 && f[i].m[4] != 0 && f[i].m[6] != 0;
+    return r;
+}
+
 int main() {
     std::mt19937_64 gen(11);
     std::normal_distribution<double> nd;
     const int n = 8, k = 6;  // tile = bits 0..5; bits 6, 7 outside
     std::vector<int> pos(n, -1);
     for (int q = 0; q < k; q++) pos[size_t(q)] = q;
-    long tables = 0, folded_gates = 0, gates_total = 0;
-    for (int trial = 0; trial < 400; trial++) {
-        const int cnt = 1 + int(gen() % 40);
+    long tables = 0, folded_gates = 0, gates_total = 0, split_kept = 0;
+    for (int trial = 0; trial < 600; trial++) {
+        const bool layered = trial >= 400;  // dense unitaries on every tile bit, then CNOTs
+        const int cnt = layered ? 3 * (k + 3) : 1 + int(gen() % 40);
         std::vector<lgpu_fused_gate_t> g(static_cast<size_t>(cnt));
+        for (int gi = 0; gi < cnt && layered; gi++) {
+            auto &x = g[size_t(gi)];
+            x = lgpu_fused_gate_t{};
+            x.ntgt = 1;
+            const int r = gi % (k + 3);
+            if (r < k) {
+                x.tgt[0] = r;
+                random_unitary(gen, x.m);
+            } else {  // CNOT
+                x.tgt[0] = int(gen() % k);
+                do x.ctrl[0] = int(gen() % k); while (x.ctrl[0] == x.tgt[0]);
+                x.ctrl_val[0] = 1;
+                x.nctrl = 1;
+                x.m[2] = x.m[4] = 1.0;
+            }
+        }
         for (auto &x : g) {
+            if (layered) break;
             x = lgpu_fused_gate_t{};
             const bool two = gen() % 6 == 0;
             x.ntgt = two ? 2 : 1;
@@ -92,6 +135,10 @@ int main() {
                 x.nctrl++;
             }
             const int d = two ? 4 : 2;
+            if (!two && gen() % 3 == 0) {  // a dense unitary (split candidate)
+                random_unitary(gen, x.m);
+                continue;
+            }
             const bool diag = !two && gen() % 2 == 0;
             const bool sign = diag && gen() % 4 == 0;  // diag(+-1, +-1): stays a sign flip
             for (int r = 0; r < d; r++)
@@ -101,8 +148,13 @@ int main() {
                     x.m[2 * (r * d + c) + 1] = zero || sign ? 0.0 : nd(gen);
                 }
         }
+        size_t plain_records = 0;
+        for (int split = 0; split < 2; split++) {
         std::vector<char> internal;
-        const auto f = lgpu::fold_diagonal_gates(g.data(), uint32_t(cnt), pos, internal);
+        const auto f = lgpu::fold_diagonal_gates(g.data(), uint32_t(cnt), pos, internal, split != 0);
+        if (split == 0) plain_records = f.size();
+        else if (launches(f.size()) > launches(plain_records)) fail("splits add a launch", trial, double(f.size()));
+        if (split && layered) split_kept += long(real_records(f, internal));
         if (internal.size() != f.size()) fail("flag count", trial, double(internal.size()));
         for (size_t i = 0; i < f.size(); i++) {
             const bool tab = internal[i] != 0;
@@ -125,10 +177,13 @@ int main() {
             long before = 0, after = 0;
             for (const auto &x : g) before += is_sign(x);
             for (size_t i = 0; i < f.size(); i++) after += !internal[i] && is_sign(f[i]);
-            if (before != after) fail("sign-diagonal gate folded", trial, double(before - after));
+            if (after < before || (!split && before != after))
+                fail("sign-diagonal gate folded", trial, double(before - after));
         }
-        gates_total += cnt;
-        folded_gates += cnt - long(f.size());
+        if (!split) {
+            gates_total += cnt;
+            folded_gates += cnt - long(f.size());
+        }
         for (int rep = 0; rep < 2; rep++) {
             std::vector<cd> a(size_t(1) << n), b;
             for (auto &z : a) z = cd(nd(gen), nd(gen));
@@ -142,9 +197,11 @@ int main() {
             }
             if (err > 1e-12 * scale) fail("state differs", trial, err / scale);
         }
+        }
     }
     if (tables == 0) fail("no table formed", 0, 0);
-    std::printf("blocks 400 gates %ld tables %ld gates folded away %ld bad %ld\n", gates_total, tables, folded_gates,
-                bad);
+    if (split_kept == 0) fail("no split kept", 0, 0);
+    std::printf("blocks 600 gates %ld tables %ld gates folded away %ld real bodies in split layers %ld bad %ld\n",
+                gates_total, tables, folded_gates, split_kept, bad);
     return bad == 0 ? 0 : 1;
 }
