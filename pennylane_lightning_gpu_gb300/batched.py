@@ -30,24 +30,17 @@ class BatchedExecutor:
         self.n_circuits = 0
 
     def add(self, n, ops, observable):
-        names = [o[0] for o in ops]
-        wires = [list(o[1]) for o in ops]
-        params = [[float(x) for x in o[2]] for o in ops]
-        inv = [bool(o[3]) if len(o) > 3 else False for o in ops]
-        obs = [(float(c), str(w), list(ws)) for c, w, ws in observable]
+        """Add a circuit; the op tuples and terms are read by the native side
+        in one pass (no per-op Python work)."""
+        idx = self._ex.add_circuit(int(n), ops, observable)
         self.n_circuits += 1
-        return self._ex.add_circuit(int(n), names, wires, params, inv, obs)
+        return idx
 
     def add_template(self, n, ops, observable):
         """A circuit structure shared by many parameter sets, lowered and fused
         once; returns its id.  The parameters of the parametric gates in `ops`
         are placeholders (template_num_params(tid) of them, in op order)."""
-        names = [o[0] for o in ops]
-        wires = [list(o[1]) for o in ops]
-        params = [[float(x) for x in o[2]] for o in ops]
-        inv = [bool(o[3]) if len(o) > 3 else False for o in ops]
-        obs = [(float(c), str(w), list(ws)) for c, w, ws in observable]
-        return self._ex.add_template(int(n), names, wires, params, inv, obs)
+        return self._ex.add_template(int(n), ops, observable)
 
     def template_num_params(self, tid):
         return self._ex.template_num_params(int(tid))

@@ -530,6 +530,52 @@ template <class PrecisionT, class ParamT> void sv_class_bindings(py::module_ &m)
             });
 }
 
+// Operations as the Python list of (name, wires, params[, inverse]) tuples and
+// the observable as (coeff, word, wires) terms, unpacked in one pass here
+// (wires and params: any iterables of integers and numbers).
+struct BatchOps {
+    std::vector<std::string> names;
+    std::vector<std::vector<size_t>> wires;
+    std::vector<std::vector<double>> params;
+    std::vector<bool> inverses;
+};
+
+inline BatchOps unpack_batch_ops(const py::sequence &ops) {
+    BatchOps L;
+    const size_t n = py::len(ops);
+    L.names.reserve(n);
+    L.wires.reserve(n);
+    L.params.reserve(n);
+    L.inverses.reserve(n);
+    for (py::handle h : ops) {
+        const auto o = py::reinterpret_borrow<py::sequence>(h);
+        const size_t len = py::len(o);
+        PL_ABORT_IF(len < 3, "an operation is (name, wires, params[, inverse])");
+        L.names.push_back(o[0].cast<std::string>());
+        std::vector<size_t> w;
+        for (py::handle x : py::object(o[1])) w.push_back(x.cast<size_t>());
+        std::vector<double> p;
+        for (py::handle x : py::object(o[2])) p.push_back(x.cast<double>());
+        L.wires.push_back(std::move(w));
+        L.params.push_back(std::move(p));
+        L.inverses.push_back(len > 3 ? py::object(o[3]).cast<bool>() : false);
+    }
+    return L;
+}
+
+template <class Term> std::vector<Term> unpack_batch_terms(const py::sequence &obs) {
+    std::vector<Term> terms;
+    terms.reserve(py::len(obs));
+    for (py::handle h : obs) {
+        const auto t = py::reinterpret_borrow<py::sequence>(h);
+        PL_ABORT_IF(py::len(t) != 3, "an observable term is (coeff, word, wires)");
+        std::vector<size_t> w;
+        for (py::handle x : py::object(t[2])) w.push_back(x.cast<size_t>());
+        terms.push_back({py::object(t[0]).cast<double>(), py::object(t[1]).cast<std::string>(), std::move(w)});
+    }
+    return terms;
+}
+
 template <class PrecisionT> void batched_bindings(py::module_ &m) {
     using BE = BatchedExecutor<PrecisionT>;
     const std::string name = std::string("BatchedExecutor_C") + (std::is_same_v<PrecisionT, double> ? "128" : "64");
@@ -537,24 +583,20 @@ template <class PrecisionT> void batched_bindings(py::module_ &m) {
         .def(py::init<int, int, int>(), py::arg("kmax") = 0, py::arg("threads") = 256, py::arg("grid") = 0)
         .def(
             "add_circuit",
-            [](BE &be, size_t n, const std::vector<std::string> &names, const std::vector<std::vector<size_t>> &wires,
-               const std::vector<std::vector<double>> &params, const std::vector<bool> &inverses,
-               const std::vector<std::tuple<double, std::string, std::vector<size_t>>> &obs) {
-                std::vector<typename BE::PTerm> terms;
-                for (const auto &t : obs) terms.push_back({std::get<0>(t), std::get<1>(t), std::get<2>(t)});
-                return be.addCircuit(n, names, wires, params, inverses, terms);
+            [](BE &be, size_t n, const py::sequence &ops, const py::sequence &obs) {
+                const BatchOps L = unpack_batch_ops(ops);
+                const auto terms = unpack_batch_terms<typename BE::PTerm>(obs);
+                return be.addCircuit(n, L.names, L.wires, L.params, L.inverses, terms);
             },
-            "Add a circuit (ops as names/wires/params/inverses, observable as (coeff, word, wires) terms).")
+            "Add a circuit: ops as (name, wires, params[, inverse]) tuples, observable as (coeff, word, wires) terms.")
         .def(
             "add_template",
-            [](BE &be, size_t n, const std::vector<std::string> &names, const std::vector<std::vector<size_t>> &wires,
-               const std::vector<std::vector<double>> &params, const std::vector<bool> &inverses,
-               const std::vector<std::tuple<double, std::string, std::vector<size_t>>> &obs) {
-                std::vector<typename BE::PTerm> terms;
-                for (const auto &t : obs) terms.push_back({std::get<0>(t), std::get<1>(t), std::get<2>(t)});
-                return be.addTemplate(n, names, wires, params, inverses, terms);
+            [](BE &be, size_t n, const py::sequence &ops, const py::sequence &obs) {
+                const BatchOps L = unpack_batch_ops(ops);
+                const auto terms = unpack_batch_terms<typename BE::PTerm>(obs);
+                return be.addTemplate(n, L.names, L.wires, L.params, L.inverses, terms);
             },
-            "Add a circuit structure shared by many parameter sets; returns its id.")
+            "Add a circuit structure shared by many parameter sets (same arguments as add_circuit); returns its id.")
         .def("template_num_params", &BE::templateNumParams)
         .def(
             "add_instances",

@@ -11,10 +11,13 @@
 #pragma once
 
 #include <algorithm>
+#include <atomic>
 #include <cstring>
+#include <exception>
 #include <memory>
 #include <numeric>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "GateLowering.hpp"
@@ -113,6 +116,7 @@ template <class Precision> class BatchedExecutor {
         std::vector<double> pool;
         std::vector<double> cost(circuits_.size());
         size_t max_big = 0;
+        planShapes();
         for (size_t ci = 0; ci < circuits_.size(); ci++) {
             const Shape &c = *circuits_[ci].shape;
             const size_t param_off = circuits_[ci].param_off;
@@ -333,6 +337,38 @@ template <class Precision> class BatchedExecutor {
         }
         sh->nparams = pvec.size() - base;
         return sh;
+    }
+
+    // Plan every distinct unplanned shape, on up to 16 host threads (a batch of
+    // distinct circuits has as many shapes as circuits; planning one touches
+    // only that shape).  An error in any shape is raised here.
+    void planShapes() {
+        std::vector<Shape *> todo;
+        for (const auto &c : circuits_)
+            if (!c.shape->planned) todo.push_back(c.shape.get());
+        std::sort(todo.begin(), todo.end());
+        todo.erase(std::unique(todo.begin(), todo.end()), todo.end());
+        const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+        const size_t nthreads = std::min<size_t>({size_t(16), size_t(hw), (todo.size() + 63) / 64});
+        if (nthreads <= 1) {
+            for (Shape *sh : todo) planBlocks(*sh);
+            return;
+        }
+        std::atomic<size_t> next{0};
+        std::vector<std::exception_ptr> errs(nthreads);
+        std::vector<std::thread> pool;
+        for (size_t t = 0; t < nthreads; t++)
+            pool.emplace_back([&, t] {
+                try {
+                    for (size_t i = next.fetch_add(1); i < todo.size(); i = next.fetch_add(1)) planBlocks(*todo[i]);
+                } catch (...) {
+                    errs[t] = std::current_exception();
+                    next.store(todo.size());
+                }
+            });
+        for (auto &th : pool) th.join();
+        for (auto &e : errs)
+            if (e) std::rethrow_exception(e);
     }
 
     // Fused blocks of a shape (computed on first use): one block holding the

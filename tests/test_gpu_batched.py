@@ -88,3 +88,30 @@ def test_templates_match_per_circuit_adds(dtype):
     base = np.cumsum([0] + [p.shape[0] for _, p in templates])
     got = np.array([b[base[ti] + row] for ti, row in order])
     assert np.array_equal(got, a)
+
+
+def test_add_reads_op_tuples_of_any_numeric_type(oracle):
+    """add() hands the op tuples to the native side as they are: numpy wires
+    and parameters, ops without the inverse flag, numpy booleans and tuples
+    instead of lists give the same circuit; a malformed op raises."""
+    n = 9
+    rng = np.random.default_rng(3)
+    ops = workloads.random_circuit(n, 2, rng) + [("PhaseShift", [4], [0.3], True), ("CRX", [2, 5], [0.9], True)]
+    obs = workloads.random_pauli_hamiltonian(n, 5, rng, max_wires=3)
+    odd_ops = []
+    for i, (name, wires, params, inv) in enumerate(ops):
+        if i % 2 == 0 and not inv:
+            odd_ops.append((name, np.array(wires, np.int64), np.array(params, np.float64)))
+        else:
+            odd_ops.append((name, tuple(wires), tuple(np.float64(x) for x in params), np.bool_(inv)))
+    odd_obs = [(np.float64(c), w, np.array(ws)) for c, w, ws in obs]
+    ex = batched.BatchedExecutor(np.complex128)
+    ex.add(n, ops, obs)
+    ex.add(n, odd_ops, odd_obs)
+    ex.prepare(capture=False)
+    a, b = ex.run()
+    assert abs(a - _oracle_value(oracle, n, ops, obs)) < 1e-10
+    assert a == b
+    bad = batched.BatchedExecutor(np.complex128)
+    with pytest.raises(Exception):
+        bad.add(n, [("RX", [0])], obs)
