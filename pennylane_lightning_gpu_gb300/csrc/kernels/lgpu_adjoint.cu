@@ -8,8 +8,11 @@
 // which replaces the reference's per-op sequence of a D2D copy of lambda,
 // U^dag on lambda, G on mu, K cuBLAS dot products and U^dag on K bras
 // (AdjointDiffGPU.hpp:560-595).
+#include <algorithm>
+#include <complex>
 #include <cstddef>
 #include <memory>
+#include <vector>
 
 #include "lgpu_bodies.cuh"
 #include "lgpu_df2.cuh"
@@ -649,16 +652,25 @@ constexpr int kAdjBlockSteps = 48;
 constexpr int kAdjBlockBras = 2;
 constexpr int kAdjBlockThreads = 256;
 
+constexpr int kAdjGroupBits = 3;   // phase group: table over at most 3 tile positions
+constexpr int kAdjGroupGrads = 4;  // and at most 4 gradient steps
+constexpr uint8_t kAdjPhaseGroup = 2;
+
 struct AStep {
     uint8_t q;      // tile position of the target
     uint8_t body;   // Body1 of U^dag
     int8_t gk;      // GenKind, G_NONE: no gradient
-    uint8_t pad;    // 1: U^dag = diag(+-1, +-1), sign flips
+    uint8_t pad;    // 1: U^dag = diag(+-1, +-1), sign flips; kAdjPhaseGroup: a phase group
     int32_t slot;   // accumulator slot of a gradient step
-    uint32_t in_mask, in_val;    // controls inside the tile
+    uint32_t in_mask, in_val;    // controls inside the tile (phase group: the table positions)
     uint64_t out_mask, out_val;  // controls outside the tile (state bits)
-    DF u[8];
-    DF g[8];
+    DF u[8];  // phase group: Re of the table entries
+    DF g[8];  // phase group: Im of the table entries
+    // phase group: its gradient steps (tile position, G_Z or G_P1, slot)
+    uint8_t ng;
+    uint8_t gq[kAdjGroupGrads];
+    int8_t gkd[kAdjGroupGrads];
+    int16_t gslot[kAdjGroupGrads];
 };
 
 template <class I> struct AdjBlockParams {
@@ -767,6 +779,63 @@ __device__ __forceinline__ void adj_block_step(float4 *kt, float4 *const (&bt)[k
     }
 }
 
+// A phase group (host: consecutive uncontrolled diagonal steps, RZ,
+// PhaseShift or gradient-free, on at most kAdjGroupBits tile positions).
+// Their U^dag are diagonal and commute with each other and with the
+// generators Z and P1, so every overlap Im <bra| G_j |lambda> equals its value
+// before any of the group's U^dag is applied: one product Im(conj(bra)
+// lambda) per amplitude serves all of them (G_Z: + for target bit 0, - for 1;
+// G_P1: bit 1 only), and one table of the U^dag products (staged in shared
+// memory by the caller, entries (re.hi, re.lo, im.hi, im.lo)) multiplies
+// lambda and the bras.
+template <int NB>
+__device__ __forceinline__ void adj_phase_group(float4 *kt, float4 *const (&bt)[kAdjBlockBras], int E, const AStep &st,
+                                                const float4 *tab, DF (&acc)[kAdjGroupGrads][kAdjBlockBras]) {
+    int sh[kAdjGroupBits];  // index bit b = tile bit q_b (ascending): (e >> (q_b - b)) & (1 << b)
+    {
+        uint32_t mm = st.in_mask;
+#pragma unroll
+        for (int b = 0; b < kAdjGroupBits; b++) {
+            sh[b] = mm ? (__ffs(int(mm)) - 1 - b) : (31 - b);
+            mm &= mm - 1u;
+        }
+    }
+    const int ng = st.ng;
+    for (int e = threadIdx.x; e < E; e += kAdjBlockThreads) {
+        int idx = 0;
+#pragma unroll
+        for (int b = 0; b < kAdjGroupBits; b++) idx |= (e >> sh[b]) & (1 << b);
+        const float4 t = tab[idx];
+        const DF2 c1{f2_pack(t.x, t.x), f2_pack(t.y, t.y)}, c2{f2_pack(-t.z, t.z), f2_pack(-t.w, t.w)};
+        auto phase = [&](float4 &a) {
+            const DF2 x{f2_pack(a.x, a.y), f2_pack(a.z, a.w)}, xs{f2_pack(a.y, a.x), f2_pack(a.w, a.z)};
+            const DF2 y = df2_sum<2>({df2_mul(c1, x), df2_mul(c2, xs)});
+            a = make_float4(f2_x(y.hi), f2_y(y.hi), f2_x(y.lo), f2_y(y.lo));
+        };
+        const int si = swz<double>(e);
+        float4 kv = kt[si];
+        const DF kr{kv.x, kv.z}, ki{kv.y, kv.w};
+#pragma unroll
+        for (int b = 0; b < NB; b++) {
+            float4 bv = bt[b][si];
+            if (ng > 0) {
+                const DF pr = df_sum<2>({df_mul(DF{bv.x, bv.z}, ki), df_neg(df_mul(DF{bv.y, bv.w}, kr))});
+#pragma unroll
+                for (int j = 0; j < kAdjGroupGrads; j++) {
+                    if (j >= ng) break;
+                    const int bit = (e >> st.gq[j]) & 1;
+                    const DF c = st.gkd[j] == G_Z ? (bit ? df_neg(pr) : pr) : (bit ? pr : DF{0.0f, 0.0f});
+                    acc[j][b] = df_sum<2>({acc[j][b], c});
+                }
+            }
+            phase(bv);
+            bt[b][si] = bv;
+        }
+        phase(kv);
+        kt[si] = kv;
+    }
+}
+
 template <int NB>
 __device__ __forceinline__ void adj_block_dispatch(float4 *kt, float4 *const (&bt)[kAdjBlockBras], int E,
                                                    const AStep &st, DF (&acc)[kAdjBlockBras]) {
@@ -838,6 +907,35 @@ __global__ void __launch_bounds__(kAdjBlockThreads, 3) adjoint_block_kernel(cons
         for (int si = 0; si < p.nsteps; si++) {
             const AStep &st = p.steps[si];
             if ((uint64_t(base) & st.out_mask) != st.out_val) continue;  // tile-uniform
+            if (st.pad == kAdjPhaseGroup) {
+                float4 *tab = reinterpret_cast<float4 *>(wacc + size_t(p.nslots) * NB * W);
+                if (threadIdx.x < (1 << kAdjGroupBits))
+                    tab[threadIdx.x] = make_float4(st.u[threadIdx.x].hi, st.u[threadIdx.x].lo, st.g[threadIdx.x].hi,
+                                                   st.g[threadIdx.x].lo);
+                __syncthreads();
+                DF gacc[kAdjGroupGrads][kAdjBlockBras];
+#pragma unroll
+                for (int j = 0; j < kAdjGroupGrads; j++)
+#pragma unroll
+                    for (int b = 0; b < kAdjBlockBras; b++) gacc[j][b] = DF{0.0f, 0.0f};
+                adj_phase_group<NB>(kt, bt, E, st, tab, gacc);
+#pragma unroll
+                for (int j = 0; j < kAdjGroupGrads; j++) {
+                    if (j >= st.ng) break;
+#pragma unroll
+                    for (int b = 0; b < NB; b++) {
+                        DF v = gacc[j][b];
+#pragma unroll
+                        for (int o = 16; o > 0; o >>= 1) v = df_sum<2>({v, df_shfl_xor(v, o)});
+                        if (lane == 0) {
+                            DF &slot = wacc[(st.gslot[j] * NB + b) * W + warp];
+                            slot = df_sum<2>({slot, v});
+                        }
+                    }
+                }
+                __syncthreads();
+                continue;
+            }
             DF acc[kAdjBlockBras];
 #pragma unroll
             for (int b = 0; b < kAdjBlockBras; b++) acc[b] = DF{0.0f, 0.0f};
@@ -1348,9 +1446,85 @@ static lgpu_status_t adjoint_block_t(lgpu_context_t ctx, void *ket, void *const 
         }
     }
     p->nslots = int(cols.size());
+    if (!c64 && adj_phase_groups_enabled()) {
+        // Phase groups: uncontrolled diagonal steps (RZ, PhaseShift, or
+        // without gradient) on at most kAdjGroupBits tile positions, at most
+        // kAdjGroupGrads of them with a gradient.  A group starts at such a
+        // step and takes later ones moved back past the steps in between: a
+        // diagonal step commutes (with its generator, Z or P1) with every
+        // diagonal step and with every step that targets another position
+        // (controls are diagonal), so only a non-diagonal step on its
+        // position blocks the move.  The steps left behind keep their order.
+        auto groupable = [&](const AStep &st) {
+            return st.body == B_DIAG && st.pad == 0 && st.in_mask == 0 && st.out_mask == 0 &&
+                   (st.gk == G_NONE || st.gk == G_Z || st.gk == G_P1);
+        };
+        auto diagonal = [&](const AStep &st) { return st.body == B_DIAG || st.pad == 1; };
+        std::vector<AStep> in(p->steps, p->steps + nsteps), out;
+        std::vector<char> used(nsteps, 0);
+        for (uint32_t i = 0; i < nsteps; i++) {
+            if (used[i]) continue;
+            if (!groupable(in[i])) {
+                out.push_back(in[i]);
+                continue;
+            }
+            std::vector<uint32_t> mem{i};
+            uint32_t pm = 1u << in[i].q, blocked = 0;
+            int ng = in[i].gk != G_NONE ? 1 : 0;
+            for (uint32_t j = i + 1; j < nsteps; j++) {
+                if (used[j]) continue;
+                const AStep &st = in[j];
+                const bool can = groupable(st) && !((blocked >> st.q) & 1u) &&
+                                 __builtin_popcount(pm | (1u << st.q)) <= kAdjGroupBits &&
+                                 ng + (st.gk != G_NONE ? 1 : 0) <= kAdjGroupGrads;
+                if (can) {
+                    mem.push_back(j);
+                    pm |= 1u << st.q;
+                    ng += st.gk != G_NONE ? 1 : 0;
+                } else if (!diagonal(st)) {
+                    blocked |= 1u << st.q;  // later steps on this position stay behind it
+                }
+            }
+            if (mem.size() < 2) {
+                out.push_back(in[i]);
+                continue;
+            }
+            AStep gs{};
+            gs.pad = kAdjPhaseGroup;
+            gs.gk = int8_t(G_NONE);
+            gs.slot = -1;
+            gs.in_mask = pm;
+            std::vector<int> bits;  // table positions, ascending
+            for (int q = 0; q < 32; q++)
+                if ((pm >> q) & 1u) bits.push_back(q);
+            for (int idx = 0; idx < (1 << kAdjGroupBits); idx++) {
+                std::complex<double> t(1.0, 0.0);
+                for (uint32_t r : mem) {
+                    const double *u = steps[r].u;
+                    const int rank = int(std::find(bits.begin(), bits.end(), int(in[r].q)) - bits.begin());
+                    t *= ((idx >> rank) & 1) ? std::complex<double>(u[6], u[7]) : std::complex<double>(u[0], u[1]);
+                }
+                gs.u[idx] = df_split_host(t.real());
+                gs.g[idx] = df_split_host(t.imag());
+            }
+            for (uint32_t r : mem) {
+                used[r] = 1;
+                if (in[r].gk == G_NONE) continue;
+                gs.gq[gs.ng] = in[r].q;
+                gs.gkd[gs.ng] = in[r].gk;
+                gs.gslot[gs.ng] = int16_t(in[r].slot);
+                gs.ng++;
+            }
+            out.push_back(gs);
+        }
+        for (size_t r = 0; r < out.size(); r++) p->steps[r] = out[r];
+        p->nsteps = int(out.size());
+    }
     if (c64 && m < 1) return fail(LGPU_ERR_INVALID_ARG, "adjoint block: complex64 tiles need bit 0");
     const size_t tile_bytes = (size_t(1) << k) * (c64 ? 8 : 16);
-    const size_t smem = (nbras + 1) * tile_bytes + size_t(std::max(p->nslots, 1)) * nbras * 8 * sizeof(DF);
+    // tiles, the per-warp sums, then the phase-group table (complex128)
+    const size_t smem = (nbras + 1) * tile_bytes + size_t(std::max(p->nslots, 1)) * nbras * 8 * sizeof(DF) +
+                        (c64 ? 0 : (size_t(16) << kAdjGroupBits));
     const int per_sm = std::max(1, std::min(3, int((220 * 1024) / smem)));
     const unsigned grid = unsigned(std::min<uint64_t>(uint64_t(p->ntiles), uint64_t(sm_count()) * per_sm));
     // scratch: [reduction counter, 256 B, untouched][columns][partials]

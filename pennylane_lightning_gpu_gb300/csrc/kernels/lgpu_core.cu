@@ -71,6 +71,18 @@ int fused_df_enabled() {
 
 static std::atomic<int> g_diag_fold_mode{-1};
 
+static std::atomic<int> g_adj_groups_mode{-1};
+
+int adj_phase_groups_enabled() {
+    int m = g_adj_groups_mode.load(std::memory_order_relaxed);
+    if (m < 0) {
+        const char *e = std::getenv("LGPU_ADJ_GROUPS");
+        m = (e && e[0] == '0') ? 0 : 1;
+        g_adj_groups_mode.store(m, std::memory_order_relaxed);
+    }
+    return m;
+}
+
 int fused_diag_fold_enabled() {
     int m = g_diag_fold_mode.load(std::memory_order_relaxed);
     if (m < 0) {

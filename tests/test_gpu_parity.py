@@ -531,6 +531,45 @@ def test_adjoint_fused_blocks(native, oracle, n, nobs, dtype):
     assert np.max(np.abs(ref)) > 1e-3  # the circuit has gradients to compare
 
 
+@pytest.mark.parametrize("n,nobs", [(14, 1), (14, 2), (15, 3)])
+def test_adjoint_phase_groups(native, oracle, n, nobs):
+    """complex128 fused adjoint blocks take runs of uncontrolled diagonal
+    steps (RZ, PhaseShift, trainable or not, adjoint or not) on up to 3 tile
+    positions as phase groups: one overlap product per amplitude for all of
+    them, then one phase table.  Layers of RY / RZ / PhaseShift runs with CZ
+    and CNOT between them, a trainable subset, 1 to 3 observables: against
+    the oracle adjoint at 50 x 1e-10."""
+    rng = np.random.default_rng(4100 + n + nobs)
+    ops = [("Hadamard", [w], [], False) for w in range(n)]
+    for layer in range(4):
+        for w in range(n):
+            ops.append(("RY", [w], [float(rng.uniform(0, 2 * np.pi))], bool(rng.integers(2))))
+        for w in rng.permutation(n):  # diagonal runs, several gates on one wire at times
+            name = ("RZ", "PhaseShift")[int(rng.integers(2))]
+            ops.append((name, [int(w)], [float(rng.uniform(0, 2 * np.pi))], bool(rng.integers(2))))
+            if rng.integers(4) == 0:
+                ops.append(("RZ", [int(w)], [float(rng.uniform(0, 2 * np.pi))], False))
+        for w in range(0, n - 1, 2):
+            ops.append((("CZ", "CNOT")[layer % 2], [w, w + 1], [], False))
+    nparam = sum(1 for o in ops if o[2])
+    tp = sorted(int(x) for x in rng.choice(nparam, size=nparam * 2 // 3, replace=False))
+    obs_specs = [(True, [(0.6, [("PauliZ", [1], None)]), (-0.4, [("PauliX", [0], None), ("PauliY", [n - 1], None)])]),
+                 (False, [(1.0, [("PauliY", [3], None)])]),
+                 (False, [(1.0, [("PauliX", [n - 2], None), ("PauliZ", [5], None)])])][:nobs]
+    sv = getattr(native, cls_name("c128"))(n)
+    apply_ops(sv, ops)
+    adj = native.AdjointJacobianGPU_C128()
+    opsd = adj.create_ops_list([o[0] for o in ops], [np.array(o[2], np.float64) for o in ops], [o[1] for o in ops],
+                               [o[3] for o in ops], [np.zeros(0, np.complex128) for o in ops])
+    obs = [_obs_native(native, "c128", s) for s in obs_specs]
+    jac = np.asarray(adj.adjoint_jacobian(sv, obs, opsd, tp))
+    final = oracle.run(n, to_oracle_ops(ops))
+    oobs = [(s[0], [(c, [(nm, w, m) for nm, w, m in f]) for c, f in s[1]]) for s in obs_specs]
+    ref = oracle.adjoint_jacobian(final, to_oracle_ops(ops), oobs, tp)
+    assert np.max(np.abs(jac - ref)) < tol("c128") * 50, np.max(np.abs(jac - ref))
+    assert np.max(np.abs(ref)) > 1e-3
+
+
 @pytest.mark.parametrize("dtype", DTYPES)
 def test_adjoint_rejects_multiparam(native, dtype):
     suf = "C128" if dtype == "c128" else "C64"
