@@ -14,6 +14,7 @@
 #include <memory>
 #include <vector>
 
+#include "lgpu_adj_plan.h"
 #include "lgpu_bodies.cuh"
 #include "lgpu_df2.cuh"
 #include "lgpu_df64.cuh"
@@ -1447,78 +1448,53 @@ static lgpu_status_t adjoint_block_t(lgpu_context_t ctx, void *ket, void *const 
     }
     p->nslots = int(cols.size());
     if (!c64 && adj_phase_groups_enabled()) {
-        // Phase groups: uncontrolled diagonal steps (RZ, PhaseShift, or
-        // without gradient) on at most kAdjGroupBits tile positions, at most
-        // kAdjGroupGrads of them with a gradient.  A group starts at such a
-        // step and takes later ones moved back past the steps in between: a
-        // diagonal step commutes (with its generator, Z or P1) with every
-        // diagonal step and with every step that targets another position
-        // (controls are diagonal), so only a non-diagonal step on its
-        // position blocks the move.  The steps left behind keep their order.
-        auto groupable = [&](const AStep &st) {
-            return st.body == B_DIAG && st.pad == 0 && st.in_mask == 0 && st.out_mask == 0 &&
-                   (st.gk == G_NONE || st.gk == G_Z || st.gk == G_P1);
-        };
-        auto diagonal = [&](const AStep &st) { return st.body == B_DIAG || st.pad == 1; };
-        std::vector<AStep> in(p->steps, p->steps + nsteps), out;
-        std::vector<char> used(nsteps, 0);
+        // phase groups (lgpu_adj_plan.h): uncontrolled diagonal steps (RZ,
+        // PhaseShift, or without gradient) gathered into one step each
+        std::vector<AStep> in(p->steps, p->steps + nsteps);
+        std::vector<AdjPlanStep> ps(nsteps);
         for (uint32_t i = 0; i < nsteps; i++) {
-            if (used[i]) continue;
-            if (!groupable(in[i])) {
-                out.push_back(in[i]);
-                continue;
-            }
-            std::vector<uint32_t> mem{i};
-            uint32_t pm = 1u << in[i].q, blocked = 0;
-            int ng = in[i].gk != G_NONE ? 1 : 0;
-            for (uint32_t j = i + 1; j < nsteps; j++) {
-                if (used[j]) continue;
-                const AStep &st = in[j];
-                const bool can = groupable(st) && !((blocked >> st.q) & 1u) &&
-                                 __builtin_popcount(pm | (1u << st.q)) <= kAdjGroupBits &&
-                                 ng + (st.gk != G_NONE ? 1 : 0) <= kAdjGroupGrads;
-                if (can) {
-                    mem.push_back(j);
-                    pm |= 1u << st.q;
-                    ng += st.gk != G_NONE ? 1 : 0;
-                } else if (!diagonal(st)) {
-                    blocked |= 1u << st.q;  // later steps on this position stay behind it
-                }
-            }
-            if (mem.size() < 2) {
-                out.push_back(in[i]);
+            const AStep &st = in[i];
+            ps[i].q = st.q;
+            ps[i].diagonal = st.body == B_DIAG || st.pad == 1;
+            ps[i].groupable = st.body == B_DIAG && st.pad == 0 && st.in_mask == 0 && st.out_mask == 0 &&
+                              (st.gk == G_NONE || st.gk == G_Z || st.gk == G_P1);
+            ps[i].grad = st.gk != G_NONE;
+        }
+        const auto plan = plan_phase_groups(ps, kAdjGroupBits, kAdjGroupGrads);
+        for (size_t r = 0; r < plan.size(); r++) {
+            const auto &mem = plan[r];
+            if (mem.size() == 1) {
+                p->steps[r] = in[mem[0]];
                 continue;
             }
             AStep gs{};
             gs.pad = kAdjPhaseGroup;
             gs.gk = int8_t(G_NONE);
             gs.slot = -1;
-            gs.in_mask = pm;
+            for (uint32_t i : mem) gs.in_mask |= 1u << in[i].q;
             std::vector<int> bits;  // table positions, ascending
             for (int q = 0; q < 32; q++)
-                if ((pm >> q) & 1u) bits.push_back(q);
+                if ((gs.in_mask >> q) & 1u) bits.push_back(q);
             for (int idx = 0; idx < (1 << kAdjGroupBits); idx++) {
                 std::complex<double> t(1.0, 0.0);
-                for (uint32_t r : mem) {
-                    const double *u = steps[r].u;
-                    const int rank = int(std::find(bits.begin(), bits.end(), int(in[r].q)) - bits.begin());
+                for (uint32_t i : mem) {
+                    const double *u = steps[i].u;
+                    const int rank = int(std::find(bits.begin(), bits.end(), int(in[i].q)) - bits.begin());
                     t *= ((idx >> rank) & 1) ? std::complex<double>(u[6], u[7]) : std::complex<double>(u[0], u[1]);
                 }
                 gs.u[idx] = df_split_host(t.real());
                 gs.g[idx] = df_split_host(t.imag());
             }
-            for (uint32_t r : mem) {
-                used[r] = 1;
-                if (in[r].gk == G_NONE) continue;
-                gs.gq[gs.ng] = in[r].q;
-                gs.gkd[gs.ng] = in[r].gk;
-                gs.gslot[gs.ng] = int16_t(in[r].slot);
+            for (uint32_t i : mem) {
+                if (in[i].gk == G_NONE) continue;
+                gs.gq[gs.ng] = in[i].q;
+                gs.gkd[gs.ng] = in[i].gk;
+                gs.gslot[gs.ng] = int16_t(in[i].slot);
                 gs.ng++;
             }
-            out.push_back(gs);
+            p->steps[r] = gs;
         }
-        for (size_t r = 0; r < out.size(); r++) p->steps[r] = out[r];
-        p->nsteps = int(out.size());
+        p->nsteps = int(plan.size());
     }
     if (c64 && m < 1) return fail(LGPU_ERR_INVALID_ARG, "adjoint block: complex64 tiles need bit 0");
     const size_t tile_bytes = (size_t(1) << k) * (c64 ? 8 : 16);

@@ -93,3 +93,18 @@ def test_diagonal_folding_keeps_the_state():
         assert r.returncode == 0, r.stdout + r.stderr
         assert "bad 0" in r.stdout
 
+
+
+def test_adjoint_phase_group_plan():
+    """Phase groups of the complex128 adjoint blocks
+    (lgpu_adj_plan.h::plan_phase_groups): on 500 random runs of steps the
+    planned sweep (a group's overlaps before its U^dag) gives every step's
+    overlap and the final states of the original order."""
+    with tempfile.TemporaryDirectory() as d:
+        exe = os.path.join(d, "test_adj_plan")
+        subprocess.run(["g++", "-O2", "-std=c++17",
+                        "-I" + os.path.join(ROOT, "pennylane_lightning_gpu_gb300", "csrc", "kernels"),
+                        os.path.join(ROOT, "tests", "native", "test_adj_plan.cpp"), "-o", exe], check=True)
+        r = subprocess.run([exe], capture_output=True, text=True)
+        assert r.returncode == 0, r.stdout + r.stderr
+        assert "bad 0" in r.stdout
