@@ -1,4 +1,4 @@
-// Phase groups of the complex128 adjoint blocks: which steps of a run are
+// Phase groups of the adjoint blocks: which steps of a run are
 // gathered into one group step, and in what order the steps then run.  Plain
 // C++ (no CUDA types), so the plan can be checked on the host.
 #pragma once

@@ -1031,6 +1031,47 @@ __device__ __forceinline__ void adj_block_step_f32(float2 *kt, float2 *const (&b
     }
 }
 
+// A phase group on complex64 tiles (see adj_phase_group): FP32 products,
+// the table entries as float2 (staged in shared memory by the caller).
+template <int NB>
+__device__ __forceinline__ void adj_phase_group_f32(float2 *kt, float2 *const (&bt)[kAdjBlockBras], int E,
+                                                    const AStep &st, const float2 *tab,
+                                                    float (&acc)[kAdjGroupGrads][kAdjBlockBras]) {
+    int sh[kAdjGroupBits];
+    {
+        uint32_t mm = st.in_mask;
+#pragma unroll
+        for (int b = 0; b < kAdjGroupBits; b++) {
+            sh[b] = mm ? (__ffs(int(mm)) - 1 - b) : (31 - b);
+            mm &= mm - 1u;
+        }
+    }
+    const int ng = st.ng;
+    for (int e = threadIdx.x; e < E; e += kAdjBlockThreads) {
+        int idx = 0;
+#pragma unroll
+        for (int b = 0; b < kAdjGroupBits; b++) idx |= (e >> sh[b]) & (1 << b);
+        const float2 t = tab[idx];
+        const int si = swz<float>(e);
+        float2 kv = kt[si];
+#pragma unroll
+        for (int b = 0; b < NB; b++) {
+            float2 bv = bt[b][si];
+            if (ng > 0) {
+                const float pr = bv.x * kv.y - bv.y * kv.x;
+#pragma unroll
+                for (int j = 0; j < kAdjGroupGrads; j++) {
+                    if (j >= ng) break;
+                    const int bit = (e >> st.gq[j]) & 1;
+                    acc[j][b] += st.gkd[j] == G_Z ? (bit ? -pr : pr) : (bit ? pr : 0.0f);
+                }
+            }
+            bt[b][si] = make_float2(t.x * bv.x - t.y * bv.y, t.x * bv.y + t.y * bv.x);
+        }
+        kt[si] = make_float2(t.x * kv.x - t.y * kv.y, t.x * kv.y + t.y * kv.x);
+    }
+}
+
 template <int NB>
 __device__ __forceinline__ void adj_block_dispatch_f32(float2 *kt, float2 *const (&bt)[kAdjBlockBras], int E,
                                                        const AStep &st, float (&acc)[kAdjBlockBras]) {
@@ -1099,6 +1140,31 @@ __global__ void __launch_bounds__(kAdjBlockThreads, 3) adjoint_block_f32_kernel(
         for (int si = 0; si < p.nsteps; si++) {
             const AStep &st = p.steps[si];
             if ((uint64_t(base) & st.out_mask) != st.out_val) continue;  // tile-uniform
+            if (st.pad == kAdjPhaseGroup) {
+                float2 *tab = reinterpret_cast<float2 *>(wacc + size_t(p.nslots) * NB * W);
+                if (threadIdx.x < (1 << kAdjGroupBits))
+                    tab[threadIdx.x] = make_float2(st.u[threadIdx.x].hi, st.g[threadIdx.x].hi);
+                __syncthreads();
+                float gacc[kAdjGroupGrads][kAdjBlockBras];
+#pragma unroll
+                for (int j = 0; j < kAdjGroupGrads; j++)
+#pragma unroll
+                    for (int b = 0; b < kAdjBlockBras; b++) gacc[j][b] = 0.0f;
+                adj_phase_group_f32<NB>(kt, bt, E, st, tab, gacc);
+#pragma unroll
+                for (int j = 0; j < kAdjGroupGrads; j++) {
+                    if (j >= st.ng) break;
+#pragma unroll
+                    for (int b = 0; b < NB; b++) {
+                        float v = gacc[j][b];
+#pragma unroll
+                        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+                        if (lane == 0) wacc[(st.gslot[j] * NB + b) * W + warp] += double(v);
+                    }
+                }
+                __syncthreads();
+                continue;
+            }
             float acc[kAdjBlockBras];
 #pragma unroll
             for (int b = 0; b < kAdjBlockBras; b++) acc[b] = 0.0f;
@@ -1447,7 +1513,7 @@ static lgpu_status_t adjoint_block_t(lgpu_context_t ctx, void *ket, void *const 
         }
     }
     p->nslots = int(cols.size());
-    if (!c64 && adj_phase_groups_enabled()) {
+    if (adj_phase_groups_enabled()) {
         // phase groups (lgpu_adj_plan.h): uncontrolled diagonal steps (RZ,
         // PhaseShift, or without gradient) gathered into one step each
         std::vector<AStep> in(p->steps, p->steps + nsteps);
@@ -1498,9 +1564,9 @@ static lgpu_status_t adjoint_block_t(lgpu_context_t ctx, void *ket, void *const 
     }
     if (c64 && m < 1) return fail(LGPU_ERR_INVALID_ARG, "adjoint block: complex64 tiles need bit 0");
     const size_t tile_bytes = (size_t(1) << k) * (c64 ? 8 : 16);
-    // tiles, the per-warp sums, then the phase-group table (complex128)
+    // tiles, the per-warp sums, then the phase-group table
     const size_t smem = (nbras + 1) * tile_bytes + size_t(std::max(p->nslots, 1)) * nbras * 8 * sizeof(DF) +
-                        (c64 ? 0 : (size_t(16) << kAdjGroupBits));
+                        (size_t(16) << kAdjGroupBits);
     const int per_sm = std::max(1, std::min(3, int((220 * 1024) / smem)));
     const unsigned grid = unsigned(std::min<uint64_t>(uint64_t(p->ntiles), uint64_t(sm_count()) * per_sm));
     // scratch: [reduction counter, 256 B, untouched][columns][partials]

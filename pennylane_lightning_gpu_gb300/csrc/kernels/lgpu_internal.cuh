@@ -58,9 +58,9 @@ int fused_df_enabled();
 // real rotation where that pays; 1 = fold without splits; 0 = off
 // (environment LGPU_DIAG_FOLD).
 int fused_diag_fold_enabled();
-// Phase groups in the complex128 adjoint blocks (consecutive uncontrolled
-// diagonal steps share one overlap product and one phase table): 1 (default)
-// = on, 0 = off (environment LGPU_ADJ_GROUPS).
+// Phase groups in the adjoint blocks (uncontrolled diagonal steps share one
+// overlap product and one phase table): 1 (default) = on, 0 = off
+// (environment LGPU_ADJ_GROUPS).
 int adj_phase_groups_enabled();
 // Uncontrolled 1-target gates use the bulk-copy pipelined kernel when 1
 // (default); the grid-stride kernel when 0.  See lgpu_set_stream_mode().

@@ -1,4 +1,4 @@
-// Host test of the phase groups of the complex128 adjoint blocks
+// Host test of the phase groups of the adjoint blocks
 // (lgpu_adj_plan.h::plan_phase_groups).  Random runs of steps on 6 qubits:
 // RZ and PhaseShift (diagonal, generators Z and P1, the groupable ones,
 // with or without a gradient), RX and RY with gradients, Hadamard-like dense

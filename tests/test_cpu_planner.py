@@ -96,7 +96,7 @@ def test_diagonal_folding_keeps_the_state():
 
 
 def test_adjoint_phase_group_plan():
-    """Phase groups of the complex128 adjoint blocks
+    """Phase groups of the adjoint blocks
     (lgpu_adj_plan.h::plan_phase_groups): on 500 random runs of steps the
     planned sweep (a group's overlaps before its U^dag) gives every step's
     overlap and the final states of the original order."""

@@ -531,14 +531,15 @@ def test_adjoint_fused_blocks(native, oracle, n, nobs, dtype):
     assert np.max(np.abs(ref)) > 1e-3  # the circuit has gradients to compare
 
 
-@pytest.mark.parametrize("n,nobs", [(14, 1), (14, 2), (15, 3)])
-def test_adjoint_phase_groups(native, oracle, n, nobs):
-    """complex128 fused adjoint blocks take runs of uncontrolled diagonal
+@pytest.mark.parametrize("n,nobs,dtype", [(14, 1, "c128"), (14, 2, "c128"), (15, 3, "c128"), (14, 1, "c64"),
+                                          (15, 3, "c64")])
+def test_adjoint_phase_groups(native, oracle, n, nobs, dtype):
+    """Fused adjoint blocks (complex128 and complex64) take runs of uncontrolled diagonal
     steps (RZ, PhaseShift, trainable or not, adjoint or not) on up to 3 tile
     positions as phase groups: one overlap product per amplitude for all of
     them, then one phase table.  Layers of RY / RZ / PhaseShift runs with CZ
     and CNOT between them, a trainable subset, 1 to 3 observables: against
-    the oracle adjoint at 50 x 1e-10."""
+    the oracle adjoint at 50 x the dtype tolerance (1e-10 / 1e-5)."""
     rng = np.random.default_rng(4100 + n + nobs)
     ops = [("Hadamard", [w], [], False) for w in range(n)]
     for layer in range(4):
@@ -556,17 +557,19 @@ def test_adjoint_phase_groups(native, oracle, n, nobs):
     obs_specs = [(True, [(0.6, [("PauliZ", [1], None)]), (-0.4, [("PauliX", [0], None), ("PauliY", [n - 1], None)])]),
                  (False, [(1.0, [("PauliY", [3], None)])]),
                  (False, [(1.0, [("PauliX", [n - 2], None), ("PauliZ", [5], None)])])][:nobs]
-    sv = getattr(native, cls_name("c128"))(n)
+    suf = "C128" if dtype == "c128" else "C64"
+    rdt = np.float64 if dtype == "c128" else np.float32
+    sv = getattr(native, cls_name(dtype))(n)
     apply_ops(sv, ops)
-    adj = native.AdjointJacobianGPU_C128()
-    opsd = adj.create_ops_list([o[0] for o in ops], [np.array(o[2], np.float64) for o in ops], [o[1] for o in ops],
-                               [o[3] for o in ops], [np.zeros(0, np.complex128) for o in ops])
-    obs = [_obs_native(native, "c128", s) for s in obs_specs]
+    adj = getattr(native, "AdjointJacobianGPU_" + suf)()
+    opsd = adj.create_ops_list([o[0] for o in ops], [np.array(o[2], rdt) for o in ops], [o[1] for o in ops],
+                               [o[3] for o in ops], [np.zeros(0, np_dtype(dtype)) for o in ops])
+    obs = [_obs_native(native, dtype, s) for s in obs_specs]
     jac = np.asarray(adj.adjoint_jacobian(sv, obs, opsd, tp))
     final = oracle.run(n, to_oracle_ops(ops))
     oobs = [(s[0], [(c, [(nm, w, m) for nm, w, m in f]) for c, f in s[1]]) for s in obs_specs]
     ref = oracle.adjoint_jacobian(final, to_oracle_ops(ops), oobs, tp)
-    assert np.max(np.abs(jac - ref)) < tol("c128") * 50, np.max(np.abs(jac - ref))
+    assert np.max(np.abs(jac - ref)) < tol(dtype) * 50, np.max(np.abs(jac - ref))
     assert np.max(np.abs(ref)) > 1e-3
 
 
