@@ -653,7 +653,7 @@ constexpr int kAdjBlockSteps = 48;
 constexpr int kAdjBlockBras = 2;
 constexpr int kAdjBlockThreads = 256;
 
-constexpr int kAdjGroupBits = 3;   // phase group: table over at most 3 tile positions
+constexpr int kAdjGroupBits = 4;   // phase group: table over at most 4 tile positions
 constexpr int kAdjGroupGrads = 4;  // and at most 4 gradient steps
 constexpr uint8_t kAdjPhaseGroup = 2;
 
@@ -662,11 +662,11 @@ struct AStep {
     uint8_t body;   // Body1 of U^dag
     int8_t gk;      // GenKind, G_NONE: no gradient
     uint8_t pad;    // 1: U^dag = diag(+-1, +-1), sign flips; kAdjPhaseGroup: a phase group
-    int32_t slot;   // accumulator slot of a gradient step
+    int32_t slot;   // accumulator slot of a gradient step (phase group: its table in gtab)
     uint32_t in_mask, in_val;    // controls inside the tile (phase group: the table positions)
     uint64_t out_mask, out_val;  // controls outside the tile (state bits)
-    DF u[8];  // phase group: Re of the table entries
-    DF g[8];  // phase group: Im of the table entries
+    DF u[8];
+    DF g[8];
     // phase group: its gradient steps (tile position, G_Z or G_P1, slot)
     uint8_t ng;
     uint8_t gq[kAdjGroupGrads];
@@ -685,7 +685,10 @@ template <class I> struct AdjBlockParams {
     double *partials;  // [gridDim.x][nslots][nb]
     int in_ff, out_ff;  // complex128: the states are read / left in float-float form
     AStep steps[kAdjBlockSteps];
+    // phase-group tables (a group step's slot indexes them): entries (re.hi, re.lo, im.hi, im.lo)
+    float4 gtab[kAdjBlockSteps / 2][1 << kAdjGroupBits];
 };
+static_assert(sizeof(AdjBlockParams<uint64_t>) <= 32000, "adjoint block parameters exceed the 32 KB limit");
 
 __device__ __forceinline__ void adj_cp_async16(void *smem_dst, const void *gsrc) {
     asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(static_cast<uint32_t>(__cvta_generic_to_shared(smem_dst))),
@@ -911,8 +914,7 @@ __global__ void __launch_bounds__(kAdjBlockThreads, 3) adjoint_block_kernel(cons
             if (st.pad == kAdjPhaseGroup) {
                 float4 *tab = reinterpret_cast<float4 *>(wacc + size_t(p.nslots) * NB * W);
                 if (threadIdx.x < (1 << kAdjGroupBits))
-                    tab[threadIdx.x] = make_float4(st.u[threadIdx.x].hi, st.u[threadIdx.x].lo, st.g[threadIdx.x].hi,
-                                                   st.g[threadIdx.x].lo);
+                    tab[threadIdx.x] = p.gtab[st.slot][threadIdx.x];
                 __syncthreads();
                 DF gacc[kAdjGroupGrads][kAdjBlockBras];
 #pragma unroll
@@ -1143,7 +1145,7 @@ __global__ void __launch_bounds__(kAdjBlockThreads, 3) adjoint_block_f32_kernel(
             if (st.pad == kAdjPhaseGroup) {
                 float2 *tab = reinterpret_cast<float2 *>(wacc + size_t(p.nslots) * NB * W);
                 if (threadIdx.x < (1 << kAdjGroupBits))
-                    tab[threadIdx.x] = make_float2(st.u[threadIdx.x].hi, st.g[threadIdx.x].hi);
+                    tab[threadIdx.x] = make_float2(p.gtab[st.slot][threadIdx.x].x, p.gtab[st.slot][threadIdx.x].z);
                 __syncthreads();
                 float gacc[kAdjGroupGrads][kAdjBlockBras];
 #pragma unroll
@@ -1527,6 +1529,7 @@ static lgpu_status_t adjoint_block_t(lgpu_context_t ctx, void *ket, void *const 
             ps[i].grad = st.gk != G_NONE;
         }
         const auto plan = plan_phase_groups(ps, kAdjGroupBits, kAdjGroupGrads);
+        int ntab = 0;  // groups have two or more steps: at most kAdjBlockSteps / 2 tables
         for (size_t r = 0; r < plan.size(); r++) {
             const auto &mem = plan[r];
             if (mem.size() == 1) {
@@ -1536,7 +1539,7 @@ static lgpu_status_t adjoint_block_t(lgpu_context_t ctx, void *ket, void *const 
             AStep gs{};
             gs.pad = kAdjPhaseGroup;
             gs.gk = int8_t(G_NONE);
-            gs.slot = -1;
+            gs.slot = ntab;  // its table in gtab
             for (uint32_t i : mem) gs.in_mask |= 1u << in[i].q;
             std::vector<int> bits;  // table positions, ascending
             for (int q = 0; q < 32; q++)
@@ -1548,8 +1551,8 @@ static lgpu_status_t adjoint_block_t(lgpu_context_t ctx, void *ket, void *const 
                     const int rank = int(std::find(bits.begin(), bits.end(), int(in[i].q)) - bits.begin());
                     t *= ((idx >> rank) & 1) ? std::complex<double>(u[6], u[7]) : std::complex<double>(u[0], u[1]);
                 }
-                gs.u[idx] = df_split_host(t.real());
-                gs.g[idx] = df_split_host(t.imag());
+                const DF re = df_split_host(t.real()), im = df_split_host(t.imag());
+                p->gtab[ntab][idx] = make_float4(re.hi, re.lo, im.hi, im.lo);
             }
             for (uint32_t i : mem) {
                 if (in[i].gk == G_NONE) continue;
@@ -1559,6 +1562,7 @@ static lgpu_status_t adjoint_block_t(lgpu_context_t ctx, void *ket, void *const 
                 gs.ng++;
             }
             p->steps[r] = gs;
+            ntab++;
         }
         p->nsteps = int(plan.size());
     }

@@ -6,8 +6,8 @@
 // controlled steps.  Each step of the reverse sweep takes Im <bra| G |ket>
 // and then applies U^dag to both states.  The planned sweep takes every
 // group's overlaps before any of its U^dag, then applies them.  Checks: every
-// step appears once; groups hold only groupable steps, at most max_bits
-// positions and max_grads gradients; the overlaps of every step and the final
+// step appears once; groups hold only groupable steps, at most max_bits (3 or
+// 4) positions and max_grads gradients; the overlaps of every step and the final
 // states equal those of the original order (within 1e-12) for random states.
 #include <algorithm>
 #include <cmath>
@@ -71,9 +71,10 @@ int main() {
     std::uniform_real_distribution<double> ang(-3.1, 3.1);
     std::normal_distribution<double> nd;
     const int n = 6;
-    const int max_bits = 3, max_grads = 4;
+    const int max_grads = 4;
     long groups = 0, grouped = 0, moved = 0;
     for (int trial = 0; trial < 500; trial++) {
+        const int max_bits = 3 + trial % 2;  // the tables of 3 and 4 positions
         const int len = 2 + int(gen() % 46);
         std::vector<Step> st(static_cast<size_t>(len), Step{});
         std::vector<lgpu::AdjPlanStep> ps(static_cast<size_t>(len));

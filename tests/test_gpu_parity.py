@@ -535,7 +535,7 @@ def test_adjoint_fused_blocks(native, oracle, n, nobs, dtype):
                                           (15, 3, "c64")])
 def test_adjoint_phase_groups(native, oracle, n, nobs, dtype):
     """Fused adjoint blocks (complex128 and complex64) take runs of uncontrolled diagonal
-    steps (RZ, PhaseShift, trainable or not, adjoint or not) on up to 3 tile
+    steps (RZ, PhaseShift, trainable or not, adjoint or not) on up to 4 tile
     positions as phase groups: one overlap product per amplitude for all of
     them, then one phase table.  Layers of RY / RZ / PhaseShift runs with CZ
     and CNOT between them, a trainable subset, 1 to 3 observables: against
