@@ -9,6 +9,8 @@
 // exactly when they are tables, diag(+-1, +-1) gates must stay as they are,
 // and the splits must add no launch of kFusedMaxGates records.  Layer-shaped
 // blocks (dense unitaries on every tile bit, then CNOTs) must keep splits.
+// split_dense_1q's edge cases are checked on their own (split_edge_cases).
+#include <cmath>
 #include <complex>
 #include <cstdio>
 #include <random>
@@ -87,7 +89,61 @@ static size_t real_records(const std::vector<lgpu_fused_gate_t> &f, const std::v
     return r;
 }
 
+// split_dense_1q on its edge cases: structured and non-unitary matrices are
+// not split; unitaries with tiny off-diagonal or diagonal entries, and with
+// controls, split into parts whose product is the matrix within 1e-13, the
+// middle part real and the outer ones diagonal.
+static void split_edge_cases() {
+    auto mk = [](const cd (&u)[4]) {
+        lgpu_fused_gate_t g{};
+        g.ntgt = 1;
+        g.tgt[0] = 2;
+        for (int e = 0; e < 4; e++) {
+            g.m[2 * e] = u[e].real();
+            g.m[2 * e + 1] = u[e].imag();
+        }
+        return g;
+    };
+    lgpu_fused_gate_t f[3];
+    const double s = 1 / std::sqrt(2.0);
+    const cd diag[4] = {std::polar(1.0, 0.3), 0, 0, std::polar(1.0, -0.3)};
+    const cd anti[4] = {0, cd(0, -1), cd(0, 1), 0};
+    const cd real[4] = {s, -s, s, s};
+    const cd rx[4] = {std::cos(0.4), cd(0, -std::sin(0.4)), cd(0, -std::sin(0.4)), std::cos(0.4)};
+    const cd nonu[4] = {cd(1, 1), cd(0.5, 0), cd(0, 0.5), cd(2, 0)};
+    for (const auto *u : {&diag, &anti, &real, &rx, &nonu})
+        if (lgpu::split_dense_1q(mk(*u), f)) fail("structured or non-unitary matrix split", -1, 0);
+    for (double th : {1e-9, 1e-4, 0.7, 3.1415926, 3.14159265358979}) {
+        // Rot(phi, th, om) with small or near-pi theta, and a control
+        const double ph = 0.37, om = -1.21;
+        const cd u[4] = {std::polar(std::cos(th / 2), -(ph + om) / 2), -std::polar(std::sin(th / 2), (ph - om) / 2),
+                         std::polar(std::sin(th / 2), -(ph - om) / 2), std::polar(std::cos(th / 2), (ph + om) / 2)};
+        lgpu_fused_gate_t g = mk(u);
+        g.nctrl = 1;
+        g.ctrl[0] = 5;
+        g.ctrl_val[0] = 1;
+        if (!lgpu::split_dense_1q(g, f)) {
+            fail("dense unitary not split", -1, th);
+            continue;
+        }
+        auto m = [](const lgpu_fused_gate_t &x, int e) { return cd(x.m[2 * e], x.m[2 * e + 1]); };
+        for (int k = 0; k < 3; k++)
+            if (f[k].nctrl != 1 || f[k].ctrl[0] != 5 || f[k].tgt[0] != 2) fail("split part lost its wires", -1, k);
+        if (m(f[0], 1) != 0.0 || m(f[0], 2) != 0.0 || m(f[2], 1) != 0.0 || m(f[2], 2) != 0.0)
+            fail("outer split part not diagonal", -1, th);
+        for (int e = 0; e < 4; e++)
+            if (f[1].m[2 * e + 1] != 0.0) fail("middle split part not real", -1, th);
+        // product D_L R D_R
+        cd q[4];
+        for (int r = 0; r < 2; r++)
+            for (int c = 0; c < 2; c++) q[2 * r + c] = m(f[2], 3 * r) * m(f[1], 2 * r + c) * m(f[0], 3 * c);
+        for (int e = 0; e < 4; e++)
+            if (std::abs(q[e] - u[e]) > 1e-13) fail("split product differs", -1, std::abs(q[e] - u[e]));
+    }
+}
+
 int main() {
+    split_edge_cases();
     std::mt19937_64 gen(11);
     std::normal_distribution<double> nd;
     const int n = 8, k = 6;  // tile = bits 0..5; bits 6, 7 outside
